@@ -1,0 +1,173 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes front end of the CPU oracle.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline
+legs may import this module, and only as the checker or as the timed CPU
+baseline.  The product path (``d2_kmeans_gb300``) never imports it.
+
+Two back ends share one plain-array C interface (``d2_oracle.h``):
+
+* ``port``      - ``liboracle.so``, the C restatement of the reference B-ADMM
+                  update (src/d2/centroid_Bregman.c:95-318); builds anywhere.
+* ``reference`` - ``_ref/libd2ref.so``, the reference's own sources compiled
+                  unmodified by ``oracle/Makefile``; exists only where the
+                  reference tree was present at build time.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_LIB = os.path.join(HERE, "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libd2ref.so")
+REF_TREE = "/root/reference"
+
+METRIC = {"euclidean": 0, "histogram": 5, "embed": 7, "sparse_histogram": 12}
+
+
+class _Phase(C.Structure):
+    _fields_ = [
+        ("metric", C.c_int), ("dim", C.c_int), ("str", C.c_int),
+        ("size", C.c_size_t), ("col", C.c_size_t),
+        ("p_str", C.c_void_p), ("p_w", C.c_void_p), ("p_supp", C.c_void_p),
+        ("p_supp_sym", C.c_void_p), ("vocab_vec", C.c_void_p), ("vocab_size", C.c_int),
+        ("dist_mat", C.c_void_p), ("label", C.c_void_p), ("num_of_labels", C.c_int),
+        ("label_switch", C.c_void_p), ("global_size", C.c_size_t),
+    ]
+
+
+class _Opts(C.Structure):
+    _fields_ = [("maxIters", C.c_int), ("rhoCoeff", C.c_double),
+                ("updatePerLoops", C.c_int), ("time_budget", C.c_double)]
+
+
+def build(reference: bool | None = None) -> None:
+    """Compile the restatement (always) and the reference (when its tree exists)."""
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    if reference is None:
+        reference = os.path.isdir(os.path.join(REF_TREE, "src", "d2"))
+    if reference:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_TREE}"], check=True)
+
+
+_libs: dict[str, C.CDLL] = {}
+
+
+def available(kind: str) -> bool:
+    return os.path.exists(PORT_LIB if kind == "port" else REF_LIB)
+
+
+def _lib(kind: str) -> C.CDLL:
+    if kind not in _libs:
+        path = PORT_LIB if kind == "port" else REF_LIB
+        if not os.path.exists(path):
+            raise FileNotFoundError(f"oracle library {path} not built")
+        lib = C.CDLL(path)
+        fn = lib.d2o_badmm if kind == "port" else lib.d2r_badmm
+        fn.restype = C.c_int
+        fn.argtypes = [C.POINTER(_Phase), C.POINTER(_Opts)] + [C.c_void_p] * 10
+        if kind == "port":
+            lib.d2o_serve_query.restype = C.c_int
+            lib.d2o_serve_query.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                            C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                            C.c_double, C.c_void_p]
+        _libs[kind] = lib
+    return _libs[kind]
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def badmm(phase: dict, centroids: dict, opts: dict, kind: str = "port",
+          want=("X", "Y", "C")) -> dict:
+    """Run one B-ADMM centroid update on the CPU.
+
+    ``phase`` holds the reference's d2 arrays (``p_str``, ``p_w``, ``p_supp`` or
+    ``p_supp_sym`` + ``vocab_vec`` or ``dist_mat``, ``label``, ``num_of_labels``,
+    ``label_switch``, ``metric``, ``dim``, ``str``); ``centroids`` holds ``c_w``
+    (k*str) and ``c_supp`` (k*str*dim) plus optionally a warm-start ``Z``.
+    Returns the updated centroids, Z, optional X/Y/C, the obj/primres/dualres
+    trace and rho.
+    """
+    lib = _lib(kind)
+    p_str = np.ascontiguousarray(phase["p_str"], dtype=np.int32)
+    size = p_str.size
+    col = int(p_str.sum())
+    m = int(phase["str"])
+    dim = int(phase.get("dim", 0))
+    k = int(phase["num_of_labels"])
+    keep = []
+
+    def arr(name, dtype):
+        a = phase.get(name)
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=dtype)
+        keep.append(a)
+        return a
+
+    ph = _Phase()
+    ph.metric = METRIC[phase["metric"]] if isinstance(phase["metric"], str) else int(phase["metric"])
+    ph.dim, ph.str, ph.size, ph.col = dim, m, size, col
+    ph.p_str = p_str.ctypes.data
+    ph.p_w = _ptr(arr("p_w", np.float64))
+    ph.p_supp = _ptr(arr("p_supp", np.float64))
+    ph.p_supp_sym = _ptr(arr("p_supp_sym", np.int32))
+    ph.vocab_vec = _ptr(arr("vocab_vec", np.float64))
+    ph.vocab_size = int(phase.get("vocab_size", 0))
+    ph.dist_mat = _ptr(arr("dist_mat", np.float64))
+    ph.label = _ptr(arr("label", np.int32))
+    ph.num_of_labels = k
+    ls = phase.get("label_switch")
+    ls = np.ones(size, np.int8) if ls is None else np.ascontiguousarray(ls, dtype=np.int8)
+    keep.append(ls)
+    ph.label_switch = ls.ctypes.data
+    ph.global_size = int(phase.get("global_size", size))
+
+    op = _Opts()
+    op.maxIters = int(opts.get("maxIters", 100))
+    op.rhoCoeff = float(opts.get("rhoCoeff", 2.0))
+    op.updatePerLoops = int(opts.get("updatePerLoops", 10))
+    op.time_budget = float(opts.get("time_budget", 1e300))
+
+    c_w = np.array(centroids["c_w"], dtype=np.float64, copy=True).reshape(-1)
+    cs = centroids.get("c_supp")
+    c_supp = (np.zeros(max(k * m * dim, 1)) if cs is None
+              else np.array(cs, dtype=np.float64, copy=True).reshape(-1))
+    Z = centroids.get("Z")
+    Z = np.zeros(m * col) if Z is None else np.array(Z, dtype=np.float64, copy=True).reshape(-1)
+    outs = {n: (np.empty(m * col) if n in want else None) for n in ("X", "Y", "C")}
+    nchk = op.maxIters // 20 + 8
+    trace = np.zeros(4 * nchk)
+    ntrace = C.c_int(0)
+    rho = C.c_double(0)
+    iters = C.c_int(0)
+    fn = lib.d2o_badmm if kind == "port" else lib.d2r_badmm
+    rc = fn(C.byref(ph), C.byref(op), c_w.ctypes.data, c_supp.ctypes.data, Z.ctypes.data,
+            _ptr(outs["X"]), _ptr(outs["Y"]), _ptr(outs["C"]), trace.ctypes.data,
+            C.addressof(ntrace), C.addressof(rho), C.addressof(iters))
+    res = {"rc": rc, "c_w": c_w, "c_supp": c_supp, "Z": Z,
+           "trace": trace[: 4 * ntrace.value].reshape(-1, 4), "rho": rho.value,
+           "iters": iters.value}
+    res.update({n: v for n, v in outs.items() if v is not None})
+    return res
+
+
+def serve_query(c_w, c_supp, w_q, supp_q, iters=200, rho_coeff=2.0):
+    """Fixed-centroid transport solve of one query against all k centroids."""
+    lib = _lib("port")
+    c_w = np.ascontiguousarray(c_w, dtype=np.float64)
+    k, m = c_w.shape
+    c_supp = np.ascontiguousarray(c_supp, dtype=np.float64)
+    dim = c_supp.shape[-1]
+    w_q = np.ascontiguousarray(w_q, dtype=np.float64)
+    supp_q = np.ascontiguousarray(supp_q, dtype=np.float64)
+    cost = np.zeros(k)
+    best = lib.d2o_serve_query(dim, m, k, c_w.ctypes.data, c_supp.ctypes.data, w_q.size,
+                               w_q.ctypes.data, supp_q.ctypes.data, int(iters),
+                               float(rho_coeff), cost.ctypes.data)
+    return best, cost
