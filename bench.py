@@ -1,0 +1,324 @@
+#!/usr/bin/env python
+"""Benchmark of the B-ADMM centroid update on GB300.
+
+One step = one full centroid update (maxIters=200, i.e. 201 B-ADMM
+iterations) over the batched uneven-size Euclidean workload: n=200000 D2
+instances in d=3, support sizes log-uniform 8..128 from a 64-component
+Gaussian mixture, Dirichlet(0.5) weights, k=64 centroids with m=32 supports,
+rhoCoeff=2, updatePerLoops=10.  Seeded synthetic data (no dataset download).
+
+Prints one JSON line:
+  value      plan-updates/s of the batched FP32 form, inputs resident in HBM,
+             CUDA events on the library's stream around K steps
+  e2e        the same metric through the reference-facing C entry point
+             d2_centroid_sphBregman with host buffers (inputs from pinned host
+             memory, results back to the caller's arrays) inside the timing
+  plain_gpu  the plain FP64 one-kernel-per-step GPU form on the same inputs
+  roofline   the plan-update kernel against the measured HBM copy bandwidth
+  cpu_baseline  the C restatement of the reference (oracle port) on the host
+
+--impl reference times the reference algorithm's CPU implementation (the
+oracle port; the reference tree itself is not on the GPU host) with every
+host core, one process per core on a shard of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "B-ADMM plan-updates/sec (batched vs plain GPU) at obj err ≤1e-5; serve p50/p99"
+UNIT = "plan-updates/s"
+WORKLOAD = ("batched uneven sizes: n=200000 Euclidean D2 instances, d=3, m_i log-uniform 8-128, "
+            "64-component GMM supports, Dirichlet(0.5) weights; k=64 centroids, m=32; "
+            "rhoCoeff=2, updatePerLoops=10, maxIters=200 (201 iterations)")
+HBM_FALLBACK_GBS = 6800.0
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+
+    def summary(self):
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU legs
+def _cpu_shard(args):
+    """One process: the oracle port on a shard of the workload."""
+    scale, seed, shard, nshard, iters = args
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np  # noqa: F401
+    import oracle
+    from d2_kmeans_gb300 import synth
+    ph, c, opts = synth.workload("batched", seed=seed + shard, scale=scale)
+    opts = dict(opts, maxIters=iters - 1)
+    t = time.perf_counter()
+    r = oracle.badmm(ph, c, opts, "port", want=())
+    el = time.perf_counter() - t
+    assert r["rc"] == 0, r["rc"]
+    return len(ph["p_str"]) * r["iters"], el
+
+
+def cpu_baseline(procs: int, scale: float, iters: int, seed: int = 100):
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs) as pool:
+        res = pool.map(_cpu_shard, [(scale, seed, s, procs, iters) for s in range(procs)])
+    units = sum(u for u, _ in res)
+    wall = max(t for _, t in res)
+    return units / wall, units, wall
+
+
+def ensure_oracle():
+    import oracle
+    if not oracle.available("port"):
+        oracle.build(reference=False)
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    ensure_oracle()
+    procs = os.cpu_count() or 1
+    # per step, each core runs 1000 instances (1/200 of the workload) for 21 iterations
+    scale, iters = 1000 / 200000, 21
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, units, wall = cpu_baseline(procs, scale, iters, seed=200 + i)
+        if i >= args.warmup:
+            vals.append((v, wall))
+    value = statistics.mean(v for v, _ in vals)
+    ms = 1e3 * statistics.mean(w for _, w in vals)
+    sample = (f"per step, {procs} processes (one per host core) each run the oracle port on its own "
+              f"1000-instance shard of the workload for 21 iterations; no cross-shard reduction")
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "sample": sample},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+# ------------------------------------------------------------------ GPU legs
+def time_steps(P, c, opts, steps):
+    import torch
+    st = torch.cuda.ExternalStream(P.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(steps):
+        r = P.run(c, opts)
+    e1.record(st)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps, r
+
+
+def e2e_steps(ph, c, opts, steps, warmup):
+    """Through d2_centroid_sphBregman with host buffers: pinned inputs,
+    results into the caller's arrays (c->p_w, c->p_supp, work Z)."""
+    import numpy as np
+    import torch
+    from d2_kmeans_gb300 import badmm
+
+    def pinned(a):
+        if a is None:
+            return None
+        t = torch.empty(a.size, dtype=getattr(torch, str(a.dtype)) if a.dtype != np.int8 else torch.int8,
+                        pin_memory=True)
+        v = t.numpy()
+        v[:] = a.reshape(-1)
+        return v
+    php = {k: (pinned(v) if isinstance(v, np.ndarray) else v) for k, v in ph.items()}
+    d = badmm.DropIn(php, c)
+    h2d = sum(php[k].nbytes for k in ("p_str", "p_w", "p_supp", "label", "label_switch")) + \
+        d.c_w.nbytes + d.c_supp.nbytes
+    d2h = d.c_w.nbytes + d.c_supp.nbytes + 8 * d.m * d.col
+    times = []
+    for i in range(warmup + steps):
+        d.c_w[:] = c["c_w"]
+        d.c_supp[:] = c["c_supp"]
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        rc = d.call(opts)
+        el = time.perf_counter() - t
+        assert rc == 0, rc
+        if i >= warmup:
+            times.append(el)
+    d.close()
+    return statistics.mean(times), h2d, d2h
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip", default="", help="comma list of legs to skip: e2e,plain,cpu,profile")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:  # one process per GPU: each rank sees its own GPU as device 0
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    if args.impl == "reference":
+        return run_reference(args, rank)
+    skip = set(x for x in args.skip.split(",") if x)
+
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    from d2_kmeans_gb300 import badmm, synth
+    from d2_kmeans_gb300.build import build as build_lib
+
+    if not os.path.exists(os.path.join(ROOT, "d2_kmeans_gb300", "libd2g.so")):
+        build_lib()
+    torch.cuda.set_device(0)
+    if world > 1:
+        dist.init_process_group("nccl")
+    badmm.set_config(verbose=0, precision=0, use_graph=1, profile=0)
+
+    ph, c, opts = synth.workload("batched", seed=0)
+    n = len(ph["p_str"])
+    P = badmm.Phase(ph, 0)
+    for _ in range(args.warmup):
+        P.run(c, opts)
+    gpu = int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0)
+    if world > 1:
+        dist.barrier()
+    with ClockSampler(gpu if world > 1 else 0) as clk:
+        ms, r = time_steps(P, c, opts, args.steps)
+    clocks = clk.summary()
+    stats = P.stats()
+    iters = stats["iterations"]
+    ms_t = torch.tensor([ms], device="cuda")
+    if world > 1:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms = float(ms_t.item())
+    value = world * n * iters / (ms / 1e3)
+
+    hbm, peak_kind = peaks()
+    roof = None
+    if "profile" not in skip:
+        badmm.set_config(profile=1)
+        P.run(c, opts)
+        ps = P.stats()
+        badmm.set_config(profile=0)
+        achieved = ps["plan_bytes"] / (ps["plan_ms_avg"] / 1e3) / 1e9
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", "plan_kernel_traffic.json")
+        if os.path.exists(tp):
+            with open(tp) as f:
+                traffic = json.load(f).get("traffic_bytes_per_launch")
+        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
+                "kernel": "plan_kernel_tma<32, EUCLID4>",
+                "algo_bytes_per_launch": ps["plan_bytes"], "ms_per_launch": ps["plan_ms_avg"]}
+    trace_b = r["trace"]
+    cw_b = r["c_w"].copy()
+    P.close()
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32 plans, f64 cross-plan reductions",
+           "data": "synthetic (seeded GMM / Dirichlet; no dataset)",
+           "config": {"workload": WORKLOAD, "iterations_per_step": iters,
+                      "parallelism": "replicas" if world > 1 else "1 GPU",
+                      "l2": "inputs larger than L2: Z and Y are 1.1 GB each",
+                      "plan_entries": int(stats["plan_entries"])},
+           "clocks": clocks, "gpu_launches": int(stats["kernel_launches"]) * args.steps,
+           "roofline": roof}
+
+    if "plain" not in skip and rank == 0:
+        Q = badmm.Phase(ph, 1)
+        ms_p, rp = time_steps(Q, c, opts, 1)
+        Q.close()
+        obj_err = float(np.max(np.abs(trace_b[:, 1] - rp["trace"][:, 1]) / np.abs(rp["trace"][:, 1])))
+        cw_l1 = float(np.abs(cw_b.reshape(64, 32) - rp["c_w"].reshape(64, 32)).sum(1).max())
+        vp = n * iters / (ms_p / 1e3)
+        out["plain_gpu"] = {"value": vp, "unit": UNIT, "ms_per_step": ms_p,
+                            "form": "FP64, one kernel per reference step, C/X/Z0 in HBM",
+                            "batched_over_plain": value / world / vp,
+                            "obj_rel_err_batched_vs_fp64": obj_err, "c_w_l1_vs_fp64": cw_l1}
+    if "e2e" not in skip:
+        sec, h2d, d2h = e2e_steps(ph, c, opts, max(1, min(args.steps, 3)), 1)
+        out["e2e"] = {"value": world * n * iters / sec, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                      "d2h_bytes_per_step": d2h, "seconds_per_step": sec,
+                      "api": "d2_centroid_sphBregman (reference structs, host buffers)"}
+    if "cpu" not in skip and rank == 0:
+        ensure_oracle()
+        v, units, wall = cpu_baseline(1, 20000 / 200000, 21, seed=100)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": f"oracle port (C restatement of the reference, FP64, 1 core) "
+                                         f"on 20000 instances of the workload for 21 iterations: "
+                                         f"{units} plan-updates in {wall:.1f} s"}
+    if world > 1:
+        dist.barrier()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

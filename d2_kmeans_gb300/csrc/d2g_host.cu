@@ -1,0 +1,1087 @@
+// Host side of libd2g: device state of one phase, packing of plans into
+// thread blocks, the B-ADMM iteration loop (captured as one CUDA graph), and
+// the resident C API (d2g_phase_*, d2g_badmm_run).
+//
+// Iteration loop, per iteration `it` (src/d2/centroid_Bregman.c:150-319):
+//   plan_kernel            steps 1-3, row sums, [moments], [residual partials]
+//   cluster_partial/final  step 4 (+ step 5 supports on update iterations)
+//   [obj_kernel]           obj after a support update on a check iteration
+//   [resid_final]          step 6 on check iterations
+// The plain FP64 form runs one kernel per reference step instead.
+#include <algorithm>
+#include <climits>
+#include <cstdlib>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "d2g_internal.cuh"
+
+namespace d2g {
+
+static thread_local std::string g_last_error;
+void set_error(const std::string &msg) { g_last_error = msg; }
+int cuda_fail(cudaError_t e, const char *what) {
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  cudaGetLastError();  // clear a sticky launch error so the context stays usable
+  return e == cudaErrorMemoryAllocation ? D2G_E_NOMEM : D2G_E_CUDA;
+}
+static int fail(int code, const std::string &msg) {
+  set_error(msg);
+  return code;
+}
+
+std::mutex g_cfg_mu;
+d2g_config g_cfg = {0, 1, 1, 0, 0};
+d2g_config cfg_snapshot() {
+  std::lock_guard<std::mutex> lk(g_cfg_mu);
+  return g_cfg;
+}
+
+template <typename T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t cnt) {
+    if (cnt == 0) cnt = 1;
+    if (p && cnt <= n) return cudaSuccess;
+    release();
+    cudaError_t e = cudaMalloc(&p, cnt * sizeof(T));
+    if (e == cudaSuccess)
+      n = cnt;
+    else
+      p = nullptr;
+    return e;
+  }
+};
+
+static inline bool is_check_iter(int it) { return (it % 100 == 99) || (it < 100 && it % 20 == 19); }
+static inline int next_pow2(int v) {
+  int p = 1;
+  while (p < v) p <<= 1;
+  return p;
+}
+
+}  // namespace d2g
+
+using namespace d2g;
+
+struct d2g_phase {
+  // ---- description
+  int metric = 0, dim = 0, str = 0, K = 0, vocab_size = 0;
+  size_t size = 0, col = 0, global_size = 0;
+  int path = 0;  // 0 batched FP32, 1 plain FP64
+  std::vector<int> p_str, label;
+  std::vector<long long> cum;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  // ---- common device state
+  DBuf<Ctl> ctl;
+  DBuf<double> trace;
+  int max_checks = 0;
+  DBuf<double> cw64, cs64;
+  DBuf<double> stage;  // reference-layout FP64 staging
+  DBuf<double> part;   // cluster partials
+  int chunk = 256, nchunk = 1;
+  DBuf<int> cl_ptr, cl_plans;
+  DBuf<char> reinit;
+
+  // ---- batched form
+  Geo geo{};
+  int MP = 0, DS = 4, mode = COST_EUCLID4;
+  long long ncols_packed = 0;
+  int ngroups = 0, nplans = 0;
+  struct Bucket {
+    int cs, nitems, item_off, block_off;
+  };
+  std::vector<Bucket> buckets;
+  int total_blocks = 0;
+  std::vector<int> plan_inst, inst_plan;
+  DBuf<float> Z, Y, Xp, col_w, col_supp, rowsum, xmom, cw32, cs32, ctab;
+  DBuf<int> col_sym, grp_meta, plan_g0, plan_ng, plan_label, item_g0, item_ng;
+  DBuf<long long> plan_cum;
+  DBuf<int4> grp_rec;
+  DBuf<int> plan_slot;
+  std::vector<int4> h_grp_rec;  // slot and label fields rewritten when labels change
+  std::vector<int> h_grp_plan;  // plan of each group
+  DBuf<double> resid_part, rho_part;
+  size_t smem_plan = 0, smem_plan_upd = 0;
+  int use_tma = 1;  // persistent TMA-pipelined kernel for single-CTA items (D2G_PLAN_KERNEL=v1 turns it off)
+
+  // ---- plain form
+  DBuf<double> pC, pX, pY, pZ, pZ0, pw, psupp, pvocab, pdist, pzr, pxmom;
+  DBuf<int> psym, pcol_inst, pp_str, plabel;
+  DBuf<long long> pcum;
+
+  // ---- graph cache (valid while every buffer and value it captured is unchanged)
+  cudaGraphExec_t gexec = nullptr;
+  int g_maxIters = -1, g_upl = -1;
+  std::vector<unsigned long long> g_sig;
+  long long g_launches = 0;  // kernels in the captured loop
+
+  // ---- last run
+  d2g_run_stats stats{};
+  std::vector<double> h_trace;
+  int ntrace = 0;
+  bool plans_valid = false;  // device Z holds plans from an earlier call / set_plans
+
+  ~d2g_phase() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (st) cudaStreamDestroy(st);
+  }
+};
+
+namespace d2g {
+
+static bool batched_supported(const d2g_phase_desc *d, std::string *why) {
+  if (d->str > 256) {
+    *why = "str > 256";
+    return false;
+  }
+  if (d->metric_type == D2_EUCLIDEAN_L2) {
+    if (d->dim < 1 || d->dim > 8) {
+      *why = "Euclidean dim outside 1..8";
+      return false;
+    }
+    return true;
+  }
+  if (d->metric_type == D2_HISTOGRAM || d->metric_type == D2_SPARSE_HISTOGRAM) return true;
+  *why = "metric type";
+  return false;
+}
+
+// ------------------------------------------------------------------ packing
+// Best-fit-decreasing packing of plans (in S-column groups) into items of G
+// groups; plans needing more than G groups get a cluster of 2/4/8 CTAs.
+static int build_packing(d2g_phase *ph) {
+  const int G = ph->geo.G;
+  const size_t n = ph->size;
+  std::vector<int> ng(n), csz(n);
+  for (size_t i = 0; i < n; ++i) {
+    ng[i] = (ph->p_str[i] + kS - 1) / kS;
+    int c = (ng[i] + G - 1) / G;
+    c = next_pow2(c);
+    if (c > kMaxCluster) return fail(D2G_E_UNSUPPORTED, "instance support size exceeds 8 CTAs");
+    csz[i] = c;
+  }
+  std::vector<int> order;
+  order.reserve(n);
+  for (size_t i = 0; i < n; ++i)
+    if (csz[i] == 1) order.push_back((int)i);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return ng[a] > ng[b]; });
+  std::vector<std::vector<int>> items;
+  std::vector<std::vector<int>> open(G + 1);
+  for (int i : order) {
+    int it = -1, rem = -1;
+    for (int r = ng[i]; r <= G; ++r)
+      if (!open[r].empty()) {
+        it = open[r].back();
+        open[r].pop_back();
+        rem = r;
+        break;
+      }
+    if (it < 0) {
+      it = (int)items.size();
+      items.emplace_back();
+      rem = G;
+    }
+    items[it].push_back(i);
+    rem -= ng[i];
+    if (rem > 0) open[rem].push_back(it);
+  }
+  // assign packed plan ids / groups
+  ph->plan_inst.clear();
+  ph->inst_plan.assign(n, -1);
+  ph->h_grp_rec.clear();
+  ph->h_grp_plan.clear();
+  std::vector<int> h_item_g0, h_item_ng, h_plan_g0, h_plan_ng, h_meta;
+  std::vector<long long> h_plan_cum;
+  ph->buckets.clear();
+  int g = 0, blocks = 0;
+  auto add_plan = [&](int i) {
+    const int p = (int)ph->plan_inst.size();
+    ph->plan_inst.push_back(i);
+    ph->inst_plan[i] = p;
+    h_plan_g0.push_back(g);
+    h_plan_ng.push_back(ng[i]);
+    h_plan_cum.push_back(ph->cum[i]);
+    for (int q = 0; q < ng[i]; ++q) {
+      const int nv = std::min(kS, ph->p_str[i] - q * kS);
+      h_meta.push_back((p << 4) | nv);
+      ph->h_grp_rec.push_back(make_int4(p, g, 0, (ng[i] << 4) | nv));
+      ph->h_grp_plan.push_back(p);
+    }
+    g += ng[i];
+  };
+  {
+    d2g_phase::Bucket b{1, (int)items.size(), 0, 0};
+    for (auto &itv : items) {
+      h_item_g0.push_back(g);
+      int tot = 0;
+      for (int i : itv) {
+        add_plan(i);
+        tot += ng[i];
+      }
+      h_item_ng.push_back(tot);
+    }
+    blocks += b.nitems;
+    ph->buckets.push_back(b);
+  }
+  for (int c = 2; c <= kMaxCluster; c <<= 1) {
+    d2g_phase::Bucket b{c, 0, (int)h_item_g0.size(), blocks};
+    for (size_t i = 0; i < n; ++i)
+      if (csz[i] == c) {
+        h_item_g0.push_back(g);
+        h_item_ng.push_back(ng[i]);
+        add_plan((int)i);
+        ++b.nitems;
+      }
+    blocks += b.nitems * c;
+    if (b.nitems) ph->buckets.push_back(b);
+  }
+  if (ph->buckets[0].nitems == 0) ph->buckets.erase(ph->buckets.begin());
+  ph->total_blocks = blocks;
+  ph->ngroups = g;
+  ph->nplans = (int)n;
+  ph->ncols_packed = (long long)g * kS;
+  if (ph->ncols_packed * ph->MP > (1LL << 40)) return fail(D2G_E_UNSUPPORTED, "phase too large");
+
+  D2G_CUDA(ph->grp_meta.alloc(h_meta.size()));
+  D2G_CUDA(ph->plan_g0.alloc(n));
+  D2G_CUDA(ph->plan_ng.alloc(n));
+  D2G_CUDA(ph->plan_label.alloc(n));
+  D2G_CUDA(ph->plan_cum.alloc(n));
+  D2G_CUDA(ph->item_g0.alloc(h_item_g0.size()));
+  D2G_CUDA(ph->item_ng.alloc(h_item_ng.size()));
+  D2G_CUDA(cudaMemcpyAsync(ph->grp_meta.p, h_meta.data(), h_meta.size() * 4, cudaMemcpyHostToDevice, ph->st));
+  D2G_CUDA(cudaMemcpyAsync(ph->plan_g0.p, h_plan_g0.data(), n * 4, cudaMemcpyHostToDevice, ph->st));
+  D2G_CUDA(cudaMemcpyAsync(ph->plan_ng.p, h_plan_ng.data(), n * 4, cudaMemcpyHostToDevice, ph->st));
+  D2G_CUDA(cudaMemcpyAsync(ph->plan_cum.p, h_plan_cum.data(), n * 8, cudaMemcpyHostToDevice, ph->st));
+  D2G_CUDA(cudaMemcpyAsync(ph->item_g0.p, h_item_g0.data(), h_item_g0.size() * 4, cudaMemcpyHostToDevice, ph->st));
+  D2G_CUDA(cudaMemcpyAsync(ph->item_ng.p, h_item_ng.data(), h_item_ng.size() * 4, cudaMemcpyHostToDevice, ph->st));
+  D2G_CUDA(cudaStreamSynchronize(ph->st));
+  return D2G_OK;
+}
+
+static PlanArgs base_args(d2g_phase *ph) {
+  PlanArgs a{};
+  a.Z = ph->Z.p;
+  a.Y = ph->Y.p;
+  a.col_w = ph->col_w.p;
+  a.col_supp = ph->col_supp.p;
+  a.col_sym = ph->col_sym.p;
+  a.grp_meta = ph->grp_meta.p;
+  a.plan_g0 = ph->plan_g0.p;
+  a.plan_ng = ph->plan_ng.p;
+  a.plan_label = ph->plan_label.p;
+  a.cw32 = ph->cw32.p;
+  a.cs32 = ph->cs32.p;
+  a.ctab = ph->ctab.p;
+  a.ctab_lstride = 0;
+  a.rowsum_out = ph->rowsum.p;
+  a.xmom_out = ph->xmom.p;
+  a.X_out = ph->Xp.p;
+  a.resid_part = ph->resid_part.p;
+  a.ctl = ph->ctl.p;
+  a.m = ph->str;
+  a.dim = ph->metric == D2_EUCLIDEAN_L2 ? ph->dim : 0;
+  a.use_tma = ph->use_tma;
+  a.grp_rec = ph->grp_rec.p;
+  a.plan_slot = ph->plan_slot.p;
+  return a;
+}
+
+static PlanArgs bucket_args(d2g_phase *ph, const PlanArgs &base, const d2g_phase::Bucket &b) {
+  PlanArgs a = base;
+  a.item_g0 = ph->item_g0.p + b.item_off;
+  a.item_ng = ph->item_ng.p + b.item_off;
+  a.cs = b.cs;
+  a.resid_off = b.block_off;
+  return a;
+}
+
+// ---------------------------------------------------------- labels / lists
+static int set_labels_impl(d2g_phase *ph, const int *label) {
+  const size_t n = ph->size;
+  for (size_t i = 0; i < n; ++i)
+    if (label[i] < 0 || label[i] >= ph->K) return fail(D2G_E_INVAL, "label out of range");
+  ph->label.assign(label, label + n);
+  std::vector<int> cnt(ph->K + 1, 0);
+  for (size_t i = 0; i < n; ++i) ++cnt[label[i] + 1];
+  int maxc = 0;
+  for (int l = 0; l < ph->K; ++l) {
+    if (cnt[l + 1] == 0)
+      return fail(D2G_E_EMPTY_CLUSTER, "cluster " + std::to_string(l) + " has no instance");
+    maxc = std::max(maxc, cnt[l + 1]);
+  }
+  for (int l = 0; l < ph->K; ++l) cnt[l + 1] += cnt[l];
+  std::vector<int> pos(cnt.begin(), cnt.end() - 1), lists(n);
+  const bool batched = ph->path == 0;
+  for (size_t i = 0; i < n; ++i) lists[pos[label[i]]++] = batched ? ph->inst_plan[i] : (int)i;
+  D2G_CUDA(ph->cl_ptr.alloc(ph->K + 1));
+  D2G_CUDA(ph->cl_plans.alloc(n));
+  D2G_CUDA(cudaMemcpyAsync(ph->cl_ptr.p, cnt.data(), (ph->K + 1) * 4, cudaMemcpyHostToDevice, ph->st));
+  D2G_CUDA(cudaMemcpyAsync(ph->cl_plans.p, lists.data(), n * 4, cudaMemcpyHostToDevice, ph->st));
+  ph->nchunk = (maxc + ph->chunk - 1) / ph->chunk;
+  const int dimp = (ph->metric == D2_EUCLIDEAN_L2 || ph->metric == D2_WORD_EMBED) ? ph->dim : 0;
+  D2G_CUDA(ph->part.alloc((size_t)ph->K * (dimp + 2) * ph->nchunk * ph->str));
+  if (batched) {
+    std::vector<int> pl(n);
+    for (size_t p = 0; p < n; ++p) pl[p] = label[ph->plan_inst[p]];
+    D2G_CUDA(cudaMemcpyAsync(ph->plan_label.p, pl.data(), n * 4, cudaMemcpyHostToDevice, ph->st));
+    // slot of each plan: its position in the cluster-sorted order
+    std::vector<int> slot(n);
+    for (size_t q = 0; q < n; ++q) slot[lists[q]] = (int)q;
+    D2G_CUDA(ph->plan_slot.alloc(n));
+    D2G_CUDA(cudaMemcpyAsync(ph->plan_slot.p, slot.data(), n * 4, cudaMemcpyHostToDevice, ph->st));
+    // group records: {slot, plan's first group, label, groups << 4 | valid}
+    const std::vector<int> &gplan = ph->h_grp_plan;
+    for (size_t gi = 0; gi < ph->h_grp_rec.size(); ++gi) {
+      const int p = gplan[gi];
+      ph->h_grp_rec[gi].x = slot[p];
+      ph->h_grp_rec[gi].z = pl[p];
+    }
+    D2G_CUDA(ph->grp_rec.alloc(ph->h_grp_rec.size()));
+    D2G_CUDA(cudaMemcpyAsync(ph->grp_rec.p, ph->h_grp_rec.data(), ph->h_grp_rec.size() * sizeof(int4),
+                             cudaMemcpyHostToDevice, ph->st));
+  } else {
+    D2G_CUDA(cudaMemcpyAsync(ph->plabel.p, label, n * 4, cudaMemcpyHostToDevice, ph->st));
+  }
+  D2G_CUDA(cudaStreamSynchronize(ph->st));
+  return D2G_OK;
+}
+
+// ------------------------------------------------------------------ create
+// per-column data: reference layout -> staging -> packed FP32 (+ histogram cost table)
+static int upload_columns_batched(d2g_phase *ph, const d2g_phase_desc *d) {
+  const bool euc = ph->metric == D2_EUCLIDEAN_L2;
+  const size_t ns = ph->col * (size_t)(1 + (euc ? ph->dim : 0));
+  DBuf<double> tmp;
+  DBuf<int> tsym;
+  D2G_CUDA(tmp.alloc(ns));
+  D2G_CUDA(cudaMemcpyAsync(tmp.p, d->p_w, ph->col * 8, cudaMemcpyHostToDevice, ph->st));
+  if (euc)
+    D2G_CUDA(cudaMemcpyAsync(tmp.p + ph->col, d->p_supp, ph->col * ph->dim * 8, cudaMemcpyHostToDevice, ph->st));
+  if (ph->metric == D2_SPARSE_HISTOGRAM) {
+    D2G_CUDA(tsym.alloc(ph->col));
+    D2G_CUDA(cudaMemcpyAsync(tsym.p, d->p_supp_sym, ph->col * 4, cudaMemcpyHostToDevice, ph->st));
+  }
+  PlanArgs base = base_args(ph);
+  for (auto &b : ph->buckets) {
+    PlanArgs a = bucket_args(ph, base, b);
+    D2G_CUDA(launch_pack_columns(ph->MP, a, b.nitems, ph->plan_cum.p, tmp.p,
+                                 euc ? tmp.p + ph->col : nullptr, tsym.p, ph->col_w.p,
+                                 euc ? ph->col_supp.p : nullptr, euc ? nullptr : ph->col_sym.p,
+                                 ph->dim, ph->DS, ph->metric == D2_HISTOGRAM ? 1 : 0, ph->st));
+  }
+  if (!euc) {  // histogram cost table: row v = cost from bin v to every centroid bin
+    const int V = ph->vocab_size;
+    std::vector<float> t((size_t)V * ph->MP, 0.f);
+    for (int v = 0; v < V; ++v)
+      for (int k = 0; k < ph->str; ++k) t[(size_t)v * ph->MP + k] = (float)d->dist_mat[(size_t)v * V + k];
+    D2G_CUDA(ph->ctab.alloc(t.size()));
+    D2G_CUDA(cudaMemcpyAsync(ph->ctab.p, t.data(), t.size() * 4, cudaMemcpyHostToDevice, ph->st));
+    D2G_CUDA(cudaStreamSynchronize(ph->st));
+  }
+  D2G_CUDA(cudaStreamSynchronize(ph->st));
+  return D2G_OK;
+}
+
+static int create_batched(d2g_phase *ph, const d2g_phase_desc *d) {
+  ph->MP = std::max(4, next_pow2(ph->str));
+  ph->geo = geo_for(ph->MP);
+  if (ph->metric == D2_EUCLIDEAN_L2) {
+    ph->mode = ph->dim <= 4 ? COST_EUCLID4 : COST_EUCLID8;
+    ph->DS = ph->dim <= 4 ? 4 : 8;
+  } else {
+    ph->mode = COST_TABLE;
+    ph->DS = 4;
+  }
+  int rc = build_packing(ph);
+  if (rc) return rc;
+  const size_t nz = (size_t)ph->ncols_packed * ph->MP;
+  D2G_CUDA(ph->Z.alloc(nz));
+  D2G_CUDA(ph->Y.alloc(nz));
+  D2G_CUDA(cudaMemsetAsync(ph->Z.p, 0, nz * 4, ph->st));
+  D2G_CUDA(cudaMemsetAsync(ph->Y.p, 0, nz * 4, ph->st));
+  D2G_CUDA(ph->col_w.alloc(ph->ncols_packed));
+  const bool euc = ph->metric == D2_EUCLIDEAN_L2;
+  if (euc) D2G_CUDA(ph->col_supp.alloc((size_t)ph->ncols_packed * ph->DS));
+  else D2G_CUDA(ph->col_sym.alloc(ph->ncols_packed));
+  D2G_CUDA(ph->rowsum.alloc((size_t)ph->nplans * ph->MP));
+  if (euc) D2G_CUDA(ph->xmom.alloc((size_t)ph->nplans * (ph->dim + 1) * ph->MP));
+  D2G_CUDA(ph->cw32.alloc((size_t)ph->K * ph->MP));
+  if (euc) D2G_CUDA(ph->cs32.alloc((size_t)ph->K * ph->MP * ph->DS));
+  D2G_CUDA(ph->resid_part.alloc((size_t)ph->total_blocks * 4));
+  D2G_CUDA(ph->rho_part.alloc(ph->total_blocks));
+  D2G_CUDA(ph->reinit.alloc(ph->size));
+
+  int rc2 = upload_columns_batched(ph, d);
+  if (rc2) return rc2;
+  const char *pk = getenv("D2G_PLAN_KERNEL");
+  ph->use_tma = !(pk && std::string(pk) == "v1");
+  PlanArgs base = base_args(ph);
+  ph->smem_plan = plan_smem_bytes(ph->MP, 0, 1);
+  ph->smem_plan_upd = plan_smem_bytes(ph->MP, euc ? ph->dim : 0, 1);
+  // raise the shared-memory limits of the plan kernels before any stream capture
+  for (int cs = 1; cs <= 2; ++cs) {
+    PlanArgs a = base;
+    a.cs = cs;
+    for (int chk = 0; chk < 2; ++chk)
+      D2G_CUDA(launch_plan(ph->MP, ph->mode, chk, a, 0, ph->smem_plan_upd, ph->st));
+  }
+  return D2G_OK;
+}
+
+static int upload_columns_plain(d2g_phase *ph, const d2g_phase_desc *d) {
+  const size_t col = ph->col;
+  D2G_CUDA(ph->pw.alloc(col));
+  D2G_CUDA(cudaMemcpyAsync(ph->pw.p, d->p_w, col * 8, cudaMemcpyHostToDevice, ph->st));
+  const bool euc = ph->metric == D2_EUCLIDEAN_L2, emb = ph->metric == D2_WORD_EMBED;
+  if (euc) {
+    D2G_CUDA(ph->psupp.alloc(col * ph->dim));
+    D2G_CUDA(cudaMemcpyAsync(ph->psupp.p, d->p_supp, col * ph->dim * 8, cudaMemcpyHostToDevice, ph->st));
+  }
+  if (emb || ph->metric == D2_SPARSE_HISTOGRAM) {
+    D2G_CUDA(ph->psym.alloc(col));
+    D2G_CUDA(cudaMemcpyAsync(ph->psym.p, d->p_supp_sym, col * 4, cudaMemcpyHostToDevice, ph->st));
+  }
+  if (emb) {
+    D2G_CUDA(ph->pvocab.alloc((size_t)ph->vocab_size * ph->dim));
+    D2G_CUDA(cudaMemcpyAsync(ph->pvocab.p, d->vocab_vec, (size_t)ph->vocab_size * ph->dim * 8,
+                             cudaMemcpyHostToDevice, ph->st));
+  }
+  if (ph->metric == D2_HISTOGRAM || ph->metric == D2_SPARSE_HISTOGRAM) {
+    D2G_CUDA(ph->pdist.alloc((size_t)ph->vocab_size * ph->vocab_size));
+    D2G_CUDA(cudaMemcpyAsync(ph->pdist.p, d->dist_mat, (size_t)ph->vocab_size * ph->vocab_size * 8,
+                             cudaMemcpyHostToDevice, ph->st));
+  }
+  D2G_CUDA(cudaStreamSynchronize(ph->st));
+  return D2G_OK;
+}
+
+static int create_plain(d2g_phase *ph, const d2g_phase_desc *d) {
+  const size_t n = ph->size, col = ph->col, nent = (size_t)ph->str * col;
+  D2G_CUDA(ph->pC.alloc(nent));
+  D2G_CUDA(ph->pX.alloc(nent));
+  D2G_CUDA(ph->pY.alloc(nent));
+  D2G_CUDA(ph->pZ.alloc(nent));
+  D2G_CUDA(ph->pZ0.alloc(nent));
+  D2G_CUDA(cudaMemsetAsync(ph->pZ.p, 0, nent * 8, ph->st));
+  const bool euc = ph->metric == D2_EUCLIDEAN_L2, emb = ph->metric == D2_WORD_EMBED;
+  int rc = upload_columns_plain(ph, d);
+  if (rc) return rc;
+  std::vector<int> ci(col);
+  for (size_t i = 0; i < n; ++i)
+    for (int j = 0; j < ph->p_str[i]; ++j) ci[ph->cum[i] + j] = (int)i;
+  D2G_CUDA(ph->pcol_inst.alloc(col));
+  D2G_CUDA(cudaMemcpyAsync(ph->pcol_inst.p, ci.data(), col * 4, cudaMemcpyHostToDevice, ph->st));
+  D2G_CUDA(ph->pp_str.alloc(n));
+  D2G_CUDA(cudaMemcpyAsync(ph->pp_str.p, ph->p_str.data(), n * 4, cudaMemcpyHostToDevice, ph->st));
+  D2G_CUDA(ph->pcum.alloc(n));
+  D2G_CUDA(cudaMemcpyAsync(ph->pcum.p, ph->cum.data(), n * 8, cudaMemcpyHostToDevice, ph->st));
+  D2G_CUDA(ph->plabel.alloc(n));
+  D2G_CUDA(ph->pzr.alloc(n * ph->str));
+  if (euc || emb) D2G_CUDA(ph->pxmom.alloc(n * (ph->dim + 1) * ph->str));
+  D2G_CUDA(ph->reinit.alloc(n));
+  D2G_CUDA(ph->resid_part.alloc((size_t)plain_check_blocks((long long)nent) * 4));
+  D2G_CUDA(ph->rho_part.alloc(plain_check_blocks((long long)nent)));
+  D2G_CUDA(cudaStreamSynchronize(ph->st));
+  return D2G_OK;
+}
+
+static PlainArgs plain_args(d2g_phase *ph, int iter) {
+  PlainArgs a{};
+  a.C = ph->pC.p;
+  a.X = ph->pX.p;
+  a.Y = ph->pY.p;
+  a.Z = ph->pZ.p;
+  a.Z0 = ph->pZ0.p;
+  a.w = ph->pw.p;
+  a.supp = ph->psupp.p;
+  a.vocab = ph->pvocab.p;
+  a.dist = ph->pdist.p;
+  a.sym = ph->psym.p;
+  a.col_inst = ph->pcol_inst.p;
+  a.p_str = ph->pp_str.p;
+  a.label = ph->plabel.p;
+  a.cum = ph->pcum.p;
+  a.reinit = ph->reinit.p;
+  a.zr = ph->pzr.p;
+  a.xmom = ph->pxmom.p;
+  a.cw64 = ph->cw64.p;
+  a.cs64 = ph->cs64.p;
+  a.part = ph->resid_part.p;
+  a.ctl = ph->ctl.p;
+  a.col = (long long)ph->col;
+  a.nent = (long long)ph->col * ph->str;
+  a.size = (int)ph->size;
+  a.str = ph->str;
+  a.dim = ph->dim;
+  a.metric = ph->metric;
+  a.vocab_size = ph->vocab_size;
+  a.iter = iter;
+  return a;
+}
+
+static ClusterArgs cluster_args(d2g_phase *ph, int iter, bool moments) {
+  ClusterArgs c{};
+  const bool batched = ph->path == 0;
+  c.rowsum32 = batched ? ph->rowsum.p : nullptr;
+  c.rowsum64 = batched ? nullptr : ph->pzr.p;
+  c.xmom32 = batched ? ph->xmom.p : nullptr;
+  c.xmom64 = batched ? nullptr : ph->pxmom.p;
+  c.rstride = batched ? ph->MP : ph->str;
+  c.cl_ptr = ph->cl_ptr.p;
+  c.cl_plans = batched ? nullptr : ph->cl_plans.p;  // batched outputs are in slot order
+  c.K = ph->K;
+  c.m = ph->str;
+  c.dim = (ph->metric == D2_EUCLIDEAN_L2 || ph->metric == D2_WORD_EMBED) ? ph->dim : 0;
+  c.chunk = ph->chunk;
+  c.nchunk = ph->nchunk;
+  c.part = ph->part.p;
+  c.cw64 = ph->cw64.p;
+  c.cs64 = ph->cs64.p;
+  c.cw32 = batched ? ph->cw32.p : nullptr;
+  c.cs32 = batched ? ph->cs32.p : nullptr;
+  c.MP = batched ? ph->MP : ph->str;
+  c.DS = ph->DS;
+  c.ctl = ph->ctl.p;
+  c.iter = iter;
+  c.do_weights = 1;
+  c.do_moments = moments ? 1 : 0;
+  return c;
+}
+
+// Everything the captured loop bakes into kernel arguments.
+static std::vector<unsigned long long> loop_signature(d2g_phase *ph) {
+  auto u = [](const void *p) { return (unsigned long long)(uintptr_t)p; };
+  return {u(ph->part.p), u(ph->trace.p), u(ph->Xp.p), u(ph->cl_ptr.p), u(ph->cl_plans.p),
+          u(ph->cw64.p), u(ph->cs64.p), u(ph->ctl.p), u(ph->resid_part.p), u(ph->ctab.p),
+          u(ph->grp_rec.p), u(ph->plan_slot.p),
+          (unsigned long long)ph->nchunk, (unsigned long long)ph->chunk,
+          (unsigned long long)ph->global_size};
+}
+
+static bool has_collision(int maxIters, int upl) {
+  for (int it = 0; it <= maxIters; ++it)
+    if (it % upl == 0 && is_check_iter(it)) return true;
+  return false;
+}
+
+// ------------------------------------------------------------- the loop
+static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long long *launches,
+                        double *plan_ms, int *plan_timed) {
+  const bool euc = ph->metric == D2_EUCLIDEAN_L2, emb = ph->metric == D2_WORD_EMBED;
+  int chk_idx = 0;
+  long long nl = 0;
+  std::vector<cudaEvent_t> evs;
+  if (ph->path == 0) {
+    PlanArgs base = base_args(ph);
+    for (int it = 0; it <= maxIters; ++it) {
+      const bool upd = (it % upl == 0) && (euc || emb);
+      const bool chk = is_check_iter(it);
+      const bool collide = upd && chk;
+      int flags = (upd && euc ? PF_UPDATE : 0) | (chk ? PF_CHECK : 0) | (collide ? PF_WRITE_X : 0);
+      if (profile) {
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        evs.push_back(a);
+        evs.push_back(b);
+        cudaEventRecord(a, ph->st);
+      }
+      for (auto &b : ph->buckets) {
+        PlanArgs a = bucket_args(ph, base, b);
+        a.iter = it;
+        a.flags = flags;
+        D2G_CUDA(launch_plan(ph->MP, ph->mode, chk, a, b.nitems,
+                             (upd && euc) ? ph->smem_plan_upd : ph->smem_plan, ph->st));
+        ++nl;
+      }
+      if (profile) cudaEventRecord(evs.back(), ph->st);
+      D2G_CUDA(launch_cluster_reduce(cluster_args(ph, it, upd && euc), ph->st));
+      nl += 2;
+      if (collide) {
+        for (auto &b : ph->buckets) {
+          PlanArgs a = bucket_args(ph, base, b);
+          a.iter = it;
+          D2G_CUDA(launch_obj(ph->MP, ph->mode, a, b.nitems, ph->st));
+          ++nl;
+        }
+      }
+      if (chk) {
+        D2G_CUDA(launch_resid_final(ph->resid_part.p, ph->total_blocks, ph->ctl.p,
+                                    ph->trace.p + 4 * chk_idx, it, collide, ph->st));
+        ++nl;
+        ++chk_idx;
+      }
+    }
+  } else {
+    const unsigned nb = plain_check_blocks((long long)ph->col * ph->str);
+    for (int it = 0; it <= maxIters; ++it) {
+      const bool upd = (it % upl == 0) && (euc || emb);
+      const bool chk = is_check_iter(it);
+      PlainArgs a = plain_args(ph, it);
+      if (profile) {
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        evs.push_back(e0);
+        evs.push_back(e1);
+        cudaEventRecord(e0, ph->st);
+      }
+      D2G_CUDA(plain_iter_steps(a, upd, ph->st));
+      D2G_CUDA(launch_cluster_reduce(cluster_args(ph, it, upd), ph->st));
+      if (upd) D2G_CUDA(plain_cost(a, ph->st));
+      if (chk) {
+        D2G_CUDA(plain_check(a, ph->st));
+        D2G_CUDA(launch_resid_final(ph->resid_part.p, (int)nb, ph->ctl.p, ph->trace.p + 4 * chk_idx,
+                                    it, false, ph->st));
+        ++chk_idx;
+      }
+      if (profile) cudaEventRecord(evs.back(), ph->st);
+      nl += plain_launches_per_iter(upd, chk);
+    }
+  }
+  if (profile) {
+    D2G_CUDA(cudaStreamSynchronize(ph->st));
+    double tot = 0;
+    for (size_t i = 0; i + 1 < evs.size(); i += 2) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, evs[i], evs[i + 1]);
+      tot += ms;
+    }
+    *plan_ms = evs.empty() ? 0 : tot / (evs.size() / 2);
+    *plan_timed = (int)(evs.size() / 2);
+    for (auto e : evs) cudaEventDestroy(e);
+  }
+  *launches = nl;
+  return D2G_OK;
+}
+
+static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, double *c_supp,
+                    const char *label_switch) {
+  const d2g_config cfg = cfg_snapshot();
+  if (!opt || opt->maxIters < 0 || opt->updatePerLoops <= 0 || !(opt->rhoCoeff > 0) || !c_w)
+    return fail(D2G_E_INVAL, "bad B-ADMM options");
+  const bool euc = ph->metric == D2_EUCLIDEAN_L2, emb = ph->metric == D2_WORD_EMBED;
+  if ((euc || emb) && !c_supp) return fail(D2G_E_INVAL, "c_supp required for this metric");
+  const int K = ph->K, m = ph->str, dim = ph->dim;
+  const size_t n = ph->size;
+
+  // re-initialisation flags (per plan)
+  std::vector<char> re(n, 1);
+  bool any_warm = false;
+  if (label_switch)
+    for (size_t i = 0; i < n; ++i) {
+      const size_t p = ph->path == 0 ? (size_t)ph->inst_plan[i] : i;
+      re[p] = label_switch[i] == 1;
+      any_warm |= !re[p];
+    }
+  if (any_warm && !ph->plans_valid)
+    return fail(D2G_E_INVAL, "warm start requested but no plans were set");
+  D2G_CUDA(cudaMemcpyAsync(ph->reinit.p, re.data(), n, cudaMemcpyHostToDevice, ph->st));
+
+  // centroids and control block
+  D2G_CUDA(ph->cw64.alloc((size_t)K * m));
+  D2G_CUDA(cudaMemcpyAsync(ph->cw64.p, c_w, (size_t)K * m * 8, cudaMemcpyHostToDevice, ph->st));
+  if (euc || emb) {
+    D2G_CUDA(ph->cs64.alloc((size_t)K * m * dim));
+    D2G_CUDA(cudaMemcpyAsync(ph->cs64.p, c_supp, (size_t)K * m * dim * 8, cudaMemcpyHostToDevice, ph->st));
+  }
+  ph->max_checks = opt->maxIters / 20 + 8;
+  D2G_CUDA(ph->trace.alloc((size_t)4 * ph->max_checks));
+  D2G_CUDA(ph->ctl.alloc(1));
+  Ctl h{};
+  h.stop_iter = INT_MAX;
+  const double tb = opt->time_budget;
+  h.budget_ns = (tb > 0 && tb < 1.8e10) ? (unsigned long long)(tb * 1e9) : ~0ULL;
+  h.rho_coeff = opt->rhoCoeff;
+  h.global_size = (double)ph->global_size;
+  D2G_CUDA(cudaMemcpyAsync(ph->ctl.p, &h, sizeof h, cudaMemcpyHostToDevice, ph->st));
+
+  long long launches = 0;
+  if (ph->path == 0 && (euc || emb) && has_collision(opt->maxIters, opt->updatePerLoops))
+    D2G_CUDA(ph->Xp.alloc((size_t)ph->ncols_packed * ph->MP));  // X kept for obj after step 5
+  if (ph->path == 0) {
+    D2G_CUDA(launch_centroid_to_f32(ph->cw64.p, euc ? ph->cs64.p : nullptr, ph->cw32.p,
+                                    euc ? ph->cs32.p : nullptr, K, m, dim, ph->MP, ph->DS, ph->st));
+    PlanArgs base = base_args(ph);
+    for (auto &b : ph->buckets) {
+      PlanArgs a = bucket_args(ph, base, b);
+      D2G_CUDA(launch_rho_partial(ph->MP, ph->mode, a, b.nitems, ph->rho_part.p + b.block_off, ph->st));
+    }
+    D2G_CUDA(launch_rho_final(ph->rho_part.p, ph->total_blocks, ph->ctl.p, (double)ph->col * m, ph->st));
+    D2G_CUDA(cudaMemsetAsync(ph->Y.p, 0, (size_t)ph->ncols_packed * ph->MP * 4, ph->st));
+    for (auto &b : ph->buckets) {
+      PlanArgs a = bucket_args(ph, base, b);
+      D2G_CUDA(launch_pack_convert(ph->MP, 2, a, b.nitems, nullptr, ph->plan_cum.p, ph->reinit.p,
+                                   ph->cw64.p, m, ph->st));
+    }
+    launches += 2 + 2 * (long long)ph->buckets.size() + 1;
+  } else {
+    PlainArgs a = plain_args(ph, -1);
+    a.part = ph->rho_part.p;
+    D2G_CUDA(plain_cost(a, ph->st));
+    D2G_CUDA(plain_rho(a, ph->st));
+    D2G_CUDA(plain_init(a, ph->st));
+    launches += 5;
+  }
+
+  const bool profile = cfg.profile != 0;
+  double plan_ms = 0;
+  int plan_timed = 0;
+  long long nl = 0;
+  D2G_CUDA(cudaEventRecord(ph->ev0, ph->st));
+  if (profile || !cfg.use_graph) {
+    int rc = enqueue_loop(ph, opt->maxIters, opt->updatePerLoops, profile, &nl, &plan_ms, &plan_timed);
+    if (rc) return rc;
+  } else {
+    const std::vector<unsigned long long> sig = loop_signature(ph);
+    if (!ph->gexec || ph->g_maxIters != opt->maxIters || ph->g_upl != opt->updatePerLoops ||
+        ph->g_sig != sig) {
+      if (ph->gexec) cudaGraphExecDestroy(ph->gexec);
+      ph->gexec = nullptr;
+      cudaGraph_t g;
+      D2G_CUDA(cudaStreamBeginCapture(ph->st, cudaStreamCaptureModeThreadLocal));
+      int rc = enqueue_loop(ph, opt->maxIters, opt->updatePerLoops, false, &nl, &plan_ms, &plan_timed);
+      cudaError_t ce = cudaStreamEndCapture(ph->st, &g);
+      if (rc) return rc;
+      D2G_CUDA(ce);
+      D2G_CUDA(cudaGraphInstantiate(&ph->gexec, g, 0));
+      cudaGraphDestroy(g);
+      ph->g_maxIters = opt->maxIters;
+      ph->g_upl = opt->updatePerLoops;
+      ph->g_sig = sig;
+      ph->g_launches = nl;
+    }
+    nl = ph->g_launches;
+    D2G_CUDA(cudaGraphLaunch(ph->gexec, ph->st));
+  }
+  D2G_CUDA(cudaEventRecord(ph->ev1, ph->st));
+
+  // results
+  D2G_CUDA(cudaMemcpyAsync(c_w, ph->cw64.p, (size_t)K * m * 8, cudaMemcpyDeviceToHost, ph->st));
+  if (euc || emb)
+    D2G_CUDA(cudaMemcpyAsync(c_supp, ph->cs64.p, (size_t)K * m * dim * 8, cudaMemcpyDeviceToHost, ph->st));
+  ph->h_trace.assign((size_t)4 * ph->max_checks, 0.0);
+  D2G_CUDA(cudaMemcpyAsync(ph->h_trace.data(), ph->trace.p, ph->h_trace.size() * 8, cudaMemcpyDeviceToHost, ph->st));
+  D2G_CUDA(cudaMemcpyAsync(&h, ph->ctl.p, sizeof h, cudaMemcpyDeviceToHost, ph->st));
+  D2G_CUDA(cudaStreamSynchronize(ph->st));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ph->ev0, ph->ev1);
+  int nchk = 0;
+  for (int it = 0; it < h.iters_done; ++it) nchk += is_check_iter(it);
+  ph->ntrace = nchk;
+  ph->plans_valid = true;
+  ph->stats.iterations = h.iters_done;
+  ph->stats.rho = h.rho;
+  ph->stats.total_ms = ms;
+  ph->stats.plan_ms_avg = plan_ms;
+  ph->stats.plan_launches = plan_timed;
+  ph->stats.kernel_launches = launches + nl;
+  ph->stats.plan_entries = ph->col * m;
+  ph->stats.path = ph->path;
+  {
+    const double ent = (double)ph->col * m;
+    const double colb = ph->path == 0 ? (double)ph->col * (euc ? 4.0 * (1 + dim) : 8.0) : 0.0;
+    ph->stats.plan_bytes = ph->path == 0 ? 16.0 * ent + colb + 4.0 * m * (double)n : 136.0 * ent;
+  }
+  if (h.err) return fail(D2G_E_NUMERIC, "non-positive or non-finite normaliser (device code " +
+                                            std::to_string(h.err) + ")");
+  return D2G_OK;
+}
+
+
+// FP64 ground costs of every instance against its labelled centroid, the
+// reference layout; backs the calculate_distmat drop-in.
+int distmat_fp64(int dim, int str, size_t size, const int *p_str, int metric, const double *supp,
+                 const int *sym, const double *vocab, int V, const int *label, const double *c_supp,
+                 size_t K, double *C_host) {
+  if (dim < 1 || str < 1 || !p_str || !label || !c_supp || !C_host) return fail(D2G_E_INVAL, "distmat args");
+  std::vector<long long> cum(size);
+  long long col = 0;
+  for (size_t i = 0; i < size; ++i) {
+    if (label[i] < 0 || (size_t)label[i] >= K) return fail(D2G_E_INVAL, "label out of range");
+    cum[i] = col;
+    col += p_str[i];
+  }
+  std::vector<int> ci(col);
+  for (size_t i = 0; i < size; ++i)
+    for (int j = 0; j < p_str[i]; ++j) ci[cum[i] + j] = (int)i;
+  cudaStream_t st;
+  D2G_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  struct Guard {
+    cudaStream_t s;
+    ~Guard() { cudaStreamDestroy(s); }
+  } guard{st};
+  DBuf<double> dC, dS, dV, dCS;
+  DBuf<int> dSym, dCI, dL;
+  DBuf<long long> dCum;
+  const size_t nent = (size_t)col * str;
+  D2G_CUDA(dC.alloc(nent));
+  D2G_CUDA(dCS.alloc(K * str * dim));
+  D2G_CUDA(cudaMemcpyAsync(dCS.p, c_supp, K * str * dim * 8, cudaMemcpyHostToDevice, st));
+  if (metric == D2_EUCLIDEAN_L2) {
+    D2G_CUDA(dS.alloc((size_t)col * dim));
+    D2G_CUDA(cudaMemcpyAsync(dS.p, supp, (size_t)col * dim * 8, cudaMemcpyHostToDevice, st));
+  } else {
+    D2G_CUDA(dSym.alloc(col));
+    D2G_CUDA(dV.alloc((size_t)V * dim));
+    D2G_CUDA(cudaMemcpyAsync(dSym.p, sym, col * 4, cudaMemcpyHostToDevice, st));
+    D2G_CUDA(cudaMemcpyAsync(dV.p, vocab, (size_t)V * dim * 8, cudaMemcpyHostToDevice, st));
+  }
+  D2G_CUDA(dCI.alloc(col));
+  D2G_CUDA(dL.alloc(size));
+  D2G_CUDA(dCum.alloc(size));
+  D2G_CUDA(cudaMemcpyAsync(dCI.p, ci.data(), col * 4, cudaMemcpyHostToDevice, st));
+  D2G_CUDA(cudaMemcpyAsync(dL.p, label, size * 4, cudaMemcpyHostToDevice, st));
+  D2G_CUDA(cudaMemcpyAsync(dCum.p, cum.data(), size * 8, cudaMemcpyHostToDevice, st));
+  PlainArgs a{};
+  a.C = dC.p;
+  a.supp = dS.p;
+  a.vocab = dV.p;
+  a.sym = dSym.p;
+  a.col_inst = dCI.p;
+  a.label = dL.p;
+  a.cum = dCum.p;
+  a.cs64 = dCS.p;
+  a.col = col;
+  a.nent = (long long)nent;
+  a.size = (int)size;
+  a.str = str;
+  a.dim = dim;
+  a.metric = metric;
+  a.vocab_size = V;
+  a.iter = -1;
+  D2G_CUDA(plain_cost(a, st));
+  D2G_CUDA(cudaMemcpyAsync(C_host, dC.p, nent * 8, cudaMemcpyDeviceToHost, st));
+  D2G_CUDA(cudaStreamSynchronize(st));
+  return D2G_OK;
+}
+
+}  // namespace d2g
+
+// =================================================================== C API
+extern "C" {
+
+int d2g_get_config(d2g_config *cfg) {
+  if (!cfg) return D2G_E_INVAL;
+  *cfg = cfg_snapshot();
+  return D2G_OK;
+}
+
+int d2g_set_config(const d2g_config *cfg) {
+  if (!cfg || cfg->precision < 0 || cfg->precision > 1) return D2G_E_INVAL;
+  std::lock_guard<std::mutex> lk(g_cfg_mu);
+  g_cfg = *cfg;
+  return D2G_OK;
+}
+
+const char *d2g_error_string(int code) {
+  switch (code) {
+    case D2G_OK: return "ok";
+    case D2G_E_INVAL: return "invalid argument";
+    case D2G_E_CUDA: return "CUDA error";
+    case D2G_E_NOMEM: return "out of memory";
+    case D2G_E_UNSUPPORTED: return "unsupported metric type or shape";
+    case D2G_E_EMPTY_CLUSTER: return "empty cluster";
+    case D2G_E_NUMERIC: return "non-positive or non-finite normaliser";
+    case D2G_E_ADMISSION: return "request refused by admission control";
+    case D2G_E_NOTFOUND: return "unknown ticket";
+    default: return "unknown error";
+  }
+}
+
+const char *d2g_last_error(void) { return d2g::g_last_error.c_str(); }
+
+int d2g_phase_create(const d2g_phase_desc *d, int precision, d2g_phase **out) {
+  if (!d || !out || d->size == 0 || d->str <= 0 || d->num_of_labels <= 0 || !d->p_str || !d->p_w ||
+      !d->label)
+    return fail(D2G_E_INVAL, "incomplete phase description");
+  const int mt = d->metric_type;
+  if (mt == D2_N_GRAM || mt == D2_CITYBLOCK_L1)
+    return fail(D2G_E_UNSUPPORTED, "metric type " + std::to_string(mt) + " is not supported");
+  if (mt != D2_EUCLIDEAN_L2 && mt != D2_WORD_EMBED && mt != D2_HISTOGRAM && mt != D2_SPARSE_HISTOGRAM)
+    return fail(D2G_E_INVAL, "unknown metric type");
+  if (mt == D2_EUCLIDEAN_L2 && (d->dim < 1 || !d->p_supp)) return fail(D2G_E_INVAL, "supports missing");
+  if (mt == D2_WORD_EMBED && (d->dim < 1 || !d->p_supp_sym || !d->vocab_vec || d->vocab_size < 1))
+    return fail(D2G_E_INVAL, "embedding phase needs ids and vocabulary");
+  if ((mt == D2_HISTOGRAM || mt == D2_SPARSE_HISTOGRAM) && (!d->dist_mat || d->vocab_size != d->str))
+    return fail(D2G_E_INVAL, "histogram phase needs a str x str cost matrix");
+  if (mt == D2_SPARSE_HISTOGRAM && !d->p_supp_sym) return fail(D2G_E_INVAL, "sparse histogram ids missing");
+  if (mt == D2_HISTOGRAM)  // the plan of a dense histogram indexes the cost by bin: m_i <= bins
+    for (size_t i = 0; i < d->size; ++i)
+      if (d->p_str[i] > d->vocab_size) return fail(D2G_E_INVAL, "histogram with more bins than the cost matrix");
+  if (d->str > 256) return fail(D2G_E_UNSUPPORTED, "str > 256");
+
+  d2g_phase *ph = new d2g_phase();
+  ph->metric = mt;
+  ph->dim = (mt == D2_EUCLIDEAN_L2 || mt == D2_WORD_EMBED) ? d->dim : 0;
+  ph->str = d->str;
+  ph->K = d->num_of_labels;
+  ph->vocab_size = d->vocab_size;
+  ph->size = d->size;
+  ph->global_size = d->global_size ? d->global_size : d->size;
+  ph->p_str.assign(d->p_str, d->p_str + d->size);
+  ph->cum.resize(d->size);
+  long long c = 0;
+  for (size_t i = 0; i < d->size; ++i) {
+    if (d->p_str[i] < 1) {
+      delete ph;
+      return fail(D2G_E_INVAL, "instance with no support point");
+    }
+    ph->cum[i] = c;
+    c += d->p_str[i];
+  }
+  ph->col = (size_t)c;
+  if (mt == D2_SPARSE_HISTOGRAM || mt == D2_WORD_EMBED)
+    for (size_t j = 0; j < ph->col; ++j)
+      if (d->p_supp_sym[j] < 0 || d->p_supp_sym[j] >= d->vocab_size) {
+        delete ph;
+        return fail(D2G_E_INVAL, "vocabulary id out of range");
+      }
+  std::string why;
+  ph->path = (precision == 1 || !batched_supported(d, &why)) ? 1 : 0;
+  int rc = D2G_OK;
+  if (cudaStreamCreateWithFlags(&ph->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&ph->ev0) != cudaSuccess || cudaEventCreate(&ph->ev1) != cudaSuccess) {
+    delete ph;
+    return fail(D2G_E_CUDA, "stream/event creation failed (no usable GPU?)");
+  }
+  rc = ph->path == 0 ? create_batched(ph, d) : D2G_E_UNSUPPORTED;
+  if (rc == D2G_E_UNSUPPORTED) {  // shapes the batched form does not pack: FP64 form
+    ph->path = 1;
+    rc = create_plain(ph, d);
+  }
+  if (!rc) rc = set_labels_impl(ph, d->label);
+  if (rc) {
+    delete ph;
+    return rc;
+  }
+  *out = ph;
+  return D2G_OK;
+}
+
+int d2g_phase_refresh(d2g_phase *ph, const d2g_phase_desc *d) {
+  if (!ph || !d || d->size != ph->size || d->str != ph->str || d->metric_type != ph->metric ||
+      d->num_of_labels != ph->K || !d->p_w || !d->label)
+    return fail(D2G_E_INVAL, "refresh needs the phase's own shape");
+  for (size_t i = 0; i < ph->size; ++i)
+    if (d->p_str[i] != ph->p_str[i]) return fail(D2G_E_INVAL, "support sizes changed");
+  int rc = ph->path == 0 ? upload_columns_batched(ph, d) : upload_columns_plain(ph, d);
+  if (rc) return rc;
+  ph->global_size = d->global_size ? d->global_size : d->size;
+  return set_labels_impl(ph, d->label);
+}
+
+int d2g_phase_destroy(d2g_phase *ph) {
+  if (!ph) return D2G_E_INVAL;
+  cudaStreamSynchronize(ph->st);
+  delete ph;
+  return D2G_OK;
+}
+
+int d2g_phase_set_labels(d2g_phase *ph, const int *label) {
+  if (!ph || !label) return D2G_E_INVAL;
+  return set_labels_impl(ph, label);
+}
+
+int d2g_phase_set_plans(d2g_phase *ph, const double *Z) {
+  if (!ph || !Z) return D2G_E_INVAL;
+  const size_t nent = ph->col * (size_t)ph->str;
+  if (ph->path == 1) {
+    D2G_CUDA(cudaMemcpyAsync(ph->pZ.p, Z, nent * 8, cudaMemcpyHostToDevice, ph->st));
+  } else {
+    D2G_CUDA(ph->stage.alloc(nent));
+    D2G_CUDA(cudaMemcpyAsync(ph->stage.p, Z, nent * 8, cudaMemcpyHostToDevice, ph->st));
+    PlanArgs base = base_args(ph);
+    for (auto &b : ph->buckets) {
+      PlanArgs a = bucket_args(ph, base, b);
+      D2G_CUDA(launch_pack_convert(ph->MP, 0, a, b.nitems, ph->stage.p, ph->plan_cum.p, nullptr,
+                                   nullptr, ph->str, ph->st));
+    }
+  }
+  D2G_CUDA(cudaStreamSynchronize(ph->st));
+  ph->plans_valid = true;
+  return D2G_OK;
+}
+
+static int unpack_to_host(d2g_phase *ph, float *packed, double *out, int dir = 1) {
+  const size_t nent = ph->col * (size_t)ph->str;
+  D2G_CUDA(ph->stage.alloc(nent));
+  PlanArgs base = base_args(ph);
+  base.Z = packed;
+  for (auto &b : ph->buckets) {
+    PlanArgs a = bucket_args(ph, base, b);
+    D2G_CUDA(launch_pack_convert(ph->MP, dir, a, b.nitems, ph->stage.p, ph->plan_cum.p, nullptr,
+                                 nullptr, ph->str, ph->st));
+  }
+  D2G_CUDA(cudaMemcpyAsync(out, ph->stage.p, nent * 8, cudaMemcpyDeviceToHost, ph->st));
+  D2G_CUDA(cudaStreamSynchronize(ph->st));
+  return D2G_OK;
+}
+
+int d2g_phase_get_plans(d2g_phase *ph, double *Z) {
+  if (!ph || !Z) return D2G_E_INVAL;
+  if (ph->path == 1) {
+    D2G_CUDA(cudaMemcpyAsync(Z, ph->pZ.p, ph->col * (size_t)ph->str * 8, cudaMemcpyDeviceToHost, ph->st));
+    D2G_CUDA(cudaStreamSynchronize(ph->st));
+    return D2G_OK;
+  }
+  return unpack_to_host(ph, ph->Z.p, Z);
+}
+
+int d2g_phase_get_scratch(d2g_phase *ph, double *X, double *Y, double *C) {
+  if (!ph) return D2G_E_INVAL;
+  const size_t nb = ph->col * (size_t)ph->str * 8;
+  if (ph->path == 1) {
+    if (X) D2G_CUDA(cudaMemcpyAsync(X, ph->pX.p, nb, cudaMemcpyDeviceToHost, ph->st));
+    if (Y) D2G_CUDA(cudaMemcpyAsync(Y, ph->pY.p, nb, cudaMemcpyDeviceToHost, ph->st));
+    if (C) D2G_CUDA(cudaMemcpyAsync(C, ph->pC.p, nb, cudaMemcpyDeviceToHost, ph->st));
+    D2G_CUDA(cudaStreamSynchronize(ph->st));
+    return D2G_OK;
+  }
+  if (X || C) return fail(D2G_E_UNSUPPORTED, "the batched form keeps neither X nor C");
+  if (Y) return unpack_to_host(ph, ph->Y.p, Y, 3);  // stored times log2(e)
+  return D2G_OK;
+}
+
+int d2g_badmm_run(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, double *c_supp,
+                  const char *label_switch) {
+  if (!ph) return D2G_E_INVAL;
+  return run_impl(ph, opt, c_w, c_supp, label_switch);
+}
+
+int d2g_phase_trace(d2g_phase *ph, double *trace, int cap, int *n) {
+  if (!ph || (!trace && cap > 0)) return D2G_E_INVAL;
+  const int k = std::min(cap, ph->ntrace);
+  for (int i = 0; i < 4 * k; ++i) trace[i] = ph->h_trace[i];
+  if (n) *n = ph->ntrace;
+  return D2G_OK;
+}
+
+void *d2g_phase_stream(d2g_phase *ph) { return ph ? (void *)ph->st : nullptr; }
+
+int d2g_phase_stats(d2g_phase *ph, d2g_run_stats *st) {
+  if (!ph || !st) return D2G_E_INVAL;
+  *st = ph->stats;
+  return D2G_OK;
+}
+
+}  // extern "C"

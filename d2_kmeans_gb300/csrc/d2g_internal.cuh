@@ -1,0 +1,175 @@
+// Internal declarations shared by the d2g CUDA translation units.
+//
+// Device layout of one phase in the batched (FP32-plan) form
+// --------------------------------------------------------------
+// Plans are stored "packed": the centroid support axis is padded to MP, a
+// power of two >= max(str, 4), and each plan (instance) is column-major
+// MP x m_i with its columns rounded up to whole groups of S columns.  Plans
+// are reordered so that the plans sharing one thread block ("item") are
+// contiguous; item sizes come from a best-fit-decreasing packing over the
+// per-instance column counts.  A plan larger than one block's columns spans a
+// thread-block cluster of 2, 4 or 8 CTAs and is an item on its own.
+//
+//   Z, Y        float [MP * ncols_packed]   transport plan and scaled dual
+//   col_w       float [ncols_packed]        instance weights (0 in pad columns)
+//   col_supp    float [ncols_packed * DS]   Euclidean supports (DS = 4 or 8)
+//   col_sym     int   [ncols_packed]        table row (bin / vocabulary id)
+//   grp_meta    int   [ngroups]             plan << 4 | valid columns (1..S)
+//   grp_rec     int4  [ngroups]             {plan, plan's first group, label,
+//                                            plan's groups << 4 | valid columns}
+//   plan_*      int   [nplans]              first group, group count, label,
+//                                           instance id, m_i
+//   rowsum      float [nplans * MP]         per-plan row sums of step 2, normalised
+//                                           to sum 1 (step 4's Zr), by cluster slot
+//   xmom        float [nplans * (dim+1) * MP]  per-plan X moments (step 5), by slot
+//
+// A plan's slot is its position in the cluster-sorted plan order (clusters in
+// label order, plans in instance order), so the cluster reductions read each
+// cluster's per-plan outputs as one contiguous run.
+//
+// Cluster-level state is FP64 (cw64 [k*str], cs64 [k*str*dim]) with FP32
+// copies padded to MP for the plan kernel (cw32 [k*MP], cs32 [k*MP*DS]).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/d2g.h"
+
+namespace d2g {
+
+constexpr int kS = 4;         // columns per thread (one column group)
+constexpr int kThreads = 256; // threads per plan-update CTA
+constexpr int kMaxCluster = 8;
+constexpr float kRoundoff = 1e-9f;  // ROUNDOFF, src/d2/centroid_Bregman.c:20
+
+enum CostMode { COST_EUCLID4 = 0, COST_EUCLID8 = 1, COST_TABLE = 2 };
+
+enum PlanFlags {
+  PF_UPDATE = 1,   // support-update iteration: emit X moments (Euclidean)
+  PF_WRITE_X = 2,  // store X (packed) for a later pass
+  PF_CHECK = 4,    // residual-check iteration
+};
+
+// Device control block, one per phase.  Everything an iteration reads that
+// changes between calls lives here, so a captured graph stays valid.
+struct Ctl {
+  double rho;
+  float inv_rho;
+  float inv_rho_l2;          // log2(e)/rho (the batched form works in base 2)
+  int stop_iter;             // first iteration that must not run
+  unsigned long long t_start_ns;
+  unsigned long long budget_ns;
+  int iters_done;
+  int err;                   // nonzero: numeric failure seen on device
+  double rho_coeff;
+  double global_size;
+};
+
+struct PlanArgs {
+  float *Z, *Y;
+  const float *col_w, *col_supp;
+  const int *col_sym;
+  const int *grp_meta, *plan_g0, *plan_ng, *plan_label;
+  const int *item_g0, *item_ng;
+  const float *cw32, *cs32;
+  const float *ctab;
+  long long ctab_lstride;   // floats between labels' tables (0: one shared table)
+  float *rowsum_out, *xmom_out, *X_out;
+  double *resid_part;       // 4 doubles per CTA (obj, primres, dualres, -)
+  Ctl *ctl;
+  int m, dim, flags, cs, iter, resid_off;
+  int use_tma;              // single-CTA items: persistent TMA-pipelined kernel
+  const int4 *grp_rec;      // per group {plan slot, plan first group, label, plan groups << 4 | valid}
+  const int *plan_slot;     // plan -> slot: position in cluster-sorted order (row-sum outputs)
+};
+
+// per-MP launch geometry
+struct Geo {
+  int MP, RPT, TPC, G, JC;
+};
+Geo geo_for(int MP);
+
+// kernels_plan.cu
+cudaError_t launch_plan(int MP, int mode, bool check, const PlanArgs &a, int nitems,
+                        size_t smem, cudaStream_t st);
+size_t plan_smem_bytes(int MP, int dim, int cs);
+cudaError_t launch_rho_partial(int MP, int mode, const PlanArgs &a, int nitems, double *part,
+                               cudaStream_t st);
+cudaError_t launch_pack_convert(int MP, int dir, const PlanArgs &a, int nitems,
+                                double *ref, const long long *plan_refcol,
+                                const char *plan_reinit, const double *cw64, int str,
+                                cudaStream_t st);
+cudaError_t launch_pack_columns(int MP, const PlanArgs &a, int nitems, const long long *plan_refcol,
+                                const double *w_ref, const double *supp_ref, const int *sym_ref,
+                                float *col_w, float *col_supp, int *col_sym, int dim, int DS,
+                                int dense_hist, cudaStream_t st);
+cudaError_t launch_obj(int MP, int mode, const PlanArgs &a, int nitems, cudaStream_t st);
+
+// kernels_reduce.cu
+struct ClusterArgs {
+  const float *rowsum32;     // batched: [nplans * MP]
+  const double *rowsum64;    // plain:   [nplans * str]
+  const float *xmom32;       // batched: [nplans * (dim+1) * MP]
+  const double *xmom64;      // plain:   [nplans * (dim+1) * str]
+  int rstride;               // row stride of rowsum / xmom planes (MP or str)
+  const int *cl_ptr, *cl_plans;  // cl_plans == nullptr: outputs already in slot order
+  int K, m, dim, chunk, nchunk;
+  double *part;              // [K][nplane][nchunk][m]
+  double *cw64, *cs64;
+  float *cw32, *cs32;
+  int MP, DS;
+  Ctl *ctl;
+  int iter;
+  int do_weights, do_moments;
+};
+cudaError_t launch_cluster_reduce(const ClusterArgs &a, cudaStream_t st);
+cudaError_t launch_rho_final(const double *part, int n, Ctl *ctl, double nent,
+                             cudaStream_t st);
+cudaError_t launch_resid_final(const double *part, int n, Ctl *ctl, double *trace_slot,
+                               int iter, bool obj_from_slot3, cudaStream_t st);
+cudaError_t launch_centroid_to_f32(const double *cw64, const double *cs64, float *cw32,
+                                   float *cs32, int K, int m, int dim, int MP, int DS,
+                                   cudaStream_t st);
+
+// kernels_plain.cu (FP64, reference layout)
+struct PlainArgs {
+  double *C, *X, *Y, *Z, *Z0;
+  const double *w, *supp, *vocab, *dist;
+  const int *sym, *col_inst, *p_str, *label;
+  const long long *cum;     // p_str_cum
+  const char *reinit;
+  double *zr;               // [size * str] row sums
+  double *xmom;             // [size * (dim+1) * str]
+  double *cw64, *cs64;
+  double *part;
+  Ctl *ctl;
+  long long col, nent;
+  int size, str, dim, metric, vocab_size, iter;
+};
+cudaError_t plain_cost(const PlainArgs &a, cudaStream_t st);
+cudaError_t plain_rho(const PlainArgs &a, cudaStream_t st);
+cudaError_t plain_init(const PlainArgs &a, cudaStream_t st);
+cudaError_t plain_iter_steps(const PlainArgs &a, bool update, cudaStream_t st);
+cudaError_t plain_check(const PlainArgs &a, cudaStream_t st);
+unsigned plain_check_blocks(long long nent);
+int plain_launches_per_iter(bool update, bool check);
+
+// d2g_host.cu
+int distmat_fp64(int dim, int str, size_t size, const int *p_str, int metric, const double *supp,
+                 const int *sym, const double *vocab, int V, const int *label, const double *c_supp,
+                 size_t K, double *C_host);
+
+// error helpers (d2g_host.cu)
+void set_error(const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+}  // namespace d2g
+
+#define D2G_CUDA(call)                                     \
+  do {                                                     \
+    cudaError_t e_ = (call);                               \
+    if (e_ != cudaSuccess) return d2g::cuda_fail(e_, #call); \
+  } while (0)

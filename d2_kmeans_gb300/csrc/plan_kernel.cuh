@@ -1,0 +1,1130 @@
+// Fused B-ADMM plan update (batched FP32 form).
+//
+// One pass over every transport plan per iteration, steps 1-3 of
+// src/d2/centroid_Bregman.c:155-175 plus the per-plan reductions that feed
+// steps 4-6:
+//
+//   T = Z * exp(-(C + Y)) + 1e-9              C computed in registers (Euclidean)
+//                                              or read from an L2-resident table
+//   X = T / colsum(T) * w_j                    column sums: in-thread + shuffles
+//   Z' = X * exp(Y) + 1e-9
+//   Z  = Z' * (c_w[label] / rowsum(Z'))        row sums: smem (+ DSMEM in a cluster)
+//   Y += X - Z
+//
+// Z and Y are read once and written once (16 B per plan entry, the HBM
+// roofline), with 128-bit streaming loads/stores.  X is never stored unless a
+// later pass needs it.  Per plan the kernel emits the row sums of Z' (step 4's
+// Zr), on support-update iterations the X moments sum_j X[k,j]*(1, s_j)
+// (step 5), and on check iterations per-CTA partials of <C,X>, |X-Z|, |Z-Z0|
+// (step 6).
+//
+// Thread mapping: a CTA of kThreads threads owns JC = G*S columns; TPC
+// threads share one column (RPT rows each, MP = TPC*RPT), each thread holds S
+// consecutive columns.  Plans start on S-column group boundaries, so a thread
+// never straddles two plans.
+#pragma once
+
+#include <cooperative_groups.h>
+
+#include "d2g_internal.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace d2g {
+
+template <int MP>
+struct GeoT {
+  static constexpr int RPT = MP >= 256 ? 8 : 4;
+  static constexpr int TPC = MP / RPT;
+  static constexpr int G = kThreads / TPC;
+  static constexpr int JC = G * kS;
+  static_assert(TPC >= 1 && TPC <= 32 && (32 % TPC) == 0, "TPC must divide a warp");
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// 2^x on the MUFU unit (PTX ex2.approx).  The plan update works in base 2:
+// exp(v) = 2^(v*log2(e)), with Y stored pre-multiplied by log2(e) and the
+// cost scale 1/rho folded into log2(e)/rho, so each exponential is one FMA and
+// one ex2.
+__device__ __forceinline__ float ex2f(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+constexpr float kLog2e = 1.4426950408889634f;  // log2(e)
+constexpr float kLn2 = 0.6931471805599453f;    // ln(2) = 1/log2(e)
+
+template <int TPC>
+__device__ __forceinline__ float seg_sum(float v) {
+#pragma unroll
+  for (int o = TPC / 2; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide fixed-order sum of 3 doubles; thread 0 gets the result.
+template <int NT>
+__device__ __forceinline__ void block_sum3(double v0, double v1, double v2, double *out) {
+  __shared__ double red[NT / 32][3];
+  v0 = warp_sum_d(v0);
+  v1 = warp_sum_d(v1);
+  v2 = warp_sum_d(v2);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    red[w][0] = v0;
+    red[w][1] = v1;
+    red[w][2] = v2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0, b = 0, c = 0;
+    for (int i = 0; i < NT / 32; ++i) {
+      a += red[i][0];
+      b += red[i][1];
+      c += red[i][2];
+    }
+    out[0] = a;
+    out[1] = b;
+    out[2] = c;
+  }
+}
+
+// Per-thread view of its S columns x RPT rows.
+template <int MP, int MODE>
+struct Tile {
+  using Gm = GeoT<MP>;
+  static constexpr int RPT = Gm::RPT, TPC = Gm::TPC, G = Gm::G, S = kS;
+  static constexpr bool EUC = MODE != COST_TABLE;
+  static constexpr int DS = MODE == COST_EUCLID8 ? 8 : 4;
+
+  int g, r, k0, rank, cta_g0, cta_ng, p, nvalid, pl_g0, pl_ng, lab;
+  bool active;
+  size_t colbase;
+  float sp[EUC ? S : 1][DS];      // column supports
+  float cc[EUC ? RPT : 1][DS];    // centroid supports of this thread's rows
+  int sym[S];
+  const float *tab;
+
+  __device__ __forceinline__ void init(const PlanArgs &a) {
+    const int item = blockIdx.x / a.cs;
+    init_at(a, item, blockIdx.x - item * a.cs);
+  }
+
+  __device__ __forceinline__ void init_at(const PlanArgs &a, int item, int rank_) {
+    const int tid = threadIdx.x;
+    g = tid / TPC;
+    r = tid % TPC;
+    k0 = r * RPT;
+    rank = rank_;
+    const int ig0 = a.item_g0[item], ing = a.item_ng[item];
+    cta_g0 = ig0 + rank * G;
+    cta_ng = min(G, ing - rank * G);
+    active = g < cta_ng;
+    const int gg = cta_g0 + g;
+    p = 0;
+    nvalid = 0;
+    pl_g0 = 0;
+    pl_ng = 0;
+    lab = 0;
+    if (active) {
+      const int meta = a.grp_meta[gg];
+      p = meta >> 4;
+      nvalid = meta & 15;
+      pl_g0 = a.plan_g0[p];
+      pl_ng = a.plan_ng[p];
+      lab = a.plan_label[p];
+    }
+    colbase = (size_t)gg * S;
+  }
+
+  // item-local view from a staged group record (persistent TMA kernel)
+  __device__ __forceinline__ void init_rec(int4 rec, int item_g0, int item_ng) {
+    const int tid = threadIdx.x;
+    g = tid / TPC;
+    r = tid % TPC;
+    k0 = r * RPT;
+    rank = 0;
+    cta_g0 = item_g0;
+    cta_ng = item_ng;
+    active = g < cta_ng;
+    p = 0;
+    nvalid = 0;
+    pl_g0 = 0;
+    pl_ng = 0;
+    lab = 0;
+    if (active) {
+      p = rec.x;
+      pl_g0 = rec.y;
+      lab = rec.z;
+      pl_ng = rec.w >> 4;
+      nvalid = rec.w & 15;
+    }
+    colbase = (size_t)(item_g0 + g) * S;
+  }
+
+  // costs from staged column data: supports sp_sm [JC][DS] or table rows sym_sm [JC]
+  __device__ __forceinline__ void load_costs_staged(const PlanArgs &a, const float *sp_sm,
+                                                    const int *sym_sm) {
+    const int lc = g * S;
+    if constexpr (EUC) {
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+#pragma unroll
+        for (int t4 = 0; t4 < DS / 4; ++t4) {
+          float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (s < nvalid) v = *((const float4 *)(sp_sm + (lc + s) * DS) + t4);
+          sp[s][4 * t4 + 0] = v.x;
+          sp[s][4 * t4 + 1] = v.y;
+          sp[s][4 * t4 + 2] = v.z;
+          sp[s][4 * t4 + 3] = v.w;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+#pragma unroll
+        for (int t4 = 0; t4 < DS / 4; ++t4) {
+          const float4 v =
+              __ldg((const float4 *)(a.cs32 + ((size_t)lab * MP + k0 + q) * DS) + t4);
+          cc[q][4 * t4 + 0] = v.x;
+          cc[q][4 * t4 + 1] = v.y;
+          cc[q][4 * t4 + 2] = v.z;
+          cc[q][4 * t4 + 3] = v.w;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int s = 0; s < S; ++s) sym[s] = s < nvalid ? sym_sm[lc + s] : 0;
+      tab = a.ctab + (size_t)lab * a.ctab_lstride;
+    }
+  }
+
+  __device__ __forceinline__ void load_costs(const PlanArgs &a) {
+    if constexpr (EUC) {
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+#pragma unroll
+        for (int t4 = 0; t4 < DS / 4; ++t4) {
+          float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (s < nvalid) v = __ldg((const float4 *)(a.col_supp + (colbase + s) * DS) + t4);
+          sp[s][4 * t4 + 0] = v.x;
+          sp[s][4 * t4 + 1] = v.y;
+          sp[s][4 * t4 + 2] = v.z;
+          sp[s][4 * t4 + 3] = v.w;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+#pragma unroll
+        for (int t4 = 0; t4 < DS / 4; ++t4) {
+          const float4 v =
+              __ldg((const float4 *)(a.cs32 + ((size_t)lab * MP + k0 + q) * DS) + t4);
+          cc[q][4 * t4 + 0] = v.x;
+          cc[q][4 * t4 + 1] = v.y;
+          cc[q][4 * t4 + 2] = v.z;
+          cc[q][4 * t4 + 3] = v.w;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int s = 0; s < S; ++s) sym[s] = s < nvalid ? __ldg(a.col_sym + colbase + s) : 0;
+      tab = a.ctab + (size_t)lab * a.ctab_lstride;
+    }
+  }
+
+  // ground cost of column s for this thread's RPT rows (not divided by rho)
+  __device__ __forceinline__ void costs(int s, float (&c)[RPT]) const {
+    if constexpr (EUC) {
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        float acc = 0.f;
+#pragma unroll
+        for (int t = 0; t < DS; ++t) {
+          const float d = cc[q][t] - sp[s][t];
+          acc = fmaf(d, d, acc);
+        }
+        c[q] = acc;
+      }
+    } else {
+      const float *row = tab + (size_t)sym[s] * MP + k0;
+#pragma unroll
+      for (int q4 = 0; q4 < RPT / 4; ++q4) {
+        const float4 v = __ldg((const float4 *)row + q4);
+        c[4 * q4 + 0] = v.x;
+        c[4 * q4 + 1] = v.y;
+        c[4 * q4 + 2] = v.z;
+        c[4 * q4 + 3] = v.w;
+      }
+    }
+  }
+};
+
+template <int N>
+__device__ __forceinline__ void ld_rows(const float *p, float (&v)[N], bool ok) {
+#pragma unroll
+  for (int q4 = 0; q4 < N / 4; ++q4) {
+    float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (ok) t = __ldcs((const float4 *)p + q4);
+    v[4 * q4 + 0] = t.x;
+    v[4 * q4 + 1] = t.y;
+    v[4 * q4 + 2] = t.z;
+    v[4 * q4 + 3] = t.w;
+  }
+}
+
+// streaming (evict-first) 128-bit stores: global memory only
+template <int N>
+__device__ __forceinline__ void st_rows(float *p, const float (&v)[N]) {
+#pragma unroll
+  for (int q4 = 0; q4 < N / 4; ++q4)
+    __stcs((float4 *)p + q4, make_float4(v[4 * q4], v[4 * q4 + 1], v[4 * q4 + 2], v[4 * q4 + 3]));
+}
+
+// 128-bit stores to shared memory
+template <int N>
+__device__ __forceinline__ void st_rows_sm(float *p, const float (&v)[N]) {
+#pragma unroll
+  for (int q4 = 0; q4 < N / 4; ++q4)
+    ((float4 *)p)[q4] = make_float4(v[4 * q4], v[4 * q4 + 1], v[4 * q4 + 2], v[4 * q4 + 3]);
+}
+
+template <int MP, int MODE, bool CHECK>
+__global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2) plan_kernel(const PlanArgs a) {
+  using T = Tile<MP, MODE>;
+  constexpr int RPT = T::RPT, TPC = T::TPC, G = T::G, S = kS;
+  extern __shared__ __align__(16) float smem[];
+  float *sm_rs = smem;              // [G][MP] per-group row partials of Z'
+  float *sm_tot = sm_rs + G * MP;   // [MP] CTA partial row sums (cluster exchange)
+
+  if (a.iter >= a.ctl->stop_iter) return;  // time budget hit in an earlier iteration
+  if (a.iter == 0 && a.resid_off == 0 && blockIdx.x == 0 && threadIdx.x == 0)
+    a.ctl->t_start_ns = global_ns();
+
+  T t;
+  t.init(a);
+  const int m = a.m;
+  const float inv_rho = a.ctl->inv_rho;
+  const float ir2 = a.ctl->inv_rho_l2;  // Y is kept scaled by log2(e): base-2 exponents
+  const bool update = a.flags & PF_UPDATE;
+
+  float z[S][RPT], y[S][RPT], x[S][RPT];
+  float zold[CHECK ? S : 1][RPT];
+  float w[S];
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    const size_t off = (t.colbase + s) * MP + t.k0;
+    ld_rows(a.Z + off, z[s], s < t.nvalid);
+    ld_rows(a.Y + off, y[s], s < t.nvalid);
+    w[s] = s < t.nvalid ? __ldg(a.col_w + t.colbase + s) : 0.f;
+  }
+  t.load_costs(a);
+
+  // step 1: X = Z exp(-(C+Y)) + ROUNDOFF, column-normalised, times w_j
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    float c[RPT];
+    t.costs(s, c);
+    float csum = 0.f;
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+      const bool ok = s < t.nvalid && t.k0 + q < m;
+      const float v = ok ? fmaf(z[s][q], ex2f(-fmaf(c[q], ir2, y[s][q])), kRoundoff) : 0.f;
+      x[s][q] = v;
+      csum += v;
+    }
+    csum = seg_sum<TPC>(csum);
+    const float f = s < t.nvalid ? w[s] / csum : 0.f;
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) x[s][q] *= f;
+  }
+
+  // step 2 (first half): Z' = X exp(Y) + ROUNDOFF, row partials
+  float rp[RPT];
+#pragma unroll
+  for (int q = 0; q < RPT; ++q) rp[q] = 0.f;
+#pragma unroll
+  for (int s = 0; s < S; ++s)
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+      const bool ok = s < t.nvalid && t.k0 + q < m;
+      if constexpr (CHECK) zold[s][q] = z[s][q];
+      const float v = ok ? fmaf(x[s][q], ex2f(y[s][q]), kRoundoff) : 0.f;
+      z[s][q] = v;
+      rp[q] += v;
+    }
+  st_rows_sm(sm_rs + t.g * MP + t.k0, rp);
+
+  // step 5 inputs: per-group X moments sum_j X[k,j]*(s_j[0..dim), 1)
+  float *sm_mom = sm_tot + MP;             // [dim+1][G][MP]
+  float *sm_momx = sm_mom + (a.dim + 1) * G * MP;  // [dim+1][MP] cluster exchange
+  if constexpr (T::EUC) {
+    if (update) {
+      for (int d = 0; d <= a.dim; ++d) {
+        float mv[RPT];
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+          float acc = 0.f;
+#pragma unroll
+          for (int s = 0; s < S; ++s) {
+            float sv = 1.f;  // plane dim: the X row sum (denominator)
+            if (d < a.dim) {
+#pragma unroll
+              for (int tt = 0; tt < T::DS; ++tt)
+                if (tt == d) sv = t.sp[s][tt];
+            }
+            acc = fmaf(x[s][q], sv, acc);
+          }
+          mv[q] = acc;
+        }
+        st_rows_sm(sm_mom + (d * G + t.g) * MP + t.k0, mv);
+      }
+    }
+  }
+  __syncthreads();
+
+  // plan totals over this CTA's groups of the plan
+  int lo = 0, hi = 0;
+  if (t.active) {
+    lo = max(t.pl_g0, t.cta_g0) - t.cta_g0;
+    hi = min(t.pl_g0 + t.pl_ng, t.cta_g0 + t.cta_ng) - t.cta_g0;
+  }
+  float tot[RPT];
+#pragma unroll
+  for (int q = 0; q < RPT; ++q) tot[q] = 0.f;
+  for (int j = lo; j < hi; ++j) {
+    float v[RPT];
+#pragma unroll
+    for (int q4 = 0; q4 < RPT / 4; ++q4) {
+      const float4 u = *((const float4 *)(sm_rs + j * MP + t.k0) + q4);
+      v[4 * q4] = u.x;
+      v[4 * q4 + 1] = u.y;
+      v[4 * q4 + 2] = u.z;
+      v[4 * q4 + 3] = u.w;
+    }
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) tot[q] += v[q];
+  }
+  // the thread set that owns the plan's output rows: first group of the plan
+  const bool writer = t.active && (t.cta_g0 + t.g) == t.pl_g0;
+  const bool upd_euc = T::EUC && update;
+
+  if (a.cs > 1) {
+    // one plan spans the cluster: exchange CTA partials through DSMEM
+    cg::cluster_group cl = cg::this_cluster();
+    if (t.g == 0) {
+      st_rows_sm(sm_tot + t.k0, tot);
+      if (upd_euc) {
+        for (int d = 0; d <= a.dim; ++d) {
+          float mv[RPT];
+#pragma unroll
+          for (int q = 0; q < RPT; ++q) mv[q] = 0.f;
+          for (int j = lo; j < hi; ++j)
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) mv[q] += sm_mom[(d * G + j) * MP + t.k0 + q];
+          st_rows_sm(sm_momx + d * MP + t.k0, mv);
+        }
+      }
+    }
+    cl.sync();
+    float sum[RPT];
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) sum[q] = 0.f;
+    for (int rk = 0; rk < a.cs; ++rk) {
+      const float *rem = cl.map_shared_rank(sm_tot, rk);
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) sum[q] += rem[t.k0 + q];
+    }
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) tot[q] = sum[q];
+    if (upd_euc && writer) {
+      float *xo = a.xmom_out + (size_t)a.plan_slot[t.p] * (a.dim + 1) * MP;
+      for (int d = 0; d <= a.dim; ++d) {
+        float mv[RPT];
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) mv[q] = 0.f;
+        for (int rk = 0; rk < a.cs; ++rk) {
+          const float *rem = cl.map_shared_rank(sm_momx, rk);
+#pragma unroll
+          for (int q = 0; q < RPT; ++q) mv[q] += rem[d * MP + t.k0 + q];
+        }
+        st_rows(xo + d * MP + t.k0, mv);
+      }
+    }
+    cl.sync();  // no CTA leaves while a peer still reads its shared memory
+  } else if (upd_euc && writer) {
+    float *xo = a.xmom_out + (size_t)a.plan_slot[t.p] * (a.dim + 1) * MP;
+    for (int d = 0; d <= a.dim; ++d) {
+      float mv[RPT];
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) mv[q] = 0.f;
+      for (int j = lo; j < hi; ++j)
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) mv[q] += sm_mom[(d * G + j) * MP + t.k0 + q];
+      st_rows(xo + d * MP + t.k0, mv);
+    }
+  }
+  {  // step 4's per-instance normalisation of Zr (:180), by slot
+    float rs = 0.f;
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) rs += t.k0 + q < m ? tot[q] : 0.f;
+    rs = seg_sum<TPC>(rs);
+    if (writer) {
+      float zr[RPT];
+      const float inv = 1.f / rs;
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) zr[q] = tot[q] * inv;
+      st_rows(a.rowsum_out + (size_t)a.plan_slot[t.p] * MP + t.k0, zr);
+    }
+  }
+
+  // step 2 (second half) and step 3
+  float sc[RPT];
+#pragma unroll
+  for (int q = 0; q < RPT; ++q) {
+    const bool ok = t.active && t.k0 + q < m;
+    sc[q] = ok ? __ldg(a.cw32 + (size_t)t.lab * MP + t.k0 + q) / tot[q] : 0.f;
+  }
+  float s_obj = 0.f, s_pr = 0.f, s_dr = 0.f;
+  const bool write_x = a.flags & PF_WRITE_X;
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    if (s < t.nvalid) {
+      float zn[RPT], yn[RPT];
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        zn[q] = z[s][q] * sc[q];
+        yn[q] = fmaf(kLog2e, x[s][q] - zn[q], y[s][q]);
+      }
+      if constexpr (CHECK) {
+        float c[RPT];
+        t.costs(s, c);
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+          s_obj = fmaf(c[q] * inv_rho, x[s][q], s_obj);
+          s_pr += fabsf(x[s][q] - zn[q]);
+          s_dr += fabsf(zn[q] - zold[s][q]);
+        }
+      }
+      const size_t off = (t.colbase + s) * MP + t.k0;
+      st_rows(a.Z + off, zn);
+      st_rows(a.Y + off, yn);
+      if (write_x) st_rows(a.X_out + off, x[s]);
+    }
+  }
+  if constexpr (CHECK) {
+    block_sum3<kThreads>(s_obj, s_pr, s_dr, a.resid_part + (size_t)(a.resid_off + blockIdx.x) * 4);
+  }
+}
+
+// Sum of the initial ground costs (for rho), FP32 costs accumulated in FP64.
+template <int MP, int MODE>
+__global__ void __launch_bounds__(kThreads) rho_partial_kernel(const PlanArgs a, double *part) {
+  using T = Tile<MP, MODE>;
+  constexpr int RPT = T::RPT, S = kS;
+  T t;
+  t.init(a);
+  t.load_costs(a);
+  double acc = 0.0;
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    float c[RPT];
+    t.costs(s, c);
+#pragma unroll
+    for (int q = 0; q < RPT; ++q)
+      if (s < t.nvalid && t.k0 + q < a.m) acc += (double)c[q];
+  }
+  __shared__ double res[3];
+  block_sum3<kThreads>(acc, 0.0, 0.0, res);
+  if (threadIdx.x == 0) part[blockIdx.x] = res[0];
+}
+
+// Layout conversion between the packed FP32 plans and the reference layout
+// (FP64, column-major str x m_i per instance at str*p_str_cum[i]).
+//   dir 0: ref -> packed (a.Z), every plan
+//   dir 1: packed (a.Z) -> ref     (used for Z, Y and X by pointing a.Z there)
+//   dir 2: re-initialise the plans with reinit set to w_j * c_w[label]
+//          (src/d2/centroid_Bregman.c:116-124); other plans are left as they are
+//   dir 3: as dir 1, times ln(2) (Y is stored scaled by log2(e))
+template <int MP>
+__global__ void __launch_bounds__(kThreads) pack_convert_kernel(const PlanArgs a, int dir,
+                                                                double *ref,
+                                                                const long long *plan_refcol,
+                                                                const char *reinit,
+                                                                const double *cw64, int str) {
+  using T = Tile<MP, COST_TABLE>;
+  constexpr int RPT = T::RPT, S = kS;
+  T t;
+  t.init(a);
+  if (!t.active) return;
+  const long long base = plan_refcol[t.p] * str;  // plan_refcol holds p_str_cum (columns)
+  const int jj0 = (t.cta_g0 + t.g - t.pl_g0) * S;
+  if (dir == 2 && !reinit[t.p]) return;
+  for (int s = 0; s < t.nvalid; ++s) {
+    const size_t off = (t.colbase + s) * MP + t.k0;
+    const long long rc = base + (long long)(jj0 + s) * str;
+    float v[RPT];
+    if (dir == 0 || dir == 2) {
+      const double wj = (double)a.col_w[t.colbase + s];
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        const int k = t.k0 + q;
+        double val = 0.0;
+        if (k < str) val = dir == 2 ? wj * cw64[(size_t)t.lab * str + k] : ref[rc + k];
+        v[q] = (float)val;
+      }
+      st_rows(a.Z + off, v);
+    } else {
+      ld_rows(a.Z + off, v, true);
+      const double sc = dir == 3 ? (double)kLn2 : 1.0;
+#pragma unroll
+      for (int q = 0; q < RPT; ++q)
+        if (t.k0 + q < str) ref[rc + t.k0 + q] = (double)v[q] * sc;
+    }
+  }
+}
+
+
+// Scatter per-column data from the reference layout into the packed layout:
+// weights, Euclidean supports (padded to DS with zeros) and table rows (bin id
+// j for dense histograms, the vocabulary / bin id otherwise).  Pad columns get
+// zeros.
+template <int MP>
+__global__ void __launch_bounds__(kThreads) pack_columns_kernel(
+    const PlanArgs a, const long long *plan_cum, const double *w_ref, const double *supp_ref,
+    const int *sym_ref, float *col_w, float *col_supp, int *col_sym, int dim, int DS,
+    int dense_hist) {
+  using T = Tile<MP, COST_TABLE>;
+  T t;
+  t.init(a);
+  if (!t.active || t.r != 0) return;
+  const long long cum = plan_cum[t.p];
+  const int jj0 = (t.cta_g0 + t.g - t.pl_g0) * kS;
+  for (int s = 0; s < kS; ++s) {
+    const size_t pc = t.colbase + s;
+    const bool ok = s < t.nvalid;
+    const long long rc = cum + jj0 + s;
+    col_w[pc] = ok ? (float)w_ref[rc] : 0.f;
+    if (col_supp)
+      for (int d = 0; d < DS; ++d)
+        col_supp[pc * DS + d] = (ok && d < dim) ? (float)supp_ref[rc * dim + d] : 0.f;
+    if (col_sym) col_sym[pc] = ok ? (dense_hist ? jj0 + s : sym_ref[rc]) : 0;
+  }
+}
+
+// <C, X> with the cost of the current centroids over a stored X (packed):
+// the residual check of an iteration that also moved the supports (the
+// reference evaluates obj after step 5, :301).  Partial per CTA into slot 3.
+template <int MP, int MODE>
+__global__ void __launch_bounds__(kThreads) obj_kernel(const PlanArgs a) {
+  using T = Tile<MP, MODE>;
+  constexpr int RPT = T::RPT, S = kS;
+  if (a.iter >= a.ctl->stop_iter) return;
+  T t;
+  t.init(a);
+  t.load_costs(a);
+  const float inv_rho = a.ctl->inv_rho;
+  float acc = 0.f;
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    float c[RPT], x[RPT];
+    t.costs(s, c);
+    ld_rows(a.X_out + (t.colbase + s) * MP + t.k0, x, s < t.nvalid);
+#pragma unroll
+    for (int q = 0; q < RPT; ++q)
+      if (s < t.nvalid && t.k0 + q < a.m) acc = fmaf(c[q] * inv_rho, x[q], acc);
+  }
+  __shared__ double res[3];
+  block_sum3<kThreads>((double)acc, 0.0, 0.0, res);
+  if (threadIdx.x == 0) a.resid_part[(size_t)(a.resid_off + blockIdx.x) * 4 + 3] = res[0];
+}
+
+// ---------------------------------------------------------------------------
+// Persistent, TMA-pipelined form of the plan update for single-CTA items.
+//
+// Each CTA walks items blockIdx.x, +gridDim.x, ...  The item's Z and Y tiles
+// (contiguous in the packed layout) arrive in shared memory by bulk async copy
+// (cp.async.bulk + mbarrier transaction count) into one of two stages; the
+// copy of the next item is issued as soon as the current one has landed, so
+// HBM reads overlap the exp / normalisation work of the current item.  Results
+// go back with streaming 128-bit stores from registers.  Z and Y are read from
+// shared memory twice (step 1 and the final step 2/3), which keeps only X and
+// Z' in registers.
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *b, unsigned cnt) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(cnt) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes,
+                                          unsigned long long *b) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(b))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *b, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait (about one second of device time), so a lost copy reports an
+// error instead of hanging the GPU.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *b, unsigned parity) {
+  if (mbar_try_wait(b, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (;;) {
+    for (int i = 0; i < 64; ++i)
+      if (mbar_try_wait(b, parity)) return true;
+    if (global_ns() - t0 > 1000000000ull) return false;
+  }
+}
+
+template <int MP>
+__host__ __device__ constexpr int tma_tile_floats() {
+  return GeoT<MP>::G * kS * MP;
+}
+
+template <int MP, int MODE, bool CHECK, bool FULL>
+__global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
+    plan_kernel_tma(const PlanArgs a, int nitems) {
+  using T = Tile<MP, MODE>;
+  constexpr int RPT = T::RPT, TPC = T::TPC, G = T::G, S = kS;
+  constexpr int TILE = tma_tile_floats<MP>();
+  constexpr int JC = G * S;
+  constexpr int CW = T::EUC ? T::DS : 1;  // staged column data: supports or table row
+  extern __shared__ __align__(128) float smem[];
+  float *stZ = smem;                                  // [2][TILE]
+  float *stY = smem + 2 * TILE;                       // [2][TILE]
+  int4 *stR = (int4 *)(smem + 4 * TILE);              // [2][G] group records
+  float *stW = (float *)(stR + 2 * G);                // [2][JC] weights
+  float *stC = stW + 2 * JC;                          // [2][JC*CW] supports / table rows
+  float *sm_rs = stC + 2 * JC * CW;                   // [G][MP] row partials, then plan totals
+  float *sm_mom = sm_rs + G * MP;                     // [dim+1][G][MP]
+  __shared__ __align__(8) unsigned long long mbar[2];
+  __shared__ int sh_fail;
+  __shared__ int sh_g0[2], sh_ng[2];
+
+  if (a.iter >= a.ctl->stop_iter) return;
+  const int tid = threadIdx.x;
+  if (a.iter == 0 && a.resid_off == 0 && blockIdx.x == 0 && tid == 0) a.ctl->t_start_ns = global_ns();
+  // one stage = the item's Z and Y tiles, group records, weights and supports
+  auto issue = [&](int g0, int ng, int stg) {
+    const size_t off = (size_t)g0 * S * MP;
+    const unsigned bytes = (unsigned)ng * S * MP * 4u;
+    const unsigned rb = (unsigned)ng * 16u, wb = (unsigned)ng * S * 4u, cb = wb * CW;
+    mbar_expect_tx(&mbar[stg], 2u * bytes + rb + wb + cb);
+    bulk_load(stZ + stg * TILE, a.Z + off, bytes, &mbar[stg]);
+    bulk_load(stY + stg * TILE, a.Y + off, bytes, &mbar[stg]);
+    bulk_load(stR + stg * G, a.grp_rec + g0, rb, &mbar[stg]);
+    bulk_load(stW + stg * JC, a.col_w + (size_t)g0 * S, wb, &mbar[stg]);
+    if constexpr (T::EUC)
+      bulk_load(stC + stg * JC * CW, a.col_supp + (size_t)g0 * S * CW, cb, &mbar[stg]);
+    else
+      bulk_load(stC + stg * JC * CW, a.col_sym + (size_t)g0 * S, cb, &mbar[stg]);
+  };
+  // thread 0 keeps the bounds of the next item in registers, loaded one item early
+  int nx_g0 = 0, nx_ng = 0;
+  if (tid == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    sh_fail = 0;
+    mbar_fence_init();
+    if ((int)blockIdx.x < nitems) {
+      const int g0 = a.item_g0[blockIdx.x], ng = a.item_ng[blockIdx.x];
+      sh_g0[0] = g0;
+      sh_ng[0] = ng;
+      issue(g0, ng, 0);
+      const int nx = blockIdx.x + gridDim.x;
+      if (nx < nitems) {
+        nx_g0 = a.item_g0[nx];
+        nx_ng = a.item_ng[nx];
+      }
+    }
+  }
+  __syncthreads();
+
+  const int m = a.m;
+  const float inv_rho = a.ctl->inv_rho;    // for <C,X> (natural units)
+  const float ir2 = a.ctl->inv_rho_l2;     // log2(e)/rho: exponents in base 2
+  const bool update = a.flags & PF_UPDATE;
+  const bool write_x = a.flags & PF_WRITE_X;
+  double s_obj = 0.0, s_pr = 0.0, s_dr = 0.0;  // FP64 across items, FP32 within one item
+  int it = 0;
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x, ++it) {
+    const int stg = it & 1;
+    if (!mbar_wait(&mbar[stg], (it >> 1) & 1)) sh_fail = 1;
+    __syncthreads();
+    if (sh_fail) break;
+    const int cur_g0 = sh_g0[stg], cur_ng = sh_ng[stg];
+    if (tid == 0 && item + (int)gridDim.x < nitems) {
+      issue(nx_g0, nx_ng, stg ^ 1);
+      sh_g0[stg ^ 1] = nx_g0;
+      sh_ng[stg ^ 1] = nx_ng;
+      const int nx = item + 2 * (int)gridDim.x;
+      if (nx < nitems) {
+        nx_g0 = a.item_g0[nx];
+        nx_ng = a.item_ng[nx];
+      }
+    }
+
+    T t;
+    t.init_rec(stR[stg * G + (threadIdx.x / TPC)], cur_g0, cur_ng);
+    t.load_costs_staged(a, stC + stg * JC * CW, (const int *)(stC + stg * JC * CW));
+    const float *zs = stZ + stg * TILE, *ys = stY + stg * TILE;
+    const int lcol0 = t.g * S;  // the thread's first column within the item
+    float x[S][RPT], zp[S][RPT], w[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) w[s] = s < t.nvalid ? stW[stg * JC + lcol0 + s] : 0.f;
+
+    // step 1 and the first half of step 2 (Y is kept scaled by log2(e))
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      float c[RPT], z[RPT], y[RPT];
+      t.costs(s, c);
+#pragma unroll
+      for (int q4 = 0; q4 < RPT / 4; ++q4) {
+        const float4 zz = *((const float4 *)(zs + (lcol0 + s) * MP + t.k0) + q4);
+        const float4 yy = *((const float4 *)(ys + (lcol0 + s) * MP + t.k0) + q4);
+        z[4 * q4] = zz.x; z[4 * q4 + 1] = zz.y; z[4 * q4 + 2] = zz.z; z[4 * q4 + 3] = zz.w;
+        y[4 * q4] = yy.x; y[4 * q4 + 1] = yy.y; y[4 * q4 + 2] = yy.z; y[4 * q4 + 3] = yy.w;
+      }
+      const bool colok = s < t.nvalid;
+      float csum = 0.f;
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        const bool ok = colok && (FULL || t.k0 + q < m);
+        const float v = ok ? fmaf(z[q], ex2f(-fmaf(c[q], ir2, y[q])), kRoundoff) : 0.f;
+        x[s][q] = v;
+        csum += v;
+      }
+      csum = seg_sum<TPC>(csum);
+      const float f = colok ? w[s] / csum : 0.f;
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        const bool ok = colok && (FULL || t.k0 + q < m);
+        x[s][q] *= f;
+        zp[s][q] = ok ? fmaf(x[s][q], ex2f(y[q]), kRoundoff) : 0.f;
+      }
+    }
+    {
+      float rp[RPT];
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        rp[q] = 0.f;
+#pragma unroll
+        for (int s = 0; s < S; ++s) rp[q] += zp[s][q];
+      }
+      st_rows_sm(sm_rs + t.g * MP + t.k0, rp);
+    }
+    if constexpr (T::EUC) {
+      if (update) {
+        for (int d = 0; d <= a.dim; ++d) {
+          float mv[RPT];
+#pragma unroll
+          for (int q = 0; q < RPT; ++q) {
+            float acc = 0.f;
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+              float sv = 1.f;
+              if (d < a.dim) {
+#pragma unroll
+                for (int tt = 0; tt < T::DS; ++tt)
+                  if (tt == d) sv = t.sp[s][tt];
+              }
+              acc = fmaf(x[s][q], sv, acc);
+            }
+            mv[q] = acc;
+          }
+          st_rows_sm(sm_mom + (d * G + t.g) * MP + t.k0, mv);
+        }
+      }
+    }
+    __syncthreads();
+
+    // the plan's first group sums the plan's partials once and publishes the total
+    const int lo = t.active ? t.pl_g0 - t.cta_g0 : 0;
+    const bool writer = t.active && t.g == lo;
+    if (writer) {
+      float tot[RPT];
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) tot[q] = 0.f;
+      for (int j = lo; j < lo + t.pl_ng; ++j) {
+#pragma unroll
+        for (int q4 = 0; q4 < RPT / 4; ++q4) {
+          const float4 u = *((const float4 *)(sm_rs + j * MP + t.k0) + q4);
+          tot[4 * q4] += u.x;
+          tot[4 * q4 + 1] += u.y;
+          tot[4 * q4 + 2] += u.z;
+          tot[4 * q4 + 3] += u.w;
+        }
+      }
+      st_rows_sm(sm_rs + lo * MP + t.k0, tot);
+      if (T::EUC && update) {
+        float *xo = a.xmom_out + (size_t)t.p * (a.dim + 1) * MP;
+        for (int d = 0; d <= a.dim; ++d) {
+          float mv[RPT];
+#pragma unroll
+          for (int q = 0; q < RPT; ++q) mv[q] = 0.f;
+          for (int j = lo; j < lo + t.pl_ng; ++j)
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) mv[q] += sm_mom[(d * G + j) * MP + t.k0 + q];
+          st_rows(xo + d * MP + t.k0, mv);
+        }
+      }
+    }
+    __syncthreads();
+    float tot[RPT];
+#pragma unroll
+    for (int q4 = 0; q4 < RPT / 4; ++q4) {
+      const float4 u = *((const float4 *)(sm_rs + lo * MP + t.k0) + q4);
+      tot[4 * q4] = u.x;
+      tot[4 * q4 + 1] = u.y;
+      tot[4 * q4 + 2] = u.z;
+      tot[4 * q4 + 3] = u.w;
+    }
+    float rsum = 0.f;  // step 4's per-instance normalisation of Zr (:180); t.p is the slot here
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) rsum += (FULL || t.k0 + q < m) ? tot[q] : 0.f;
+    rsum = seg_sum<TPC>(rsum);
+    if (writer) {
+      float zr[RPT];
+      const float inv = 1.f / rsum;
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) zr[q] = tot[q] * inv;
+      st_rows(a.rowsum_out + (size_t)t.p * MP + t.k0, zr);
+    }
+
+    // second half of step 2, and step 3
+    float sc[RPT];
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+      const bool ok = t.active && (FULL || t.k0 + q < m);
+      sc[q] = ok ? __ldg(a.cw32 + (size_t)t.lab * MP + t.k0 + q) / tot[q] : 0.f;
+    }
+    float i_obj = 0.f, i_pr = 0.f, i_dr = 0.f;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      if (s < t.nvalid) {
+        float y[RPT], zn[RPT], yn[RPT];
+#pragma unroll
+        for (int q4 = 0; q4 < RPT / 4; ++q4) {
+          const float4 yy = *((const float4 *)(ys + (lcol0 + s) * MP + t.k0) + q4);
+          y[4 * q4] = yy.x; y[4 * q4 + 1] = yy.y; y[4 * q4 + 2] = yy.z; y[4 * q4 + 3] = yy.w;
+        }
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+          zn[q] = zp[s][q] * sc[q];
+          yn[q] = fmaf(kLog2e, x[s][q] - zn[q], y[q]);
+        }
+        if constexpr (CHECK) {
+          float c[RPT], z0[RPT];
+          t.costs(s, c);
+#pragma unroll
+          for (int q4 = 0; q4 < RPT / 4; ++q4) {
+            const float4 zz = *((const float4 *)(zs + (lcol0 + s) * MP + t.k0) + q4);
+            z0[4 * q4] = zz.x; z0[4 * q4 + 1] = zz.y; z0[4 * q4 + 2] = zz.z; z0[4 * q4 + 3] = zz.w;
+          }
+#pragma unroll
+          for (int q = 0; q < RPT; ++q) {
+            i_obj = fmaf(c[q] * inv_rho, x[s][q], i_obj);
+            i_pr += fabsf(x[s][q] - zn[q]);
+            i_dr += fabsf(zn[q] - z0[q]);
+          }
+        }
+        const size_t off = (t.colbase + s) * MP + t.k0;
+        st_rows(a.Z + off, zn);
+        st_rows(a.Y + off, yn);
+        if (write_x) st_rows(a.X_out + off, x[s]);
+      }
+    }
+    if constexpr (CHECK) {
+      s_obj += i_obj;
+      s_pr += i_pr;
+      s_dr += i_dr;
+    }
+    __syncthreads();  // the stage and the row partials are free again
+  }
+  if (sh_fail) {
+    if (tid == 0) {
+      a.ctl->err = 7;  // a bulk copy did not complete: let the copies in flight land first
+      mbar_wait(&mbar[0], 0);
+      mbar_wait(&mbar[1], 0);
+    }
+    return;
+  }
+  if constexpr (CHECK) {
+    // one partial per CTA in the slot of its first item; its other items' slots get zeros
+    __shared__ double res[3];
+    block_sum3<kThreads>(s_obj, s_pr, s_dr, res);
+    if (tid == 0) {
+      double *pp = a.resid_part + (size_t)(a.resid_off + blockIdx.x) * 4;
+      pp[0] = res[0];
+      pp[1] = res[1];
+      pp[2] = res[2];
+      for (int item = blockIdx.x + gridDim.x; item < nitems; item += gridDim.x) {
+        double *qq = a.resid_part + (size_t)(a.resid_off + item) * 4;
+        qq[0] = qq[1] = qq[2] = 0.0;
+      }
+    }
+  }
+}
+
+static inline cudaLaunchConfig_t plan_cfg(int nblocks, size_t smem, cudaStream_t st,
+                                          cudaLaunchAttribute *attr, int cs) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nblocks, 1, 1);
+  cfg.blockDim = dim3(kThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  if (cs > 1) {
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+  }
+  return cfg;
+}
+
+template <int MP, int MODE, bool CHECK, bool FULL>
+cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaStream_t st) {
+  static int grid = 0;  // CTAs resident at once (persistent grid)
+  constexpr int JC = GeoT<MP>::G * kS;
+  constexpr int CW = MODE == COST_EUCLID8 ? 8 : (MODE == COST_EUCLID4 ? 4 : 1);
+  const size_t sm = smem + (size_t)4 * tma_tile_floats<MP>() * sizeof(float) +
+                    2 * (size_t)GeoT<MP>::G * 16 + 2 * (size_t)JC * 4 * (1 + CW);
+  static size_t configured_smem = 0;
+  if (configured_smem < sm) {
+    cudaError_t e = cudaFuncSetAttribute(plan_kernel_tma<MP, MODE, CHECK, FULL>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    int dev = 0, nsm = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, plan_kernel_tma<MP, MODE, CHECK, FULL>,
+                                                      kThreads, sm);
+    if (e != cudaSuccess) return e;
+    grid = nsm * (per > 0 ? per : 1);
+    configured_smem = sm;
+  }
+  if (nitems <= 0) return cudaSuccess;
+  const int g = nitems < grid ? nitems : grid;
+  plan_kernel_tma<MP, MODE, CHECK, FULL><<<g, kThreads, sm, st>>>(a, nitems);
+  return cudaGetLastError();
+}
+
+template <int MP, int MODE, bool CHECK>
+cudaError_t launch_plan_t(const PlanArgs &a, int nitems, size_t smem, cudaStream_t st) {
+  if (a.cs == 1 && a.use_tma) {
+    if (a.m == MP) return launch_plan_tma_t<MP, MODE, CHECK, true>(a, nitems, smem, st);
+    return launch_plan_tma_t<MP, MODE, CHECK, false>(a, nitems, smem, st);
+  }
+  // the dynamic shared-memory limit is raised once per kernel, before any
+  // stream capture (launch_plan is first called with nitems == 0 for that)
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(plan_kernel<MP, MODE, CHECK>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  if (nitems <= 0) return cudaSuccess;
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = plan_cfg(nitems * a.cs, smem, st, attr, a.cs);
+  return cudaLaunchKernelEx(&cfg, plan_kernel<MP, MODE, CHECK>, a);
+}
+
+template <int MP>
+cudaError_t launch_plan_mp(int mode, bool check, const PlanArgs &a, int nitems, size_t smem,
+                           cudaStream_t st) {
+  if (mode == COST_EUCLID4)
+    return check ? launch_plan_t<MP, COST_EUCLID4, true>(a, nitems, smem, st)
+                 : launch_plan_t<MP, COST_EUCLID4, false>(a, nitems, smem, st);
+  if (mode == COST_EUCLID8)
+    return check ? launch_plan_t<MP, COST_EUCLID8, true>(a, nitems, smem, st)
+                 : launch_plan_t<MP, COST_EUCLID8, false>(a, nitems, smem, st);
+  return check ? launch_plan_t<MP, COST_TABLE, true>(a, nitems, smem, st)
+               : launch_plan_t<MP, COST_TABLE, false>(a, nitems, smem, st);
+}
+
+template <int MP>
+cudaError_t launch_rho_mp(int mode, const PlanArgs &a, int nitems, double *part, cudaStream_t st) {
+  const dim3 grid(nitems * a.cs), block(kThreads);
+  if (mode == COST_EUCLID4)
+    rho_partial_kernel<MP, COST_EUCLID4><<<grid, block, 0, st>>>(a, part);
+  else if (mode == COST_EUCLID8)
+    rho_partial_kernel<MP, COST_EUCLID8><<<grid, block, 0, st>>>(a, part);
+  else
+    rho_partial_kernel<MP, COST_TABLE><<<grid, block, 0, st>>>(a, part);
+  return cudaGetLastError();
+}
+
+template <int MP>
+cudaError_t launch_convert_mp(int dir, const PlanArgs &a, int nitems, double *ref,
+                              const long long *plan_refcol, const char *reinit,
+                              const double *cw64, int str, cudaStream_t st) {
+  pack_convert_kernel<MP><<<nitems * a.cs, kThreads, 0, st>>>(a, dir, ref, plan_refcol, reinit,
+                                                              cw64, str);
+  return cudaGetLastError();
+}
+
+template <int MP>
+cudaError_t launch_pack_columns_mp(const PlanArgs &a, int nitems, const long long *plan_cum,
+                                   const double *w_ref, const double *supp_ref, const int *sym_ref,
+                                   float *col_w, float *col_supp, int *col_sym, int dim, int DS,
+                                   int dense_hist, cudaStream_t st) {
+  pack_columns_kernel<MP><<<nitems * a.cs, kThreads, 0, st>>>(a, plan_cum, w_ref, supp_ref, sym_ref,
+                                                              col_w, col_supp, col_sym, dim, DS,
+                                                              dense_hist);
+  return cudaGetLastError();
+}
+
+template <int MP>
+cudaError_t launch_obj_mp(int mode, const PlanArgs &a, int nitems, cudaStream_t st) {
+  if (mode == COST_EUCLID4)
+    obj_kernel<MP, COST_EUCLID4><<<nitems * a.cs, kThreads, 0, st>>>(a);
+  else if (mode == COST_EUCLID8)
+    obj_kernel<MP, COST_EUCLID8><<<nitems * a.cs, kThreads, 0, st>>>(a);
+  else
+    obj_kernel<MP, COST_TABLE><<<nitems * a.cs, kThreads, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+#define D2G_INSTANTIATE_MP(MPV)                                                                \
+  template cudaError_t launch_plan_mp<MPV>(int, bool, const PlanArgs &, int, size_t,           \
+                                           cudaStream_t);                                      \
+  template cudaError_t launch_rho_mp<MPV>(int, const PlanArgs &, int, double *, cudaStream_t); \
+  template cudaError_t launch_convert_mp<MPV>(int, const PlanArgs &, int, double *,            \
+                                              const long long *, const char *, const double *, \
+                                              int, cudaStream_t);                          \
+  template cudaError_t launch_pack_columns_mp<MPV>(const PlanArgs &, int, const long long *,   \
+                                                   const double *, const double *, const int *, \
+                                                   float *, float *, int *, int, int, int,      \
+                                                   cudaStream_t);                               \
+  template cudaError_t launch_obj_mp<MPV>(int, const PlanArgs &, int, cudaStream_t);
+
+}  // namespace d2g

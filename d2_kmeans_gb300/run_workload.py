@@ -1,0 +1,42 @@
+"""Run one B-ADMM centroid update on a seeded synthetic workload.
+
+    python -m d2_kmeans_gb300.run_workload --workload batched --scale 0.1 --iters 3
+
+Workloads (d2_kmeans_gb300.synth.workload): plain, batched, hist,
+twophase_euclid, embed.  --scale shrinks the number of instances only;
+--iters sets maxIters (the loop runs maxIters+1 iterations); --precision 1
+selects the FP64 form.  Prints the run statistics as one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+from . import badmm, synth
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="batched")
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--iters", type=int, default=None)
+    ap.add_argument("--precision", type=int, default=0)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--repeat", type=int, default=1)
+    args = ap.parse_args(argv)
+    badmm.set_config(verbose=0)
+    ph, c, opts = synth.workload(args.workload, seed=args.seed, scale=args.scale)
+    if args.iters is not None:
+        opts = dict(opts, maxIters=args.iters)
+    P = badmm.Phase(ph, args.precision)
+    for _ in range(args.repeat):
+        r = P.run(c, opts)
+    st = P.stats()
+    P.close()
+    st["n"] = len(ph["p_str"])
+    st["obj_last"] = float(r["trace"][-1, 1]) if len(r["trace"]) else None
+    print(json.dumps(st))
+
+
+if __name__ == "__main__":
+    main()

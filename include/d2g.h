@@ -1,0 +1,266 @@
+/*
+ * d2g - GB300-native B-ADMM Wasserstein-barycenter centroid update for
+ * discrete-distribution (D2) clustering.  C ABI of libd2g.so.
+ *
+ * Two layers:
+ *
+ * 1. Drop-in entry points with the reference's own names, signatures and
+ *    data layout (bobye/d2_kmeans, include/d2/clustering.h).  A program built
+ *    against the reference links libd2g.so in place of
+ *    src/d2/centroid_Bregman.o (and src/d2/centroid_util.o) and its
+ *    d2_clustering() loop runs the centroid update on the GPU.
+ *
+ * 2. A resident API (d2g_phase_*, d2g_badmm_run) that keeps one phase's
+ *    supports, weights and transport plans in HBM across calls, and a
+ *    serving API (d2g_server_*) for fixed-centroid transport solves of
+ *    arriving query distributions.
+ *
+ * All entry points return 0 on success and a negative D2G_E* code on failure;
+ * none aborts the process (the reference assert()s instead).
+ */
+#ifndef D2G_H_
+#define D2G_H_
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ errors */
+#define D2G_OK 0
+#define D2G_E_INVAL (-1)         /* invalid argument or shape */
+#define D2G_E_CUDA (-2)          /* CUDA runtime / launch failure */
+#define D2G_E_NOMEM (-3)         /* device or pinned host allocation failed */
+#define D2G_E_UNSUPPORTED (-4)   /* metric type or shape this build does not run */
+#define D2G_E_EMPTY_CLUSTER (-5) /* a cluster has no instance (reference: assert, centroid_Bregman.c:144) */
+#define D2G_E_NUMERIC (-6)       /* non-positive or non-finite normaliser (reference: assert, blas_like64.c:131,148) */
+#define D2G_E_ADMISSION (-7)     /* serving: request refused by the HBM budget or queue bound */
+#define D2G_E_NOTFOUND (-8)      /* serving: unknown ticket */
+
+/* -------------------------------------------- reference data model (ABI) */
+/* Layout-identical to include/d2/clustering.h:14-200 and include/d2/param.h:4-8
+ * of the reference built with _D2_DOUBLE (SCALAR = double, the default of
+ * make.inc.Linux64:14).  Skipped when the reference header is already
+ * included, so reference code can include both. */
+#ifndef _D2_CLUSTERING_H_
+typedef struct {
+  int dim, str, max_str;
+  size_t col, max_col;
+  int *p_str;
+  size_t *p_str_cum;
+  double *p_w;
+  int metric_type;
+  double *p_supp;
+  int *p_supp_sym;
+  double *dist_mat;
+  int vocab_size;
+  double *vocab_vec;
+  char is_meta_allocated;
+} sph;
+
+typedef struct {
+  double *l, *u, *s, *c;
+  char *r;
+} trieq;
+
+typedef struct {
+  int s_ph;
+  size_t size;
+  size_t global_size;
+  int *label;
+  int num_of_labels;
+  sph *ph;
+} mph;
+
+typedef struct {
+  double *C;
+  double *X;
+  double *L;
+} var_sph;
+
+typedef struct {
+  double *X, *Z;
+  double *Y;
+  double *Xc, *Zr;
+} var_sphBregman;
+
+typedef struct {
+  int s_ph;
+  var_sph *g_var;
+  var_sphBregman *l_var_sphBregman;
+  char *label_switch;
+  trieq tr;
+} var_mph;
+#endif /* _D2_CLUSTERING_H_ */
+
+#ifndef _D2_PARAM_H_
+typedef struct {
+  int maxIters;
+  double rhoCoeff;
+  int updatePerLoops;
+} BADMM_options;
+#define D2_EUCLIDEAN_L2 (0)
+#define D2_CITYBLOCK_L1 (1)
+#define D2_HISTOGRAM (5)
+#define D2_N_GRAM (6)
+#define D2_WORD_EMBED (7)
+#define D2_SPARSE_HISTOGRAM (12)
+#endif /* _D2_PARAM_H_ */
+
+/* ------------------------------------------------- drop-in entry points */
+
+/* Replaces d2_allocate_work_sphBregman, src/d2/centroid_Bregman.c:26-35
+ * (declared include/d2/clustering.h:223-224).  Allocates the same host work
+ * buffers X, Z, Y (str*col), Xc (col) and Zr (str*size). */
+int d2_allocate_work_sphBregman(sph *ph, size_t size, var_sphBregman *var_phwork);
+
+/* Replaces d2_free_work_sphBregman, src/d2/centroid_Bregman.c:37-44
+ * (clustering.h:225).  Also releases the device state kept for this work
+ * object. */
+int d2_free_work_sphBregman(var_sphBregman *var_phwork);
+
+/* Replaces d2_centroid_sphBregman, src/d2/centroid_Bregman.c:51-325
+ * (clustering.h:226-230).  Same inputs (phase idx_ph of p_data, labels,
+ * label_switch, c0 as the warm start), same outputs: c->p_w and c->p_supp
+ * updated in place, the plans Z left in var_work->l_var_sphBregman[idx_ph].Z
+ * for the next call's warm start.  Honours p_badmm_options (maxIters+1
+ * iterations, rhoCoeff, updatePerLoops) and the global time_budget.
+ * Metric types: D2_EUCLIDEAN_L2, D2_WORD_EMBED, D2_HISTOGRAM,
+ * D2_SPARSE_HISTOGRAM; D2_N_GRAM returns D2G_E_UNSUPPORTED.  The host X, Y
+ * and C buffers are scratch for the reference's callers and are only written
+ * back when d2g_config.sync_scratch is set. */
+int d2_centroid_sphBregman(mph *p_data, var_mph *var_work, int idx_ph, sph *c0, sph *c);
+
+/* Replaces calculate_distmat, src/d2/centroid_util.c:8-36 (declared
+ * include/d2/centroid_util.h:40): the per-instance str x p_str[i] ground-cost
+ * blocks between each instance and its labelled centroid, written into the
+ * host array C at offset str*p_str_cum[i].  Computed on the GPU in FP64. */
+void calculate_distmat(sph *data_ph, int *label, size_t size, sph *c, double *C);
+
+/* Option structs of src/d2/centroid_Bregman.c:17-22 (the caller swaps
+ * p_badmm_options, e.g. src/app/main.cc:234-236). */
+extern BADMM_options badmm_clu_options;
+extern BADMM_options badmm_cen_options;
+extern BADMM_options *p_badmm_options;
+
+/* Seconds after which the B-ADMM loop stops (centroid_Bregman.c:24,318).
+ * The reference's driver defines and sets it (src/d2/clustering.c:21,240,373);
+ * libd2g.so carries a weak definition, initialised to 1e300, for programs
+ * that link it without that driver. */
+extern double time_budget;
+
+/* ------------------------------------------------------- library control */
+typedef struct {
+  int precision;    /* 0: FP32 plans + FP64 reductions (default); 1: FP64 throughout */
+  int verbose;      /* 1: print the reference's iter/obj/primres/dualres lines */
+  int use_graph;    /* 1: replay the iteration loop as one CUDA graph (default) */
+  int sync_scratch; /* 1: also write the host X, Y and C back after a drop-in call */
+  int profile;      /* 1: time every plan-update launch with CUDA events (no graph) */
+} d2g_config;
+
+int d2g_get_config(d2g_config *cfg);
+int d2g_set_config(const d2g_config *cfg);
+const char *d2g_error_string(int code);
+/* last error message of this thread, "" if none */
+const char *d2g_last_error(void);
+
+/* ------------------------------------------------------------ resident API */
+typedef struct d2g_phase d2g_phase;
+
+typedef struct {
+  int metric_type;          /* D2_EUCLIDEAN_L2, D2_WORD_EMBED, D2_HISTOGRAM, D2_SPARSE_HISTOGRAM */
+  int dim;                  /* support dimension (0 for histograms) */
+  int str;                  /* centroid support size m */
+  size_t size;              /* instances n */
+  const int *p_str;         /* [size] */
+  const double *p_w;        /* [col] */
+  const double *p_supp;     /* [col*dim] Euclidean supports */
+  const int *p_supp_sym;    /* [col] 0-based ids (embedding, sparse histogram) */
+  const double *vocab_vec;  /* [vocab_size*dim] embedding vectors */
+  const double *dist_mat;   /* [vocab_size*vocab_size] histogram bin cost */
+  int vocab_size;           /* vocabulary size / number of bins */
+  const int *label;         /* [size] */
+  int num_of_labels;        /* k */
+  size_t global_size;       /* N normalising obj/primres/dualres (0 = size) */
+} d2g_phase_desc;
+
+typedef struct {
+  int maxIters;             /* maxIters+1 iterations, as the reference */
+  double rhoCoeff;
+  int updatePerLoops;
+  double time_budget;       /* seconds; <= 0 means unlimited */
+} d2g_badmm_opts;
+
+typedef struct {
+  int iterations;           /* iterations run by the last call */
+  double rho;
+  double total_ms;          /* device time of the last call's iteration loop */
+  double plan_ms_avg;       /* mean plan-update launch time (profile mode) */
+  int plan_launches;        /* plan-update launches timed (profile mode) */
+  long long kernel_launches;/* kernels launched by the last call */
+  double plan_bytes;        /* algorithmic HBM bytes of one plan-update pass */
+  size_t plan_entries;      /* str * col */
+  int path;                 /* 0 batched FP32, 1 plain FP64 */
+} d2g_run_stats;
+
+/* Upload a phase.  Host arrays are copied; labels can change later. */
+int d2g_phase_create(const d2g_phase_desc *desc, int precision, d2g_phase **out);
+int d2g_phase_destroy(d2g_phase *ph);
+/* Re-send weights, supports / ids, cost data and labels of a phase whose
+ * shape (metric, dim, str, size, p_str) is unchanged. */
+int d2g_phase_refresh(d2g_phase *ph, const d2g_phase_desc *desc);
+/* new labels (k-means reassignment) */
+int d2g_phase_set_labels(d2g_phase *ph, const int *label);
+/* warm-start plans in the reference layout (str*col, column-major per instance) */
+int d2g_phase_set_plans(d2g_phase *ph, const double *Z);
+int d2g_phase_get_plans(d2g_phase *ph, double *Z);
+/* One centroid update.  c_w [k*str] and c_supp [k*str*dim] (NULL for
+ * histograms) are host arrays, read as the start point and overwritten with
+ * the result.  label_switch [size] (NULL = all 1) selects plans to re-initialise. */
+int d2g_badmm_run(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, double *c_supp,
+                  const char *label_switch);
+/* obj/primres/dualres of the last run: 4 doubles (iter+1, obj, primres, dualres) per check */
+int d2g_phase_trace(d2g_phase *ph, double *trace, int cap, int *n);
+int d2g_phase_stats(d2g_phase *ph, d2g_run_stats *st);
+/* the CUDA stream (cudaStream_t) every kernel of this phase is launched on */
+void *d2g_phase_stream(d2g_phase *ph);
+/* the last run's X (after step 1, or X-Z after a check iteration as the
+ * reference leaves it), Y and C (divided by rho), reference layout, FP64 */
+int d2g_phase_get_scratch(d2g_phase *ph, double *X, double *Y, double *C);
+
+/* ------------------------------------------------------------- serving API */
+typedef struct d2g_server d2g_server;
+
+typedef struct {
+  int num_of_labels;        /* k resident centroids */
+  int str;                  /* centroid support size m */
+  int dim;                  /* support dimension */
+  const double *c_w;        /* [k*str] */
+  const double *c_supp;     /* [k*str*dim] */
+  int iters;                /* B-ADMM iterations per solve */
+  double rhoCoeff;
+  size_t hbm_budget_bytes;  /* admission bound on in-flight request state */
+  int max_queue;            /* admission bound on queued requests */
+  int max_batch_entries;    /* plan entries per device batch (0 = default) */
+} d2g_server_desc;
+
+int d2g_server_create(const d2g_server_desc *desc, d2g_server **out);
+int d2g_server_destroy(d2g_server *s);
+/* Admit one query distribution (m_q supports in R^dim).  Copies the data.
+ * Returns D2G_E_ADMISSION when the HBM budget or queue bound refuses it. */
+int d2g_server_submit(d2g_server *s, int m_q, const double *w_q, const double *supp_q,
+                      long long *ticket);
+/* Advance the device loop: launch whatever is admitted and collect finished
+ * batches.  Non-blocking unless wait != 0.  Returns the number of requests
+ * completed by this call. */
+int d2g_server_progress(d2g_server *s, int wait);
+/* 1 and the result when done, 0 while pending; costs [k] may be NULL.
+ * A finished ticket is released by the call that returns 1. */
+int d2g_server_result(d2g_server *s, long long ticket, int *label, double *costs,
+                      double *latency_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* D2G_H_ */

@@ -1,0 +1,125 @@
+"""Generate the golden fixtures of the B-ADMM centroid update.
+
+Runs the reference's own d2_centroid_sphBregman (compiled unmodified from the
+reference tree by oracle/Makefile into oracle/_ref/) on small seeded inputs
+and stores inputs and outputs as .npz files next to this script.  The
+reference publishes no golden vectors and has no unit tests, so these
+fixtures are the pin: tests check the C restatement (oracle/liboracle.so,
+which also builds on the GPU machine) and the CUDA paths against them.
+
+Run from the repository root where the reference tree is present:
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import oracle  # noqa: E402
+from d2_kmeans_gb300 import synth  # noqa: E402
+
+REF_DATA = "/root/reference/data"
+
+
+def digest(z: np.ndarray) -> np.ndarray:
+    """Order-sensitive summary of a plan array: sums, moments, samples."""
+    idx = np.arange(0, z.size, max(1, z.size // 64))
+    w = np.cos(np.arange(z.size) * 0.001)
+    return np.concatenate([[z.sum(), (z * z).sum(), (z * w).sum()], z[idx]])
+
+
+def read_simple():
+    """The reference's 5 three-bin histograms (data/simple.d2, .hist0)."""
+    toks = open(os.path.join(REF_DATA, "simple.d2")).read().split()
+    vals = list(map(float, toks))
+    w = []
+    i = 0
+    while i < len(vals):
+        n = int(vals[i + 1])
+        w.extend(vals[i + 2:i + 2 + n])
+        i += 2 + n
+    h = list(map(float, open(os.path.join(REF_DATA, "simple.d2.hist0")).read().split()))
+    nb = int(h[0])
+    return np.array(w).reshape(-1, nb), np.array(h[1:1 + nb * nb]).reshape(nb, nb)
+
+
+def cases():
+    out = {}
+    ph, c = synth.euclidean_phase(300, 6, 16, 3, (4, 16), False, 10, 1.0, seed=11)
+    out["euclid_small"] = (ph, c, dict(maxIters=100, rhoCoeff=2.0, updatePerLoops=10))
+    ph, c = synth.euclidean_phase(200, 5, 6, 3, (2, 16), False, 10, 1.0, seed=12)
+    out["euclid_oddm"] = (ph, c, dict(maxIters=60, rhoCoeff=2.0, updatePerLoops=10))
+    ph, c = synth.euclidean_phase(150, 4, 8, 2, (3, 12), False, 6, 1.0, seed=13)
+    out["euclid_collide"] = (ph, c, dict(maxIters=40, rhoCoeff=2.0, updatePerLoops=3))
+    ph, c = synth.euclidean_phase(12, 3, 32, 5, (129, 520), False, 8, 1.0, seed=15)
+    out["euclid_bigplans_d5"] = (ph, c, dict(maxIters=40, rhoCoeff=1.0, updatePerLoops=10))
+    ph, c = synth.histogram_phase(120, 4, side=4, alpha=0.1, seed=14)
+    out["hist_small"] = (ph, c, dict(maxIters=60, rhoCoeff=2.0, updatePerLoops=10))
+    w, D = read_simple()
+    n, nb = w.shape
+    ph = dict(metric=5, dim=0, str=nb, p_str=np.full(n, nb, np.int32), p_w=w.reshape(-1),
+              dist_mat=D.reshape(-1), vocab_size=nb, label=np.array([0, 1, 0, 1, 0], np.int32),
+              num_of_labels=2, label_switch=np.ones(n, np.int8))
+    c = dict(c_w=np.full(2 * nb, 1.0 / nb), c_supp=None)
+    out["simple_kat"] = (ph, c, dict(maxIters=100, rhoCoeff=2.0, updatePerLoops=10))
+    return out
+
+
+def pack(name, ph, c, opts, res, extra=None):
+    d = {"opts": np.array([opts["maxIters"], opts["rhoCoeff"], opts["updatePerLoops"]])}
+    for k, v in ph.items():
+        if isinstance(v, np.ndarray):
+            d["in_" + k] = v
+        else:
+            d["meta_" + k] = np.array(v)
+    d["c0_w"] = np.asarray(c["c_w"]).reshape(-1)
+    if c.get("c_supp") is not None:
+        d["c0_supp"] = np.asarray(c["c_supp"]).reshape(-1)
+    d["out_c_w"] = res["c_w"]
+    if c.get("c_supp") is not None:
+        d["out_c_supp"] = res["c_supp"]
+    d["out_trace"] = res["trace"]
+    d["out_Z_digest"] = digest(res["Z"])
+    if extra:
+        d.update(extra)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+
+
+def main():
+    if not oracle.available("reference"):
+        oracle.build(reference=True)
+    for name, (ph, c, opts) in cases().items():
+        res = oracle.badmm(ph, c, opts, "reference", want=())
+        port = oracle.badmm(ph, c, opts, "port", want=())
+        assert res["rc"] == 0 and port["rc"] == 0
+        assert np.array_equal(res["c_w"], port["c_w"]) and np.array_equal(res["Z"], port["Z"])
+        pack(name, ph, c, opts, res)
+        print(name, "col", int(np.sum(ph["p_str"])), "trace", res["trace"][:, 1])
+    # warm start: second call after a k-means reassignment of ~10% of the instances
+    ph, c, opts = cases()["euclid_small"]
+    r1 = oracle.badmm(ph, c, opts, "reference", want=())
+    rng = np.random.default_rng(99)
+    lab2 = ph["label"].copy()
+    mv = rng.random(lab2.size) < 0.1
+    lab2[mv] = rng.integers(0, ph["num_of_labels"], size=int(mv.sum()))
+    lab2[: ph["num_of_labels"]] = np.arange(ph["num_of_labels"])
+    ls2 = (lab2 != ph["label"]).astype(np.int8)
+    ph2 = dict(ph, label=lab2, label_switch=ls2)
+    c2 = dict(c_w=r1["c_w"], c_supp=r1["c_supp"], Z=r1["Z"])
+    r2 = oracle.badmm(ph2, c2, opts, "reference", want=())
+    p2 = oracle.badmm(ph2, c2, opts, "port", want=())
+    assert np.array_equal(r2["c_w"], p2["c_w"])
+    pack("euclid_warm", ph2, dict(c_w=r1["c_w"], c_supp=r1["c_supp"]), opts, r2,
+         extra={"first_c_w": c["c_w"], "first_c_supp": c["c_supp"], "first_label": ph["label"]})
+    print("euclid_warm switched", int(ls2.sum()))
+
+
+if __name__ == "__main__":
+    main()

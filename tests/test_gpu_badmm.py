@@ -1,0 +1,213 @@
+"""Parity of the CUDA B-ADMM centroid update (libd2g.so, through its C ABI)
+against the reference's FP64 results: the committed golden fixtures (made by
+the reference compiled from its own sources) and the C restatement of the
+oracle on the same seeded inputs.
+
+Tolerances (FP32 plans + FP64 cross-plan reductions against FP64):
+  relative objective error            <= 1e-5   (every residual check)
+  centroid weights, L1 per cluster    <= 1e-4
+  support locations                   <= 1e-4 relative
+The FP64 path (precision=1) is held to 1e-9.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+from golden.make_golden import digest
+from d2_kmeans_gb300 import synth
+from d2_kmeans_gb300._lib import D2GError, D2G_E_EMPTY_CLUSTER
+
+pytestmark = pytest.mark.gpu
+
+OBJ_TOL, CW_TOL, SUPP_TOL = 1e-5, 1e-4, 1e-4
+
+
+def assert_close(res, ref, k, m, fp64=False, trace_atol=0.0):
+    """res / ref: dicts with c_w, c_supp, trace (iter, obj, primres, dualres)."""
+    cw = np.asarray(res["c_w"]).reshape(k, m)
+    cwr = np.asarray(ref["c_w"]).reshape(k, m)
+    l1 = np.abs(cw - cwr).sum(axis=1).max()
+    assert l1 <= (1e-10 if fp64 else CW_TOL), f"c_w L1 {l1}"
+    if ref.get("c_supp") is not None and res.get("c_supp") is not None:
+        s = np.asarray(res["c_supp"]).reshape(-1)
+        sr = np.asarray(ref["c_supp"]).reshape(-1)
+        scale = np.maximum(np.abs(sr), 1e-3 * np.abs(sr).max())
+        rel = (np.abs(s - sr) / scale).max()
+        assert rel <= (1e-9 if fp64 else SUPP_TOL), f"support rel err {rel}"
+    tr, trr = np.asarray(res["trace"]), np.asarray(ref["trace"])
+    assert tr.shape == trr.shape, (tr.shape, trr.shape)
+    if trr.size == 0:
+        return
+    np.testing.assert_array_equal(tr[:, 0], trr[:, 0])
+    obj_err = np.abs(tr[:, 1] - trr[:, 1]) / np.abs(trr[:, 1])
+    assert obj_err.max() <= (1e-9 if fp64 else OBJ_TOL) + trace_atol / np.abs(trr[:, 1]).min(), \
+        f"objective rel err {obj_err}"
+
+
+def golden_ref(exp):
+    return {"c_w": exp["out_c_w"], "c_supp": exp.get("out_c_supp"), "trace": exp["out_trace"]}
+
+
+def run_phase(d2g, ph, c0, opts, precision, exp=None):
+    """One resident-API call; for the warm fixture, the two-call sequence."""
+    if exp is not None and "first_label" in exp:
+        first = dict(ph, label=exp["first_label"])
+        P = d2g.Phase(first, precision)
+        r1 = P.run({"c_w": exp["first_c_w"], "c_supp": exp["first_c_supp"]}, opts)
+        P.set_labels(ph["label"])
+        r = P.run({"c_w": r1["c_w"], "c_supp": r1["c_supp"]}, opts, label_switch=ph["label_switch"])
+    else:
+        P = d2g.Phase(ph, precision)
+        r = P.run(c0, opts)
+    r["Z"] = P.get_plans()
+    P.close()
+    return r
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_batched_fp32_matches_golden(d2g, name):
+    ph, c0, opts, exp = load_golden(name)
+    r = run_phase(d2g, ph, c0, opts, 0, exp)
+    assert r["stats"]["path"] == 0
+    assert_close(r, golden_ref(exp), ph["num_of_labels"], ph["str"], trace_atol=5.1e-7)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_plain_fp64_matches_golden(d2g, name):
+    ph, c0, opts, exp = load_golden(name)
+    r = run_phase(d2g, ph, c0, opts, 1, exp)
+    assert r["stats"]["path"] == 1
+    assert_close(r, golden_ref(exp), ph["num_of_labels"], ph["str"], fp64=True, trace_atol=5.1e-7)
+    np.testing.assert_allclose(digest(r["Z"]), exp["out_Z_digest"], rtol=1e-9, atol=1e-15)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_dropin_matches_golden(d2g, name):
+    """Through d2_centroid_sphBregman with the reference's own structures."""
+    ph, c0, opts, exp = load_golden(name)
+    if "first_label" in exp:
+        first = dict(ph, label=exp["first_label"])
+        d = d2g.DropIn(first, {"c_w": exp["first_c_w"], "c_supp": exp["first_c_supp"]})
+        assert d.call(opts) == 0
+        assert d.call(opts, label_switch=ph["label_switch"], labels=ph["label"]) == 0
+    else:
+        d = d2g.DropIn(ph, c0)
+        assert d.call(opts) == 0
+    res = {"c_w": d.c_w, "c_supp": d.c_supp}
+    Z = d.Z()
+    d.close()
+    ref = golden_ref(exp)
+    ref["trace"] = np.zeros((0, 4))
+    res["trace"] = np.zeros((0, 4))
+    assert_close(res, ref, ph["num_of_labels"], ph["str"])
+    dz = digest(Z)
+    np.testing.assert_allclose(dz[:3], exp["out_Z_digest"][:3], rtol=1e-4)
+
+
+def _port(oracle_mod, ph, c, opts):
+    r = oracle_mod.badmm(ph, c, opts, "port", want=())
+    assert r["rc"] == 0
+    return r
+
+
+def test_plain_config_full_size(d2g, oracle_mod):
+    """The n=2000, d=3, m_i 4..16, k=10, m=16, 100-iteration workload, both forms."""
+    ph, c, opts = synth.workload("plain", seed=0)
+    ref = _port(oracle_mod, ph, c, opts)
+    for precision in (0, 1):
+        P = d2g.Phase(ph, precision)
+        r = P.run(c, opts)
+        assert_close(r, ref, 10, 16, fp64=precision == 1)
+        assert r["stats"]["iterations"] == 101
+        np.testing.assert_allclose(r["stats"]["rho"], ref["rho"], rtol=1e-6 if precision == 0 else 1e-13)
+        P.close()
+
+
+@pytest.mark.parametrize("m,dim,lo,hi,k,seed", [
+    (5, 1, 1, 9, 3, 21), (12, 2, 3, 40, 4, 22), (40, 6, 10, 300, 3, 23),
+    (100, 8, 2, 64, 3, 24), (64, 3, 200, 700, 2, 25), (3, 4, 1, 4, 2, 26),
+])
+def test_batched_odd_shapes(d2g, oracle_mod, m, dim, lo, hi, k, seed):
+    ph, c = synth.euclidean_phase(40, k, m, dim, (lo, hi), False, 5, 1.0, seed=seed)
+    opts = dict(maxIters=30, rhoCoeff=2.0, updatePerLoops=10)
+    ref = _port(oracle_mod, ph, c, opts)
+    P = d2g.Phase(ph, 0)
+    r = P.run(c, opts)
+    # plans wider than an 8-CTA cluster run on the FP64 form
+    assert_close(r, ref, k, m, fp64=r["stats"]["path"] == 1)
+    P.close()
+
+
+def test_histogram_256_bins_cluster_path(d2g, oracle_mod):
+    """256-bin plans span an 8-CTA thread-block cluster (DSMEM row sums)."""
+    ph, c = synth.histogram_phase(10, 2, side=16, alpha=0.1, seed=31)
+    opts = dict(maxIters=30, rhoCoeff=2.0, updatePerLoops=10)
+    ref = _port(oracle_mod, ph, c, opts)
+    P = d2g.Phase(ph, 0)
+    assert_close(P.run(c, opts), ref, 2, 256)
+    P.close()
+
+
+def test_sparse_histogram(d2g, oracle_mod):
+    rng = np.random.default_rng(5)
+    V, n, k = 24, 30, 3
+    D = synth.grid_cost(int(np.sqrt(V))) if False else np.abs(
+        np.subtract.outer(np.arange(V), np.arange(V))).astype(float) ** 1.5
+    p_str = rng.integers(2, 10, size=n).astype(np.int32)
+    syms = np.concatenate([np.sort(rng.choice(V, size=s, replace=False)) for s in p_str]).astype(np.int32)
+    w = np.concatenate([rng.dirichlet(np.ones(s)) for s in p_str])
+    lab = np.concatenate([np.arange(k), rng.integers(0, k, size=n - k)]).astype(np.int32)
+    ph = dict(metric=12, dim=0, str=V, p_str=p_str, p_w=w, p_supp_sym=syms, dist_mat=D.reshape(-1),
+              vocab_size=V, label=lab, num_of_labels=k, label_switch=np.ones(n, np.int8))
+    c = dict(c_w=rng.dirichlet(np.ones(V), size=k).reshape(-1), c_supp=None)
+    opts = dict(maxIters=40, rhoCoeff=2.0, updatePerLoops=10)
+    ref = _port(oracle_mod, ph, c, opts)
+    for precision in (0, 1):
+        P = d2g.Phase(ph, precision)
+        assert_close(P.run(c, opts), ref, k, V, fp64=precision == 1)
+        P.close()
+
+
+def test_time_budget_stops_after_first_iteration(d2g, oracle_mod):
+    ph, c = synth.euclidean_phase(60, 3, 8, 3, (4, 12), seed=41)
+    ref = _port(oracle_mod, ph, c, dict(maxIters=0, rhoCoeff=2.0, updatePerLoops=10))
+    for precision in (0, 1):
+        P = d2g.Phase(ph, precision)
+        r = P.run(c, dict(maxIters=50, rhoCoeff=2.0, updatePerLoops=10, time_budget=1e-9))
+        assert r["stats"]["iterations"] == 1
+        cw = np.asarray(r["c_w"]).reshape(3, 8)
+        assert np.abs(cw - ref["c_w"].reshape(3, 8)).sum(1).max() < 1e-5
+        P.close()
+
+
+def test_empty_cluster_is_an_error(d2g):
+    ph, c = synth.euclidean_phase(30, 4, 8, 3, (4, 10), seed=42)
+    ph["label"][:] = 0
+    ph["label"][1] = 1
+    with pytest.raises(D2GError) as e:
+        d2g.Phase(ph, 0)
+    assert e.value.code == D2G_E_EMPTY_CLUSTER
+
+
+def test_bitwise_reproducible_and_graph_equals_direct(d2g):
+    ph, c, opts = synth.workload("plain", seed=3, scale=0.5)
+    outs = []
+    for graph in (1, 1, 0):
+        d2g.set_config(use_graph=graph)
+        P = d2g.Phase(ph, 0)
+        r = P.run(c, opts)
+        outs.append((r["c_w"], r["c_supp"], P.get_plans(), r["trace"]))
+        P.close()
+    d2g.set_config(use_graph=1)
+    for o in outs[1:]:
+        for a, b in zip(outs[0], o):
+            np.testing.assert_array_equal(a, b)
+
+
+def test_repeated_runs_reuse_the_graph(d2g):
+    ph, c, opts = synth.workload("plain", seed=4, scale=0.3)
+    P = d2g.Phase(ph, 0)
+    a = P.run(c, opts)
+    b = P.run(c, opts)
+    np.testing.assert_array_equal(a["c_w"], b["c_w"])
+    P.close()
