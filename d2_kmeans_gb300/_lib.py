@@ -98,6 +98,9 @@ SIGNATURES = {
     "d2_centroid_sphBregman": (C.c_int, [C.POINTER(mph), C.POINTER(var_mph), C.c_int,
                                          C.POINTER(sph), C.POINTER(sph)]),
     "calculate_distmat": (None, [C.POINTER(sph), ip, C.c_size_t, C.POINTER(sph), dp]),
+    "d2g_distmat_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_size_t, C.c_size_t] +
+                            [C.c_void_p] * 4 + [C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                                C.c_void_p, C.c_void_p]),
     "d2g_get_config": (C.c_int, [C.POINTER(d2g_config)]),
     "d2g_set_config": (C.c_int, [C.POINTER(d2g_config)]),
     "d2g_error_string": (C.c_char_p, [C.c_int]),

@@ -138,6 +138,25 @@ int d2_centroid_sphBregman(mph *p_data, var_mph *var_work, int idx_ph, sph *c0, 
  * host array C at offset str*p_str_cum[i].  Computed on the GPU in FP64. */
 void calculate_distmat(sph *data_ph, int *label, size_t size, sph *c, double *C);
 
+/* No counterpart in the reference.  The ground costs of calculate_distmat for
+ * callers that cannot allocate GPU memory (code that runs inside another
+ * runtime's allocator or is handed only pre-allocated device buffers): every
+ * pointer is a device pointer the caller owns - p_str [size], p_supp
+ * [col*dim] or p_supp_sym [col] + vocab_vec [vocab_size*dim], label [size],
+ * c_supp [num_of_labels*str*dim] in, C [str*col] out - and the working data
+ * (prefix sums, column map) lives in an 8 MiB array fixed inside libd2g.so
+ * on each GPU, so the call allocates nothing.  Needs 8*size + 4*col + 256
+ * bytes of that array and returns D2G_E_INVAL beyond it.  Calls share the
+ * array: calls whose GPU work overlaps race, so serialise them.  The first
+ * call on a device looks up the array's address; make it before any stream
+ * capture.  Runs on `stream` (a cudaStream_t, NULL for the default stream)
+ * and returns after the inputs are validated, with the cost kernel queued.
+ * Euclidean and word-embedding phases only. */
+int d2g_distmat_noalloc(int metric_type, int dim, int str, size_t size, size_t col,
+                        const int *p_str, const double *p_supp, const int *p_supp_sym,
+                        const double *vocab_vec, int vocab_size, const int *label,
+                        int num_of_labels, const double *c_supp, double *C, void *stream);
+
 /* Option structs of src/d2/centroid_Bregman.c:17-22 (the caller swaps
  * p_badmm_options, e.g. src/app/main.cc:234-236). */
 extern BADMM_options badmm_clu_options;
