@@ -208,13 +208,35 @@ def e2e_steps(ph, c, opts, steps, warmup):
     return statistics.mean(times), h2d, d2h
 
 
+SERVE_WORKLOAD = ("serving: k=256 resident centroids, m=64, d=64; queries with m_q log-uniform 4-512, "
+                  "GMM supports, Dirichlet(1) weights; 200 B-ADMM iterations per solve against all "
+                  "centroids + argmin; Poisson arrivals")
+
+
+def serve_leg(rates=(2000.0, 5000.0, 10000.0, 20000.0), per_rate=1500):
+    from d2_kmeans_gb300 import serve, synth
+    c_w, c_supp, means = synth.serving_centroids(k=256, m=64, dim=64, n_comp=32, seed=0)
+    S = serve.Server(c_w, c_supp, iters=200, rho_coeff=2.0, hbm_budget_bytes=4 << 30, max_queue=4096)
+    warm = synth.serving_queries(64, means, sizes=(4, 512), seed=99)
+    serve.poisson_run(S, warm, rate=1e6, seed=0)
+    out = []
+    for i, rate in enumerate(rates):
+        qs = synth.serving_queries(per_rate, means, sizes=(4, 512), seed=100 + i)
+        r = serve.poisson_run(S, qs, rate=rate, seed=i)
+        r.pop("results")
+        out.append(r)
+    S.close()
+    return {"workload": SERVE_WORKLOAD, "per_rate": out,
+            "capacity_req_per_s": max(r["throughput"] for r in out)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--skip", default="", help="comma list of legs to skip: e2e,plain,cpu,profile")
+    ap.add_argument("--skip", default="", help="comma list of legs to skip: e2e,plain,cpu,profile,serve")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -305,6 +327,8 @@ def main():
         out["e2e"] = {"value": world * n * iters / sec, "unit": UNIT, "h2d_bytes_per_step": h2d,
                       "d2h_bytes_per_step": d2h, "seconds_per_step": sec,
                       "api": "d2_centroid_sphBregman (reference structs, host buffers)"}
+    if "serve" not in skip and rank == 0:
+        out["serve"] = serve_leg()
     if "cpu" not in skip and rank == 0:
         ensure_oracle()
         v, units, wall = cpu_baseline(1, 20000 / 200000, 21, seed=100)

@@ -11,7 +11,8 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libd2g.so")
+# D2G_LIB selects another build of the library (e.g. an instrumented one)
+LIB_PATH = os.environ.get("D2G_LIB") or os.path.join(HERE, "libd2g.so")
 
 D2_EUCLIDEAN_L2, D2_CITYBLOCK_L1, D2_HISTOGRAM, D2_N_GRAM, D2_WORD_EMBED, D2_SPARSE_HISTOGRAM = (
     0, 1, 5, 6, 7, 12)

@@ -157,6 +157,20 @@ cudaError_t plain_check(const PlainArgs &a, cudaStream_t st);
 unsigned plain_check_blocks(long long nent);
 int plain_launches_per_iter(bool update, bool check);
 
+// serve_kernel.cu
+struct ServeArgs {
+  const float *q_w;       // [cols] query weights of the batch
+  const float *q_supp;    // [cols * dim] query supports
+  const float *c_w32;     // [K * MP] centroid weights (0 in padded rows)
+  const float *c_supp32;  // [K * MP * dim] centroid supports
+  const int4 *items;      // {request, first centroid, plans in the item, groups per plan}
+  const float4 *reqs;     // per request {column offset (int bits), m_q (int bits), log2(e)/rho, 0}
+  float *cost_out;        // [requests * K]
+  int K, m, dim, iters, cs;
+};
+cudaError_t launch_serve(int MP, const ServeArgs &a, int nitems, cudaStream_t st);
+constexpr int serve_groups_per_cta(int MP) { return 1024 / MP; }  // 256 threads, 4 rows x 4 columns
+
 // d2g_host.cu
 int distmat_fp64(int dim, int str, size_t size, const int *p_str, int metric, const double *supp,
                  const int *sym, const double *vocab, int V, const int *label, const double *c_supp,

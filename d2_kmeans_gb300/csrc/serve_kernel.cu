@@ -1,0 +1,253 @@
+// Fixed-centroid transport solves for the serving loop.
+//
+// A request is one query distribution (m_q supports in R^d, weights w_q); it
+// is solved against all K resident centroids (str = m supports each, fixed
+// weights c_w[l]) with B-ADMM steps 1-3 of src/d2/centroid_Bregman.c:155-175
+// for `iters` iterations, from Z = w_q (x) c_w[l] and Y = 0, with
+// rho = rhoCoeff * mean(C) over the request's K plans; the answer is
+// cost_l = <C_l, X_l> for every centroid and its argmin.
+//
+// With the centroid weights fixed there is no coupling between plans, so a
+// plan's whole iteration loop runs on chip: C, Z and Y stay in registers,
+// column sums use shuffles, row sums go through shared memory (and DSMEM when a
+// plan spans a thread-block cluster).  Nothing touches HBM inside the loop;
+// the kernel is bound by MUFU ex2 and FP32 issue.
+//
+// Work items come from compact descriptors, not per-group tables:
+//   item = {request, first centroid l0, plans in the item, groups per plan}
+// Plans of one item are consecutive centroids of one request, each ng = ceil(m_q/4)
+// groups of 4 columns; an item either packs several plans into one CTA or
+// spreads one plan over a cluster of cs CTAs.
+#include <cooperative_groups.h>
+
+#include "d2g_internal.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace d2g {
+
+
+
+__device__ __forceinline__ float sv_ex2(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+template <int TPC>
+__device__ __forceinline__ float sv_seg_sum(float v) {
+#pragma unroll
+  for (int o = TPC / 2; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int MP, bool FULL>
+__global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
+  constexpr int RPT = 4, TPC = MP / RPT, G = 256 / TPC, S = 4;
+  constexpr float kL2e = 1.4426950408889634f;  // log2(e)
+  __shared__ __align__(16) float sm_c[G * S * MP];       // ground costs of the CTA's entries
+  __shared__ __align__(16) float sm_rs[2][G * MP];       // per-group row partials, by parity
+  __shared__ __align__(16) float sm_x[2][8][MP];         // cluster: every rank's partial, by parity
+  __shared__ double sm_cost[G];
+
+  const int tid = threadIdx.x, g = tid / TPC, r = tid % TPC, k0 = r * RPT;
+  const int cs = a.cs;
+  const int item_i = blockIdx.x / cs, rank = blockIdx.x - item_i * cs;
+  const int4 it = a.items[item_i];
+  const int req = it.x, l0 = it.y, nplans = it.z, ng = it.w;
+  const float4 rq = a.reqs[req];
+  const int qcol0 = __float_as_int(rq.x), mq = __float_as_int(rq.y);
+  const float ir2 = rq.z;
+
+  // this thread's plan, group within the plan, and columns
+  int plan, gq;
+  if (cs == 1) {
+    plan = g / ng;
+    gq = g - plan * ng;
+  } else {
+    plan = 0;
+    gq = rank * G + g;
+  }
+  const bool active = cs == 1 ? plan < nplans : gq < ng;
+  const int l = l0 + (active ? plan : 0);
+  const int c0 = gq * S;  // first column of the group within the query
+  const int nvalid = active ? min(S, mq - c0) : 0;
+  // groups of this thread's plan inside this CTA (for the row sums)
+  const int lo = cs == 1 ? plan * ng : 0;
+  const int hi = cs == 1 ? lo + ng : min(G, ng - rank * G);
+  float *cme = sm_c + (g * S) * MP + k0;  // this thread's costs: column s at cme[s*MP + q]
+
+  // costs (to shared memory), weights, start point
+  float z[S][RPT], y[S][RPT], w[S], cw[RPT];
+#pragma unroll
+  for (int q = 0; q < RPT; ++q) cw[q] = __ldg(a.c_w32 + (size_t)l * MP + k0 + q);
+  {
+    float c[S][RPT];
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      const bool ok = s < nvalid;
+      w[s] = ok ? __ldg(a.q_w + qcol0 + c0 + s) : 0.f;
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        c[s][q] = 0.f;
+        z[s][q] = ok ? w[s] * cw[q] : 0.f;
+        y[s][q] = 0.f;
+      }
+    }
+    for (int t = 0; t < a.dim; ++t) {
+      float cv[RPT], qv[S];
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) cv[q] = __ldg(a.c_supp32 + ((size_t)l * MP + k0 + q) * a.dim + t);
+#pragma unroll
+      for (int s = 0; s < S; ++s)
+        qv[s] = s < nvalid ? __ldg(a.q_supp + (size_t)(qcol0 + c0 + s) * a.dim + t) : 0.f;
+#pragma unroll
+      for (int s = 0; s < S; ++s)
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+          const float d = cv[q] - qv[s];
+          c[s][q] = fmaf(d, d, c[s][q]);
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+      *((float4 *)(cme + s * MP)) = make_float4(c[s][0], c[s][1], c[s][2], c[s][3]);
+  }
+  const int m = a.m;
+  float x[S][RPT];
+  for (int iter = 0; iter < a.iters; ++iter) {
+    const int buf = iter & 1;
+    float rp[RPT] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      const bool colok = s < nvalid;
+      const float4 cc = *((const float4 *)(cme + s * MP));
+      const float c[RPT] = {cc.x, cc.y, cc.z, cc.w};
+      float csum = 0.f;
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        const bool ok = colok && (FULL || k0 + q < m);
+        const float v = ok ? fmaf(z[s][q], sv_ex2(-fmaf(c[q], ir2, y[s][q])), kRoundoff) : 0.f;
+        x[s][q] = v;
+        csum += v;
+      }
+      csum = sv_seg_sum<TPC>(csum);
+      const float f = colok ? w[s] / csum : 0.f;
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        const bool ok = colok && (FULL || k0 + q < m);
+        x[s][q] *= f;
+        const float zp = ok ? fmaf(x[s][q], sv_ex2(y[s][q]), kRoundoff) : 0.f;
+        z[s][q] = zp;
+        rp[q] += zp;
+      }
+    }
+    *((float4 *)(sm_rs[buf] + g * MP + k0)) = make_float4(rp[0], rp[1], rp[2], rp[3]);
+    __syncthreads();
+    float tot[RPT] = {0.f, 0.f, 0.f, 0.f};
+    if (cs == 1) {
+      // every thread sums its own plan's partials (no second barrier: the
+      // partials are double-buffered by iteration parity)
+      for (int j = lo; j < hi; ++j) {
+        const float4 u = *((const float4 *)(sm_rs[buf] + j * MP + k0));
+        tot[0] += u.x; tot[1] += u.y; tot[2] += u.z; tot[3] += u.w;
+      }
+    } else {
+      cg::cluster_group cl = cg::this_cluster();
+      if (g == 0) {  // this CTA's partial, pushed into every rank's shared memory
+        float4 pt = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int j = 0; j < hi; ++j) {
+          const float4 u = *((const float4 *)(sm_rs[buf] + j * MP + k0));
+          pt.x += u.x; pt.y += u.y; pt.z += u.z; pt.w += u.w;
+        }
+        for (int rk = 0; rk < cs; ++rk)
+          *((float4 *)(cl.map_shared_rank(&sm_x[buf][rank][0], rk) + k0)) = pt;
+      }
+      cl.sync();
+      for (int rk = 0; rk < cs; ++rk) {
+        const float4 u = *((const float4 *)(&sm_x[buf][rk][0] + k0));
+        tot[0] += u.x; tot[1] += u.y; tot[2] += u.z; tot[3] += u.w;
+      }
+    }
+    // second half of step 2 with the fixed centroid weights, and step 3
+    float sc[RPT];
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) sc[q] = cw[q] / tot[q];
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        const bool ok = s < nvalid && (FULL || k0 + q < m);
+        const float zn = ok ? z[s][q] * sc[q] : 0.f;
+        y[s][q] = ok ? fmaf(kL2e, x[s][q] - zn, y[s][q]) : 0.f;
+        z[s][q] = zn;
+      }
+  }
+  // cost_l = <C, X> of the last iteration, per plan
+  float pc = 0.f;
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    const float4 cc = *((const float4 *)(cme + s * MP));
+    pc = fmaf(cc.x, x[s][0], pc);
+    pc = fmaf(cc.y, x[s][1], pc);
+    pc = fmaf(cc.z, x[s][2], pc);
+    pc = fmaf(cc.w, x[s][3], pc);
+  }
+  pc = sv_seg_sum<TPC>(pc);
+  if (r == 0) sm_cost[g] = (double)pc;
+  if (cs == 1) {
+    __syncthreads();
+    if (active && g == lo && r == 0) {
+      double t = 0.0;
+      for (int j = lo; j < hi; ++j) t += sm_cost[j];
+      a.cost_out[(size_t)req * a.K + l] = (float)t;
+    }
+  } else {
+    cg::cluster_group cl = cg::this_cluster();
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int j = 0; j < hi; ++j) t += sm_cost[j];
+      sm_cost[0] = t;
+    }
+    cl.sync();
+    if (rank == 0 && tid == 0) {
+      double t = 0.0;
+      for (int rk = 0; rk < cs; ++rk) t += *cl.map_shared_rank(&sm_cost[0], rk);
+      a.cost_out[(size_t)req * a.K + l] = (float)t;
+    }
+    cl.sync();
+  }
+}
+
+template <int MP, bool FULL>
+static cudaError_t launch_serve_mp(const ServeArgs &a, int nitems, cudaStream_t st) {
+  if (nitems <= 0) return cudaSuccess;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nitems * a.cs);
+  cfg.blockDim = dim3(256);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  if (a.cs > 1) {
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = a.cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+  }
+  return cudaLaunchKernelEx(&cfg, serve_kernel<MP, FULL>, a);
+}
+
+cudaError_t launch_serve(int MP, const ServeArgs &a, int nitems, cudaStream_t st) {
+  const bool full = a.m == MP;
+  switch (MP) {
+    case 16: return full ? launch_serve_mp<16, true>(a, nitems, st) : launch_serve_mp<16, false>(a, nitems, st);
+    case 32: return full ? launch_serve_mp<32, true>(a, nitems, st) : launch_serve_mp<32, false>(a, nitems, st);
+    case 64: return full ? launch_serve_mp<64, true>(a, nitems, st) : launch_serve_mp<64, false>(a, nitems, st);
+    case 128: return full ? launch_serve_mp<128, true>(a, nitems, st) : launch_serve_mp<128, false>(a, nitems, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace d2g

@@ -6,6 +6,11 @@ Workloads (d2_kmeans_gb300.synth.workload): plain, batched, hist,
 twophase_euclid, embed.  --scale shrinks the number of instances only;
 --iters sets maxIters (the loop runs maxIters+1 iterations); --precision 1
 selects the FP64 form.  Prints the run statistics as one JSON line.
+
+    python -m d2_kmeans_gb300.run_workload --workload serve --requests 64
+
+runs that many serving requests (k=256 centroids, m=64, d=64, m_q
+log-uniform 4..512, 200 iterations) back to back through the server.
 """
 from __future__ import annotations
 
@@ -23,8 +28,23 @@ def main(argv=None):
     ap.add_argument("--precision", type=int, default=0)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--repeat", type=int, default=1)
+    ap.add_argument("--requests", type=int, default=64)
     args = ap.parse_args(argv)
     badmm.set_config(verbose=0)
+    if args.workload == "serve":
+        import time
+
+        from . import serve
+        c_w, c_supp, means = synth.serving_centroids(k=256, m=64, dim=64, n_comp=32, seed=args.seed)
+        S = serve.Server(c_w, c_supp, iters=args.iters or 200)
+        qs = synth.serving_queries(args.requests, means, sizes=(4, 512), seed=args.seed + 1)
+        t = time.perf_counter()
+        out = serve.poisson_run(S, qs, rate=1e9, seed=0)
+        out.pop("results")
+        out["seconds"] = time.perf_counter() - t
+        S.close()
+        print(json.dumps(out))
+        return
     ph, c, opts = synth.workload(args.workload, seed=args.seed, scale=args.scale)
     if args.iters is not None:
         opts = dict(opts, maxIters=args.iters)
