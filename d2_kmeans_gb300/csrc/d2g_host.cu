@@ -120,6 +120,12 @@ struct d2g_phase {
   size_t smem_plan = 0, smem_plan_upd = 0;
   int use_tma = 1;  // persistent TMA-pipelined kernel for single-CTA items (D2G_PLAN_KERNEL=v1 turns it off)
 
+  // ---- word-embedding phase (batched form)
+  std::vector<int> h_sym;  // token id per reference column
+  DBuf<float> vocab32, vnorm, cnorm, cs32f, W, epart;
+  DBuf<int> pair_key, pair_ptr, occ_col;
+  int npairs = 0, echunk = 0, enchunk = 0;
+
   // ---- plain form
   DBuf<double> pC, pX, pY, pZ, pZ0, pw, psupp, pvocab, pdist, pzr, pxmom;
   DBuf<int> psym, pcol_inst, pp_str, plabel;
@@ -160,6 +166,7 @@ static bool batched_supported(const d2g_phase_desc *d, std::string *why) {
     return true;
   }
   if (d->metric_type == D2_HISTOGRAM || d->metric_type == D2_SPARSE_HISTOGRAM) return true;
+  if (d->metric_type == D2_WORD_EMBED) return d->dim >= 1;
   *why = "metric type";
   return false;
 }
@@ -291,7 +298,7 @@ static PlanArgs base_args(d2g_phase *ph) {
   a.cw32 = ph->cw32.p;
   a.cs32 = ph->cs32.p;
   a.ctab = ph->ctab.p;
-  a.ctab_lstride = 0;
+  a.ctab_lstride = ph->metric == D2_WORD_EMBED ? (long long)ph->vocab_size * ph->MP : 0;
   a.rowsum_out = ph->rowsum.p;
   a.xmom_out = ph->xmom.p;
   a.X_out = ph->Xp.p;
@@ -355,6 +362,41 @@ static int set_labels_impl(d2g_phase *ph, const int *label) {
       ph->h_grp_rec[gi].x = slot[p];
       ph->h_grp_rec[gi].z = pl[p];
     }
+    if (ph->metric == D2_WORD_EMBED) {
+      // occurrence lists: for each (cluster, token) the packed columns carrying it,
+      // ordered by packed column (counting sort on the key label*V + token)
+      const int V = ph->vocab_size;
+      std::vector<int> key_of(ph->ncols_packed, -1);
+      for (size_t gi = 0; gi < ph->h_grp_rec.size(); ++gi) {
+        const int p = gplan[gi];
+        const int nv = ph->h_grp_rec[gi].w & 15;
+        const int jj0 = (int)(gi - ph->h_grp_rec[gi].y) * kS;
+        const long long c0 = ph->cum[ph->plan_inst[p]];
+        for (int s2 = 0; s2 < nv; ++s2)
+          key_of[gi * kS + s2] = pl[p] * V + ph->h_sym[c0 + jj0 + s2];
+      }
+      std::vector<int> cnt((size_t)ph->K * V + 1, 0);
+      for (int k2 : key_of)
+        if (k2 >= 0) ++cnt[k2 + 1];
+      std::vector<int> keys, ptr(1, 0);
+      for (size_t k2 = 0; k2 < (size_t)ph->K * V; ++k2)
+        if (cnt[k2 + 1]) {
+          keys.push_back((int)k2);
+          ptr.push_back(ptr.back() + cnt[k2 + 1]);
+        }
+      for (size_t k2 = 1; k2 < cnt.size(); ++k2) cnt[k2] += cnt[k2 - 1];
+      std::vector<int> occ(ptr.back());
+      for (long long pc = 0; pc < ph->ncols_packed; ++pc)
+        if (key_of[pc] >= 0) occ[cnt[key_of[pc]]++] = (int)pc;
+      ph->npairs = (int)keys.size();
+      D2G_CUDA(ph->pair_key.alloc(keys.size()));
+      D2G_CUDA(ph->pair_ptr.alloc(ptr.size()));
+      D2G_CUDA(ph->occ_col.alloc(occ.size()));
+      D2G_CUDA(cudaMemcpyAsync(ph->pair_key.p, keys.data(), keys.size() * 4, cudaMemcpyHostToDevice, ph->st));
+      D2G_CUDA(cudaMemcpyAsync(ph->pair_ptr.p, ptr.data(), ptr.size() * 4, cudaMemcpyHostToDevice, ph->st));
+      D2G_CUDA(cudaMemcpyAsync(ph->occ_col.p, occ.data(), occ.size() * 4, cudaMemcpyHostToDevice, ph->st));
+      D2G_CUDA(cudaStreamSynchronize(ph->st));
+    }
     D2G_CUDA(ph->grp_rec.alloc(ph->h_grp_rec.size()));
     D2G_CUDA(cudaMemcpyAsync(ph->grp_rec.p, ph->h_grp_rec.data(), ph->h_grp_rec.size() * sizeof(int4),
                              cudaMemcpyHostToDevice, ph->st));
@@ -376,7 +418,7 @@ static int upload_columns_batched(d2g_phase *ph, const d2g_phase_desc *d) {
   D2G_CUDA(cudaMemcpyAsync(tmp.p, d->p_w, ph->col * 8, cudaMemcpyHostToDevice, ph->st));
   if (euc)
     D2G_CUDA(cudaMemcpyAsync(tmp.p + ph->col, d->p_supp, ph->col * ph->dim * 8, cudaMemcpyHostToDevice, ph->st));
-  if (ph->metric == D2_SPARSE_HISTOGRAM) {
+  if (ph->metric == D2_SPARSE_HISTOGRAM || ph->metric == D2_WORD_EMBED) {
     D2G_CUDA(tsym.alloc(ph->col));
     D2G_CUDA(cudaMemcpyAsync(tsym.p, d->p_supp_sym, ph->col * 4, cudaMemcpyHostToDevice, ph->st));
   }
@@ -388,7 +430,17 @@ static int upload_columns_batched(d2g_phase *ph, const d2g_phase_desc *d) {
                                  euc ? ph->col_supp.p : nullptr, euc ? nullptr : ph->col_sym.p,
                                  ph->dim, ph->DS, ph->metric == D2_HISTOGRAM ? 1 : 0, ph->st));
   }
-  if (!euc) {  // histogram cost table: row v = cost from bin v to every centroid bin
+  if (ph->metric == D2_WORD_EMBED) {  // vocabulary (FP32) and its norms; the cost table is per run
+    const size_t vd = (size_t)ph->vocab_size * ph->dim;
+    std::vector<float> v32(vd);
+    for (size_t i = 0; i < vd; ++i) v32[i] = (float)d->vocab_vec[i];
+    D2G_CUDA(ph->vocab32.alloc(vd));
+    D2G_CUDA(cudaMemcpyAsync(ph->vocab32.p, v32.data(), vd * 4, cudaMemcpyHostToDevice, ph->st));
+    D2G_CUDA(ph->vnorm.alloc(ph->vocab_size));
+    D2G_CUDA(launch_vocab_norms(ph->vocab32.p, ph->vocab_size, ph->dim, ph->vnorm.p, ph->st));
+    ph->h_sym.assign(d->p_supp_sym, d->p_supp_sym + ph->col);
+    D2G_CUDA(cudaStreamSynchronize(ph->st));
+  } else if (!euc) {  // histogram cost table: row v = cost from bin v to every centroid bin
     const int V = ph->vocab_size;
     std::vector<float> t((size_t)V * ph->MP, 0.f);
     for (int v = 0; v < V; ++v)
@@ -429,6 +481,18 @@ static int create_batched(d2g_phase *ph, const d2g_phase_desc *d) {
   D2G_CUDA(ph->resid_part.alloc((size_t)ph->total_blocks * 4));
   D2G_CUDA(ph->rho_part.alloc(ph->total_blocks));
   D2G_CUDA(ph->reinit.alloc(ph->size));
+  if (ph->metric == D2_WORD_EMBED) {
+    const size_t KV = (size_t)ph->K * d->vocab_size;
+    D2G_CUDA(ph->ctab.alloc(KV * ph->MP));
+    D2G_CUDA(cudaMemsetAsync(ph->ctab.p, 0, KV * ph->MP * 4, ph->st));  // padded rows stay 0
+    D2G_CUDA(ph->W.alloc(KV * ph->MP));
+    D2G_CUDA(ph->Xp.alloc(nz));
+    D2G_CUDA(ph->cnorm.alloc((size_t)ph->K * ph->str));
+    D2G_CUDA(ph->cs32f.alloc((size_t)ph->K * ph->str * d->dim));
+    ph->enchunk = std::max(1, std::min(64, (d->vocab_size + 511) / 512));
+    ph->echunk = (d->vocab_size + ph->enchunk - 1) / ph->enchunk;
+    D2G_CUDA(ph->epart.alloc((size_t)ph->enchunk * ph->K * ph->MP * (d->dim + 1)));
+  }
 
   int rc2 = upload_columns_batched(ph, d);
   if (rc2) return rc2;
@@ -437,8 +501,11 @@ static int create_batched(d2g_phase *ph, const d2g_phase_desc *d) {
   PlanArgs base = base_args(ph);
   ph->smem_plan = plan_smem_bytes(ph->MP, 0, 1);
   ph->smem_plan_upd = plan_smem_bytes(ph->MP, euc ? ph->dim : 0, 1);
-  // raise the shared-memory limits of the plan kernels before any stream capture
-  for (int cs = 1; cs <= 2; ++cs) {
+  // raise the shared-memory limits and size the persistent grids of the plan
+  // kernels for every cluster size in use, before any stream capture
+  std::vector<int> sizes = {1};
+  for (auto &b : ph->buckets) sizes.push_back(b.cs);
+  for (int cs : sizes) {
     PlanArgs a = base;
     a.cs = cs;
     for (int chk = 0; chk < 2; ++chk)
@@ -572,7 +639,8 @@ static std::vector<unsigned long long> loop_signature(d2g_phase *ph) {
   auto u = [](const void *p) { return (unsigned long long)(uintptr_t)p; };
   return {u(ph->part.p), u(ph->trace.p), u(ph->Xp.p), u(ph->cl_ptr.p), u(ph->cl_plans.p),
           u(ph->cw64.p), u(ph->cs64.p), u(ph->ctl.p), u(ph->resid_part.p), u(ph->ctab.p),
-          u(ph->grp_rec.p), u(ph->plan_slot.p),
+          u(ph->grp_rec.p), u(ph->plan_slot.p), u(ph->pair_key.p), u(ph->pair_ptr.p),
+          u(ph->occ_col.p), (unsigned long long)ph->npairs,
           (unsigned long long)ph->nchunk, (unsigned long long)ph->chunk,
           (unsigned long long)ph->global_size};
 }
@@ -581,6 +649,33 @@ static bool has_collision(int maxIters, int upl) {
   for (int it = 0; it <= maxIters; ++it)
     if (it % upl == 0 && is_check_iter(it)) return true;
   return false;
+}
+
+static EmbedArgs embed_args(d2g_phase *ph, int iter) {
+  EmbedArgs e{};
+  e.pair_key = ph->pair_key.p;
+  e.pair_ptr = ph->pair_ptr.p;
+  e.occ_col = ph->occ_col.p;
+  e.npairs = ph->npairs;
+  e.X = ph->Xp.p;
+  e.W = ph->W.p;
+  e.vocab = ph->vocab32.p;
+  e.vnorm = ph->vnorm.p;
+  e.cnorm = ph->cnorm.p;
+  e.part = ph->epart.p;
+  e.nchunk = ph->enchunk;
+  e.chunk = ph->echunk;
+  e.cs64 = ph->cs64.p;
+  e.cs32f = ph->cs32f.p;
+  e.T = ph->ctab.p;
+  e.ctl = ph->ctl.p;
+  e.iter = iter;
+  e.K = ph->K;
+  e.m = ph->str;
+  e.MP = ph->MP;
+  e.V = ph->vocab_size;
+  e.d = ph->dim;
+  return e;
 }
 
 // ------------------------------------------------------------- the loop
@@ -596,7 +691,8 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
       const bool upd = (it % upl == 0) && (euc || emb);
       const bool chk = is_check_iter(it);
       const bool collide = upd && chk;
-      int flags = (upd && euc ? PF_UPDATE : 0) | (chk ? PF_CHECK : 0) | (collide ? PF_WRITE_X : 0);
+      int flags = (upd && euc ? PF_UPDATE : 0) | (chk ? PF_CHECK : 0) |
+                  ((collide || (upd && emb)) ? PF_WRITE_X : 0);
       if (profile) {
         cudaEvent_t a, b;
         cudaEventCreate(&a);
@@ -616,6 +712,10 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
       if (profile) cudaEventRecord(evs.back(), ph->st);
       D2G_CUDA(launch_cluster_reduce(cluster_args(ph, it, upd && euc), ph->st));
       nl += 2;
+      if (upd && emb) {  // step 5 for word embeddings, then the new cost table
+        D2G_CUDA(launch_embed_support(embed_args(ph, it), ph->st));
+        nl += 6;
+      }
       if (collide) {
         for (auto &b : ph->buckets) {
           PlanArgs a = bucket_args(ph, base, b);
@@ -721,6 +821,12 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
   if (ph->path == 0) {
     D2G_CUDA(launch_centroid_to_f32(ph->cw64.p, euc ? ph->cs64.p : nullptr, ph->cw32.p,
                                     euc ? ph->cs32.p : nullptr, K, m, dim, ph->MP, ph->DS, ph->st));
+    if (emb) {  // the cost table of the initial centroids
+      D2G_CUDA(launch_to_f32(ph->cs64.p, (size_t)K * m * dim, ph->cs32f.p, ph->st));
+      D2G_CUDA(launch_cost_table(ph->cs32f.p, K, m, ph->vocab32.p, ph->vocab_size, dim, ph->cnorm.p,
+                                 ph->vnorm.p, ph->MP, ph->ctab.p, ph->st));
+      launches += 3;
+    }
     PlanArgs base = base_args(ph);
     for (auto &b : ph->buckets) {
       PlanArgs a = bucket_args(ph, base, b);
@@ -800,6 +906,7 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
   {
     const double ent = (double)ph->col * m;
     const double colb = ph->path == 0 ? (double)ph->col * (euc ? 4.0 * (1 + dim) : 8.0) : 0.0;
+    // (table-mode costs are read from an L2-resident table and are not counted as HBM bytes)
     ph->stats.plan_bytes = ph->path == 0 ? 16.0 * ent + colb + 4.0 * m * (double)n : 136.0 * ent;
   }
   if (h.err) return fail(D2G_E_NUMERIC, "non-positive or non-finite normaliser (device code " +

@@ -171,6 +171,29 @@ struct ServeArgs {
 cudaError_t launch_serve(int MP, const ServeArgs &a, int nitems, cudaStream_t st);
 constexpr int serve_groups_per_cta(int MP) { return 1024 / MP; }  // 256 threads, 4 rows x 4 columns
 
+// embed_kernels.cu (word-embedding phase, batched form)
+struct EmbedArgs {
+  const int *pair_key, *pair_ptr, *occ_col;  // occupied (cluster, token) pairs and their columns
+  int npairs;
+  const float *X;        // packed X of the update iteration
+  float *W;              // [K][V][MP]
+  const float *vocab;    // [V][d]
+  const float *vnorm;    // [V]
+  float *cnorm;          // [K*m]
+  float *part;           // [nchunk][K][MP][d+1]
+  int nchunk, chunk;
+  double *cs64;          // [K*m*d]
+  float *cs32f;          // [K*m*d] row-major copy for the cost table
+  float *T;              // [K][V][MP] cost table
+  Ctl *ctl;
+  int iter, K, m, MP, V, d;
+};
+cudaError_t launch_cost_table(const float *cs, int K, int m, const float *vocab, int V, int d,
+                              float *cnorm, const float *vnorm, int MP, float *T, cudaStream_t st);
+cudaError_t launch_vocab_norms(const float *vocab, int V, int d, float *vnorm, cudaStream_t st);
+cudaError_t launch_to_f32(const double *a, size_t n, float *b, cudaStream_t st);
+cudaError_t launch_embed_support(const EmbedArgs &e, cudaStream_t st);
+
 // d2g_host.cu
 int distmat_fp64(int dim, int str, size_t size, const int *p_str, int metric, const double *supp,
                  const int *sym, const double *vocab, int V, const int *label, const double *c_supp,

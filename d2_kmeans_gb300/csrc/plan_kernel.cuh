@@ -721,7 +721,9 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
   int4 *stR = (int4 *)(smem + 4 * TILE);              // [2][G] group records
   float *stW = (float *)(stR + 2 * G);                // [2][JC] weights
   float *stC = stW + 2 * JC;                          // [2][JC*CW] supports / table rows
-  float *sm_rs = stC + 2 * JC * CW;                   // [G][MP] row partials, then plan totals
+  float *sm_x = stC + 2 * JC * CW;                    // [2][8][MP] cluster: every rank's row totals
+  float *sm_momx = sm_x + 2 * 8 * MP;                 // [2][dim+1][MP] cluster: this CTA's moments
+  float *sm_rs = sm_momx + 2 * (a.dim + 1) * MP;      // [G][MP] row partials, then plan totals
   float *sm_mom = sm_rs + G * MP;                     // [dim+1][G][MP]
   __shared__ __align__(8) unsigned long long mbar[2];
   __shared__ int sh_fail;
@@ -729,13 +731,18 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
 
   if (a.iter >= a.ctl->stop_iter) return;
   const int tid = threadIdx.x;
+  // A plan wider than one CTA is an item of a cluster of CS CTAs; every CTA
+  // of the cluster works on its own slice (rank) of the same item.
+  const int CS = a.cs;
+  const int rank = blockIdx.x % CS, cl_id = blockIdx.x / CS, ncl = gridDim.x / CS;
   if (a.iter == 0 && a.resid_off == 0 && blockIdx.x == 0 && tid == 0) a.ctl->t_start_ns = global_ns();
-  // one stage = the item's Z and Y tiles, group records, weights and supports
+  // one stage = the slice's Z and Y tiles, group records, weights and supports
   auto issue = [&](int g0, int ng, int stg) {
     const size_t off = (size_t)g0 * S * MP;
     const unsigned bytes = (unsigned)ng * S * MP * 4u;
     const unsigned rb = (unsigned)ng * 16u, wb = (unsigned)ng * S * 4u, cb = wb * CW;
     mbar_expect_tx(&mbar[stg], 2u * bytes + rb + wb + cb);
+    if (ng <= 0) return;  // an empty slice: the phase completes on the arrival alone
     bulk_load(stZ + stg * TILE, a.Z + off, bytes, &mbar[stg]);
     bulk_load(stY + stg * TILE, a.Y + off, bytes, &mbar[stg]);
     bulk_load(stR + stg * G, a.grp_rec + g0, rb, &mbar[stg]);
@@ -745,23 +752,25 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
     else
       bulk_load(stC + stg * JC * CW, a.col_sym + (size_t)g0 * S, cb, &mbar[stg]);
   };
-  // thread 0 keeps the bounds of the next item in registers, loaded one item early
+  auto slice = [&](int item, int &g0, int &ng) {
+    g0 = a.item_g0[item] + rank * G;
+    ng = min(G, a.item_ng[item] - rank * G);
+    if (ng < 0) ng = 0;
+  };
+  // thread 0 keeps the bounds of the next slice in registers, loaded one item early
   int nx_g0 = 0, nx_ng = 0;
   if (tid == 0) {
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
     sh_fail = 0;
     mbar_fence_init();
-    if ((int)blockIdx.x < nitems) {
-      const int g0 = a.item_g0[blockIdx.x], ng = a.item_ng[blockIdx.x];
+    if (cl_id < nitems) {
+      int g0, ng;
+      slice(cl_id, g0, ng);
       sh_g0[0] = g0;
       sh_ng[0] = ng;
       issue(g0, ng, 0);
-      const int nx = blockIdx.x + gridDim.x;
-      if (nx < nitems) {
-        nx_g0 = a.item_g0[nx];
-        nx_ng = a.item_ng[nx];
-      }
+      if (cl_id + ncl < nitems) slice(cl_id + ncl, nx_g0, nx_ng);
     }
   }
   __syncthreads();
@@ -773,28 +782,24 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
   const bool write_x = a.flags & PF_WRITE_X;
   double s_obj = 0.0, s_pr = 0.0, s_dr = 0.0;  // FP64 across items, FP32 within one item
   int it = 0;
-  for (int item = blockIdx.x; item < nitems; item += gridDim.x, ++it) {
+  for (int item = cl_id; item < nitems; item += ncl, ++it) {
     const int stg = it & 1;
     if (!mbar_wait(&mbar[stg], (it >> 1) & 1)) sh_fail = 1;
     __syncthreads();
     if (sh_fail) break;
     const int cur_g0 = sh_g0[stg], cur_ng = sh_ng[stg];
-    if (tid == 0 && item + (int)gridDim.x < nitems) {
+    if (tid == 0 && item + ncl < nitems) {
       issue(nx_g0, nx_ng, stg ^ 1);
       sh_g0[stg ^ 1] = nx_g0;
       sh_ng[stg ^ 1] = nx_ng;
-      const int nx = item + 2 * (int)gridDim.x;
-      if (nx < nitems) {
-        nx_g0 = a.item_g0[nx];
-        nx_ng = a.item_ng[nx];
-      }
+      if (item + 2 * ncl < nitems) slice(item + 2 * ncl, nx_g0, nx_ng);
     }
 
     T t;
     t.init_rec(stR[stg * G + (threadIdx.x / TPC)], cur_g0, cur_ng);
     t.load_costs_staged(a, stC + stg * JC * CW, (const int *)(stC + stg * JC * CW));
     const float *zs = stZ + stg * TILE, *ys = stY + stg * TILE;
-    const int lcol0 = t.g * S;  // the thread's first column within the item
+    const int lcol0 = t.g * S;  // the thread's first column within the slice
     float x[S][RPT], zp[S][RPT], w[S];
 #pragma unroll
     for (int s = 0; s < S; ++s) w[s] = s < t.nvalid ? stW[stg * JC + lcol0 + s] : 0.f;
@@ -864,46 +869,114 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
     }
     __syncthreads();
 
-    // the plan's first group sums the plan's partials once and publishes the total
-    const int lo = t.active ? t.pl_g0 - t.cta_g0 : 0;
-    const bool writer = t.active && t.g == lo;
-    if (writer) {
-      float tot[RPT];
+    float tot[RPT];
+    bool writer;
+    const bool upd_euc = T::EUC && update;
+    if (CS == 1) {
+      // the plan's first group sums the plan's partials once and publishes the total
+      const int lo = t.active ? t.pl_g0 - t.cta_g0 : 0;
+      writer = t.active && t.g == lo;
+      if (writer) {
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) tot[q] = 0.f;
+        for (int j = lo; j < lo + t.pl_ng; ++j) {
+#pragma unroll
+          for (int q4 = 0; q4 < RPT / 4; ++q4) {
+            const float4 u = *((const float4 *)(sm_rs + j * MP + t.k0) + q4);
+            tot[4 * q4] += u.x;
+            tot[4 * q4 + 1] += u.y;
+            tot[4 * q4 + 2] += u.z;
+            tot[4 * q4 + 3] += u.w;
+          }
+        }
+        st_rows_sm(sm_rs + lo * MP + t.k0, tot);
+        if (upd_euc) {
+          float *xo = a.xmom_out + (size_t)t.p * (a.dim + 1) * MP;
+          for (int d = 0; d <= a.dim; ++d) {
+            float mv[RPT];
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) mv[q] = 0.f;
+            for (int j = lo; j < lo + t.pl_ng; ++j)
+#pragma unroll
+              for (int q = 0; q < RPT; ++q) mv[q] += sm_mom[(d * G + j) * MP + t.k0 + q];
+            st_rows(xo + d * MP + t.k0, mv);
+          }
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int q4 = 0; q4 < RPT / 4; ++q4) {
+        const float4 u = *((const float4 *)(sm_rs + lo * MP + t.k0) + q4);
+        tot[4 * q4] = u.x;
+        tot[4 * q4 + 1] = u.y;
+        tot[4 * q4 + 2] = u.z;
+        tot[4 * q4 + 3] = u.w;
+      }
+    } else {
+      // one plan across the cluster: this CTA's partial is pushed into every
+      // rank's shared memory (double-buffered by stage), one cluster barrier,
+      // then every rank adds the CS partials from its own shared memory
+      cg::cluster_group cl = cg::this_cluster();
+      writer = rank == 0 && t.g == 0 && t.active;
+      if (t.g == 0) {
+        float pt[RPT];
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) pt[q] = 0.f;
+        for (int j = 0; j < cur_ng; ++j) {
+#pragma unroll
+          for (int q4 = 0; q4 < RPT / 4; ++q4) {
+            const float4 u = *((const float4 *)(sm_rs + j * MP + t.k0) + q4);
+            pt[4 * q4] += u.x;
+            pt[4 * q4 + 1] += u.y;
+            pt[4 * q4 + 2] += u.z;
+            pt[4 * q4 + 3] += u.w;
+          }
+        }
+        for (int rk = 0; rk < CS; ++rk) {
+          float *dst = cl.map_shared_rank(sm_x + (stg * 8 + rank) * MP, rk) + t.k0;
+#pragma unroll
+          for (int q4 = 0; q4 < RPT / 4; ++q4)
+            ((float4 *)dst)[q4] = make_float4(pt[4 * q4], pt[4 * q4 + 1], pt[4 * q4 + 2], pt[4 * q4 + 3]);
+        }
+        if (upd_euc) {
+          for (int d = 0; d <= a.dim; ++d) {
+            float mv[RPT];
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) mv[q] = 0.f;
+            for (int j = 0; j < cur_ng; ++j)
+#pragma unroll
+              for (int q = 0; q < RPT; ++q) mv[q] += sm_mom[(d * G + j) * MP + t.k0 + q];
+            st_rows_sm(sm_momx + (stg * (a.dim + 1) + d) * MP + t.k0, mv);
+          }
+        }
+      }
+      cl.sync();
 #pragma unroll
       for (int q = 0; q < RPT; ++q) tot[q] = 0.f;
-      for (int j = lo; j < lo + t.pl_ng; ++j) {
+      for (int rk = 0; rk < CS; ++rk) {
 #pragma unroll
         for (int q4 = 0; q4 < RPT / 4; ++q4) {
-          const float4 u = *((const float4 *)(sm_rs + j * MP + t.k0) + q4);
+          const float4 u = *((const float4 *)(sm_x + (stg * 8 + rk) * MP + t.k0) + q4);
           tot[4 * q4] += u.x;
           tot[4 * q4 + 1] += u.y;
           tot[4 * q4 + 2] += u.z;
           tot[4 * q4 + 3] += u.w;
         }
       }
-      st_rows_sm(sm_rs + lo * MP + t.k0, tot);
-      if (T::EUC && update) {
+      if (writer && upd_euc) {  // moments: pulled from the ranks on update iterations only
         float *xo = a.xmom_out + (size_t)t.p * (a.dim + 1) * MP;
         for (int d = 0; d <= a.dim; ++d) {
           float mv[RPT];
 #pragma unroll
           for (int q = 0; q < RPT; ++q) mv[q] = 0.f;
-          for (int j = lo; j < lo + t.pl_ng; ++j)
+          for (int rk = 0; rk < CS; ++rk) {
+            const float *rem = cl.map_shared_rank(sm_momx + (stg * (a.dim + 1) + d) * MP, rk);
 #pragma unroll
-            for (int q = 0; q < RPT; ++q) mv[q] += sm_mom[(d * G + j) * MP + t.k0 + q];
+            for (int q = 0; q < RPT; ++q) mv[q] += rem[t.k0 + q];
+          }
           st_rows(xo + d * MP + t.k0, mv);
         }
       }
-    }
-    __syncthreads();
-    float tot[RPT];
-#pragma unroll
-    for (int q4 = 0; q4 < RPT / 4; ++q4) {
-      const float4 u = *((const float4 *)(sm_rs + lo * MP + t.k0) + q4);
-      tot[4 * q4] = u.x;
-      tot[4 * q4 + 1] = u.y;
-      tot[4 * q4 + 2] = u.z;
-      tot[4 * q4 + 3] = u.w;
     }
     float rsum = 0.f;  // step 4's per-instance normalisation of Zr (:180); t.p is the slot here
 #pragma unroll
@@ -967,6 +1040,9 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
     }
     __syncthreads();  // the stage and the row partials are free again
   }
+  // rank 0 may still be reading a peer's shared memory (the moments of the
+  // last item): no CTA of a cluster leaves before all of them are done
+  if (CS > 1 && !sh_fail) cg::this_cluster().sync();
   if (sh_fail) {
     if (tid == 0) {
       a.ctl->err = 7;  // a bulk copy did not complete: let the copies in flight land first
@@ -976,16 +1052,16 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
     return;
   }
   if constexpr (CHECK) {
-    // one partial per CTA in the slot of its first item; its other items' slots get zeros
+    // one partial per CTA in the slot of its first (item, rank); its other slots get zeros
     __shared__ double res[3];
     block_sum3<kThreads>(s_obj, s_pr, s_dr, res);
-    if (tid == 0) {
-      double *pp = a.resid_part + (size_t)(a.resid_off + blockIdx.x) * 4;
+    if (tid == 0 && cl_id < nitems) {
+      double *pp = a.resid_part + (size_t)(a.resid_off + cl_id * CS + rank) * 4;
       pp[0] = res[0];
       pp[1] = res[1];
       pp[2] = res[2];
-      for (int item = blockIdx.x + gridDim.x; item < nitems; item += gridDim.x) {
-        double *qq = a.resid_part + (size_t)(a.resid_off + item) * 4;
+      for (int item = cl_id + ncl; item < nitems; item += ncl) {
+        double *qq = a.resid_part + (size_t)(a.resid_off + item * CS + rank) * 4;
         qq[0] = qq[1] = qq[2] = 0.0;
       }
     }
@@ -1012,34 +1088,55 @@ static inline cudaLaunchConfig_t plan_cfg(int nblocks, size_t smem, cudaStream_t
 
 template <int MP, int MODE, bool CHECK, bool FULL>
 cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaStream_t st) {
-  static int grid = 0;  // CTAs resident at once (persistent grid)
+  // persistent grid: as many clusters of a.cs CTAs as are resident at once
+  static int grid[kMaxCluster + 1] = {0};
   constexpr int JC = GeoT<MP>::G * kS;
   constexpr int CW = MODE == COST_EUCLID8 ? 8 : (MODE == COST_EUCLID4 ? 4 : 1);
   const size_t sm = smem + (size_t)4 * tma_tile_floats<MP>() * sizeof(float) +
-                    2 * (size_t)GeoT<MP>::G * 16 + 2 * (size_t)JC * 4 * (1 + CW);
+                    2 * (size_t)GeoT<MP>::G * 16 + 2 * (size_t)JC * 4 * (1 + CW) +
+                    (size_t)2 * 8 * MP * 4 + (size_t)2 * (a.dim + 1) * MP * 4;
   static size_t configured_smem = 0;
+  static bool nonportable = false;
+  auto kern = plan_kernel_tma<MP, MODE, CHECK, FULL>;
   if (configured_smem < sm) {
-    cudaError_t e = cudaFuncSetAttribute(plan_kernel_tma<MP, MODE, CHECK, FULL>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    int dev = 0, nsm = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, plan_kernel_tma<MP, MODE, CHECK, FULL>,
-                                                      kThreads, sm);
-    if (e != cudaSuccess) return e;
-    grid = nsm * (per > 0 ? per : 1);
+    for (int c = 0; c <= kMaxCluster; ++c) grid[c] = 0;
     configured_smem = sm;
   }
+  (void)nonportable;
+  const int cs = a.cs;
+  if (grid[cs] == 0) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cs * 1024, 1, 1);
+    cfg.blockDim = dim3(kThreads, 1, 1);
+    cfg.dynamicSmemBytes = sm;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int ncl = 0;
+    cudaError_t e = cudaOccupancyMaxActiveClusters(&ncl, kern, &cfg);
+    if (e != cudaSuccess) return e;
+    grid[cs] = (ncl > 0 ? ncl : 1) * cs;
+  }
   if (nitems <= 0) return cudaSuccess;
-  const int g = nitems < grid ? nitems : grid;
-  plan_kernel_tma<MP, MODE, CHECK, FULL><<<g, kThreads, sm, st>>>(a, nitems);
-  return cudaGetLastError();
+  const int g = (nitems * cs < grid[cs]) ? nitems * cs : grid[cs];
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = plan_cfg(g, sm, st, attr, cs);
+  if (cs == 1) {  // a cluster of one CTA: plain launch
+    cfg.attrs = nullptr;
+    cfg.numAttrs = 0;
+  }
+  return cudaLaunchKernelEx(&cfg, kern, a, nitems);
 }
 
 template <int MP, int MODE, bool CHECK>
 cudaError_t launch_plan_t(const PlanArgs &a, int nitems, size_t smem, cudaStream_t st) {
-  if (a.cs == 1 && a.use_tma) {
+  if (a.use_tma) {
     if (a.m == MP) return launch_plan_tma_t<MP, MODE, CHECK, true>(a, nitems, smem, st);
     return launch_plan_tma_t<MP, MODE, CHECK, false>(a, nitems, smem, st);
   }
