@@ -30,7 +30,7 @@ def _arr(a, dtype):
 
 def set_config(**kw) -> dict:
     """Update the library configuration (precision, verbose, use_graph,
-    sync_scratch, profile); returns the previous values."""
+    sync_scratch, profile, cost_gemm); returns the previous values."""
     lib = L.load()
     cfg = L.d2g_config()
     L.check(lib.d2g_get_config(C.byref(cfg)), "d2g_get_config")

@@ -34,7 +34,7 @@ static int fail(int code, const std::string &msg) {
 }
 
 std::mutex g_cfg_mu;
-d2g_config g_cfg = {0, 1, 1, 0, 0};
+d2g_config g_cfg = {0, 1, 1, 0, 0, 0};
 d2g_config cfg_snapshot() {
   std::lock_guard<std::mutex> lk(g_cfg_mu);
   return g_cfg;
@@ -82,6 +82,7 @@ struct d2g_phase {
   int metric = 0, dim = 0, str = 0, K = 0, vocab_size = 0;
   size_t size = 0, col = 0, global_size = 0;
   int path = 0;  // 0 batched FP32, 1 plain FP64
+  int cost_gemm = 0;  // word-embedding cost table: 0 tensor cores, 1 CUDA cores (per run)
   std::vector<int> p_str, label;
   std::vector<long long> cum;
   cudaStream_t st = nullptr;
@@ -642,7 +643,7 @@ static std::vector<unsigned long long> loop_signature(d2g_phase *ph) {
           u(ph->grp_rec.p), u(ph->plan_slot.p), u(ph->pair_key.p), u(ph->pair_ptr.p),
           u(ph->occ_col.p), (unsigned long long)ph->npairs,
           (unsigned long long)ph->nchunk, (unsigned long long)ph->chunk,
-          (unsigned long long)ph->global_size};
+          (unsigned long long)ph->global_size, (unsigned long long)ph->cost_gemm};
 }
 
 static bool has_collision(int maxIters, int upl) {
@@ -675,6 +676,7 @@ static EmbedArgs embed_args(d2g_phase *ph, int iter) {
   e.MP = ph->MP;
   e.V = ph->vocab_size;
   e.d = ph->dim;
+  e.gemm = ph->cost_gemm;
   return e;
 }
 
@@ -777,6 +779,7 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
 static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, double *c_supp,
                     const char *label_switch) {
   const d2g_config cfg = cfg_snapshot();
+  ph->cost_gemm = cfg.cost_gemm;
   if (!opt || opt->maxIters < 0 || opt->updatePerLoops <= 0 || !(opt->rhoCoeff > 0) || !c_w)
     return fail(D2G_E_INVAL, "bad B-ADMM options");
   const bool euc = ph->metric == D2_EUCLIDEAN_L2, emb = ph->metric == D2_WORD_EMBED;
@@ -824,7 +827,8 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
     if (emb) {  // the cost table of the initial centroids
       D2G_CUDA(launch_to_f32(ph->cs64.p, (size_t)K * m * dim, ph->cs32f.p, ph->st));
       D2G_CUDA(launch_cost_table(ph->cs32f.p, K, m, ph->vocab32.p, ph->vocab_size, dim, ph->cnorm.p,
-                                 ph->vnorm.p, ph->MP, ph->ctab.p, ph->st));
+                                 ph->vnorm.p, ph->MP, ph->ctab.p, ph->cost_gemm, &ph->ctl.p->err,
+                                 ph->st));
       launches += 3;
     }
     PlanArgs base = base_args(ph);
@@ -909,6 +913,8 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
     // (table-mode costs are read from an L2-resident table and are not counted as HBM bytes)
     ph->stats.plan_bytes = ph->path == 0 ? 16.0 * ent + colb + 4.0 * m * (double)n : 136.0 * ent;
   }
+  if (h.err == kErrTcTimeout)
+    return fail(D2G_E_CUDA, "tensor-core cost table: wait for the MMA completion timed out");
   if (h.err) return fail(D2G_E_NUMERIC, "non-positive or non-finite normaliser (device code " +
                                             std::to_string(h.err) + ")");
   return D2G_OK;
@@ -994,7 +1000,8 @@ int d2g_get_config(d2g_config *cfg) {
 }
 
 int d2g_set_config(const d2g_config *cfg) {
-  if (!cfg || cfg->precision < 0 || cfg->precision > 1) return D2G_E_INVAL;
+  if (!cfg || cfg->precision < 0 || cfg->precision > 1 || cfg->cost_gemm < 0 || cfg->cost_gemm > 1)
+    return D2G_E_INVAL;
   std::lock_guard<std::mutex> lk(g_cfg_mu);
   g_cfg = *cfg;
   return D2G_OK;

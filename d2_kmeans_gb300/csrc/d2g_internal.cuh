@@ -187,9 +187,16 @@ struct EmbedArgs {
   float *T;              // [K][V][MP] cost table
   Ctl *ctl;
   int iter, K, m, MP, V, d;
+  int gemm;              // cost table: 0 tensor cores (3xTF32), 1 FP32 CUDA cores
 };
+// Ctl::err value of a tensor-core wait that ran out
+constexpr int kErrTcTimeout = 3;
 cudaError_t launch_cost_table(const float *cs, int K, int m, const float *vocab, int V, int d,
-                              float *cnorm, const float *vnorm, int MP, float *T, cudaStream_t st);
+                              float *cnorm, const float *vnorm, int MP, float *T, int gemm,
+                              int *err, cudaStream_t st);
+cudaError_t launch_cost_table_tc(const float *cs, int nrows, const float *vocab, int V, int d,
+                                 const float *cnorm, const float *vnorm, int m, int MP, float *T,
+                                 int *err, cudaStream_t st);
 cudaError_t launch_vocab_norms(const float *vocab, int V, int d, float *vnorm, cudaStream_t st);
 cudaError_t launch_to_f32(const double *a, size_t n, float *b, cudaStream_t st);
 cudaError_t launch_embed_support(const EmbedArgs &e, cudaStream_t st);

@@ -183,10 +183,11 @@ __global__ void to_f32_kernel(const double *__restrict__ a, size_t n, float *__r
 }
 
 cudaError_t launch_cost_table(const float *cs, int K, int m, const float *vocab, int V, int d,
-                              float *cnorm, const float *vnorm, int MP, float *T,
-                              cudaStream_t st) {
+                              float *cnorm, const float *vnorm, int MP, float *T, int gemm,
+                              int *err, cudaStream_t st) {
   const int nrows = K * m;
   row_norms_kernel<<<(nrows + 255) / 256, 256, 0, st>>>(cs, nrows, d, cnorm);
+  if (gemm == 0) return launch_cost_table_tc(cs, nrows, vocab, V, d, cnorm, vnorm, m, MP, T, err, st);
   dim3 grid((V + kTile - 1) / kTile, (nrows + kTile - 1) / kTile);
   cost_table_kernel<<<grid, 256, 0, st>>>(cs, nrows, vocab, V, d, cnorm, vnorm, m, MP, T);
   return cudaGetLastError();
@@ -214,7 +215,8 @@ cudaError_t launch_embed_support(const EmbedArgs &e, cudaStream_t st) {
                                             e.ctl, e.iter);
   err = cudaGetLastError();
   if (err != cudaSuccess) return err;
-  return launch_cost_table(e.cs32f, e.K, e.m, e.vocab, e.V, e.d, e.cnorm, e.vnorm, e.MP, e.T, st);
+  return launch_cost_table(e.cs32f, e.K, e.m, e.vocab, e.V, e.d, e.cnorm, e.vnorm, e.MP, e.T, e.gemm,
+                           &e.ctl->err, st);
 }
 
 }  // namespace d2g

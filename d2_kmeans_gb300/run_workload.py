@@ -5,7 +5,9 @@
 Workloads (d2_kmeans_gb300.synth.workload): plain, batched, hist,
 twophase_euclid, embed.  --scale shrinks the number of instances only;
 --iters sets maxIters (the loop runs maxIters+1 iterations); --precision 1
-selects the FP64 form.  Prints the run statistics as one JSON line.
+selects the FP64 form; --cost-gemm 1 computes the word-embedding cost table
+on FP32 CUDA cores instead of the tensor cores.  Prints the run statistics
+as one JSON line.
 
     python -m d2_kmeans_gb300.run_workload --workload serve --requests 64
 
@@ -29,8 +31,9 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--requests", type=int, default=64)
+    ap.add_argument("--cost-gemm", type=int, default=0)
     args = ap.parse_args(argv)
-    badmm.set_config(verbose=0)
+    badmm.set_config(verbose=0, cost_gemm=args.cost_gemm)
     if args.workload == "serve":
         import time
 

@@ -176,6 +176,8 @@ typedef struct {
   int use_graph;    /* 1: replay the iteration loop as one CUDA graph (default) */
   int sync_scratch; /* 1: also write the host X, Y and C back after a drop-in call */
   int profile;      /* 1: time every plan-update launch with CUDA events (no graph) */
+  int cost_gemm;    /* word-embedding cost table: 0 tensor cores, 3xTF32 (default);
+                       1 FP32 CUDA cores */
 } d2g_config;
 
 int d2g_get_config(d2g_config *cfg);

@@ -30,7 +30,7 @@ def d2g():
     from d2_kmeans_gb300.build import build as build_lib
     from d2_kmeans_gb300 import badmm
     build_lib()
-    badmm.set_config(verbose=0, precision=0, use_graph=1, profile=0, sync_scratch=0)
+    badmm.set_config(verbose=0, precision=0, use_graph=1, profile=0, sync_scratch=0, cost_gemm=0)
     return badmm
 
 

@@ -59,7 +59,7 @@ def test_error_strings_and_config_roundtrip(lib):
         assert lib.d2g_error_string(code)
     cfg = L.d2g_config()
     assert lib.d2g_get_config(C.byref(cfg)) == 0
-    bad = L.d2g_config(7, 1, 1, 0, 0)
+    bad = L.d2g_config(7, 1, 1, 0, 0, 0)
     assert lib.d2g_set_config(C.byref(bad)) == L.D2G_E_INVAL
     assert lib.d2g_set_config(C.byref(cfg)) == 0
 

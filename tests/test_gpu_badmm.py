@@ -216,18 +216,45 @@ def test_repeated_runs_reuse_the_graph(d2g):
     P.close()
 
 
+@pytest.mark.parametrize("gemm", [0, 1], ids=["tcgen05_3xtf32", "fp32_cuda_cores"])
 @pytest.mark.parametrize("n,k,m,V,dim,sizes,seed", [
     (60, 3, 8, 300, 12, (3, 25), 61),       # small: several plans per CTA
     (120, 4, 64, 2000, 300, (20, 400), 62),  # the embedding workload's shape: d=300, m=64, plans up to 400 wide
+    (80, 5, 24, 517, 13, (5, 60), 63),      # ragged: d % 4 != 0, k*m and V not multiples of the 128 x 256 tile
 ])
-def test_word_embedding_batched(d2g, oracle_mod, n, k, m, V, dim, sizes, seed):
-    """Cost table T[l][v][k] from a (k*m) x V x d contraction, support update from the
-    stored X through per-(cluster, token) occurrence lists."""
+def test_word_embedding_batched(d2g, oracle_mod, gemm, n, k, m, V, dim, sizes, seed):
+    """Cost table T[l][v][k] from a (k*m) x V x d contraction (tensor cores in
+    3xTF32, or FP32 CUDA cores), support update from the stored X through
+    per-(cluster, token) occurrence lists."""
     ph, c = synth.embed_phase(n, k, m, V=V, dim=dim, sizes=sizes, seed=seed)
     opts = dict(maxIters=30, rhoCoeff=2.0, updatePerLoops=10)
     ref = _port(oracle_mod, ph, c, opts)
-    P = d2g.Phase(ph, 0)
-    r = P.run(c, opts)
+    old = d2g.set_config(cost_gemm=gemm)
+    try:
+        P = d2g.Phase(ph, 0)
+        r = P.run(c, opts)
+    finally:
+        d2g.set_config(**old)
     assert r["stats"]["path"] == 0
     assert_close(r, ref, k, m)
     P.close()
+
+
+def test_word_embedding_cost_table_paths_agree(d2g):
+    """The tensor-core (3xTF32) and CUDA-core (FP32) cost tables give the same
+    B-ADMM run up to FP32 rounding: objectives within 2e-6 relative, centroid
+    weights within 1e-5 in L1."""
+    ph, c = synth.embed_phase(200, 6, 64, V=3000, dim=300, sizes=(20, 200), seed=64)
+    opts = dict(maxIters=40, rhoCoeff=2.0, updatePerLoops=10)
+    out = []
+    for gemm in (0, 1):
+        old = d2g.set_config(cost_gemm=gemm)
+        try:
+            P = d2g.Phase(ph, 0)
+            out.append(P.run(c, opts))
+            P.close()
+        finally:
+            d2g.set_config(**old)
+    a, b = out
+    np.testing.assert_allclose(a["trace"][:, 1], b["trace"][:, 1], rtol=2e-6)
+    assert np.abs(a["c_w"] - b["c_w"]).sum() <= 1e-5 * 6
