@@ -120,6 +120,13 @@ struct d2g_phase {
   DBuf<double> resid_part, rho_part;
   size_t smem_plan = 0, smem_plan_upd = 0;
   int use_tma = 1;  // persistent TMA-pipelined kernel for single-CTA items (D2G_PLAN_KERNEL=v1 turns it off)
+  // plans wider than one CTA (packed ids wide_p0 ..): deferred row normalisation
+  int wide_p0 = 0, nwide = 0;
+  bool defer = false;
+  DBuf<float> rowpart, rowsc;
+  DBuf<int4> wide;                       // {slot, slices with columns, label, 0} per wide plan
+  DBuf<unsigned char> def_iter;          // per iteration: 1 if it ran deferred
+  std::vector<unsigned char> h_def_iter;
 
   // ---- word-embedding phase (batched form)
   std::vector<int> h_sym;  // token id per reference column
@@ -249,6 +256,8 @@ static int build_packing(d2g_phase *ph) {
     blocks += b.nitems;
     ph->buckets.push_back(b);
   }
+  ph->wide_p0 = (int)ph->plan_inst.size();
+  ph->nwide = (int)n - ph->wide_p0;
   for (int c = 2; c <= kMaxCluster; c <<= 1) {
     d2g_phase::Bucket b{c, 0, (int)h_item_g0.size(), blocks};
     for (size_t i = 0; i < n; ++i)
@@ -310,6 +319,8 @@ static PlanArgs base_args(d2g_phase *ph) {
   a.use_tma = ph->use_tma;
   a.grp_rec = ph->grp_rec.p;
   a.plan_slot = ph->plan_slot.p;
+  a.rowpart = ph->rowpart.p;
+  a.rowsc = ph->rowsc.p;
   return a;
 }
 
@@ -362,6 +373,18 @@ static int set_labels_impl(d2g_phase *ph, const int *label) {
       const int p = gplan[gi];
       ph->h_grp_rec[gi].x = slot[p];
       ph->h_grp_rec[gi].z = pl[p];
+    }
+    if (ph->nwide > 0) {  // wide plans: {slot, slices with columns, label}
+      std::vector<int4> wl(ph->nwide);
+      for (int q = 0; q < ph->nwide; ++q) {
+        const int p = ph->wide_p0 + q;
+        const int ngp = (ph->p_str[ph->plan_inst[p]] + kS - 1) / kS;
+        wl[q] = make_int4(slot[p], (ngp + ph->geo.G - 1) / ph->geo.G, pl[p], 0);
+      }
+      D2G_CUDA(ph->wide.alloc(ph->nwide));
+      D2G_CUDA(cudaMemcpyAsync(ph->wide.p, wl.data(), wl.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                               ph->st));
+      D2G_CUDA(cudaStreamSynchronize(ph->st));
     }
     if (ph->metric == D2_WORD_EMBED) {
       // occurrence lists: for each (cluster, token) the packed columns carrying it,
@@ -499,6 +522,12 @@ static int create_batched(d2g_phase *ph, const d2g_phase_desc *d) {
   if (rc2) return rc2;
   const char *pk = getenv("D2G_PLAN_KERNEL");
   ph->use_tma = !(pk && std::string(pk) == "v1");
+  const char *dx = getenv("D2G_WIDE_EXCHANGE");  // "cluster": synchronous DSMEM exchange always
+  ph->defer = ph->use_tma && ph->nwide > 0 && !(dx && std::string(dx) == "cluster");
+  if (ph->nwide > 0) {
+    D2G_CUDA(ph->rowpart.alloc((size_t)ph->nplans * kMaxCluster * ph->MP));
+    D2G_CUDA(ph->rowsc.alloc((size_t)ph->nplans * ph->MP));
+  }
   PlanArgs base = base_args(ph);
   ph->smem_plan = plan_smem_bytes(ph->MP, 0, 1);
   ph->smem_plan_upd = plan_smem_bytes(ph->MP, euc ? ph->dim : 0, 1);
@@ -643,7 +672,9 @@ static std::vector<unsigned long long> loop_signature(d2g_phase *ph) {
           u(ph->grp_rec.p), u(ph->plan_slot.p), u(ph->pair_key.p), u(ph->pair_ptr.p),
           u(ph->occ_col.p), (unsigned long long)ph->npairs,
           (unsigned long long)ph->nchunk, (unsigned long long)ph->chunk,
-          (unsigned long long)ph->global_size, (unsigned long long)ph->cost_gemm};
+          (unsigned long long)ph->global_size, (unsigned long long)ph->cost_gemm,
+          u(ph->wide.p), u(ph->def_iter.p), u(ph->rowpart.p), u(ph->rowsc.p),
+          (unsigned long long)ph->defer};
 }
 
 static bool has_collision(int maxIters, int upl) {
@@ -695,6 +726,9 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
       const bool collide = upd && chk;
       int flags = (upd && euc ? PF_UPDATE : 0) | (chk ? PF_CHECK : 0) |
                   ((collide || (upd && emb)) ? PF_WRITE_X : 0);
+      // wide plans: deferred row normalisation except on check iterations and
+      // Euclidean support updates (those exchange synchronously in a cluster)
+      const bool def = ph->h_def_iter[it] != 0, prev_def = it > 0 && ph->h_def_iter[it - 1];
       if (profile) {
         cudaEvent_t a, b;
         cudaEventCreate(&a);
@@ -707,8 +741,14 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
         PlanArgs a = bucket_args(ph, base, b);
         a.iter = it;
         a.flags = flags;
+        if (b.cs > 1) a.flags |= (def ? PF_OUT_DEF : 0) | (prev_def ? PF_IN_DEF : 0);
         D2G_CUDA(launch_plan(ph->MP, ph->mode, chk, a, b.nitems,
                              (upd && euc) ? ph->smem_plan_upd : ph->smem_plan, ph->st));
+        ++nl;
+      }
+      if (def) {
+        D2G_CUDA(launch_rowsum_combine(ph->wide.p, ph->nwide, ph->rowpart.p, ph->cw32.p, ph->MP,
+                                       ph->str, ph->rowsum.p, ph->rowsc.p, ph->ctl.p, it, ph->st));
         ++nl;
       }
       if (profile) cudaEventRecord(evs.back(), ph->st);
@@ -732,6 +772,16 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
         ++nl;
         ++chk_idx;
       }
+    }
+    if (ph->defer) {  // the scale of the last iteration that ran, if it ran deferred
+      for (auto &b : ph->buckets)
+        if (b.cs > 1) {
+          D2G_CUDA(launch_plan_finalize(ph->Z.p, ph->Y.p, ph->item_g0.p + b.item_off,
+                                        ph->item_ng.p + b.item_off, b.nitems, b.cs, ph->geo.G,
+                                        ph->MP, ph->grp_rec.p, ph->rowsc.p, ph->def_iter.p,
+                                        ph->ctl.p, ph->st));
+          ++nl;
+        }
     }
   } else {
     const unsigned nb = plain_check_blocks((long long)ph->col * ph->str);
@@ -853,6 +903,18 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
     launches += 5;
   }
 
+  // deferred-exchange schedule of the wide plans
+  ph->h_def_iter.assign((size_t)opt->maxIters + 1, 0);
+  if (ph->path == 0 && ph->defer) {
+    for (int it = 0; it <= opt->maxIters; ++it) {
+      const bool upd = (it % opt->updatePerLoops == 0) && euc;
+      ph->h_def_iter[it] = !is_check_iter(it) && !upd;
+    }
+    if (ph->def_iter.n < ph->h_def_iter.size()) D2G_CUDA(ph->def_iter.alloc(ph->h_def_iter.size()));
+    D2G_CUDA(cudaMemcpyAsync(ph->def_iter.p, ph->h_def_iter.data(), ph->h_def_iter.size(),
+                             cudaMemcpyHostToDevice, ph->st));
+    D2G_CUDA(cudaStreamSynchronize(ph->st));  // the host vector may change before the next call
+  }
   const bool profile = cfg.profile != 0;
   double plan_ms = 0;
   int plan_timed = 0;

@@ -51,6 +51,8 @@ enum PlanFlags {
   PF_UPDATE = 1,   // support-update iteration: emit X moments (Euclidean)
   PF_WRITE_X = 2,  // store X (packed) for a later pass
   PF_CHECK = 4,    // residual-check iteration
+  PF_IN_DEF = 8,   // wide plans arrive deferred: Z' and U = Y + X, scaled by rowsc on load
+  PF_OUT_DEF = 16, // wide plans leave deferred: Z', U and per-slice row partials
 };
 
 // Device control block, one per phase.  Everything an iteration reads that
@@ -84,6 +86,9 @@ struct PlanArgs {
   int use_tma;              // single-CTA items: persistent TMA-pipelined kernel
   const int4 *grp_rec;      // per group {plan slot, plan first group, label, plan groups << 4 | valid}
   const int *plan_slot;     // plan -> slot: position in cluster-sorted order (row-sum outputs)
+  float *rowpart;           // [slot][8][MP] per-slice row sums of Z' (deferred wide plans)
+  const float *rowsc;       // [slot][MP] row scale c_w / rowsum(Z') of the previous iteration
+  int ctas_per_sm;          // persistent grid of plain launches: CTAs per SM (0: occupancy limit)
 };
 
 // per-MP launch geometry
@@ -107,6 +112,15 @@ cudaError_t launch_pack_columns(int MP, const PlanArgs &a, int nitems, const lon
                                 float *col_w, float *col_supp, int *col_sym, int dim, int DS,
                                 int dense_hist, cudaStream_t st);
 cudaError_t launch_obj(int MP, int mode, const PlanArgs &a, int nitems, cudaStream_t st);
+
+// defer_kernels.cu: deferred row normalisation of plans wider than one CTA
+cudaError_t launch_rowsum_combine(const int4 *wide, int nwide, const float *rowpart,
+                                  const float *cw32, int MP, int m, float *rowsum_out,
+                                  float *rowsc, const Ctl *ctl, int iter, cudaStream_t st);
+cudaError_t launch_plan_finalize(float *Z, float *Y, const int *item_g0, const int *item_ng,
+                                 int nitems, int cs, int G, int MP, const int4 *grp_rec,
+                                 const float *rowsc, const unsigned char *def_iter, const Ctl *ctl,
+                                 cudaStream_t st);
 
 // kernels_reduce.cu
 struct ClusterArgs {

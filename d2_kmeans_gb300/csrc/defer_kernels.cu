@@ -1,0 +1,96 @@
+// Deferred row normalisation of plans wider than one CTA (the plan kernel's
+// PF_OUT_DEF / PF_IN_DEF modes).
+//
+// Step 2 of src/d2/centroid_Bregman.c:164-171 scales row k of a plan by
+// c_w[label, k] / rowsum_k(Z'), Z' = X * exp(Y) + 1e-9.  A plan split over CS
+// CTA slices needs every slice's row sums for that scale.  Instead of trading
+// them inside the iteration (a cluster barrier per plan), each slice writes
+// its partial row sums and stores Z' and U = Y + X; rowsum_combine_kernel adds
+// the partials in rank order, writes the plan's normalised row sums (step 4's
+// Zr, by slot) and the row scale; the next iteration's plan kernel applies the
+// scale as it loads the plan: Z = Z' * scale, Y = U - Z.  The arithmetic per
+// entry is that of the synchronous form: Z is the same product Z' * scale, Y
+// gets X and -Z in two roundings instead of one.  plan_finalize_kernel
+// applies the scale of the last iteration when the loop ends deferred.
+#include "d2g_internal.cuh"
+
+namespace d2g {
+
+constexpr float kLog2eF = 1.4426950408889634f;  // Y is stored multiplied by log2(e)
+
+// one block per wide plan {slot, slices holding columns, label, -}; MP <= 256
+__global__ void __launch_bounds__(256) rowsum_combine_kernel(const int4 *__restrict__ wide,
+                                                             const float *__restrict__ rowpart,
+                                                             const float *__restrict__ cw32, int MP,
+                                                             int m, float *__restrict__ rowsum_out,
+                                                             float *__restrict__ rowsc,
+                                                             const Ctl *ctl, int iter) {
+  if (iter >= ctl->stop_iter) return;
+  const int4 d = __ldg(wide + blockIdx.x);
+  const int k = threadIdx.x, lane = k & 31, warp = k >> 5;
+  float tot = 0.f;
+  if (k < MP)
+    for (int r = 0; r < d.y; ++r) tot += rowpart[((size_t)d.x * kMaxCluster + r) * MP + k];
+  // the plan's total over its m rows: warps in index order
+  __shared__ float ws[8];
+  float v = k < m ? tot : 0.f;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) ws[warp] = v;
+  __syncthreads();
+  float rsum = 0.f;
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) rsum += ws[i];
+  if (k < MP) {
+    rowsum_out[(size_t)d.x * MP + k] = tot * (1.f / rsum);
+    rowsc[(size_t)d.x * MP + k] = k < m ? __ldg(cw32 + (size_t)d.z * MP + k) / tot : 0.f;
+  }
+}
+
+// one block per (item, rank) slice of a bucket of wide plans
+__global__ void __launch_bounds__(256) plan_finalize_kernel(float *__restrict__ Z,
+                                                            float *__restrict__ Y,
+                                                            const int *__restrict__ item_g0,
+                                                            const int *__restrict__ item_ng, int cs,
+                                                            int G, int MP,
+                                                            const int4 *__restrict__ grp_rec,
+                                                            const float *__restrict__ rowsc,
+                                                            const unsigned char *__restrict__ def_iter,
+                                                            const Ctl *ctl) {
+  const int last = ctl->iters_done - 1;
+  if (last < 0 || !def_iter[last]) return;
+  const int item = blockIdx.x / cs, rk = blockIdx.x - item * cs;
+  const int g0 = item_g0[item] + rk * G;
+  const int ng = min(G, item_ng[item] - rk * G);
+  if (ng <= 0) return;
+  const int slot = grp_rec[g0].x;
+  const float *sc = rowsc + (size_t)slot * MP;
+  const size_t base = (size_t)g0 * kS * MP;
+  const int n = ng * kS * MP;
+  for (int e = threadIdx.x; e < n; e += blockDim.x) {
+    const float z = Z[base + e] * sc[e & (MP - 1)];
+    Z[base + e] = z;
+    Y[base + e] = fmaf(-kLog2eF, z, Y[base + e]);
+  }
+}
+
+cudaError_t launch_rowsum_combine(const int4 *wide, int nwide, const float *rowpart,
+                                  const float *cw32, int MP, int m, float *rowsum_out,
+                                  float *rowsc, const Ctl *ctl, int iter, cudaStream_t st) {
+  if (nwide <= 0) return cudaSuccess;
+  const int threads = MP < 32 ? 32 : MP;
+  rowsum_combine_kernel<<<nwide, threads, 0, st>>>(wide, rowpart, cw32, MP, m, rowsum_out, rowsc,
+                                                   ctl, iter);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_plan_finalize(float *Z, float *Y, const int *item_g0, const int *item_ng,
+                                 int nitems, int cs, int G, int MP, const int4 *grp_rec,
+                                 const float *rowsc, const unsigned char *def_iter, const Ctl *ctl,
+                                 cudaStream_t st) {
+  if (nitems <= 0) return cudaSuccess;
+  plan_finalize_kernel<<<nitems * cs, 256, 0, st>>>(Z, Y, item_g0, item_ng, cs, G, MP, grp_rec,
+                                                    rowsc, def_iter, ctl);
+  return cudaGetLastError();
+}
+
+}  // namespace d2g

@@ -26,6 +26,8 @@
 
 #include <cooperative_groups.h>
 
+#include <algorithm>
+
 #include "d2g_internal.cuh"
 
 namespace cg = cooperative_groups;
@@ -721,7 +723,8 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
   int4 *stR = (int4 *)(smem + 4 * TILE);              // [2][G] group records
   float *stW = (float *)(stR + 2 * G);                // [2][JC] weights
   float *stC = stW + 2 * JC;                          // [2][JC*CW] supports / table rows
-  float *sm_x = stC + 2 * JC * CW;                    // [2][8][MP] cluster: every rank's row totals
+  float *stS = stC + 2 * JC * CW;                     // [2][MP] deferred row scale of the slice's plan
+  float *sm_x = stS + 2 * MP;                         // [2][8][MP] cluster: every rank's row totals
   float *sm_momx = sm_x + 2 * 8 * MP;                 // [2][dim+1][MP] cluster: this CTA's moments
   float *sm_rs = sm_momx + 2 * (a.dim + 1) * MP;      // [G][MP] row partials, then plan totals
   float *sm_mom = sm_rs + G * MP;                     // [dim+1][G][MP]
@@ -731,17 +734,33 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
 
   if (a.iter >= a.ctl->stop_iter) return;
   const int tid = threadIdx.x;
-  // A plan wider than one CTA is an item of a cluster of CS CTAs; every CTA
-  // of the cluster works on its own slice (rank) of the same item.
+  // A plan wider than one CTA is split into CS slices (ranks) of G groups.
+  // Synchronous exchange: the CS slices of an item run on one thread-block
+  // cluster and trade row sums through DSMEM before step 2 finishes.
+  // Deferred exchange (PF_OUT_DEF): every slice is an independent unit of a
+  // plain launch; it stores Z' (step 2 before the row scaling) and
+  // U = Y + X, and its row partials go to global memory, where a combine
+  // kernel forms the plan's row scale c_w / rowsum(Z').  The next iteration
+  // applies that scale on load (PF_IN_DEF): Z = Z' * scale, Y = U - Z.
   const int CS = a.cs;
-  const int rank = blockIdx.x % CS, cl_id = blockIdx.x / CS, ncl = gridDim.x / CS;
+  const bool outdef = (a.flags & PF_OUT_DEF) != 0;
+  const bool indef = (a.flags & PF_IN_DEF) != 0 && CS > 1;
+  const bool clustered = CS > 1 && !outdef;
+  // walk: units u0, u0 + ustep, ...; a unit is an item (clustered: the rank is
+  // fixed by the CTA's place in its cluster) or one (item, rank) slice
+  const int crank = clustered ? (int)(blockIdx.x % CS) : 0;
+  const int u0 = clustered ? (int)(blockIdx.x / CS) : (int)blockIdx.x;
+  const int ustep = clustered ? (int)(gridDim.x / CS) : (int)gridDim.x;
+  const int nunits = clustered || CS == 1 ? nitems : nitems * CS;
   if (a.iter == 0 && a.resid_off == 0 && blockIdx.x == 0 && tid == 0) a.ctl->t_start_ns = global_ns();
   // one stage = the slice's Z and Y tiles, group records, weights and supports
-  auto issue = [&](int g0, int ng, int stg) {
+  // (+ the plan's deferred row scale)
+  auto issue = [&](int g0, int ng, int slot, int stg) {
     const size_t off = (size_t)g0 * S * MP;
     const unsigned bytes = (unsigned)ng * S * MP * 4u;
     const unsigned rb = (unsigned)ng * 16u, wb = (unsigned)ng * S * 4u, cb = wb * CW;
-    mbar_expect_tx(&mbar[stg], 2u * bytes + rb + wb + cb);
+    const unsigned sb = (indef && ng > 0) ? (unsigned)MP * 4u : 0u;
+    mbar_expect_tx(&mbar[stg], 2u * bytes + rb + wb + cb + sb);
     if (ng <= 0) return;  // an empty slice: the phase completes on the arrival alone
     bulk_load(stZ + stg * TILE, a.Z + off, bytes, &mbar[stg]);
     bulk_load(stY + stg * TILE, a.Y + off, bytes, &mbar[stg]);
@@ -751,26 +770,33 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
       bulk_load(stC + stg * JC * CW, a.col_supp + (size_t)g0 * S * CW, cb, &mbar[stg]);
     else
       bulk_load(stC + stg * JC * CW, a.col_sym + (size_t)g0 * S, cb, &mbar[stg]);
+    if (sb) bulk_load(stS + stg * MP, a.rowsc + (size_t)slot * MP, sb, &mbar[stg]);
   };
-  auto slice = [&](int item, int &g0, int &ng) {
-    g0 = a.item_g0[item] + rank * G;
-    ng = min(G, a.item_ng[item] - rank * G);
+  auto slice = [&](int u, int &g0, int &ng, int &slot) {
+    int item = u, rk = crank;
+    if (!clustered && CS > 1) {
+      item = u / CS;
+      rk = u - item * CS;
+    }
+    g0 = a.item_g0[item] + rk * G;
+    ng = min(G, a.item_ng[item] - rk * G);
     if (ng < 0) ng = 0;
+    slot = (indef && ng > 0) ? a.grp_rec[g0].x : 0;
   };
-  // thread 0 keeps the bounds of the next slice in registers, loaded one item early
-  int nx_g0 = 0, nx_ng = 0;
+  // thread 0 keeps the bounds of the next slice in registers, loaded one unit early
+  int nx_g0 = 0, nx_ng = 0, nx_slot = 0;
   if (tid == 0) {
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
     sh_fail = 0;
     mbar_fence_init();
-    if (cl_id < nitems) {
-      int g0, ng;
-      slice(cl_id, g0, ng);
+    if (u0 < nunits) {
+      int g0, ng, sl;
+      slice(u0, g0, ng, sl);
       sh_g0[0] = g0;
       sh_ng[0] = ng;
-      issue(g0, ng, 0);
-      if (cl_id + ncl < nitems) slice(cl_id + ncl, nx_g0, nx_ng);
+      issue(g0, ng, sl, 0);
+      if (u0 + ustep < nunits) slice(u0 + ustep, nx_g0, nx_ng, nx_slot);
     }
   }
   __syncthreads();
@@ -782,17 +808,18 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
   const bool write_x = a.flags & PF_WRITE_X;
   double s_obj = 0.0, s_pr = 0.0, s_dr = 0.0;  // FP64 across items, FP32 within one item
   int it = 0;
-  for (int item = cl_id; item < nitems; item += ncl, ++it) {
+  for (int u = u0; u < nunits; u += ustep, ++it) {
     const int stg = it & 1;
     if (!mbar_wait(&mbar[stg], (it >> 1) & 1)) sh_fail = 1;
     __syncthreads();
     if (sh_fail) break;
     const int cur_g0 = sh_g0[stg], cur_ng = sh_ng[stg];
-    if (tid == 0 && item + ncl < nitems) {
-      issue(nx_g0, nx_ng, stg ^ 1);
+    const int rank = clustered ? crank : (CS > 1 ? u % CS : 0);
+    if (tid == 0 && u + ustep < nunits) {
+      issue(nx_g0, nx_ng, nx_slot, stg ^ 1);
       sh_g0[stg ^ 1] = nx_g0;
       sh_ng[stg ^ 1] = nx_ng;
-      if (item + 2 * ncl < nitems) slice(item + 2 * ncl, nx_g0, nx_ng);
+      if (u + 2 * ustep < nunits) slice(u + 2 * ustep, nx_g0, nx_ng, nx_slot);
     }
 
     T t;
@@ -803,12 +830,12 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
     float x[S][RPT], zp[S][RPT], w[S];
 #pragma unroll
     for (int s = 0; s < S; ++s) w[s] = s < t.nvalid ? stW[stg * JC + lcol0 + s] : 0.f;
-
-    // step 1 and the first half of step 2 (Y is kept scaled by log2(e))
+    // deferred input: this thread's rows of the plan's row scale
+    float scin[RPT];
 #pragma unroll
-    for (int s = 0; s < S; ++s) {
-      float c[RPT], z[RPT], y[RPT];
-      t.costs(s, c);
+    for (int q = 0; q < RPT; ++q) scin[q] = indef ? stS[stg * MP + t.k0 + q] : 1.f;
+    // Z and Y of column s from the stage; deferred input holds Z' and U
+    auto ld_zy = [&](int s, float (&z)[RPT], float (&y)[RPT]) {
 #pragma unroll
       for (int q4 = 0; q4 < RPT / 4; ++q4) {
         const float4 zz = *((const float4 *)(zs + (lcol0 + s) * MP + t.k0) + q4);
@@ -816,6 +843,21 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
         z[4 * q4] = zz.x; z[4 * q4 + 1] = zz.y; z[4 * q4 + 2] = zz.z; z[4 * q4 + 3] = zz.w;
         y[4 * q4] = yy.x; y[4 * q4 + 1] = yy.y; y[4 * q4 + 2] = yy.z; y[4 * q4 + 3] = yy.w;
       }
+      if (indef) {
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+          z[q] *= scin[q];
+          y[q] = fmaf(-kLog2e, z[q], y[q]);
+        }
+      }
+    };
+
+    // step 1 and the first half of step 2 (Y is kept scaled by log2(e))
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      float c[RPT], z[RPT], y[RPT];
+      t.costs(s, c);
+      ld_zy(s, z, y);
       const bool colok = s < t.nvalid;
       float csum = 0.f;
 #pragma unroll
@@ -870,9 +912,29 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
     __syncthreads();
 
     float tot[RPT];
-    bool writer;
+    bool writer = false;
     const bool upd_euc = T::EUC && update;
-    if (CS == 1) {
+    if (outdef) {
+      // deferred: the slice's row partials of Z' leave for the combine kernel
+      if (t.g == 0 && t.active) {
+        float pt[RPT];
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) pt[q] = 0.f;
+        for (int j = 0; j < cur_ng; ++j) {
+#pragma unroll
+          for (int q4 = 0; q4 < RPT / 4; ++q4) {
+            const float4 u4 = *((const float4 *)(sm_rs + j * MP + t.k0) + q4);
+            pt[4 * q4] += u4.x;
+            pt[4 * q4 + 1] += u4.y;
+            pt[4 * q4 + 2] += u4.z;
+            pt[4 * q4 + 3] += u4.w;
+          }
+        }
+        st_rows(a.rowpart + ((size_t)t.p * kMaxCluster + rank) * MP + t.k0, pt);
+      }
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) tot[q] = 1.f;
+    } else if (CS == 1) {
       // the plan's first group sums the plan's partials once and publishes the total
       const int lo = t.active ? t.pl_g0 - t.cta_g0 : 0;
       writer = t.active && t.g == lo;
@@ -982,7 +1044,7 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
 #pragma unroll
     for (int q = 0; q < RPT; ++q) rsum += (FULL || t.k0 + q < m) ? tot[q] : 0.f;
     rsum = seg_sum<TPC>(rsum);
-    if (writer) {
+    if (writer && !outdef) {
       float zr[RPT];
       const float inv = 1.f / rsum;
 #pragma unroll
@@ -994,32 +1056,39 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
     float sc[RPT];
 #pragma unroll
     for (int q = 0; q < RPT; ++q) {
-      const bool ok = t.active && (FULL || t.k0 + q < m);
+      const bool ok = t.active && (FULL || t.k0 + q < m) && !outdef;
       sc[q] = ok ? __ldg(a.cw32 + (size_t)t.lab * MP + t.k0 + q) / tot[q] : 0.f;
     }
     float i_obj = 0.f, i_pr = 0.f, i_dr = 0.f;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
       if (s < t.nvalid) {
-        float y[RPT], zn[RPT], yn[RPT];
-#pragma unroll
-        for (int q4 = 0; q4 < RPT / 4; ++q4) {
-          const float4 yy = *((const float4 *)(ys + (lcol0 + s) * MP + t.k0) + q4);
-          y[4 * q4] = yy.x; y[4 * q4 + 1] = yy.y; y[4 * q4 + 2] = yy.z; y[4 * q4 + 3] = yy.w;
-        }
-#pragma unroll
-        for (int q = 0; q < RPT; ++q) {
-          zn[q] = zp[s][q] * sc[q];
-          yn[q] = fmaf(kLog2e, x[s][q] - zn[q], y[q]);
-        }
-        if constexpr (CHECK) {
-          float c[RPT], z0[RPT];
-          t.costs(s, c);
+        float y[RPT], z0[RPT], zn[RPT], yn[RPT];
+        if (CHECK || indef) {
+          ld_zy(s, z0, y);
+        } else {
 #pragma unroll
           for (int q4 = 0; q4 < RPT / 4; ++q4) {
-            const float4 zz = *((const float4 *)(zs + (lcol0 + s) * MP + t.k0) + q4);
-            z0[4 * q4] = zz.x; z0[4 * q4 + 1] = zz.y; z0[4 * q4 + 2] = zz.z; z0[4 * q4 + 3] = zz.w;
+            const float4 yy = *((const float4 *)(ys + (lcol0 + s) * MP + t.k0) + q4);
+            y[4 * q4] = yy.x; y[4 * q4 + 1] = yy.y; y[4 * q4 + 2] = yy.z; y[4 * q4 + 3] = yy.w;
           }
+        }
+        if (outdef) {  // Z' and U = Y + X
+#pragma unroll
+          for (int q = 0; q < RPT; ++q) {
+            zn[q] = zp[s][q];
+            yn[q] = fmaf(kLog2e, x[s][q], y[q]);
+          }
+        } else {
+#pragma unroll
+          for (int q = 0; q < RPT; ++q) {
+            zn[q] = zp[s][q] * sc[q];
+            yn[q] = fmaf(kLog2e, x[s][q] - zn[q], y[q]);
+          }
+        }
+        if constexpr (CHECK) {
+          float c[RPT];
+          t.costs(s, c);
 #pragma unroll
           for (int q = 0; q < RPT; ++q) {
             i_obj = fmaf(c[q] * inv_rho, x[s][q], i_obj);
@@ -1042,7 +1111,7 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
   }
   // rank 0 may still be reading a peer's shared memory (the moments of the
   // last item): no CTA of a cluster leaves before all of them are done
-  if (CS > 1 && !sh_fail) cg::this_cluster().sync();
+  if (clustered && !sh_fail) cg::this_cluster().sync();
   if (sh_fail) {
     if (tid == 0) {
       a.ctl->err = 7;  // a bulk copy did not complete: let the copies in flight land first
@@ -1055,13 +1124,14 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
     // one partial per CTA in the slot of its first (item, rank); its other slots get zeros
     __shared__ double res[3];
     block_sum3<kThreads>(s_obj, s_pr, s_dr, res);
-    if (tid == 0 && cl_id < nitems) {
-      double *pp = a.resid_part + (size_t)(a.resid_off + cl_id * CS + rank) * 4;
+    // (check iterations never run deferred: a unit is an item, the rank is crank)
+    if (tid == 0 && u0 < nitems) {
+      double *pp = a.resid_part + (size_t)(a.resid_off + u0 * CS + crank) * 4;
       pp[0] = res[0];
       pp[1] = res[1];
       pp[2] = res[2];
-      for (int item = cl_id + ncl; item < nitems; item += ncl) {
-        double *qq = a.resid_part + (size_t)(a.resid_off + item * CS + rank) * 4;
+      for (int item = u0 + ustep; item < nitems; item += ustep) {
+        double *qq = a.resid_part + (size_t)(a.resid_off + item * CS + crank) * 4;
         qq[0] = qq[1] = qq[2] = 0.0;
       }
     }
@@ -1093,7 +1163,7 @@ cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaSt
   constexpr int JC = GeoT<MP>::G * kS;
   constexpr int CW = MODE == COST_EUCLID8 ? 8 : (MODE == COST_EUCLID4 ? 4 : 1);
   const size_t sm = smem + (size_t)4 * tma_tile_floats<MP>() * sizeof(float) +
-                    2 * (size_t)GeoT<MP>::G * 16 + 2 * (size_t)JC * 4 * (1 + CW) +
+                    2 * (size_t)GeoT<MP>::G * 16 + 2 * (size_t)JC * 4 * (1 + CW) + (size_t)2 * MP * 4 +
                     (size_t)2 * 8 * MP * 4 + (size_t)2 * (a.dim + 1) * MP * 4;
   static size_t configured_smem = 0;
   static bool nonportable = false;
@@ -1123,14 +1193,24 @@ cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaSt
     if (e != cudaSuccess) return e;
     grid[cs] = (ncl > 0 ? ncl : 1) * cs;
   }
-  if (nitems <= 0) return cudaSuccess;
-  const int g = (nitems * cs < grid[cs]) ? nitems * cs : grid[cs];
-  cudaLaunchAttribute attr[1];
-  cudaLaunchConfig_t cfg = plan_cfg(g, sm, st, attr, cs);
-  if (cs == 1) {  // a cluster of one CTA: plain launch
-    cfg.attrs = nullptr;
-    cfg.numAttrs = 0;
+  static int nsm = 0;
+  if (grid[0] == 0) {  // plain launches: resident CTAs per SM x SMs
+    int dev = 0, per = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kThreads, sm);
+    if (e != cudaSuccess) return e;
+    grid[0] = (per > 0 ? per : 1) * nsm;
   }
+  if (nitems <= 0) return cudaSuccess;
+  // deferred exchange: the slices of wide plans are independent CTAs
+  const bool plain = cs == 1 || (a.flags & PF_OUT_DEF);
+  const long long units = (long long)nitems * cs;
+  int cap = plain ? grid[0] : grid[cs];
+  if (plain && a.ctas_per_sm > 0) cap = std::min(cap, a.ctas_per_sm * nsm);
+  const int g = units < cap ? (int)units : cap;
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = plan_cfg(g, sm, st, attr, plain ? 1 : cs);
   return cudaLaunchKernelEx(&cfg, kern, a, nitems);
 }
 

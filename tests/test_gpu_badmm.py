@@ -141,13 +141,69 @@ def test_batched_odd_shapes(d2g, oracle_mod, m, dim, lo, hi, k, seed):
     P.close()
 
 
-def test_histogram_256_bins_cluster_path(d2g, oracle_mod):
-    """256-bin plans span an 8-CTA thread-block cluster (DSMEM row sums)."""
+EXCHANGES = ["deferred", "cluster"]
+
+
+def _exchange(monkeypatch, exchange):
+    """Plans wider than one CTA: deferred row normalisation (default) or the
+    synchronous DSMEM exchange on a thread-block cluster."""
+    if exchange == "cluster":
+        monkeypatch.setenv("D2G_WIDE_EXCHANGE", "cluster")
+    else:
+        monkeypatch.delenv("D2G_WIDE_EXCHANGE", raising=False)
+
+
+@pytest.mark.parametrize("exchange", EXCHANGES)
+def test_histogram_256_bins_cluster_path(d2g, oracle_mod, monkeypatch, exchange):
+    """256-bin plans span 8 CTA slices (row sums exchanged deferred or in a cluster)."""
+    _exchange(monkeypatch, exchange)
     ph, c = synth.histogram_phase(10, 2, side=16, alpha=0.1, seed=31)
     opts = dict(maxIters=30, rhoCoeff=2.0, updatePerLoops=10)
     ref = _port(oracle_mod, ph, c, opts)
     P = d2g.Phase(ph, 0)
     assert_close(P.run(c, opts), ref, 2, 256)
+    P.close()
+
+
+def _plan_l1(Z, Zr):
+    return np.abs(np.asarray(Z) - np.asarray(Zr)).sum() / np.abs(np.asarray(Zr)).sum()
+
+
+@pytest.mark.parametrize("exchange", EXCHANGES)
+def test_wide_plans_warm_start(d2g, oracle_mod, monkeypatch, exchange):
+    """Two calls on wide plans, the second warm-started (label_switch = 0) from
+    the Z the first left.  The first call ends on iteration 25, which runs
+    deferred, so its Z must be the row-scaled plan; Z within 1e-4 relative L1."""
+    _exchange(monkeypatch, exchange)
+    ph, c = synth.histogram_phase(12, 3, side=16, alpha=0.1, seed=33)
+    o1 = dict(maxIters=25, rhoCoeff=2.0, updatePerLoops=10)
+    o2 = dict(maxIters=12, rhoCoeff=2.0, updatePerLoops=10)
+    r1 = oracle_mod.badmm(ph, c, o1, "port", want=())
+    ph2 = dict(ph, label_switch=np.zeros(len(ph["p_str"]), np.int8))
+    r2 = oracle_mod.badmm(ph2, dict(c_w=r1["c_w"], c_supp=None, Z=r1["Z"]), o2, "port", want=())
+    P = d2g.Phase(ph, 0)
+    g1 = P.run(c, o1)
+    assert_close(g1, r1, 3, 256)
+    assert _plan_l1(P.get_plans(), r1["Z"]) <= 1e-4
+    g2 = P.run(dict(c_w=g1["c_w"], c_supp=None), o2, label_switch=ph2["label_switch"])
+    assert_close(g2, r2, 3, 256)
+    assert _plan_l1(P.get_plans(), r2["Z"]) <= 1e-4
+    P.close()
+
+
+@pytest.mark.parametrize("exchange", EXCHANGES)
+def test_wide_plans_time_budget(d2g, oracle_mod, monkeypatch, exchange):
+    """The loop stops after iteration 0 (deferred for wide plans): c_w and the
+    plans left behind equal one iteration of the reference."""
+    _exchange(monkeypatch, exchange)
+    ph, c = synth.histogram_phase(8, 2, side=16, alpha=0.1, seed=34)
+    ref = oracle_mod.badmm(ph, c, dict(maxIters=0, rhoCoeff=2.0, updatePerLoops=10), "port", want=())
+    P = d2g.Phase(ph, 0)
+    r = P.run(c, dict(maxIters=50, rhoCoeff=2.0, updatePerLoops=10, time_budget=1e-9))
+    assert r["stats"]["iterations"] == 1
+    cw = np.asarray(r["c_w"]).reshape(2, 256)
+    assert np.abs(cw - ref["c_w"].reshape(2, 256)).sum(1).max() < 1e-5
+    assert _plan_l1(P.get_plans(), ref["Z"]) <= 1e-5
     P.close()
 
 
