@@ -112,6 +112,7 @@ struct d2g_phase {
   std::vector<int> plan_inst, inst_plan;
   DBuf<float> Z, Y, Xp, col_w, col_supp, rowsum, xmom, cw32, cs32, ctab;
   DBuf<int> col_sym, grp_meta, plan_g0, plan_ng, plan_label, item_g0, item_ng;
+  DBuf<int> col_crow;  // word embeddings: cost-table row of each packed column
   DBuf<long long> plan_cum;
   DBuf<int4> grp_rec;
   DBuf<int> plan_slot;
@@ -120,8 +121,11 @@ struct d2g_phase {
   DBuf<double> resid_part, rho_part;
   size_t smem_plan = 0, smem_plan_upd = 0;
   int use_tma = 1;  // persistent TMA-pipelined kernel for single-CTA items (D2G_PLAN_KERNEL=v1 turns it off)
-  // plans wider than one CTA (packed ids wide_p0 ..): deferred row normalisation
-  int wide_p0 = 0, nwide = 0;
+  // plans wider than one CTA: deferred row normalisation
+  std::vector<int> h_wide_plans;  // packed ids
+  Bucket units{1, 0, 0, 0};       // units of the deferred iterations
+  int stage_costs = 0;
+  int nwide = 0;
   bool defer = false;
   DBuf<float> rowpart, rowsc;
   DBuf<int4> wide;                       // {slot, slices with columns, label, 0} per wide plan
@@ -182,7 +186,19 @@ static bool batched_supported(const d2g_phase_desc *d, std::string *why) {
 // ------------------------------------------------------------------ packing
 // Best-fit-decreasing packing of plans (in S-column groups) into items of G
 // groups; plans needing more than G groups get a cluster of 2/4/8 CTAs.
-static int build_packing(d2g_phase *ph) {
+// Packing of the plans into CTA work.  Plans of at most G column groups
+// ("small") are packed best-fit-decreasing into units of G groups.  A plan of
+// more than G groups ("wide") is cut into floor(ng/G) full slices of G groups
+// and a remainder of ng mod G groups; with the deferred exchange the remainder
+// opens a unit that small plans fill.  Layout: the small-only units, then per
+// wide plan its groups followed by the small plans of its remainder unit.
+// Three partitions of that one layout are launched:
+//   - cs = 1 bucket: runs of whole small plans (synchronous iterations);
+//   - cs = 2, 4, 8 buckets: one wide plan per item on a thread-block cluster
+//     of next_pow2(ceil(ng/G)) CTAs (synchronous iterations);
+//   - units: every range above of at most G groups, at most one wide slice
+//     per unit and at its start (deferred iterations, one plain launch).
+static int build_packing(d2g_phase *ph, bool with_units) {
   const int G = ph->geo.G;
   const size_t n = ph->size;
   std::vector<int> ng(n), csz(n);
@@ -193,40 +209,55 @@ static int build_packing(d2g_phase *ph) {
     if (c > kMaxCluster) return fail(D2G_E_UNSUPPORTED, "instance support size exceeds 8 CTAs");
     csz[i] = c;
   }
+  // bins of G groups: {anchor wide plan or -1, small plans}
+  std::vector<int> bin_anchor;
+  std::vector<std::vector<int>> bin_plans;
+  std::vector<std::vector<int>> open(G + 1);  // bins by remaining capacity
+  std::vector<int> anchor_bin(n, -1);
+  if (with_units)
+    for (size_t i = 0; i < n; ++i)
+      if (csz[i] > 1 && ng[i] % G) {
+        anchor_bin[i] = (int)bin_anchor.size();
+        open[G - ng[i] % G].push_back((int)bin_anchor.size());
+        bin_anchor.push_back((int)i);
+        bin_plans.emplace_back();
+      }
   std::vector<int> order;
   order.reserve(n);
   for (size_t i = 0; i < n; ++i)
     if (csz[i] == 1) order.push_back((int)i);
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return ng[a] > ng[b]; });
-  std::vector<std::vector<int>> items;
-  std::vector<std::vector<int>> open(G + 1);
   for (int i : order) {
-    int it = -1, rem = -1;
+    int bi = -1, rem = -1;
     for (int r = ng[i]; r <= G; ++r)
       if (!open[r].empty()) {
-        it = open[r].back();
+        bi = open[r].back();
         open[r].pop_back();
         rem = r;
         break;
       }
-    if (it < 0) {
-      it = (int)items.size();
-      items.emplace_back();
+    if (bi < 0) {
+      bi = (int)bin_anchor.size();
+      bin_anchor.push_back(-1);
+      bin_plans.emplace_back();
       rem = G;
     }
-    items[it].push_back(i);
+    bin_plans[bi].push_back(i);
     rem -= ng[i];
-    if (rem > 0) open[rem].push_back(it);
+    if (rem > 0) open[rem].push_back(bi);
   }
   // assign packed plan ids / groups
   ph->plan_inst.clear();
   ph->inst_plan.assign(n, -1);
   ph->h_grp_rec.clear();
   ph->h_grp_plan.clear();
-  std::vector<int> h_item_g0, h_item_ng, h_plan_g0, h_plan_ng, h_meta;
+  ph->h_wide_plans.clear();
+  std::vector<int> h_plan_g0, h_plan_ng, h_meta;
   std::vector<long long> h_plan_cum;
+  std::vector<int> it1_g0, it1_ng, unit_g0, unit_ng;
+  std::vector<int> itc_g0[kMaxCluster + 1], itc_ng[kMaxCluster + 1];
   ph->buckets.clear();
-  int g = 0, blocks = 0;
+  int g = 0;
   auto add_plan = [&](int i) {
     const int p = (int)ph->plan_inst.size();
     ph->plan_inst.push_back(i);
@@ -242,34 +273,55 @@ static int build_packing(d2g_phase *ph) {
     }
     g += ng[i];
   };
-  {
-    d2g_phase::Bucket b{1, (int)items.size(), 0, 0};
-    for (auto &itv : items) {
-      h_item_g0.push_back(g);
-      int tot = 0;
-      for (int i : itv) {
-        add_plan(i);
-        tot += ng[i];
-      }
-      h_item_ng.push_back(tot);
+  auto add_small_run = [&](const std::vector<int> &pl, int unit_from) {
+    const int g0 = g;
+    for (int i : pl) add_plan(i);
+    if (g > g0) {
+      it1_g0.push_back(g0);
+      it1_ng.push_back(g - g0);
     }
-    blocks += b.nitems;
-    ph->buckets.push_back(b);
+    if (g > unit_from) {
+      unit_g0.push_back(unit_from);
+      unit_ng.push_back(g - unit_from);
+    }
+  };
+  for (size_t bi = 0; bi < bin_anchor.size(); ++bi)
+    if (bin_anchor[bi] < 0) add_small_run(bin_plans[bi], g);
+  for (size_t i = 0; i < n; ++i) {
+    if (csz[i] == 1) continue;
+    const int g0 = g;
+    ph->h_wide_plans.push_back((int)ph->plan_inst.size());
+    add_plan((int)i);
+    itc_g0[csz[i]].push_back(g0);
+    itc_ng[csz[i]].push_back(ng[i]);
+    const int nfull = ng[i] / G;
+    for (int k = 0; k < nfull; ++k) {
+      unit_g0.push_back(g0 + k * G);
+      unit_ng.push_back(G);
+    }
+    if (ng[i] % G) {
+      static const std::vector<int> none;
+      add_small_run(anchor_bin[i] >= 0 ? bin_plans[anchor_bin[i]] : none, g0 + nfull * G);
+    }
   }
-  ph->wide_p0 = (int)ph->plan_inst.size();
-  ph->nwide = (int)n - ph->wide_p0;
+  // item arrays: cs = 1 items, cluster items by size, then the units
+  std::vector<int> h_item_g0(it1_g0), h_item_ng(it1_ng);
+  int blocks = 0;
+  ph->buckets.push_back(d2g_phase::Bucket{1, (int)it1_g0.size(), 0, 0});
+  blocks += (int)it1_g0.size();
   for (int c = 2; c <= kMaxCluster; c <<= 1) {
-    d2g_phase::Bucket b{c, 0, (int)h_item_g0.size(), blocks};
-    for (size_t i = 0; i < n; ++i)
-      if (csz[i] == c) {
-        h_item_g0.push_back(g);
-        h_item_ng.push_back(ng[i]);
-        add_plan((int)i);
-        ++b.nitems;
-      }
-    blocks += b.nitems * c;
-    if (b.nitems) ph->buckets.push_back(b);
+    if (itc_g0[c].empty()) continue;
+    ph->buckets.push_back(d2g_phase::Bucket{c, (int)itc_g0[c].size(), (int)h_item_g0.size(), blocks});
+    h_item_g0.insert(h_item_g0.end(), itc_g0[c].begin(), itc_g0[c].end());
+    h_item_ng.insert(h_item_ng.end(), itc_ng[c].begin(), itc_ng[c].end());
+    blocks += (int)itc_g0[c].size() * c;
   }
+  ph->units = d2g_phase::Bucket{1, with_units ? (int)unit_g0.size() : 0, (int)h_item_g0.size(), 0};
+  if (with_units) {
+    h_item_g0.insert(h_item_g0.end(), unit_g0.begin(), unit_g0.end());
+    h_item_ng.insert(h_item_ng.end(), unit_ng.begin(), unit_ng.end());
+  }
+  ph->nwide = (int)ph->h_wide_plans.size();
   if (ph->buckets[0].nitems == 0) ph->buckets.erase(ph->buckets.begin());
   ph->total_blocks = blocks;
   ph->ngroups = g;
@@ -321,6 +373,8 @@ static PlanArgs base_args(d2g_phase *ph) {
   a.plan_slot = ph->plan_slot.p;
   a.rowpart = ph->rowpart.p;
   a.rowsc = ph->rowsc.p;
+  a.col_crow = ph->metric == D2_WORD_EMBED ? ph->col_crow.p : ph->col_sym.p;
+  a.stage_costs = ph->stage_costs;
   return a;
 }
 
@@ -377,7 +431,7 @@ static int set_labels_impl(d2g_phase *ph, const int *label) {
     if (ph->nwide > 0) {  // wide plans: {slot, slices with columns, label}
       std::vector<int4> wl(ph->nwide);
       for (int q = 0; q < ph->nwide; ++q) {
-        const int p = ph->wide_p0 + q;
+        const int p = ph->h_wide_plans[q];
         const int ngp = (ph->p_str[ph->plan_inst[p]] + kS - 1) / kS;
         wl[q] = make_int4(slot[p], (ngp + ph->geo.G - 1) / ph->geo.G, pl[p], 0);
       }
@@ -412,6 +466,11 @@ static int set_labels_impl(d2g_phase *ph, const int *label) {
       std::vector<int> occ(ptr.back());
       for (long long pc = 0; pc < ph->ncols_packed; ++pc)
         if (key_of[pc] >= 0) occ[cnt[key_of[pc]]++] = (int)pc;
+      // per packed column: its cost-table row label * V + token (0 in pad columns)
+      for (auto &k2 : key_of) k2 = std::max(k2, 0);
+      D2G_CUDA(ph->col_crow.alloc(key_of.size()));
+      D2G_CUDA(cudaMemcpyAsync(ph->col_crow.p, key_of.data(), key_of.size() * 4, cudaMemcpyHostToDevice,
+                               ph->st));
       ph->npairs = (int)keys.size();
       D2G_CUDA(ph->pair_key.alloc(keys.size()));
       D2G_CUDA(ph->pair_ptr.alloc(ptr.size()));
@@ -487,7 +546,11 @@ static int create_batched(d2g_phase *ph, const d2g_phase_desc *d) {
     ph->mode = COST_TABLE;
     ph->DS = 4;
   }
-  int rc = build_packing(ph);
+  const char *pk = getenv("D2G_PLAN_KERNEL");
+  ph->use_tma = !(pk && std::string(pk) == "v1");
+  const char *dx = getenv("D2G_WIDE_EXCHANGE");  // "cluster": synchronous DSMEM exchange always
+  const bool defer_ok = ph->use_tma && !(dx && std::string(dx) == "cluster");
+  int rc = build_packing(ph, defer_ok);
   if (rc) return rc;
   const size_t nz = (size_t)ph->ncols_packed * ph->MP;
   D2G_CUDA(ph->Z.alloc(nz));
@@ -520,10 +583,9 @@ static int create_batched(d2g_phase *ph, const d2g_phase_desc *d) {
 
   int rc2 = upload_columns_batched(ph, d);
   if (rc2) return rc2;
-  const char *pk = getenv("D2G_PLAN_KERNEL");
-  ph->use_tma = !(pk && std::string(pk) == "v1");
-  const char *dx = getenv("D2G_WIDE_EXCHANGE");  // "cluster": synchronous DSMEM exchange always
-  ph->defer = ph->use_tma && ph->nwide > 0 && !(dx && std::string(dx) == "cluster");
+  ph->defer = defer_ok && ph->nwide > 0;
+  const char *sc = getenv("D2G_STAGE_COSTS");
+  ph->stage_costs = sc && std::string(sc) == "1";
   if (ph->nwide > 0) {
     D2G_CUDA(ph->rowpart.alloc((size_t)ph->nplans * kMaxCluster * ph->MP));
     D2G_CUDA(ph->rowsc.alloc((size_t)ph->nplans * ph->MP));
@@ -673,7 +735,8 @@ static std::vector<unsigned long long> loop_signature(d2g_phase *ph) {
           u(ph->occ_col.p), (unsigned long long)ph->npairs,
           (unsigned long long)ph->nchunk, (unsigned long long)ph->chunk,
           (unsigned long long)ph->global_size, (unsigned long long)ph->cost_gemm,
-          u(ph->wide.p), u(ph->def_iter.p), u(ph->rowpart.p), u(ph->rowsc.p),
+          u(ph->wide.p), u(ph->def_iter.p), u(ph->rowpart.p), u(ph->rowsc.p), u(ph->col_crow.p),
+          (unsigned long long)ph->stage_costs,
           (unsigned long long)ph->defer};
 }
 
@@ -737,14 +800,21 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
         evs.push_back(b);
         cudaEventRecord(a, ph->st);
       }
-      for (auto &b : ph->buckets) {
-        PlanArgs a = bucket_args(ph, base, b);
+      if (def) {  // one plain launch over the units
+        PlanArgs a = bucket_args(ph, base, ph->units);
         a.iter = it;
-        a.flags = flags;
-        if (b.cs > 1) a.flags |= (def ? PF_OUT_DEF : 0) | (prev_def ? PF_IN_DEF : 0);
-        D2G_CUDA(launch_plan(ph->MP, ph->mode, chk, a, b.nitems,
-                             (upd && euc) ? ph->smem_plan_upd : ph->smem_plan, ph->st));
+        a.flags = flags | PF_OUT_DEF | (prev_def ? PF_IN_DEF : 0);
+        D2G_CUDA(launch_plan(ph->MP, ph->mode, chk, a, ph->units.nitems, ph->smem_plan, ph->st));
         ++nl;
+      } else {
+        for (auto &b : ph->buckets) {
+          PlanArgs a = bucket_args(ph, base, b);
+          a.iter = it;
+          a.flags = flags | (prev_def ? PF_IN_DEF : 0);
+          D2G_CUDA(launch_plan(ph->MP, ph->mode, chk, a, b.nitems,
+                               (upd && euc) ? ph->smem_plan_upd : ph->smem_plan, ph->st));
+          ++nl;
+        }
       }
       if (def) {
         D2G_CUDA(launch_rowsum_combine(ph->wide.p, ph->nwide, ph->rowpart.p, ph->cw32.p, ph->MP,

@@ -89,6 +89,8 @@ struct PlanArgs {
   float *rowpart;           // [slot][8][MP] per-slice row sums of Z' (deferred wide plans)
   const float *rowsc;       // [slot][MP] row scale c_w / rowsum(Z') of the previous iteration
   int ctas_per_sm;          // persistent grid of plain launches: CTAs per SM (0: occupancy limit)
+  const int *col_crow;      // per packed column: cost-table row (label * V + token, or the bin)
+  int stage_costs;          // table costs (16 <= MP <= 128) by bulk copy into shared memory
 };
 
 // per-MP launch geometry

@@ -709,6 +709,11 @@ __host__ __device__ constexpr int tma_tile_floats() {
   return GeoT<MP>::G * kS * MP;
 }
 
+// table costs staged in shared memory by bulk copies (one table row per column)
+__host__ __device__ constexpr bool plan_stages_costs(int MP, int MODE) {
+  return MODE == COST_TABLE && MP >= 16 && MP <= 128;
+}
+
 template <int MP, int MODE, bool CHECK, bool FULL>
 __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
     plan_kernel_tma(const PlanArgs a, int nitems) {
@@ -717,6 +722,11 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
   constexpr int TILE = tma_tile_floats<MP>();
   constexpr int JC = G * S;
   constexpr int CW = T::EUC ? T::DS : 1;  // staged column data: supports or table row
+  // table costs of MP <= 128 arrive with the stage: one bulk copy per column
+  // of the column's table row, issued by warp 0 (JC / 32 columns per lane)
+  constexpr bool SCC = plan_stages_costs(MP, MODE);
+  constexpr int CPL = SCC ? JC / 32 : 1;
+  const bool SC = SCC && a.stage_costs;
   extern __shared__ __align__(128) float smem[];
   float *stZ = smem;                                  // [2][TILE]
   float *stY = smem + 2 * TILE;                       // [2][TILE]
@@ -724,7 +734,8 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
   float *stW = (float *)(stR + 2 * G);                // [2][JC] weights
   float *stC = stW + 2 * JC;                          // [2][JC*CW] supports / table rows
   float *stS = stC + 2 * JC * CW;                     // [2][MP] deferred row scale of the slice's plan
-  float *sm_x = stS + 2 * MP;                         // [2][8][MP] cluster: every rank's row totals
+  float *stK = stS + 2 * MP;                          // [2][TILE] staged table costs (SC)
+  float *sm_x = stK + (SCC ? 2 * TILE : 0);           // [2][8][MP] cluster: every rank's row totals
   float *sm_momx = sm_x + 2 * 8 * MP;                 // [2][dim+1][MP] cluster: this CTA's moments
   float *sm_rs = sm_momx + 2 * (a.dim + 1) * MP;      // [G][MP] row partials, then plan totals
   float *sm_mom = sm_rs + G * MP;                     // [dim+1][G][MP]
@@ -734,33 +745,32 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
 
   if (a.iter >= a.ctl->stop_iter) return;
   const int tid = threadIdx.x;
-  // A plan wider than one CTA is split into CS slices (ranks) of G groups.
-  // Synchronous exchange: the CS slices of an item run on one thread-block
-  // cluster and trade row sums through DSMEM before step 2 finishes.
-  // Deferred exchange (PF_OUT_DEF): every slice is an independent unit of a
-  // plain launch; it stores Z' (step 2 before the row scaling) and
-  // U = Y + X, and its row partials go to global memory, where a combine
-  // kernel forms the plan's row scale c_w / rowsum(Z').  The next iteration
-  // applies that scale on load (PF_IN_DEF): Z = Z' * scale, Y = U - Z.
+  // A plan wider than one CTA ("wide") is cut into slices (ranks) of G groups.
+  // Synchronous exchange (CS > 1): the slices of one wide plan run on a
+  // thread-block cluster and trade row sums through DSMEM before step 2
+  // finishes.  Deferred exchange (PF_OUT_DEF, CS == 1 unit launches): a unit
+  // is a range of at most G groups holding whole small plans and at most one
+  // wide slice, at its start; the slice stores Z' (step 2 before the row
+  // scaling) and U = Y + X and its row partials go to global memory, where a
+  // combine kernel forms the plan's row scale c_w / rowsum(Z').  The next
+  // iteration applies that scale on load (PF_IN_DEF): Z = Z' * scale, Y = U - Z.
   const int CS = a.cs;
+  const bool clustered = CS > 1;
   const bool outdef = (a.flags & PF_OUT_DEF) != 0;
-  const bool indef = (a.flags & PF_IN_DEF) != 0 && CS > 1;
-  const bool clustered = CS > 1 && !outdef;
-  // walk: units u0, u0 + ustep, ...; a unit is an item (clustered: the rank is
-  // fixed by the CTA's place in its cluster) or one (item, rank) slice
+  const bool indef = (a.flags & PF_IN_DEF) != 0;
   const int crank = clustered ? (int)(blockIdx.x % CS) : 0;
   const int u0 = clustered ? (int)(blockIdx.x / CS) : (int)blockIdx.x;
   const int ustep = clustered ? (int)(gridDim.x / CS) : (int)gridDim.x;
-  const int nunits = clustered || CS == 1 ? nitems : nitems * CS;
+  const int nunits = nitems;
   if (a.iter == 0 && a.resid_off == 0 && blockIdx.x == 0 && tid == 0) a.ctl->t_start_ns = global_ns();
   // one stage = the slice's Z and Y tiles, group records, weights and supports
-  // (+ the plan's deferred row scale)
+  // (+ the deferred row scale of its wide plan, slot >= 0)
   auto issue = [&](int g0, int ng, int slot, int stg) {
     const size_t off = (size_t)g0 * S * MP;
     const unsigned bytes = (unsigned)ng * S * MP * 4u;
     const unsigned rb = (unsigned)ng * 16u, wb = (unsigned)ng * S * 4u, cb = wb * CW;
-    const unsigned sb = (indef && ng > 0) ? (unsigned)MP * 4u : 0u;
-    mbar_expect_tx(&mbar[stg], 2u * bytes + rb + wb + cb + sb);
+    const unsigned sb = slot >= 0 ? (unsigned)MP * 4u : 0u;
+    mbar_expect_tx(&mbar[stg], (SC ? 3u : 2u) * bytes + rb + wb + cb + sb);
     if (ng <= 0) return;  // an empty slice: the phase completes on the arrival alone
     bulk_load(stZ + stg * TILE, a.Z + off, bytes, &mbar[stg]);
     bulk_load(stY + stg * TILE, a.Y + off, bytes, &mbar[stg]);
@@ -772,31 +782,65 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
       bulk_load(stC + stg * JC * CW, a.col_sym + (size_t)g0 * S, cb, &mbar[stg]);
     if (sb) bulk_load(stS + stg * MP, a.rowsc + (size_t)slot * MP, sb, &mbar[stg]);
   };
+  // bounds of unit u; slot of its leading wide slice when that arrives deferred, else -1
   auto slice = [&](int u, int &g0, int &ng, int &slot) {
-    int item = u, rk = crank;
-    if (!clustered && CS > 1) {
-      item = u / CS;
-      rk = u - item * CS;
-    }
-    g0 = a.item_g0[item] + rk * G;
-    ng = min(G, a.item_ng[item] - rk * G);
+    g0 = a.item_g0[u] + crank * G;
+    ng = min(G, a.item_ng[u] - crank * G);
     if (ng < 0) ng = 0;
-    slot = (indef && ng > 0) ? a.grp_rec[g0].x : 0;
+    slot = -1;
+    if (indef && ng > 0) {
+      const int4 r = a.grp_rec[g0];
+      if ((r.w >> 4) > G) slot = r.x;
+    }
   };
-  // thread 0 keeps the bounds of the next slice in registers, loaded one unit early
-  int nx_g0 = 0, nx_ng = 0, nx_slot = 0;
-  if (tid == 0) {
-    mbar_init(&mbar[0], 1);
-    mbar_init(&mbar[1], 1);
-    sh_fail = 0;
-    mbar_fence_init();
-    if (u0 < nunits) {
-      int g0, ng, sl;
-      slice(u0, g0, ng, sl);
-      sh_g0[0] = g0;
-      sh_ng[0] = ng;
-      issue(g0, ng, sl, 0);
-      if (u0 + ustep < nunits) slice(u0 + ustep, nx_g0, nx_ng, nx_slot);
+  // staged table costs: the lanes of warp 0 copy the table rows of a slice's
+  // columns; each lane holds the rows of the slice issued next, loaded one unit early
+  const int lane = tid & 31;
+  int crow_nx[CPL];
+  auto load_crow = [&](int g0, int ng) {
+#pragma unroll
+    for (int j = 0; j < CPL; ++j) {
+      const int c = lane + 32 * j;
+      crow_nx[j] = c < ng * S ? __ldg(a.col_crow + (size_t)g0 * S + c) : 0;
+    }
+  };
+  auto issue_rows = [&](int ng, int stg) {
+#pragma unroll
+    for (int j = 0; j < CPL; ++j) {
+      const int c = lane + 32 * j;
+      if (c < ng * S)
+        bulk_load(stK + stg * TILE + c * MP, a.ctab + (size_t)crow_nx[j] * MP, MP * 4u, &mbar[stg]);
+    }
+  };
+  // lane 0 of warp 0 keeps the bounds of the next slice in registers, loaded one unit early
+  int nx_g0 = 0, nx_ng = 0, nx_slot = -1;
+  if (tid < 32) {
+    int g0 = 0, ng = 0, sl = -1;
+    if (tid == 0) {
+      mbar_init(&mbar[0], 1);
+      mbar_init(&mbar[1], 1);
+      sh_fail = 0;
+      mbar_fence_init();
+      if (u0 < nunits) {
+        slice(u0, g0, ng, sl);
+        sh_g0[0] = g0;
+        sh_ng[0] = ng;
+        issue(g0, ng, sl, 0);
+      }
+    }
+    __syncwarp();
+    if (SC) {
+      g0 = __shfl_sync(0xffffffffu, g0, 0);
+      ng = __shfl_sync(0xffffffffu, ng, 0);
+      if (u0 < nunits) {
+        load_crow(g0, ng);
+        issue_rows(ng, 0);
+      }
+    }
+    if (tid == 0 && u0 + ustep < nunits) slice(u0 + ustep, nx_g0, nx_ng, nx_slot);
+    if (SC) {
+      const int g1 = __shfl_sync(0xffffffffu, nx_g0, 0), n1 = __shfl_sync(0xffffffffu, nx_ng, 0);
+      if (u0 + ustep < nunits) load_crow(g1, n1);
     }
   }
   __syncthreads();
@@ -814,12 +858,23 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
     __syncthreads();
     if (sh_fail) break;
     const int cur_g0 = sh_g0[stg], cur_ng = sh_ng[stg];
-    const int rank = clustered ? crank : (CS > 1 ? u % CS : 0);
-    if (tid == 0 && u + ustep < nunits) {
-      issue(nx_g0, nx_ng, nx_slot, stg ^ 1);
-      sh_g0[stg ^ 1] = nx_g0;
-      sh_ng[stg ^ 1] = nx_ng;
-      if (u + 2 * ustep < nunits) slice(u + 2 * ustep, nx_g0, nx_ng, nx_slot);
+    const int rank = crank;
+    if (tid < 32 && u + ustep < nunits) {
+      const int ng1 = __shfl_sync(0xffffffffu, nx_ng, 0);
+      if (tid == 0) {
+        issue(nx_g0, nx_ng, nx_slot, stg ^ 1);
+        sh_g0[stg ^ 1] = nx_g0;
+        sh_ng[stg ^ 1] = nx_ng;
+      }
+      if (SC) {
+        __syncwarp();
+        issue_rows(ng1, stg ^ 1);
+      }
+      if (tid == 0 && u + 2 * ustep < nunits) slice(u + 2 * ustep, nx_g0, nx_ng, nx_slot);
+      if (SC) {
+        const int g2 = __shfl_sync(0xffffffffu, nx_g0, 0), n2 = __shfl_sync(0xffffffffu, nx_ng, 0);
+        if (u + 2 * ustep < nunits) load_crow(g2, n2);
+      }
     }
 
     T t;
@@ -830,10 +885,12 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
     float x[S][RPT], zp[S][RPT], w[S];
 #pragma unroll
     for (int s = 0; s < S; ++s) w[s] = s < t.nvalid ? stW[stg * JC + lcol0 + s] : 0.f;
-    // deferred input: this thread's rows of the plan's row scale
+    // groups of a wide plan: deferred input scaled on load, deferred output
+    const bool wp = t.active && t.pl_ng > G;
+    const bool sc_in = indef && wp, def_out = outdef && wp;
     float scin[RPT];
 #pragma unroll
-    for (int q = 0; q < RPT; ++q) scin[q] = indef ? stS[stg * MP + t.k0 + q] : 1.f;
+    for (int q = 0; q < RPT; ++q) scin[q] = sc_in ? stS[stg * MP + t.k0 + q] : 1.f;
     // Z and Y of column s from the stage; deferred input holds Z' and U
     auto ld_zy = [&](int s, float (&z)[RPT], float (&y)[RPT]) {
 #pragma unroll
@@ -843,7 +900,7 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
         z[4 * q4] = zz.x; z[4 * q4 + 1] = zz.y; z[4 * q4 + 2] = zz.z; z[4 * q4 + 3] = zz.w;
         y[4 * q4] = yy.x; y[4 * q4 + 1] = yy.y; y[4 * q4 + 2] = yy.z; y[4 * q4 + 3] = yy.w;
       }
-      if (indef) {
+      if (sc_in) {
 #pragma unroll
         for (int q = 0; q < RPT; ++q) {
           z[q] *= scin[q];
@@ -852,11 +909,24 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
       }
     };
 
+    // ground costs of column s for this thread's rows
+    auto costs = [&](int s, float (&c)[RPT]) {
+      if (SC) {
+#pragma unroll
+        for (int q4 = 0; q4 < RPT / 4; ++q4) {
+          const float4 v = *((const float4 *)(stK + stg * TILE + (lcol0 + s) * MP + t.k0) + q4);
+          c[4 * q4] = v.x; c[4 * q4 + 1] = v.y; c[4 * q4 + 2] = v.z; c[4 * q4 + 3] = v.w;
+        }
+      } else {
+        t.costs(s, c);
+      }
+    };
+
     // step 1 and the first half of step 2 (Y is kept scaled by log2(e))
 #pragma unroll
     for (int s = 0; s < S; ++s) {
       float c[RPT], z[RPT], y[RPT];
-      t.costs(s, c);
+      costs(s, c);
       ld_zy(s, z, y);
       const bool colok = s < t.nvalid;
       float csum = 0.f;
@@ -914,65 +984,61 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
     float tot[RPT];
     bool writer = false;
     const bool upd_euc = T::EUC && update;
-    if (outdef) {
-      // deferred: the slice's row partials of Z' leave for the combine kernel
-      if (t.g == 0 && t.active) {
-        float pt[RPT];
-#pragma unroll
-        for (int q = 0; q < RPT; ++q) pt[q] = 0.f;
-        for (int j = 0; j < cur_ng; ++j) {
-#pragma unroll
-          for (int q4 = 0; q4 < RPT / 4; ++q4) {
-            const float4 u4 = *((const float4 *)(sm_rs + j * MP + t.k0) + q4);
-            pt[4 * q4] += u4.x;
-            pt[4 * q4 + 1] += u4.y;
-            pt[4 * q4 + 2] += u4.z;
-            pt[4 * q4 + 3] += u4.w;
-          }
-        }
-        st_rows(a.rowpart + ((size_t)t.p * kMaxCluster + rank) * MP + t.k0, pt);
-      }
-#pragma unroll
-      for (int q = 0; q < RPT; ++q) tot[q] = 1.f;
-    } else if (CS == 1) {
-      // the plan's first group sums the plan's partials once and publishes the total
-      const int lo = t.active ? t.pl_g0 - t.cta_g0 : 0;
+    if (CS == 1) {
+      // the first group of each plan (or wide slice) in the unit sums its
+      // partials once: a small plan's total is published in shared memory, a
+      // wide slice's partial leaves for the combine kernel
+      const int lo = t.active ? max(t.pl_g0 - t.cta_g0, 0) : 0;
+      const int hi = t.active ? min(t.pl_g0 + t.pl_ng - t.cta_g0, t.cta_ng) : 0;
+      // a unit that is one deferred wide slice publishes nothing in shared memory
+      const int4 r0 = stR[stg * G];
+      const bool one_slice = outdef && (r0.w >> 4) > G && r0.y + (r0.w >> 4) >= cur_g0 + cur_ng;
       writer = t.active && t.g == lo;
       if (writer) {
 #pragma unroll
         for (int q = 0; q < RPT; ++q) tot[q] = 0.f;
-        for (int j = lo; j < lo + t.pl_ng; ++j) {
+        for (int j = lo; j < hi; ++j) {
 #pragma unroll
           for (int q4 = 0; q4 < RPT / 4; ++q4) {
-            const float4 u = *((const float4 *)(sm_rs + j * MP + t.k0) + q4);
-            tot[4 * q4] += u.x;
-            tot[4 * q4 + 1] += u.y;
-            tot[4 * q4 + 2] += u.z;
-            tot[4 * q4 + 3] += u.w;
+            const float4 u4 = *((const float4 *)(sm_rs + j * MP + t.k0) + q4);
+            tot[4 * q4] += u4.x;
+            tot[4 * q4 + 1] += u4.y;
+            tot[4 * q4 + 2] += u4.z;
+            tot[4 * q4 + 3] += u4.w;
           }
         }
-        st_rows_sm(sm_rs + lo * MP + t.k0, tot);
-        if (upd_euc) {
+        if (def_out) {
+          const int rk = (t.cta_g0 + lo - t.pl_g0) / G;
+          st_rows(a.rowpart + ((size_t)t.p * kMaxCluster + rk) * MP + t.k0, tot);
+        } else {
+          st_rows_sm(sm_rs + lo * MP + t.k0, tot);
+        }
+        if (upd_euc) {  // (support updates never run deferred)
           float *xo = a.xmom_out + (size_t)t.p * (a.dim + 1) * MP;
           for (int d = 0; d <= a.dim; ++d) {
             float mv[RPT];
 #pragma unroll
             for (int q = 0; q < RPT; ++q) mv[q] = 0.f;
-            for (int j = lo; j < lo + t.pl_ng; ++j)
+            for (int j = lo; j < hi; ++j)
 #pragma unroll
               for (int q = 0; q < RPT; ++q) mv[q] += sm_mom[(d * G + j) * MP + t.k0 + q];
             st_rows(xo + d * MP + t.k0, mv);
           }
         }
       }
-      __syncthreads();
+      if (one_slice) {
 #pragma unroll
-      for (int q4 = 0; q4 < RPT / 4; ++q4) {
-        const float4 u = *((const float4 *)(sm_rs + lo * MP + t.k0) + q4);
-        tot[4 * q4] = u.x;
-        tot[4 * q4 + 1] = u.y;
-        tot[4 * q4 + 2] = u.z;
-        tot[4 * q4 + 3] = u.w;
+        for (int q = 0; q < RPT; ++q) tot[q] = 1.f;
+      } else {
+        __syncthreads();
+#pragma unroll
+        for (int q4 = 0; q4 < RPT / 4; ++q4) {
+          const float4 u4 = *((const float4 *)(sm_rs + lo * MP + t.k0) + q4);
+          tot[4 * q4] = def_out ? 1.f : u4.x;
+          tot[4 * q4 + 1] = def_out ? 1.f : u4.y;
+          tot[4 * q4 + 2] = def_out ? 1.f : u4.z;
+          tot[4 * q4 + 3] = def_out ? 1.f : u4.w;
+        }
       }
     } else {
       // one plan across the cluster: this CTA's partial is pushed into every
@@ -1044,7 +1110,7 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
 #pragma unroll
     for (int q = 0; q < RPT; ++q) rsum += (FULL || t.k0 + q < m) ? tot[q] : 0.f;
     rsum = seg_sum<TPC>(rsum);
-    if (writer && !outdef) {
+    if (writer && !def_out) {
       float zr[RPT];
       const float inv = 1.f / rsum;
 #pragma unroll
@@ -1056,7 +1122,7 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
     float sc[RPT];
 #pragma unroll
     for (int q = 0; q < RPT; ++q) {
-      const bool ok = t.active && (FULL || t.k0 + q < m) && !outdef;
+      const bool ok = t.active && (FULL || t.k0 + q < m) && !def_out;
       sc[q] = ok ? __ldg(a.cw32 + (size_t)t.lab * MP + t.k0 + q) / tot[q] : 0.f;
     }
     float i_obj = 0.f, i_pr = 0.f, i_dr = 0.f;
@@ -1064,7 +1130,7 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
     for (int s = 0; s < S; ++s) {
       if (s < t.nvalid) {
         float y[RPT], z0[RPT], zn[RPT], yn[RPT];
-        if (CHECK || indef) {
+        if (CHECK || sc_in) {
           ld_zy(s, z0, y);
         } else {
 #pragma unroll
@@ -1073,7 +1139,7 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
             y[4 * q4] = yy.x; y[4 * q4 + 1] = yy.y; y[4 * q4 + 2] = yy.z; y[4 * q4 + 3] = yy.w;
           }
         }
-        if (outdef) {  // Z' and U = Y + X
+        if (def_out) {  // Z' and U = Y + X
 #pragma unroll
           for (int q = 0; q < RPT; ++q) {
             zn[q] = zp[s][q];
@@ -1088,7 +1154,7 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
         }
         if constexpr (CHECK) {
           float c[RPT];
-          t.costs(s, c);
+          costs(s, c);
 #pragma unroll
           for (int q = 0; q < RPT; ++q) {
             i_obj = fmaf(c[q] * inv_rho, x[s][q], i_obj);
@@ -1164,6 +1230,7 @@ cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaSt
   constexpr int CW = MODE == COST_EUCLID8 ? 8 : (MODE == COST_EUCLID4 ? 4 : 1);
   const size_t sm = smem + (size_t)4 * tma_tile_floats<MP>() * sizeof(float) +
                     2 * (size_t)GeoT<MP>::G * 16 + 2 * (size_t)JC * 4 * (1 + CW) + (size_t)2 * MP * 4 +
+                    (plan_stages_costs(MP, MODE) ? (size_t)2 * tma_tile_floats<MP>() * 4 : 0) +
                     (size_t)2 * 8 * MP * 4 + (size_t)2 * (a.dim + 1) * MP * 4;
   static size_t configured_smem = 0;
   static bool nonportable = false;
@@ -1203,8 +1270,7 @@ cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaSt
     grid[0] = (per > 0 ? per : 1) * nsm;
   }
   if (nitems <= 0) return cudaSuccess;
-  // deferred exchange: the slices of wide plans are independent CTAs
-  const bool plain = cs == 1 || (a.flags & PF_OUT_DEF);
+  const bool plain = cs == 1;
   const long long units = (long long)nitems * cs;
   int cap = plain ? grid[0] : grid[cs];
   if (plain && a.ctas_per_sm > 0) cap = std::min(cap, a.ctas_per_sm * nsm);
