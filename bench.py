@@ -16,6 +16,9 @@ Prints one JSON line:
   plain_gpu  the plain FP64 one-kernel-per-step GPU form on the same inputs
   roofline   the plan-update kernel against the measured HBM copy bandwidth
   cpu_baseline  the C restatement of the reference (oracle port) on the host
+  workloads  the word-embedding, 256-bin histogram and two-phase Euclidean
+             workloads: plan-updates/s and the plan kernel against the HBM peak
+  tuning     the launch shape the autotuner picked for the headline phase
 
 --impl reference times the reference algorithm's CPU implementation (the
 oracle port; the reference tree itself is not on the GPU host) with every
@@ -208,6 +211,41 @@ def e2e_steps(ph, c, opts, steps, warmup):
     return statistics.mean(times), h2d, d2h
 
 
+OTHER_WORKLOADS = {
+    "embed": "word embeddings: vocabulary 20000 x d=300, n=20000 documents of 20-400 Zipf(1.1) tokens, "
+             "k=20, m=64, 101 iterations (tensor-core 3xTF32 cost table)",
+    "hist": "two-phase set, phase 1: n=100000 dense 256-bin (16x16) histograms, Dirichlet(0.1), "
+            "squared grid-distance costs, k=32, m=256, 101 iterations",
+    "twophase_euclid": "two-phase set, phase 2: n=100000 Euclidean D2, d=3, m_i 4-32, k=32, m=16, "
+                       "101 iterations",
+}
+
+
+def workload_leg(name, steps, hbm):
+    """One secondary workload: autotuned, timed over whole centroid updates,
+    then the plan-update launches timed alone (profile mode)."""
+    from d2_kmeans_gb300 import badmm, synth
+    ph, c, opts = synth.workload(name, seed=0)
+    n = len(ph["p_str"])
+    P = badmm.Phase(ph, 0)
+    tune = P.autotune(c, dict(opts, maxIters=20))
+    P.run(c, opts)
+    ms, r = time_steps(P, c, opts, steps)
+    st = P.stats()
+    badmm.set_config(profile=1)
+    P.run(c, opts)
+    ps = P.stats()
+    badmm.set_config(profile=0)
+    P.close()
+    achieved = ps["plan_bytes"] / (ps["plan_ms_avg"] / 1e3) / 1e9
+    return {"workload": OTHER_WORKLOADS[name], "value": n * st["iterations"] / (ms / 1e3), "unit": UNIT,
+            "ms_per_step": ms, "iterations_per_step": st["iterations"],
+            "plan_entries": int(st["plan_entries"]), "tuning": tune["best"],
+            "plan_update": {"achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                            "algo_bytes_per_iteration": ps["plan_bytes"],
+                            "ms_per_iteration": ps["plan_ms_avg"]}}
+
+
 SERVE_WORKLOAD = ("serving: k=256 resident centroids, m=64, d=64; queries with m_q log-uniform 4-512, "
                   "GMM supports, Dirichlet(1) weights; 200 B-ADMM iterations per solve against all "
                   "centroids + argmin; Poisson arrivals")
@@ -236,7 +274,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--skip", default="", help="comma list of legs to skip: e2e,plain,cpu,profile,serve")
+    ap.add_argument("--skip", default="",
+                    help="comma list of legs to skip: e2e,plain,cpu,profile,serve,workloads")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -263,6 +302,7 @@ def main():
     ph, c, opts = synth.workload("batched", seed=0)
     n = len(ph["p_str"])
     P = badmm.Phase(ph, 0)
+    tuning = P.autotune(c, dict(opts, maxIters=20))
     for _ in range(args.warmup):
         P.run(c, opts)
     gpu = int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0)
@@ -309,7 +349,7 @@ def main():
                       "l2": "inputs larger than L2: Z and Y are 1.1 GB each",
                       "plan_entries": int(stats["plan_entries"])},
            "clocks": clocks, "gpu_launches": int(stats["kernel_launches"]) * args.steps,
-           "roofline": roof}
+           "roofline": roof, "tuning": tuning}
 
     if "plain" not in skip and rank == 0:
         Q = badmm.Phase(ph, 1)
@@ -329,6 +369,8 @@ def main():
                       "api": "d2_centroid_sphBregman (reference structs, host buffers)"}
     if "serve" not in skip and rank == 0:
         out["serve"] = serve_leg()
+    if "workloads" not in skip and rank == 0:
+        out["workloads"] = {w: workload_leg(w, 2, hbm) for w in OTHER_WORKLOADS}
     if "cpu" not in skip and rank == 0:
         ensure_oracle()
         v, units, wall = cpu_baseline(1, 20000 / 200000, 21, seed=100)

@@ -85,6 +85,11 @@ class d2g_run_stats(C.Structure):
                 ("plan_entries", C.c_size_t), ("path", C.c_int)]
 
 
+class d2g_tuning(C.Structure):
+    _fields_ = [("exchange", C.c_int), ("stage_costs", C.c_int), ("ctas_per_sm", C.c_int),
+                ("cost_gemm", C.c_int)]
+
+
 class d2g_server_desc(C.Structure):
     _fields_ = [("num_of_labels", C.c_int), ("str", C.c_int), ("dim", C.c_int),
                 ("c_w", C.c_void_p), ("c_supp", C.c_void_p), ("iters", C.c_int),
@@ -118,6 +123,10 @@ SIGNATURES = {
     "d2g_phase_stats": (C.c_int, [C.c_void_p, C.POINTER(d2g_run_stats)]),
     "d2g_phase_get_scratch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "d2g_phase_stream": (C.c_void_p, [C.c_void_p]),
+    "d2g_phase_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(d2g_tuning)]),
+    "d2g_phase_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(d2g_tuning)]),
+    "d2g_phase_autotune": (C.c_int, [C.c_void_p, C.POINTER(d2g_badmm_opts), C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
     "d2g_server_create": (C.c_int, [C.POINTER(d2g_server_desc), C.POINTER(C.c_void_p)]),
     "d2g_server_destroy": (C.c_int, [C.c_void_p]),
     "d2g_server_submit": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,

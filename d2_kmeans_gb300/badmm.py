@@ -122,6 +122,42 @@ class Phase:
         """cudaStream_t (as an integer) that this phase's kernels run on."""
         return self.lib.d2g_phase_stream(self.h) or 0
 
+    def tuning(self) -> dict:
+        """Launch-shape choices of this phase (d2g_tuning)."""
+        t = L.d2g_tuning()
+        L.check(self.lib.d2g_phase_get_tuning(self.h, C.byref(t)), "d2g_phase_get_tuning")
+        return {f: getattr(t, f) for f, _ in L.d2g_tuning._fields_}
+
+    def set_tuning(self, **kw) -> dict:
+        old = self.tuning()
+        t = L.d2g_tuning(**dict(old, **{k: int(v) for k, v in kw.items()}))
+        L.check(self.lib.d2g_phase_set_tuning(self.h, C.byref(t)), "d2g_phase_set_tuning")
+        return old
+
+    def autotune(self, centroids: dict, opts: dict) -> dict:
+        """Time every candidate tuning with short runs of ``opts`` (the plans
+        are restored afterwards), keep the fastest; returns the chosen tuning
+        and the candidates with their loop times in ms."""
+        o = L.d2g_badmm_opts()
+        o.maxIters = int(opts.get("maxIters", 20))
+        o.rhoCoeff = float(opts.get("rhoCoeff", 2.0))
+        o.updatePerLoops = int(opts.get("updatePerLoops", 10))
+        o.time_budget = 0.0
+        c_w = np.ascontiguousarray(centroids["c_w"], dtype=np.float64).reshape(-1)
+        cs = centroids.get("c_supp")
+        c_supp = None if cs is None else np.ascontiguousarray(cs, dtype=np.float64).reshape(-1)
+        cap = 64
+        cands = (L.d2g_tuning * cap)()
+        ms = np.zeros(cap)
+        n = C.c_int(0)
+        L.check(self.lib.d2g_phase_autotune(self.h, C.byref(o), c_w.ctypes.data,
+                                            None if c_supp is None else c_supp.ctypes.data,
+                                            cands, ms.ctypes.data, cap, C.byref(n)),
+                "d2g_phase_autotune")
+        rows = [({f: getattr(cands[i], f) for f, _ in L.d2g_tuning._fields_}, float(ms[i]))
+                for i in range(min(n.value, cap))]
+        return {"best": self.tuning(), "candidates": rows}
+
     def stats(self) -> dict:
         st = L.d2g_run_stats()
         L.check(self.lib.d2g_phase_stats(self.h, C.byref(st)), "d2g_phase_stats")

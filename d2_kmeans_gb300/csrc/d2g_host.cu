@@ -10,6 +10,7 @@
 // The plain FP64 form runs one kernel per reference step instead.
 #include <algorithm>
 #include <climits>
+#include <cstdio>
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
@@ -82,7 +83,7 @@ struct d2g_phase {
   int metric = 0, dim = 0, str = 0, K = 0, vocab_size = 0;
   size_t size = 0, col = 0, global_size = 0;
   int path = 0;  // 0 batched FP32, 1 plain FP64
-  int cost_gemm = 0;  // word-embedding cost table: 0 tensor cores, 1 CUDA cores (per run)
+  int cost_gemm = 0;  // word-embedding cost table: 0 tensor cores, 1 CUDA cores
   std::vector<int> p_str, label;
   std::vector<long long> cum;
   cudaStream_t st = nullptr;
@@ -125,6 +126,7 @@ struct d2g_phase {
   std::vector<int> h_wide_plans;  // packed ids
   Bucket units{1, 0, 0, 0};       // units of the deferred iterations
   int stage_costs = 0;
+  d2g_tuning tune{0, 0, 0, 0};    // launch-shape choices (autotuner)
   int nwide = 0;
   bool defer = false;
   DBuf<float> rowpart, rowsc;
@@ -164,6 +166,62 @@ struct d2g_phase {
 };
 
 namespace d2g {
+
+// ------------------------------------------------------------ tuning cache
+// Key: the phase's shape.  Records live in this process and, when the
+// environment names a file in D2G_TUNE_CACHE, in that file (one line per
+// record: key exchange stage_costs ctas_per_sm cost_gemm; later lines win).
+static std::string tune_key(const d2g_phase *ph) {
+  char b[256];
+  snprintf(b, sizeof b, "m%d.s%d.d%d.n%zu.c%zu.k%d.v%d.t%d", ph->metric, ph->str, ph->dim, ph->size,
+           ph->col, ph->K, ph->vocab_size, ph->use_tma);
+  return b;
+}
+static std::mutex g_tune_mu;
+static std::vector<std::pair<std::string, d2g_tuning>> g_tune_mem;
+
+static bool tune_cache_get(const std::string &key, d2g_tuning *t) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  for (auto it = g_tune_mem.rbegin(); it != g_tune_mem.rend(); ++it)
+    if (it->first == key) {
+      *t = it->second;
+      return true;
+    }
+  const char *path = getenv("D2G_TUNE_CACHE");
+  if (!path || !*path) return false;
+  FILE *f = fopen(path, "r");
+  if (!f) return false;
+  bool found = false;
+  char k[256];
+  d2g_tuning r;
+  while (fscanf(f, "%255s %d %d %d %d", k, &r.exchange, &r.stage_costs, &r.ctas_per_sm,
+                &r.cost_gemm) == 5)
+    if (key == k) {
+      *t = r;
+      found = true;
+    }
+  fclose(f);
+  return found;
+}
+
+static void tune_cache_put(const std::string &key, const d2g_tuning &t) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_mem.emplace_back(key, t);
+  const char *path = getenv("D2G_TUNE_CACHE");
+  if (!path || !*path) return;
+  FILE *f = fopen(path, "a");
+  if (!f) return;
+  fprintf(f, "%s %d %d %d %d\n", key.c_str(), t.exchange, t.stage_costs, t.ctas_per_sm, t.cost_gemm);
+  fclose(f);
+}
+
+// the run-time switches that follow from the phase's tuning
+static void apply_tuning(d2g_phase *ph) {
+  ph->defer = ph->path == 0 && ph->use_tma && ph->nwide > 0 && ph->units.nitems > 0 &&
+              ph->tune.exchange == 0;
+  ph->stage_costs = ph->tune.stage_costs;
+  ph->cost_gemm = ph->tune.cost_gemm;
+}
 
 static bool batched_supported(const d2g_phase_desc *d, std::string *why) {
   if (d->str > 256) {
@@ -366,6 +424,7 @@ static PlanArgs base_args(d2g_phase *ph) {
   a.X_out = ph->Xp.p;
   a.resid_part = ph->resid_part.p;
   a.ctl = ph->ctl.p;
+  a.ctas_per_sm = ph->tune.ctas_per_sm;
   a.m = ph->str;
   a.dim = ph->metric == D2_EUCLIDEAN_L2 ? ph->dim : 0;
   a.use_tma = ph->use_tma;
@@ -375,6 +434,7 @@ static PlanArgs base_args(d2g_phase *ph) {
   a.rowsc = ph->rowsc.p;
   a.col_crow = ph->metric == D2_WORD_EMBED ? ph->col_crow.p : ph->col_sym.p;
   a.stage_costs = ph->stage_costs;
+  a.wide = ph->nwide > 0;
   return a;
 }
 
@@ -428,7 +488,7 @@ static int set_labels_impl(d2g_phase *ph, const int *label) {
       ph->h_grp_rec[gi].x = slot[p];
       ph->h_grp_rec[gi].z = pl[p];
     }
-    if (ph->nwide > 0) {  // wide plans: {slot, slices with columns, label}
+    if (ph->nwide > 0 && ph->path == 0) {  // wide plans: {slot, slices with columns, label}
       std::vector<int4> wl(ph->nwide);
       for (int q = 0; q < ph->nwide; ++q) {
         const int p = ph->h_wide_plans[q];
@@ -548,9 +608,7 @@ static int create_batched(d2g_phase *ph, const d2g_phase_desc *d) {
   }
   const char *pk = getenv("D2G_PLAN_KERNEL");
   ph->use_tma = !(pk && std::string(pk) == "v1");
-  const char *dx = getenv("D2G_WIDE_EXCHANGE");  // "cluster": synchronous DSMEM exchange always
-  const bool defer_ok = ph->use_tma && !(dx && std::string(dx) == "cluster");
-  int rc = build_packing(ph, defer_ok);
+  int rc = build_packing(ph, ph->use_tma != 0);
   if (rc) return rc;
   const size_t nz = (size_t)ph->ncols_packed * ph->MP;
   D2G_CUDA(ph->Z.alloc(nz));
@@ -583,9 +641,18 @@ static int create_batched(d2g_phase *ph, const d2g_phase_desc *d) {
 
   int rc2 = upload_columns_batched(ph, d);
   if (rc2) return rc2;
-  ph->defer = defer_ok && ph->nwide > 0;
-  const char *sc = getenv("D2G_STAGE_COSTS");
-  ph->stage_costs = sc && std::string(sc) == "1";
+  // launch-shape defaults: the environment, the global configuration, then
+  // whatever the autotuner recorded for this shape
+  {
+    const char *dx = getenv("D2G_WIDE_EXCHANGE");  // "cluster": synchronous DSMEM exchange
+    const char *sc = getenv("D2G_STAGE_COSTS");    // "1": table costs by bulk copy
+    ph->tune.exchange = (dx && std::string(dx) == "cluster") ? 1 : 0;
+    ph->tune.stage_costs = (sc && std::string(sc) == "1") ? 1 : 0;
+    ph->tune.ctas_per_sm = 0;
+    ph->tune.cost_gemm = cfg_snapshot().cost_gemm;
+    d2g_tuning rec;
+    if (tune_cache_get(tune_key(ph), &rec)) ph->tune = rec;
+  }
   if (ph->nwide > 0) {
     D2G_CUDA(ph->rowpart.alloc((size_t)ph->nplans * kMaxCluster * ph->MP));
     D2G_CUDA(ph->rowsc.alloc((size_t)ph->nplans * ph->MP));
@@ -736,7 +803,7 @@ static std::vector<unsigned long long> loop_signature(d2g_phase *ph) {
           (unsigned long long)ph->nchunk, (unsigned long long)ph->chunk,
           (unsigned long long)ph->global_size, (unsigned long long)ph->cost_gemm,
           u(ph->wide.p), u(ph->def_iter.p), u(ph->rowpart.p), u(ph->rowsc.p), u(ph->col_crow.p),
-          (unsigned long long)ph->stage_costs,
+          (unsigned long long)ph->stage_costs, (unsigned long long)ph->tune.ctas_per_sm,
           (unsigned long long)ph->defer};
 }
 
@@ -899,7 +966,7 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
 static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, double *c_supp,
                     const char *label_switch) {
   const d2g_config cfg = cfg_snapshot();
-  ph->cost_gemm = cfg.cost_gemm;
+  apply_tuning(ph);
   if (!opt || opt->maxIters < 0 || opt->updatePerLoops <= 0 || !(opt->rhoCoeff > 0) || !c_w)
     return fail(D2G_E_INVAL, "bad B-ADMM options");
   const bool euc = ph->metric == D2_EUCLIDEAN_L2, emb = ph->metric == D2_WORD_EMBED;
@@ -1042,8 +1109,10 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
   {
     const double ent = (double)ph->col * m;
     const double colb = ph->path == 0 ? (double)ph->col * (euc ? 4.0 * (1 + dim) : 8.0) : 0.0;
-    // (table-mode costs are read from an L2-resident table and are not counted as HBM bytes)
-    ph->stats.plan_bytes = ph->path == 0 ? 16.0 * ent + colb + 4.0 * m * (double)n : 136.0 * ent;
+    // word-embedding costs stream from the per-cluster vocabulary table (4 B per
+    // entry); histogram costs come from one str x str table that stays in L2
+    ph->stats.plan_bytes = ph->path == 0 ? (emb ? 20.0 : 16.0) * ent + colb + 4.0 * m * (double)n
+                                         : 136.0 * ent;
   }
   if (h.err == kErrTcTimeout)
     return fail(D2G_E_CUDA, "tensor-core cost table: wait for the MMA completion timed out");
@@ -1312,6 +1381,82 @@ int d2g_badmm_run(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, double 
                   const char *label_switch) {
   if (!ph) return D2G_E_INVAL;
   return run_impl(ph, opt, c_w, c_supp, label_switch);
+}
+
+int d2g_phase_get_tuning(d2g_phase *ph, d2g_tuning *t) {
+  if (!ph || !t) return D2G_E_INVAL;
+  *t = ph->tune;
+  return D2G_OK;
+}
+
+int d2g_phase_set_tuning(d2g_phase *ph, const d2g_tuning *t) {
+  if (!ph || !t || t->exchange < 0 || t->exchange > 1 || t->stage_costs < 0 || t->stage_costs > 1 ||
+      t->ctas_per_sm < 0 || t->ctas_per_sm > 32 || t->cost_gemm < 0 || t->cost_gemm > 1)
+    return fail(D2G_E_INVAL, "bad tuning");
+  ph->tune = *t;
+  return D2G_OK;
+}
+
+int d2g_phase_autotune(d2g_phase *ph, const d2g_badmm_opts *opt, const double *c_w,
+                       const double *c_supp, d2g_tuning *cands, double *ms, int max_out,
+                       int *n_out) {
+  if (!ph || !opt || !c_w || max_out < 0) return fail(D2G_E_INVAL, "bad autotune arguments");
+  const bool euc = ph->metric == D2_EUCLIDEAN_L2, emb = ph->metric == D2_WORD_EMBED;
+  if ((euc || emb) && !c_supp) return fail(D2G_E_INVAL, "c_supp required for this metric");
+  if (n_out) *n_out = 0;
+  if (ph->path != 0) return D2G_OK;  // the FP64 form has no launch-shape choices
+  // candidates: every combination of the choices that apply to this phase
+  const d2g_tuning base = ph->tune;
+  std::vector<int> ex = {base.exchange}, sc = {0}, cp = {0}, cg = {base.cost_gemm};
+  if (ph->use_tma && ph->nwide > 0 && ph->units.nitems > 0) ex = {0, 1};
+  if (ph->use_tma && ph->mode == COST_TABLE && ph->MP >= 16 && ph->MP <= 128) sc = {0, 1};
+  if (ph->use_tma && ph->MP < 256) cp = {0, 1};
+  if (emb) cg = {0, 1};
+  std::vector<d2g_tuning> cand;
+  for (int e : ex)
+    for (int s2 : sc)
+      for (int c : cp)
+        for (int g : cg) cand.push_back(d2g_tuning{e, s2, c, g});
+  // the phase's plans are re-initialised by the trial runs: keep them
+  const size_t nz = (size_t)ph->ncols_packed * ph->MP;
+  const bool had_plans = ph->plans_valid;
+  DBuf<float> zsave;
+  if (had_plans) {
+    D2G_CUDA(zsave.alloc(nz));
+    D2G_CUDA(cudaMemcpyAsync(zsave.p, ph->Z.p, nz * 4, cudaMemcpyDeviceToDevice, ph->st));
+  }
+  const size_t ncw = (size_t)ph->K * ph->str, ncs = (euc || emb) ? ncw * ph->dim : 0;
+  std::vector<double> cw(ncw), cs(ncs);
+  d2g_badmm_opts o = *opt;
+  o.time_budget = 0;
+  std::vector<double> t(cand.size(), 1e300);
+  int rc = D2G_OK;
+  for (size_t i = 0; i < cand.size() && !rc; ++i) {
+    ph->tune = cand[i];
+    for (int rep = 0; rep < 3 && !rc; ++rep) {  // the first run captures the graph
+      std::copy(c_w, c_w + ncw, cw.begin());
+      if (ncs) std::copy(c_supp, c_supp + ncs, cs.begin());
+      rc = run_impl(ph, &o, cw.data(), ncs ? cs.data() : nullptr, nullptr);
+      if (!rc && rep > 0) t[i] = std::min(t[i], ph->stats.total_ms);
+    }
+  }
+  size_t best = 0;
+  for (size_t i = 1; i < cand.size(); ++i)
+    if (t[i] < t[best]) best = i;
+  ph->tune = rc ? base : cand[best];
+  if (had_plans) {
+    cudaMemcpyAsync(ph->Z.p, zsave.p, nz * 4, cudaMemcpyDeviceToDevice, ph->st);
+    cudaStreamSynchronize(ph->st);
+  }
+  ph->plans_valid = had_plans;
+  if (rc) return rc;
+  tune_cache_put(tune_key(ph), ph->tune);
+  for (int i = 0; i < (int)cand.size() && i < max_out; ++i) {
+    if (cands) cands[i] = cand[i];
+    if (ms) ms[i] = t[i];
+  }
+  if (n_out) *n_out = (int)cand.size();
+  return D2G_OK;
 }
 
 int d2g_phase_trace(d2g_phase *ph, double *trace, int cap, int *n) {

@@ -714,7 +714,9 @@ __host__ __device__ constexpr bool plan_stages_costs(int MP, int MODE) {
   return MODE == COST_TABLE && MP >= 16 && MP <= 128;
 }
 
-template <int MP, int MODE, bool CHECK, bool FULL>
+// WIDE: the phase has plans wider than one CTA (cluster launches, deferred
+// units); without them the exchange machinery compiles out.
+template <int MP, int MODE, bool CHECK, bool FULL, bool WIDE>
 __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
     plan_kernel_tma(const PlanArgs a, int nitems) {
   using T = Tile<MP, MODE>;
@@ -754,10 +756,10 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
   // scaling) and U = Y + X and its row partials go to global memory, where a
   // combine kernel forms the plan's row scale c_w / rowsum(Z').  The next
   // iteration applies that scale on load (PF_IN_DEF): Z = Z' * scale, Y = U - Z.
-  const int CS = a.cs;
-  const bool clustered = CS > 1;
-  const bool outdef = (a.flags & PF_OUT_DEF) != 0;
-  const bool indef = (a.flags & PF_IN_DEF) != 0;
+  const int CS = WIDE ? a.cs : 1;
+  const bool clustered = WIDE && CS > 1;
+  const bool outdef = WIDE && (a.flags & PF_OUT_DEF) != 0;
+  const bool indef = WIDE && (a.flags & PF_IN_DEF) != 0;
   const int crank = clustered ? (int)(blockIdx.x % CS) : 0;
   const int u0 = clustered ? (int)(blockIdx.x / CS) : (int)blockIdx.x;
   const int ustep = clustered ? (int)(gridDim.x / CS) : (int)gridDim.x;
@@ -886,7 +888,7 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
 #pragma unroll
     for (int s = 0; s < S; ++s) w[s] = s < t.nvalid ? stW[stg * JC + lcol0 + s] : 0.f;
     // groups of a wide plan: deferred input scaled on load, deferred output
-    const bool wp = t.active && t.pl_ng > G;
+    const bool wp = WIDE && t.active && t.pl_ng > G;
     const bool sc_in = indef && wp, def_out = outdef && wp;
     float scin[RPT];
 #pragma unroll
@@ -991,8 +993,11 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
       const int lo = t.active ? max(t.pl_g0 - t.cta_g0, 0) : 0;
       const int hi = t.active ? min(t.pl_g0 + t.pl_ng - t.cta_g0, t.cta_ng) : 0;
       // a unit that is one deferred wide slice publishes nothing in shared memory
-      const int4 r0 = stR[stg * G];
-      const bool one_slice = outdef && (r0.w >> 4) > G && r0.y + (r0.w >> 4) >= cur_g0 + cur_ng;
+      bool one_slice = false;
+      if (outdef) {
+        const int4 r0 = stR[stg * G];
+        one_slice = (r0.w >> 4) > G && r0.y + (r0.w >> 4) >= cur_g0 + cur_ng;
+      }
       writer = t.active && t.g == lo;
       if (writer) {
 #pragma unroll
@@ -1040,7 +1045,7 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
           tot[4 * q4 + 3] = def_out ? 1.f : u4.w;
         }
       }
-    } else {
+    } else if constexpr (WIDE) {
       // one plan across the cluster: this CTA's partial is pushed into every
       // rank's shared memory (double-buffered by stage), one cluster barrier,
       // then every rank adds the CS partials from its own shared memory
@@ -1222,7 +1227,7 @@ static inline cudaLaunchConfig_t plan_cfg(int nblocks, size_t smem, cudaStream_t
   return cfg;
 }
 
-template <int MP, int MODE, bool CHECK, bool FULL>
+template <int MP, int MODE, bool CHECK, bool FULL, bool WIDE>
 cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaStream_t st) {
   // persistent grid: as many clusters of a.cs CTAs as are resident at once
   static int grid[kMaxCluster + 1] = {0};
@@ -1234,7 +1239,7 @@ cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaSt
                     (size_t)2 * 8 * MP * 4 + (size_t)2 * (a.dim + 1) * MP * 4;
   static size_t configured_smem = 0;
   static bool nonportable = false;
-  auto kern = plan_kernel_tma<MP, MODE, CHECK, FULL>;
+  auto kern = plan_kernel_tma<MP, MODE, CHECK, FULL, WIDE>;
   if (configured_smem < sm) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
@@ -1283,8 +1288,12 @@ cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaSt
 template <int MP, int MODE, bool CHECK>
 cudaError_t launch_plan_t(const PlanArgs &a, int nitems, size_t smem, cudaStream_t st) {
   if (a.use_tma) {
-    if (a.m == MP) return launch_plan_tma_t<MP, MODE, CHECK, true>(a, nitems, smem, st);
-    return launch_plan_tma_t<MP, MODE, CHECK, false>(a, nitems, smem, st);
+    if (a.wide) {
+      if (a.m == MP) return launch_plan_tma_t<MP, MODE, CHECK, true, true>(a, nitems, smem, st);
+      return launch_plan_tma_t<MP, MODE, CHECK, false, true>(a, nitems, smem, st);
+    }
+    if (a.m == MP) return launch_plan_tma_t<MP, MODE, CHECK, true, false>(a, nitems, smem, st);
+    return launch_plan_tma_t<MP, MODE, CHECK, false, false>(a, nitems, smem, st);
   }
   // the dynamic shared-memory limit is raised once per kernel, before any
   // stream capture (launch_plan is first called with nitems == 0 for that)

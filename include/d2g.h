@@ -176,8 +176,8 @@ typedef struct {
   int use_graph;    /* 1: replay the iteration loop as one CUDA graph (default) */
   int sync_scratch; /* 1: also write the host X, Y and C back after a drop-in call */
   int profile;      /* 1: time every plan-update launch with CUDA events (no graph) */
-  int cost_gemm;    /* word-embedding cost table: 0 tensor cores, 3xTF32 (default);
-                       1 FP32 CUDA cores */
+  int cost_gemm;    /* word-embedding cost table of phases created afterwards:
+                       0 tensor cores, 3xTF32 (default); 1 FP32 CUDA cores */
 } d2g_config;
 
 int d2g_get_config(d2g_config *cfg);
@@ -249,6 +249,34 @@ void *d2g_phase_stream(d2g_phase *ph);
 /* the last run's X (after step 1, or X-Z after a check iteration as the
  * reference leaves it), Y and C (divided by rho), reference layout, FP64 */
 int d2g_phase_get_scratch(d2g_phase *ph, double *X, double *Y, double *C);
+
+/* ------------------------------------------------------------- autotuning
+ * Launch-shape choices of the batched form.  All choices compute the same
+ * B-ADMM iteration; they differ in speed (and, for exchange, in the rounding
+ * of Y's update: two FP32 roundings instead of one). */
+typedef struct {
+  int exchange;     /* plans wider than one CTA: 0 deferred row normalisation (one plain
+                       launch over packed units), 1 synchronous DSMEM exchange on a
+                       thread-block cluster per plan */
+  int stage_costs;  /* table costs (16 <= padded str <= 128) copied into shared memory with
+                       the plans (1) or read through the cache (0) */
+  int ctas_per_sm;  /* persistent plan-update grid: CTAs per SM, 0 = occupancy limit */
+  int cost_gemm;    /* word-embedding cost table: 0 tensor cores (3xTF32), 1 CUDA cores */
+} d2g_tuning;
+
+int d2g_phase_get_tuning(d2g_phase *ph, d2g_tuning *t);
+int d2g_phase_set_tuning(d2g_phase *ph, const d2g_tuning *t);
+/* Time every candidate tuning on this phase with short runs (opt->maxIters
+ * iterations from c_w / c_supp, which are not modified; plans re-initialised
+ * and restored afterwards), keep the fastest on the phase and record it under
+ * the phase's shape key: in this process, and in the text file named by the
+ * environment variable D2G_TUNE_CACHE when set.  Phases created later with
+ * the same shape start from the recorded tuning.  Up to max_out candidates
+ * and their loop times (ms, best of two graph replays) are written to cands /
+ * ms (either may be NULL); *n_out receives the number of candidates. */
+int d2g_phase_autotune(d2g_phase *ph, const d2g_badmm_opts *opt, const double *c_w,
+                       const double *c_supp, d2g_tuning *cands, double *ms, int max_out,
+                       int *n_out);
 
 /* ------------------------------------------------------------- serving API */
 typedef struct d2g_server d2g_server;

@@ -314,3 +314,34 @@ def test_word_embedding_cost_table_paths_agree(d2g):
     a, b = out
     np.testing.assert_allclose(a["trace"][:, 1], b["trace"][:, 1], rtol=2e-6)
     assert np.abs(a["c_w"] - b["c_w"]).sum() <= 1e-5 * 6
+
+
+def test_autotune_times_every_candidate_and_keeps_results(d2g, oracle_mod, tmp_path, monkeypatch):
+    """The autotuner times every candidate tuning (wide-plan exchange x table-cost
+    staging x CTAs per SM x cost-table GEMM for an embedding phase with plans
+    wider than one CTA), keeps the fastest, leaves the phase's plans as they
+    were, records the choice in the D2G_TUNE_CACHE file, and a new phase of the
+    same shape starts from it.  The tuned phase still matches the oracle."""
+    cache = tmp_path / "tune.txt"
+    monkeypatch.setenv("D2G_TUNE_CACHE", str(cache))
+    ph, c = synth.embed_phase(100, 4, 64, V=1500, dim=300, sizes=(20, 400), seed=65)
+    opts = dict(maxIters=30, rhoCoeff=2.0, updatePerLoops=10)
+    ref = _port(oracle_mod, ph, c, opts)
+    P = d2g.Phase(ph, 0)
+    P.run(c, opts)
+    z0 = P.get_plans()
+    out = P.autotune(c, dict(maxIters=12, rhoCoeff=2.0, updatePerLoops=10))
+    cands = out["candidates"]
+    assert len(cands) == 16
+    assert all(0 < ms < 1e9 for _, ms in cands)
+    fastest = min(cands, key=lambda r: r[1])[0]
+    assert out["best"] == fastest
+    np.testing.assert_array_equal(P.get_plans(), z0)
+    assert_close(P.run(c, opts), ref, 4, 64)
+    P.close()
+    rec = cache.read_text().split()
+    assert len(rec) == 5 and [int(v) for v in rec[1:]] == [fastest[k] for k in
+                                                           ("exchange", "stage_costs", "ctas_per_sm", "cost_gemm")]
+    Q = d2g.Phase(ph, 0)
+    assert Q.tuning() == fastest
+    Q.close()
