@@ -155,13 +155,15 @@ __global__ void __launch_bounds__(256) support_num_kernel(const float *__restric
 }
 
 // c_supp[l][k][t] = sum_chunks num / sum_chunks den, chunks in order, FP64.
+// grid (K, ceil(m*d / 256)): one thread per (cluster, support, coordinate).
 __global__ void support_final_kernel(const float *__restrict__ part, int nchunk, int K, int MP,
                                      int m, int d, double *__restrict__ cs64,
                                      float *__restrict__ cs32f, Ctl *ctl, int iter) {
   if (iter >= ctl->stop_iter) return;
   const int l = blockIdx.x;
   const int d1 = d + 1;
-  for (int i = threadIdx.x; i < m * d; i += blockDim.x) {
+  const int i = blockIdx.y * blockDim.x + threadIdx.x;
+  if (i < m * d) {
     const int k = i / d, t = i - k * d;
     double num = 0.0, den = 0.0;
     for (int c = 0; c < nchunk; ++c) {
@@ -211,8 +213,8 @@ cudaError_t launch_embed_support(const EmbedArgs &e, cudaStream_t st) {
                                                                  e.npairs, e.X, e.MP, e.m, e.V, e.W);
   dim3 g2((e.d + 1 + kTile - 1) / kTile, e.K, e.nchunk);
   support_num_kernel<<<g2, 256, 0, st>>>(e.W, e.vocab, e.V, e.d, e.MP, e.chunk, e.m, e.part);
-  support_final_kernel<<<e.K, 256, 0, st>>>(e.part, e.nchunk, e.K, e.MP, e.m, e.d, e.cs64, e.cs32f,
-                                            e.ctl, e.iter);
+  support_final_kernel<<<dim3(e.K, (e.m * e.d + 255) / 256), 256, 0, st>>>(
+      e.part, e.nchunk, e.K, e.MP, e.m, e.d, e.cs64, e.cs32f, e.ctl, e.iter);
   err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   return launch_cost_table(e.cs32f, e.K, e.m, e.vocab, e.V, e.d, e.cnorm, e.vnorm, e.MP, e.T, e.gemm,
