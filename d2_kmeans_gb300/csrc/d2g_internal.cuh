@@ -183,6 +183,7 @@ struct ServeArgs {
   const int4 *items;      // {request, first centroid, plans in the item, groups per plan}
   const float4 *reqs;     // per request {column offset (int bits), m_q (int bits), log2(e)/rho, 0}
   float *cost_out;        // [requests * K]
+  int *err;               // set when a cluster exchange wait ran out
   int K, m, dim, iters, cs;
 };
 cudaError_t launch_serve(int MP, const ServeArgs &a, int nitems, cudaStream_t st);

@@ -57,6 +57,7 @@ struct Slot {
   std::vector<Request *> reqs;
   // device
   float *q_w = nullptr, *q_supp = nullptr, *cost = nullptr;
+  int *err = nullptr, *h_err = nullptr;  // cluster exchange wait ran out (device, pinned copy)
   int4 *items = nullptr;
   float4 *rq = nullptr;
   size_t cap_cols = 0, cap_items = 0, cap_reqs = 0;
@@ -98,6 +99,12 @@ namespace d2g {
 namespace {
 
 int slot_reserve(d2g_server *s, Slot &sl, size_t cols, size_t nitems, size_t nreq) {
+  if (!sl.err) {
+    D2G_CUDA(cudaMalloc(&sl.err, sizeof(int)));
+    D2G_CUDA(cudaMallocHost(&sl.h_err, sizeof(int)));
+    D2G_CUDA(cudaMemset(sl.err, 0, sizeof(int)));
+    *sl.h_err = 0;
+  }
   auto grow = [](size_t want, size_t have) { return want <= have ? have : std::max(want, have * 2); };
   if (cols > sl.cap_cols) {
     const size_t c = grow(cols, sl.cap_cols);
@@ -191,6 +198,7 @@ int launch_batch(d2g_server *s, Slot &sl) {
   a.c_supp32 = s->c_supp32;
   a.reqs = sl.rq;
   a.cost_out = sl.cost;
+  a.err = sl.err;
   a.K = s->K;
   a.m = s->m;
   a.dim = s->dim;
@@ -203,6 +211,7 @@ int launch_batch(d2g_server *s, Slot &sl) {
     io += by_cs[ci].size();
   }
   D2G_CUDA(cudaMemcpyAsync(sl.h_cost, sl.cost, sl.reqs.size() * s->K * 4, cudaMemcpyDeviceToHost, sl.st));
+  D2G_CUDA(cudaMemcpyAsync(sl.h_err, sl.err, sizeof(int), cudaMemcpyDeviceToHost, sl.st));
   D2G_CUDA(cudaEventRecord(sl.ev, sl.st));
   sl.busy = true;
   return D2G_OK;
@@ -211,6 +220,10 @@ int launch_batch(d2g_server *s, Slot &sl) {
 void finish_batch(d2g_server *s, Slot &sl) {
   const double t = now_ms();
   std::lock_guard<std::mutex> lk(s->mu);
+  if (*sl.h_err && !s->error) {
+    s->error = D2G_E_CUDA;
+    s->error_msg = "serving: a cluster exchange wait ran out";
+  }
   for (size_t i = 0; i < sl.reqs.size(); ++i) {
     Request *r = sl.reqs[i];
     r->costs.resize(s->K);
@@ -360,6 +373,8 @@ int d2g_server_destroy(d2g_server *s) {
     cudaFreeHost(sl.h_cost);
     cudaFreeHost(sl.h_items);
     cudaFreeHost(sl.h_rq);
+    cudaFree(sl.err);
+    cudaFreeHost(sl.h_err);
     if (sl.ev) cudaEventDestroy(sl.ev);
     if (sl.st) cudaStreamDestroy(sl.st);
   }

@@ -34,6 +34,61 @@ __device__ __forceinline__ float sv_ex2(float x) {
   return y;
 }
 
+__device__ __forceinline__ unsigned sv_smem(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ unsigned long long sv_now() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// mbarrier in this CTA's shared memory, one arrival per phase
+__device__ __forceinline__ void sv_mbar_init(unsigned long long *b) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sv_smem(b)) : "memory");
+}
+
+__device__ __forceinline__ void sv_mbar_expect(unsigned long long *b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sv_smem(b)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool sv_mbar_test(unsigned long long *b, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(sv_smem(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait (about one second), then report
+__device__ __forceinline__ bool sv_mbar_wait(unsigned long long *b, unsigned parity) {
+  if (sv_mbar_test(b, parity)) return true;
+  const unsigned long long t0 = sv_now();
+  for (;;) {
+    for (int i = 0; i < 32; ++i)
+      if (sv_mbar_test(b, parity)) return true;
+    if (sv_now() - t0 > 1000000000ull) return false;
+  }
+}
+
+// 16 bytes into the shared memory of cluster rank `rank` at the same offset as
+// `local`, completing `bytes` on that rank's mbarrier at the offset of `bar`
+__device__ __forceinline__ void sv_push4(const float *local, const unsigned long long *bar,
+                                         unsigned rank, float4 v) {
+  unsigned ra, rb;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(sv_smem(local)), "r"(rank));
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(rb) : "r"(sv_smem(bar)), "r"(rank));
+  asm volatile(
+      "st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(ra),
+      "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w), "r"(rb)
+      : "memory");
+}
+
 template <int TPC>
 __device__ __forceinline__ float sv_seg_sum(float v) {
 #pragma unroll
@@ -49,8 +104,11 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
   __shared__ __align__(16) float sm_rs[2][G * MP];       // per-group row partials, by parity
   __shared__ __align__(16) float sm_x[2][8][MP];         // cluster: every rank's partial, by parity
   __shared__ double sm_cost[G];
+  __shared__ __align__(8) unsigned long long sm_bar[2];  // cluster: partials of all ranks landed, by parity
+  __shared__ int sm_fail;
 
   const int tid = threadIdx.x, g = tid / TPC, r = tid % TPC, k0 = r * RPT;
+  const int lane = tid & 31, warp = tid >> 5;
   const int cs = a.cs;
   const int item_i = blockIdx.x / cs, rank = blockIdx.x - item_i * cs;
   const int4 it = a.items[item_i];
@@ -114,6 +172,21 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
       *((float4 *)(cme + s * MP)) = make_float4(c[s][0], c[s][1], c[s][2], c[s][3]);
   }
   const int m = a.m;
+  const unsigned xbytes = (unsigned)cs * MP * 4u;  // one partial from every rank per iteration
+  if (cs > 1) {
+    // Row partials travel by st.async into every rank's shared memory and
+    // complete on that rank's mbarrier (one per iteration parity), so an
+    // iteration waits only for the bytes it needs, not for a cluster barrier.
+    if (tid == 0) {
+      sv_mbar_init(&sm_bar[0]);
+      sv_mbar_init(&sm_bar[1]);
+      sm_fail = 0;
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      sv_mbar_expect(&sm_bar[0], xbytes);
+      sv_mbar_expect(&sm_bar[1], xbytes);
+    }
+    cg::this_cluster().sync();  // every rank's barriers exist before the first push
+  }
   float x[S][RPT];
   for (int iter = 0; iter < a.iters; ++iter) {
     const int buf = iter & 1;
@@ -132,7 +205,7 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
         csum += v;
       }
       csum = sv_seg_sum<TPC>(csum);
-      const float f = colok ? w[s] / csum : 0.f;
+      const float f = colok ? __fdividef(w[s], csum) : 0.f;
 #pragma unroll
       for (int q = 0; q < RPT; ++q) {
         const bool ok = colok && (FULL || k0 + q < m);
@@ -142,10 +215,10 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
         rp[q] += zp;
       }
     }
-    *((float4 *)(sm_rs[buf] + g * MP + k0)) = make_float4(rp[0], rp[1], rp[2], rp[3]);
-    __syncthreads();
     float tot[RPT] = {0.f, 0.f, 0.f, 0.f};
     if (cs == 1) {
+      *((float4 *)(sm_rs[buf] + g * MP + k0)) = make_float4(rp[0], rp[1], rp[2], rp[3]);
+      __syncthreads();
       // every thread sums its own plan's partials (no second barrier: the
       // partials are double-buffered by iteration parity)
       for (int j = lo; j < hi; ++j) {
@@ -153,26 +226,38 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
         tot[0] += u.x; tot[1] += u.y; tot[2] += u.z; tot[3] += u.w;
       }
     } else {
-      cg::cluster_group cl = cg::this_cluster();
-      if (g == 0) {  // this CTA's partial, pushed into every rank's shared memory
+      // one plan over the cluster: the warp's groups are pre-added with
+      // shuffles, warp 0 adds the warps' partials and pushes the CTA's partial
+      // into every rank; each rank then adds the cs partials in rank order
+#pragma unroll
+      for (int o = TPC; o < 32; o <<= 1)
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) rp[q] += __shfl_xor_sync(0xffffffffu, rp[q], o);
+      if (lane < TPC) *((float4 *)(sm_rs[buf] + warp * MP + k0)) = make_float4(rp[0], rp[1], rp[2], rp[3]);
+      __syncthreads();
+      if (warp == 0 && lane < TPC) {
         float4 pt = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int j = 0; j < hi; ++j) {
-          const float4 u = *((const float4 *)(sm_rs[buf] + j * MP + k0));
+#pragma unroll
+        for (int w8 = 0; w8 < 8; ++w8) {
+          const float4 u = *((const float4 *)(sm_rs[buf] + w8 * MP + k0));
           pt.x += u.x; pt.y += u.y; pt.z += u.z; pt.w += u.w;
         }
-        for (int rk = 0; rk < cs; ++rk)
-          *((float4 *)(cl.map_shared_rank(&sm_x[buf][rank][0], rk) + k0)) = pt;
+        for (int rk = 0; rk < cs; ++rk) sv_push4(&sm_x[buf][rank][k0], &sm_bar[buf], (unsigned)rk, pt);
       }
-      cl.sync();
+      if (!sv_mbar_wait(&sm_bar[buf], (unsigned)(iter >> 1) & 1u)) sm_fail = 1;
       for (int rk = 0; rk < cs; ++rk) {
         const float4 u = *((const float4 *)(&sm_x[buf][rk][0] + k0));
         tot[0] += u.x; tot[1] += u.y; tot[2] += u.z; tot[3] += u.w;
       }
+      // re-arm this parity's barrier for iteration iter + 2 (every thread of
+      // this CTA has passed this iteration's wait before any rank can push
+      // iteration iter + 2's partials)
+      if (tid == 0) sv_mbar_expect(&sm_bar[buf], xbytes);
     }
     // second half of step 2 with the fixed centroid weights, and step 3
     float sc[RPT];
 #pragma unroll
-    for (int q = 0; q < RPT; ++q) sc[q] = cw[q] / tot[q];
+    for (int q = 0; q < RPT; ++q) sc[q] = __fdividef(cw[q], tot[q]);
 #pragma unroll
     for (int s = 0; s < S; ++s)
 #pragma unroll
@@ -205,6 +290,7 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
   } else {
     cg::cluster_group cl = cg::this_cluster();
     __syncthreads();
+    if (tid == 0 && sm_fail) atomicExch(a.err, 1);
     if (tid == 0) {
       double t = 0.0;
       for (int j = 0; j < hi; ++j) t += sm_cost[j];
