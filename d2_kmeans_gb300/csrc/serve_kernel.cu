@@ -131,8 +131,9 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
   const int c0 = gq * S;  // first column of the group within the query
   const int nvalid = active ? min(S, mq - c0) : 0;
   // groups of this thread's plan inside this CTA (for the row sums)
-  const int lo = cs == 1 ? plan * ng : 0;
-  const int hi = cs == 1 ? lo + ng : min(G, ng - rank * G);
+  // (threads past the CTA's plans read no partials)
+  const int lo = cs == 1 ? (active ? plan * ng : 0) : 0;
+  const int hi = cs == 1 ? (active ? lo + ng : 0) : min(G, ng - rank * G);
   float *cme = sm_c + (g * S) * MP + k0;  // this thread's costs: column s at cme[s*MP + q]
 
   // costs (to shared memory), weights, start point
@@ -187,33 +188,59 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
     }
     cg::this_cluster().sync();  // every rank's barriers exist before the first push
   }
-  float x[S][RPT];
+  // Without padded rows (FULL) the padded columns of a query's last group
+  // need no masks: their weight, Z and Y are 0, so step 1 gives X = 0 (its
+  // column sum is ROUNDOFF-positive), and step 2's ROUNDOFF is added only to
+  // valid columns, which keeps their Z' and row sums at 0.
+  //
+  // X lives only while its column is processed: step 3 is applied as
+  // Y += X right after step 2 and Y -= Z once the row scale is known, and
+  // <C, X> of the last iteration is accumulated on the way.
+  // A warp whose groups are all past the plans (the tail of a plan's last
+  // slice, or unused groups of a packed CTA) skips the arithmetic and only
+  // takes part in the row-sum exchange with zeros.
+  const bool wact = __any_sync(0xffffffffu, active);
+  float pc = 0.f;
   for (int iter = 0; iter < a.iters; ++iter) {
     const int buf = iter & 1;
+    const bool last = iter == a.iters - 1;
     float rp[RPT] = {0.f, 0.f, 0.f, 0.f};
+    if (wact) {
 #pragma unroll
     for (int s = 0; s < S; ++s) {
       const bool colok = s < nvalid;
       const float4 cc = *((const float4 *)(cme + s * MP));
       const float c[RPT] = {cc.x, cc.y, cc.z, cc.w};
-      float csum = 0.f;
+      float v[RPT], csum = 0.f;
 #pragma unroll
       for (int q = 0; q < RPT; ++q) {
-        const bool ok = colok && (FULL || k0 + q < m);
-        const float v = ok ? fmaf(z[s][q], sv_ex2(-fmaf(c[q], ir2, y[s][q])), kRoundoff) : 0.f;
-        x[s][q] = v;
-        csum += v;
+        if constexpr (FULL) {
+          v[q] = fmaf(z[s][q], sv_ex2(-fmaf(c[q], ir2, y[s][q])), kRoundoff);
+        } else {
+          const bool ok = colok && k0 + q < m;
+          v[q] = ok ? fmaf(z[s][q], sv_ex2(-fmaf(c[q], ir2, y[s][q])), kRoundoff) : 0.f;
+        }
+        csum += v[q];
       }
       csum = sv_seg_sum<TPC>(csum);
-      const float f = colok ? __fdividef(w[s], csum) : 0.f;
+      const float f = (FULL || colok) ? __fdividef(w[s], csum) : 0.f;
+      const float eps2 = colok ? kRoundoff : 0.f;
 #pragma unroll
       for (int q = 0; q < RPT; ++q) {
-        const bool ok = colok && (FULL || k0 + q < m);
-        x[s][q] *= f;
-        const float zp = ok ? fmaf(x[s][q], sv_ex2(y[s][q]), kRoundoff) : 0.f;
+        const float xv = v[q] * f;
+        float zp;
+        if constexpr (FULL) {
+          zp = fmaf(xv, sv_ex2(y[s][q]), eps2);
+        } else {
+          const bool ok = colok && k0 + q < m;
+          zp = ok ? fmaf(xv, sv_ex2(y[s][q]), kRoundoff) : 0.f;
+        }
+        y[s][q] = fmaf(kL2e, xv, y[s][q]);  // step 3, first half
         z[s][q] = zp;
         rp[q] += zp;
+        if (last) pc = fmaf(c[q], xv, pc);
       }
+    }
     }
     float tot[RPT] = {0.f, 0.f, 0.f, 0.f};
     if (cs == 1) {
@@ -257,27 +284,25 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
     // second half of step 2 with the fixed centroid weights, and step 3
     float sc[RPT];
 #pragma unroll
-    for (int q = 0; q < RPT; ++q) sc[q] = __fdividef(cw[q], tot[q]);
+    for (int q = 0; q < RPT; ++q) sc[q] = tot[q] > 0.f ? __fdividef(cw[q], tot[q]) : 0.f;
+    if (wact)
 #pragma unroll
     for (int s = 0; s < S; ++s)
 #pragma unroll
-      for (int q = 0; q < RPT; ++q) {
-        const bool ok = s < nvalid && (FULL || k0 + q < m);
-        const float zn = ok ? z[s][q] * sc[q] : 0.f;
-        y[s][q] = ok ? fmaf(kL2e, x[s][q] - zn, y[s][q]) : 0.f;
-        z[s][q] = zn;
+      for (int q = 0; q < RPT; ++q) {  // second half of step 3: Y -= Z
+        if constexpr (FULL) {  // padded columns stay at Z = Y = 0 by themselves
+          const float zn = z[s][q] * sc[q];
+          y[s][q] = fmaf(-kL2e, zn, y[s][q]);
+          z[s][q] = zn;
+        } else {
+          const bool ok = s < nvalid && k0 + q < m;
+          const float zn = ok ? z[s][q] * sc[q] : 0.f;
+          y[s][q] = ok ? fmaf(-kL2e, zn, y[s][q]) : 0.f;
+          z[s][q] = zn;
+        }
       }
   }
   // cost_l = <C, X> of the last iteration, per plan
-  float pc = 0.f;
-#pragma unroll
-  for (int s = 0; s < S; ++s) {
-    const float4 cc = *((const float4 *)(cme + s * MP));
-    pc = fmaf(cc.x, x[s][0], pc);
-    pc = fmaf(cc.y, x[s][1], pc);
-    pc = fmaf(cc.z, x[s][2], pc);
-    pc = fmaf(cc.w, x[s][3], pc);
-  }
   pc = sv_seg_sum<TPC>(pc);
   if (r == 0) sm_cost[g] = (double)pc;
   if (cs == 1) {
