@@ -645,9 +645,9 @@ static int create_batched(d2g_phase *ph, const d2g_phase_desc *d) {
   // whatever the autotuner recorded for this shape
   {
     const char *dx = getenv("D2G_WIDE_EXCHANGE");  // "cluster": synchronous DSMEM exchange
-    const char *sc = getenv("D2G_STAGE_COSTS");    // "1": table costs by bulk copy
+    const char *sc = getenv("D2G_STAGE_COSTS");    // "0": table costs through the cache
     ph->tune.exchange = (dx && std::string(dx) == "cluster") ? 1 : 0;
-    ph->tune.stage_costs = (sc && std::string(sc) == "1") ? 1 : 0;
+    ph->tune.stage_costs = (sc && std::string(sc) == "0") ? 0 : 1;
     ph->tune.ctas_per_sm = 0;
     ph->tune.cost_gemm = cfg_snapshot().cost_gemm;
     d2g_tuning rec;

@@ -724,10 +724,12 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
   constexpr int TILE = tma_tile_floats<MP>();
   constexpr int JC = G * S;
   constexpr int CW = T::EUC ? T::DS : 1;  // staged column data: supports or table row
-  // table costs of MP <= 128 arrive with the stage: one bulk copy per column
-  // of the column's table row, issued by warp 0 (JC / 32 columns per lane)
+  // table costs of 16 <= MP <= 128 can be staged in shared memory: while a
+  // unit computes, every thread copies 16-byte pieces of the next unit's
+  // table rows with cp.async (TILE / 4 pieces per unit, PPT per thread)
   constexpr bool SCC = plan_stages_costs(MP, MODE);
-  constexpr int CPL = SCC ? JC / 32 : 1;
+  constexpr int CPR = MP / 4;                                  // pieces per table row
+  constexpr int PPT = SCC ? TILE / 4 / kThreads : 1;
   const bool SC = SCC && a.stage_costs;
   extern __shared__ __align__(128) float smem[];
   float *stZ = smem;                                  // [2][TILE]
@@ -772,7 +774,7 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
     const unsigned bytes = (unsigned)ng * S * MP * 4u;
     const unsigned rb = (unsigned)ng * 16u, wb = (unsigned)ng * S * 4u, cb = wb * CW;
     const unsigned sb = slot >= 0 ? (unsigned)MP * 4u : 0u;
-    mbar_expect_tx(&mbar[stg], (SC ? 3u : 2u) * bytes + rb + wb + cb + sb);
+    mbar_expect_tx(&mbar[stg], 2u * bytes + rb + wb + cb + sb);
     if (ng <= 0) return;  // an empty slice: the phase completes on the arrival alone
     bulk_load(stZ + stg * TILE, a.Z + off, bytes, &mbar[stg]);
     bulk_load(stY + stg * TILE, a.Y + off, bytes, &mbar[stg]);
@@ -795,55 +797,47 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
       if ((r.w >> 4) > G) slot = r.x;
     }
   };
-  // staged table costs: the lanes of warp 0 copy the table rows of a slice's
-  // columns; each lane holds the rows of the slice issued next, loaded one unit early
-  const int lane = tid & 31;
-  int crow_nx[CPL];
-  auto load_crow = [&](int g0, int ng) {
+  // staged table costs: the table row of each piece of the next unit (-1: none)
+  int crow_p[PPT];
+  auto load_rows_idx = [&](int g0, int ng) {
 #pragma unroll
-    for (int j = 0; j < CPL; ++j) {
-      const int c = lane + 32 * j;
-      crow_nx[j] = c < ng * S ? __ldg(a.col_crow + (size_t)g0 * S + c) : 0;
+    for (int j = 0; j < PPT; ++j) {
+      const int c = (tid + kThreads * j) / CPR;
+      crow_p[j] = c < ng * S ? __ldg(a.col_crow + (size_t)g0 * S + c) : -1;
     }
   };
-  auto issue_rows = [&](int ng, int stg) {
+  auto issue_rows = [&](int stg) {
 #pragma unroll
-    for (int j = 0; j < CPL; ++j) {
-      const int c = lane + 32 * j;
-      if (c < ng * S)
-        bulk_load(stK + stg * TILE + c * MP, a.ctab + (size_t)crow_nx[j] * MP, MP * 4u, &mbar[stg]);
+    for (int j = 0; j < PPT; ++j) {
+      const int i = tid + kThreads * j, c = i / CPR, part = i - c * CPR;
+      if (crow_p[j] >= 0)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                         smem_u32(stK + stg * TILE + c * MP + part * 4)),
+                     "l"(a.ctab + (size_t)crow_p[j] * MP + part * 4)
+                     : "memory");
     }
+    asm volatile("cp.async.commit_group;" ::: "memory");
   };
-  // lane 0 of warp 0 keeps the bounds of the next slice in registers, loaded one unit early
+  // thread 0 keeps the bounds of the next unit in registers, loaded one unit early
   int nx_g0 = 0, nx_ng = 0, nx_slot = -1;
-  if (tid < 32) {
-    int g0 = 0, ng = 0, sl = -1;
-    if (tid == 0) {
-      mbar_init(&mbar[0], 1);
-      mbar_init(&mbar[1], 1);
-      sh_fail = 0;
-      mbar_fence_init();
-      if (u0 < nunits) {
-        slice(u0, g0, ng, sl);
-        sh_g0[0] = g0;
-        sh_ng[0] = ng;
-        issue(g0, ng, sl, 0);
-      }
+  if (tid == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    sh_fail = 0;
+    mbar_fence_init();
+    if (u0 < nunits) {
+      int g0, ng, sl;
+      slice(u0, g0, ng, sl);
+      sh_g0[0] = g0;
+      sh_ng[0] = ng;
+      issue(g0, ng, sl, 0);
+      if (u0 + ustep < nunits) slice(u0 + ustep, nx_g0, nx_ng, nx_slot);
     }
-    __syncwarp();
-    if (SC) {
-      g0 = __shfl_sync(0xffffffffu, g0, 0);
-      ng = __shfl_sync(0xffffffffu, ng, 0);
-      if (u0 < nunits) {
-        load_crow(g0, ng);
-        issue_rows(ng, 0);
-      }
-    }
-    if (tid == 0 && u0 + ustep < nunits) slice(u0 + ustep, nx_g0, nx_ng, nx_slot);
-    if (SC) {
-      const int g1 = __shfl_sync(0xffffffffu, nx_g0, 0), n1 = __shfl_sync(0xffffffffu, nx_ng, 0);
-      if (u0 + ustep < nunits) load_crow(g1, n1);
-    }
+  }
+  if (SC && u0 < nunits) {  // the first unit's rows
+    __syncthreads();
+    load_rows_idx(sh_g0[0], sh_ng[0]);
+    issue_rows(0);
   }
   __syncthreads();
 
@@ -857,27 +851,18 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
   for (int u = u0; u < nunits; u += ustep, ++it) {
     const int stg = it & 1;
     if (!mbar_wait(&mbar[stg], (it >> 1) & 1)) sh_fail = 1;
+    if (SC) asm volatile("cp.async.wait_all;" ::: "memory");  // this unit's table rows
     __syncthreads();
     if (sh_fail) break;
     const int cur_g0 = sh_g0[stg], cur_ng = sh_ng[stg];
     const int rank = crank;
-    if (tid < 32 && u + ustep < nunits) {
-      const int ng1 = __shfl_sync(0xffffffffu, nx_ng, 0);
-      if (tid == 0) {
-        issue(nx_g0, nx_ng, nx_slot, stg ^ 1);
-        sh_g0[stg ^ 1] = nx_g0;
-        sh_ng[stg ^ 1] = nx_ng;
-      }
-      if (SC) {
-        __syncwarp();
-        issue_rows(ng1, stg ^ 1);
-      }
-      if (tid == 0 && u + 2 * ustep < nunits) slice(u + 2 * ustep, nx_g0, nx_ng, nx_slot);
-      if (SC) {
-        const int g2 = __shfl_sync(0xffffffffu, nx_g0, 0), n2 = __shfl_sync(0xffffffffu, nx_ng, 0);
-        if (u + 2 * ustep < nunits) load_crow(g2, n2);
-      }
+    if (tid == 0 && u + ustep < nunits) {
+      issue(nx_g0, nx_ng, nx_slot, stg ^ 1);
+      sh_g0[stg ^ 1] = nx_g0;
+      sh_ng[stg ^ 1] = nx_ng;
+      if (u + 2 * ustep < nunits) slice(u + 2 * ustep, nx_g0, nx_ng, nx_slot);
     }
+    const bool has_next = u + ustep < nunits;
 
     T t;
     t.init_rec(stR[stg * G + (threadIdx.x / TPC)], cur_g0, cur_ng);
@@ -982,6 +967,8 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
       }
     }
     __syncthreads();
+    // the next unit's bounds are visible now: fetch its table-row indices
+    if (SC && has_next) load_rows_idx(sh_g0[stg ^ 1], sh_ng[stg ^ 1]);
 
     float tot[RPT];
     bool writer = false;
@@ -1178,11 +1165,13 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
       s_pr += i_pr;
       s_dr += i_dr;
     }
+    if (SC && has_next) issue_rows(stg ^ 1);  // lands during the next unit's wait
     __syncthreads();  // the stage and the row partials are free again
   }
   // rank 0 may still be reading a peer's shared memory (the moments of the
   // last item): no CTA of a cluster leaves before all of them are done
   if (clustered && !sh_fail) cg::this_cluster().sync();
+  if (SC) asm volatile("cp.async.wait_all;" ::: "memory");  // no table-row copy outlives the CTA
   if (sh_fail) {
     if (tid == 0) {
       a.ctl->err = 7;  // a bulk copy did not complete: let the copies in flight land first

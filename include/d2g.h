@@ -258,8 +258,9 @@ typedef struct {
   int exchange;     /* plans wider than one CTA: 0 deferred row normalisation (one plain
                        launch over packed units), 1 synchronous DSMEM exchange on a
                        thread-block cluster per plan */
-  int stage_costs;  /* table costs (16 <= padded str <= 128) copied into shared memory with
-                       the plans (1) or read through the cache (0) */
+  int stage_costs;  /* table costs (16 <= padded str <= 128): the next unit's cost-table rows
+                       copied into shared memory with cp.async while a unit computes (1,
+                       default) or read through the cache (0) */
   int ctas_per_sm;  /* persistent plan-update grid: CTAs per SM, 0 = occupancy limit */
   int cost_gemm;    /* word-embedding cost table: 0 tensor cores (3xTF32), 1 CUDA cores */
 } d2g_tuning;
