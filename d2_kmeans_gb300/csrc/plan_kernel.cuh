@@ -1166,7 +1166,9 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
       s_dr += i_dr;
     }
     if (SC && has_next) issue_rows(stg ^ 1);  // lands during the next unit's wait
-    __syncthreads();  // the stage and the row partials are free again
+    // No barrier here: every reader of this unit's stage, row partials and
+    // staged rows passes the next unit's opening barrier before thread 0
+    // reissues the stage (two units later) or anyone writes partials again.
   }
   // rank 0 may still be reading a peer's shared memory (the moments of the
   // last item): no CTA of a cluster leaves before all of them are done
