@@ -142,26 +142,23 @@ int slot_reserve(d2g_server *s, Slot &sl, size_t cols, size_t nitems, size_t nre
 }
 
 // items of one request: several plans per CTA when they fit, else one plan
-// per cluster of 2/4/8 CTAs
+// per cluster of exactly ceil(ng / G) CTAs (2..8; any cluster size up to 8
+// is a valid launch shape, so no slice of a wide plan is empty)
 void request_items(int K, int G, int mq, int req, std::vector<int4> *by_cs) {
   const int ng = (mq + 3) / 4;
   if (ng <= G) {
     const int ppc = G / ng;
-    for (int l = 0; l < K; l += ppc) by_cs[0].push_back(make_int4(req, l, std::min(ppc, K - l), ng));
+    for (int l = 0; l < K; l += ppc) by_cs[1].push_back(make_int4(req, l, std::min(ppc, K - l), ng));
   } else {
-    int cs = 1, ci = 0;
-    while (cs * G < ng) {
-      cs <<= 1;
-      ++ci;
-    }
-    for (int l = 0; l < K; ++l) by_cs[ci].push_back(make_int4(req, l, 1, ng));
+    const int cs = (ng + G - 1) / G;
+    for (int l = 0; l < K; ++l) by_cs[cs].push_back(make_int4(req, l, 1, ng));
   }
 }
 
 int launch_batch(d2g_server *s, Slot &sl) {
   size_t cols = 0;
   for (Request *r : sl.reqs) cols += r->mq;
-  std::vector<int4> by_cs[4];
+  std::vector<int4> by_cs[9];  // by cluster size 1..8
   const int G = serve_groups_per_cta(s->MP);
   for (size_t i = 0; i < sl.reqs.size(); ++i) request_items(s->K, G, sl.reqs[i]->mq, (int)i, by_cs);
   size_t nitems = 0;
@@ -204,11 +201,11 @@ int launch_batch(d2g_server *s, Slot &sl) {
   a.dim = s->dim;
   a.iters = s->iters;
   io = 0;
-  for (int ci = 0; ci < 4; ++ci) {
+  for (int cs = 1; cs <= 8; ++cs) {
     a.items = sl.items + io;
-    a.cs = 1 << ci;
-    D2G_CUDA(launch_serve(s->MP, a, (int)by_cs[ci].size(), sl.st));
-    io += by_cs[ci].size();
+    a.cs = cs;
+    D2G_CUDA(launch_serve(s->MP, a, (int)by_cs[cs].size(), sl.st));
+    io += by_cs[cs].size();
   }
   D2G_CUDA(cudaMemcpyAsync(sl.h_cost, sl.cost, sl.reqs.size() * s->K * 4, cudaMemcpyDeviceToHost, sl.st));
   D2G_CUDA(cudaMemcpyAsync(sl.h_err, sl.err, sizeof(int), cudaMemcpyDeviceToHost, sl.st));
