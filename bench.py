@@ -46,6 +46,7 @@ WORKLOAD = ("batched uneven sizes: n=200000 Euclidean D2 instances, d=3, m_i log
             "64-component GMM supports, Dirichlet(0.5) weights; k=64 centroids, m=32; "
             "rhoCoeff=2, updatePerLoops=10, maxIters=200 (201 iterations)")
 HBM_FALLBACK_GBS = 6800.0
+SKIP = set()
 
 
 def peaks():
@@ -54,6 +55,14 @@ def peaks():
             return float(json.load(f)["hbm_gbs"]), "measured"
     except Exception:
         return HBM_FALLBACK_GBS, "fallback"
+
+
+def bf16_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"])
+    except Exception:
+        return 1900.0
 
 
 class ClockSampler:
@@ -221,9 +230,39 @@ OTHER_WORKLOADS = {
 }
 
 
-def workload_leg(name, steps, hbm):
+# the FP64 check of the 256-bin histogram phase runs on a 5 000-instance subset
+# (its FP64 form moves 136 B per plan entry per iteration: 890 GB at full size)
+ERROR_CHECK_SCALE = {"embed": 1.0, "hist": 0.05, "twophase_euclid": 1.0}
+
+
+def fp64_errors(name, seed=0):
+    """Objective trace and centroid errors of the batched form against the FP64
+    form on the same inputs and iterations (both on the GPU)."""
+    import numpy as np
+    from d2_kmeans_gb300 import badmm, synth
+    ph, c, opts = synth.workload(name, seed=seed, scale=ERROR_CHECK_SCALE[name])
+    k, m = int(ph["num_of_labels"]), int(ph["str"])
+    out = []
+    for precision in (0, 1):
+        P = badmm.Phase(ph, precision)
+        out.append(P.run(c, opts))
+        P.close()
+    b, f = out
+    res = {"n": len(ph["p_str"]),
+           "obj_rel_err": float(np.max(np.abs(b["trace"][:, 1] - f["trace"][:, 1]) / np.abs(f["trace"][:, 1]))),
+           "c_w_l1": float(np.abs(b["c_w"].reshape(k, m) - f["c_w"].reshape(k, m)).sum(1).max())}
+    if b.get("c_supp") is not None:
+        s0 = np.asarray(b["c_supp"]).reshape(k * m, -1)
+        s1 = np.asarray(f["c_supp"]).reshape(k * m, -1)
+        nrm = np.linalg.norm(s1, axis=1)
+        res["supp_rel_err"] = float((np.linalg.norm(s0 - s1, axis=1) / np.maximum(nrm, 1e-3 * nrm.max())).max())
+    return res
+
+
+def workload_leg(name, steps, hbm, tf32_peak):
     """One secondary workload: autotuned, timed over whole centroid updates,
-    then the plan-update launches timed alone (profile mode)."""
+    then the plan-update (and cost-table) launches timed alone (profile mode),
+    and its error against the FP64 form."""
     from d2_kmeans_gb300 import badmm, synth
     ph, c, opts = synth.workload(name, seed=0)
     n = len(ph["p_str"])
@@ -238,12 +277,23 @@ def workload_leg(name, steps, hbm):
     badmm.set_config(profile=0)
     P.close()
     achieved = ps["plan_bytes"] / (ps["plan_ms_avg"] / 1e3) / 1e9
-    return {"workload": OTHER_WORKLOADS[name], "value": n * st["iterations"] / (ms / 1e3), "unit": UNIT,
-            "ms_per_step": ms, "iterations_per_step": st["iterations"],
-            "plan_entries": int(st["plan_entries"]), "tuning": tune["best"],
-            "plan_update": {"achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                            "algo_bytes_per_iteration": ps["plan_bytes"],
-                            "ms_per_iteration": ps["plan_ms_avg"]}}
+    out = {"workload": OTHER_WORKLOADS[name], "value": n * st["iterations"] / (ms / 1e3), "unit": UNIT,
+           "ms_per_step": ms, "iterations_per_step": st["iterations"],
+           "plan_entries": int(st["plan_entries"]), "tuning": tune["best"],
+           "plan_update": {"achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                           "algo_bytes_per_iteration": ps["plan_bytes"],
+                           "ms_per_iteration": ps["plan_ms_avg"]}}
+    if ps["table_launches"]:
+        useful = ps["table_flops"] / (ps["table_ms_avg"] / 1e3) / 1e12
+        out["cost_table"] = {"kernel": "cost_table_tc_kernel (tcgen05 kind::tf32, 3xTF32)",
+                             "ms_per_launch": ps["table_ms_avg"], "flops_per_launch": ps["table_flops"],
+                             "achieved_tflops": useful, "tf32_mma_tflops_issued": 3 * useful,
+                             "peak_tf32_tflops": tf32_peak, "frac_issued": 3 * useful / tf32_peak,
+                             "peak_kind": "half the measured bf16 cuBLAS rate (TF32 MMA runs at half "
+                                          "the BF16 rate)"}
+    if "fp64" not in SKIP:
+        out["error_vs_fp64"] = fp64_errors(name)
+    return out
 
 
 SERVE_WORKLOAD = ("serving: k=256 resident centroids, m=64, d=64; queries with m_q log-uniform 4-512, "
@@ -275,7 +325,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip", default="",
-                    help="comma list of legs to skip: e2e,plain,cpu,profile,serve,workloads")
+                    help="comma list of legs to skip: e2e,plain,cpu,profile,serve,workloads,fp64")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -285,6 +335,7 @@ def main():
     if args.impl == "reference":
         return run_reference(args, rank)
     skip = set(x for x in args.skip.split(",") if x)
+    SKIP.update(skip)
 
     import numpy as np
     import torch
@@ -370,7 +421,8 @@ def main():
     if "serve" not in skip and rank == 0:
         out["serve"] = serve_leg()
     if "workloads" not in skip and rank == 0:
-        out["workloads"] = {w: workload_leg(w, 2, hbm) for w in OTHER_WORKLOADS}
+        tf32 = bf16_peak() / 2
+        out["workloads"] = {w: workload_leg(w, 2, hbm, tf32) for w in OTHER_WORKLOADS}
     if "cpu" not in skip and rank == 0:
         ensure_oracle()
         v, units, wall = cpu_baseline(1, 20000 / 200000, 21, seed=100)

@@ -82,7 +82,8 @@ class d2g_run_stats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("rho", C.c_double), ("total_ms", C.c_double),
                 ("plan_ms_avg", C.c_double), ("plan_launches", C.c_int),
                 ("kernel_launches", C.c_longlong), ("plan_bytes", C.c_double),
-                ("plan_entries", C.c_size_t), ("path", C.c_int)]
+                ("plan_entries", C.c_size_t), ("path", C.c_int), ("table_ms_avg", C.c_double),
+                ("table_launches", C.c_int), ("table_flops", C.c_double)]
 
 
 class d2g_tuning(C.Structure):

@@ -847,7 +847,7 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
   const bool euc = ph->metric == D2_EUCLIDEAN_L2, emb = ph->metric == D2_WORD_EMBED;
   int chk_idx = 0;
   long long nl = 0;
-  std::vector<cudaEvent_t> evs;
+  std::vector<cudaEvent_t> evs, tevs;  // plan launches, cost-table launches (profile mode)
   if (ph->path == 0) {
     PlanArgs base = base_args(ph);
     for (int it = 0; it <= maxIters; ++it) {
@@ -893,6 +893,18 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
       nl += 2;
       if (upd && emb) {  // step 5 for word embeddings, then the new cost table
         D2G_CUDA(launch_embed_support(embed_args(ph, it), ph->st));
+        cudaEvent_t t0 = nullptr, t1 = nullptr;
+        if (profile) {
+          cudaEventCreate(&t0);
+          cudaEventCreate(&t1);
+          cudaEventRecord(t0, ph->st);
+        }
+        D2G_CUDA(launch_embed_table(embed_args(ph, it), ph->st));
+        if (profile) {
+          cudaEventRecord(t1, ph->st);
+          tevs.push_back(t0);
+          tevs.push_back(t1);
+        }
         nl += 6;
       }
       if (collide) {
@@ -958,6 +970,15 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
     *plan_ms = evs.empty() ? 0 : tot / (evs.size() / 2);
     *plan_timed = (int)(evs.size() / 2);
     for (auto e : evs) cudaEventDestroy(e);
+    double ttot = 0;
+    for (size_t i = 0; i + 1 < tevs.size(); i += 2) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, tevs[i], tevs[i + 1]);
+      ttot += ms;
+    }
+    ph->stats.table_ms_avg = tevs.empty() ? 0 : ttot / (tevs.size() / 2);
+    ph->stats.table_launches = (int)(tevs.size() / 2);
+    for (auto e : tevs) cudaEventDestroy(e);
   }
   *launches = nl;
   return D2G_OK;
@@ -1106,6 +1127,11 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
   ph->stats.kernel_launches = launches + nl;
   ph->stats.plan_entries = ph->col * m;
   ph->stats.path = ph->path;
+  if (!profile) {
+    ph->stats.table_ms_avg = 0;
+    ph->stats.table_launches = 0;
+  }
+  ph->stats.table_flops = (ph->path == 0 && emb) ? 2.0 * K * m * (double)ph->vocab_size * dim : 0.0;
   {
     const double ent = (double)ph->col * m;
     const double colb = ph->path == 0 ? (double)ph->col * (euc ? 4.0 * (1 + dim) : 8.0) : 0.0;

@@ -217,7 +217,9 @@ cudaError_t launch_cost_table_tc(const float *cs, int nrows, const float *vocab,
                                  int *err, cudaStream_t st);
 cudaError_t launch_vocab_norms(const float *vocab, int V, int d, float *vnorm, cudaStream_t st);
 cudaError_t launch_to_f32(const double *a, size_t n, float *b, cudaStream_t st);
+// step 5 of a word-embedding phase, then the new cost table (separate, so it can be timed)
 cudaError_t launch_embed_support(const EmbedArgs &e, cudaStream_t st);
+cudaError_t launch_embed_table(const EmbedArgs &e, cudaStream_t st);
 
 // d2g_host.cu
 int distmat_fp64(int dim, int str, size_t size, const int *p_str, int metric, const double *supp,

@@ -205,6 +205,11 @@ cudaError_t launch_to_f32(const double *a, size_t n, float *b, cudaStream_t st) 
   return cudaGetLastError();
 }
 
+cudaError_t launch_embed_table(const EmbedArgs &e, cudaStream_t st) {
+  return launch_cost_table(e.cs32f, e.K, e.m, e.vocab, e.V, e.d, e.cnorm, e.vnorm, e.MP, e.T, e.gemm,
+                           &e.ctl->err, st);
+}
+
 cudaError_t launch_embed_support(const EmbedArgs &e, cudaStream_t st) {
   cudaError_t err = cudaMemsetAsync(e.W, 0, (size_t)e.K * e.V * e.MP * sizeof(float), st);
   if (err != cudaSuccess) return err;
@@ -215,10 +220,7 @@ cudaError_t launch_embed_support(const EmbedArgs &e, cudaStream_t st) {
   support_num_kernel<<<g2, 256, 0, st>>>(e.W, e.vocab, e.V, e.d, e.MP, e.chunk, e.m, e.part);
   support_final_kernel<<<dim3(e.K, (e.m * e.d + 255) / 256), 256, 0, st>>>(
       e.part, e.nchunk, e.K, e.MP, e.m, e.d, e.cs64, e.cs32f, e.ctl, e.iter);
-  err = cudaGetLastError();
-  if (err != cudaSuccess) return err;
-  return launch_cost_table(e.cs32f, e.K, e.m, e.vocab, e.V, e.d, e.cnorm, e.vnorm, e.MP, e.T, e.gemm,
-                           &e.ctl->err, st);
+  return cudaGetLastError();
 }
 
 }  // namespace d2g

@@ -223,6 +223,9 @@ typedef struct {
   double plan_bytes;        /* algorithmic HBM bytes of one plan-update pass */
   size_t plan_entries;      /* str * col */
   int path;                 /* 0 batched FP32, 1 plain FP64 */
+  double table_ms_avg;      /* mean word-embedding cost-table launch time (profile mode) */
+  int table_launches;       /* cost-table launches timed (profile mode) */
+  double table_flops;       /* algorithmic flops of one cost table: 2 * (k*str) * V * dim */
 } d2g_run_stats;
 
 /* Upload a phase.  Host arrays are copied; labels can change later. */
