@@ -137,6 +137,7 @@ struct d2g_phase {
   // ---- word-embedding phase (batched form)
   std::vector<int> h_sym;  // token id per reference column
   DBuf<float> vocab32, vnorm, cnorm, cs32f, W, epart;
+  DBuf<float> vsplit, csplit;  // TF32 hi / lo tiles of the vocabulary and of the centroids
   DBuf<int> pair_key, pair_ptr, occ_col;
   int npairs = 0, echunk = 0, enchunk = 0;
 
@@ -581,6 +582,10 @@ static int upload_columns_batched(d2g_phase *ph, const d2g_phase_desc *d) {
     D2G_CUDA(cudaMemcpyAsync(ph->vocab32.p, v32.data(), vd * 4, cudaMemcpyHostToDevice, ph->st));
     D2G_CUDA(ph->vnorm.alloc(ph->vocab_size));
     D2G_CUDA(launch_vocab_norms(ph->vocab32.p, ph->vocab_size, ph->dim, ph->vnorm.p, ph->st));
+    // tensor-core cost table operands: the vocabulary split once, centroid space per table
+    D2G_CUDA(ph->vsplit.alloc(tf32_split_floats(ph->vocab_size, ph->dim, 256)));
+    D2G_CUDA(launch_tf32_split(ph->vocab32.p, ph->vocab_size, ph->dim, 256, ph->vsplit.p, ph->st));
+    D2G_CUDA(ph->csplit.alloc(tf32_split_floats(ph->K * ph->str, ph->dim, 128)));
     ph->h_sym.assign(d->p_supp_sym, d->p_supp_sym + ph->col);
     D2G_CUDA(cudaStreamSynchronize(ph->st));
   } else if (!euc) {  // histogram cost table: row v = cost from bin v to every centroid bin
@@ -799,7 +804,7 @@ static std::vector<unsigned long long> loop_signature(d2g_phase *ph) {
   return {u(ph->part.p), u(ph->trace.p), u(ph->Xp.p), u(ph->cl_ptr.p), u(ph->cl_plans.p),
           u(ph->cw64.p), u(ph->cs64.p), u(ph->ctl.p), u(ph->resid_part.p), u(ph->ctab.p),
           u(ph->grp_rec.p), u(ph->plan_slot.p), u(ph->pair_key.p), u(ph->pair_ptr.p),
-          u(ph->occ_col.p), (unsigned long long)ph->npairs,
+          u(ph->occ_col.p), (unsigned long long)ph->npairs, u(ph->vsplit.p), u(ph->csplit.p),
           (unsigned long long)ph->nchunk, (unsigned long long)ph->chunk,
           (unsigned long long)ph->global_size, (unsigned long long)ph->cost_gemm,
           u(ph->wide.p), u(ph->def_iter.p), u(ph->rowpart.p), u(ph->rowsc.p), u(ph->col_crow.p),
@@ -823,6 +828,8 @@ static EmbedArgs embed_args(d2g_phase *ph, int iter) {
   e.W = ph->W.p;
   e.vocab = ph->vocab32.p;
   e.vnorm = ph->vnorm.p;
+  e.vsplit = ph->vsplit.p;
+  e.csplit = ph->csplit.p;
   e.cnorm = ph->cnorm.p;
   e.part = ph->epart.p;
   e.nchunk = ph->enchunk;
@@ -1035,8 +1042,8 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
     if (emb) {  // the cost table of the initial centroids
       D2G_CUDA(launch_to_f32(ph->cs64.p, (size_t)K * m * dim, ph->cs32f.p, ph->st));
       D2G_CUDA(launch_cost_table(ph->cs32f.p, K, m, ph->vocab32.p, ph->vocab_size, dim, ph->cnorm.p,
-                                 ph->vnorm.p, ph->MP, ph->ctab.p, ph->cost_gemm, &ph->ctl.p->err,
-                                 ph->st));
+                                 ph->vnorm.p, ph->MP, ph->ctab.p, ph->cost_gemm, ph->vsplit.p,
+                                 ph->csplit.p, &ph->ctl.p->err, ph->st));
       launches += 3;
     }
     PlanArgs base = base_args(ph);

@@ -206,15 +206,20 @@ struct EmbedArgs {
   Ctl *ctl;
   int iter, K, m, MP, V, d;
   int gemm;              // cost table: 0 tensor cores (3xTF32), 1 FP32 CUDA cores
+  const float *vsplit;   // vocabulary split into TF32 hi / lo tiles (tensor-core table)
+  float *csplit;         // centroids split likewise, rebuilt per table
 };
 // Ctl::err value of a tensor-core wait that ran out
 constexpr int kErrTcTimeout = 3;
 cudaError_t launch_cost_table(const float *cs, int K, int m, const float *vocab, int V, int d,
                               float *cnorm, const float *vnorm, int MP, float *T, int gemm,
-                              int *err, cudaStream_t st);
-cudaError_t launch_cost_table_tc(const float *cs, int nrows, const float *vocab, int V, int d,
+                              const float *vsplit, float *csplit, int *err, cudaStream_t st);
+// tc_cost_table.cu: blocked TF32 hi / lo operands (rows in tiles of BR) and the table
+size_t tf32_split_floats(int R, int d, int BR);
+cudaError_t launch_tf32_split(const float *src, int R, int d, int BR, float *dst, cudaStream_t st);
+cudaError_t launch_cost_table_tc(const float *cs, int nrows, const float *vsplit, int V, int d,
                                  const float *cnorm, const float *vnorm, int m, int MP, float *T,
-                                 int *err, cudaStream_t st);
+                                 float *csplit, int *err, cudaStream_t st);
 cudaError_t launch_vocab_norms(const float *vocab, int V, int d, float *vnorm, cudaStream_t st);
 cudaError_t launch_to_f32(const double *a, size_t n, float *b, cudaStream_t st);
 // step 5 of a word-embedding phase, then the new cost table (separate, so it can be timed)

@@ -186,10 +186,11 @@ __global__ void to_f32_kernel(const double *__restrict__ a, size_t n, float *__r
 
 cudaError_t launch_cost_table(const float *cs, int K, int m, const float *vocab, int V, int d,
                               float *cnorm, const float *vnorm, int MP, float *T, int gemm,
-                              int *err, cudaStream_t st) {
+                              const float *vsplit, float *csplit, int *err, cudaStream_t st) {
   const int nrows = K * m;
   row_norms_kernel<<<(nrows + 255) / 256, 256, 0, st>>>(cs, nrows, d, cnorm);
-  if (gemm == 0) return launch_cost_table_tc(cs, nrows, vocab, V, d, cnorm, vnorm, m, MP, T, err, st);
+  if (gemm == 0)
+    return launch_cost_table_tc(cs, nrows, vsplit, V, d, cnorm, vnorm, m, MP, T, csplit, err, st);
   dim3 grid((V + kTile - 1) / kTile, (nrows + kTile - 1) / kTile);
   cost_table_kernel<<<grid, 256, 0, st>>>(cs, nrows, vocab, V, d, cnorm, vnorm, m, MP, T);
   return cudaGetLastError();
@@ -207,7 +208,7 @@ cudaError_t launch_to_f32(const double *a, size_t n, float *b, cudaStream_t st) 
 
 cudaError_t launch_embed_table(const EmbedArgs &e, cudaStream_t st) {
   return launch_cost_table(e.cs32f, e.K, e.m, e.vocab, e.V, e.d, e.cnorm, e.vnorm, e.MP, e.T, e.gemm,
-                           &e.ctl->err, st);
+                           e.vsplit, e.csplit, &e.ctl->err, st);
 }
 
 cudaError_t launch_embed_support(const EmbedArgs &e, cudaStream_t st) {

@@ -8,14 +8,21 @@
 // the TF32 rounding of lo leave an error near 2^-22 of |c||v| per product,
 // which keeps the |c|^2 + |v|^2 - 2 c.v cancellation at FP32 accuracy.
 //
-// One CTA = one warpgroup = one 128 x 256 output tile (M x N).  Per K block of
-// 32 TF32 values, the warpgroup loads the A (128 x 32) and B (256 x 32) slices,
-// splits them and stores hi / lo in the no-swizzle K-major core-matrix layout
+// Operands are split once into a blocked layout that is the shared-memory
+// image of one (row tile, K block): for each tile of BR rows and each K block
+// of 32 values, hi then lo, each in the no-swizzle K-major core-matrix order
 // (8 rows x 16 bytes per core matrix, core matrices adjacent along K 128 bytes
-// apart, 8-row groups 1024 bytes apart); one thread issues the 4 k-steps x 3
-// MMAs and a tcgen05.commit that arrives on an mbarrier.  The epilogue reads
-// the accumulator with tcgen05.ld (each warp its 32 lanes = 32 rows) and writes
-// T, one coalesced 128-byte row segment per vocabulary column and warp.
+// apart, 8-row groups 1024 bytes apart).  The vocabulary is split once per
+// phase (it never changes), the centroids once per table.
+//
+// One CTA of 128 threads computes one 128 x 256 output tile.  Thread 0 runs a
+// two-stage pipeline: a K block of A (hi + lo, 32 KB) and B (hi + lo, 64 KB)
+// arrives by two bulk copies on the stage's "full" mbarrier; four k-steps x
+// three MMAs accumulate into a 256-column TMEM accumulator; tcgen05.commit
+// arrives on the stage's "empty" mbarrier, after which the stage is refilled
+// with the block two ahead.  The epilogue reads TMEM with tcgen05.ld (each
+// warp its 32 lanes = 32 rows) and writes T, one coalesced 128-byte row
+// segment per vocabulary column and warp.  Every wait is bounded.
 #include <cstdint>
 
 #include "d2g_internal.cuh"
@@ -32,7 +39,9 @@ constexpr int CORE = 32;                // floats per core matrix (8 rows x 4)
 constexpr uint32_t kLBO = 128;          // bytes between core matrices along K
 constexpr uint32_t kSBO = KC * 128;     // bytes between 8-row groups
 constexpr int kTmemCols = 256;
-constexpr size_t kSmemBytes = (size_t)(2 * TM + 2 * TN) * TKB * 4;  // A hi/lo, B hi/lo
+constexpr int SA = TM * TKB, SB = TN * TKB;   // floats of one hi (or lo) block of A / B
+constexpr int STAGE = 2 * SA + 2 * SB;        // A hi, A lo, B hi, B lo
+constexpr size_t kSmemBytes = (size_t)2 * STAGE * 4;  // two stages, 192 KB
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -66,7 +75,20 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64
 
 __device__ __forceinline__ void mbar_init1(uint64_t *b) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(b)) : "memory");
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect(uint64_t *b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(b)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *b) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(b))
+      : "memory");
 }
 
 __device__ __forceinline__ bool mbar_test(uint64_t *b, uint32_t parity) {
@@ -96,52 +118,51 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *b, uint32_t parity) 
   }
 }
 
-// Load rows [r0, r0+R) x K block [t0, t0+TKB) of a row-major FP32 matrix
-// (nr x d), split into TF32 hi / lo and store both in the core-matrix layout.
-// Out-of-range entries are zero.  128 threads.
-__device__ __forceinline__ void stage_split(const float *__restrict__ a, int nr, int d, int r0,
-                                            int t0, int R, bool vec, float *hi, float *lo) {
-  const int tid = threadIdx.x;
-  for (int q = tid; q < R * KC; q += 128) {
-    // q -> (row & 7) fastest, then chunk, then row group
-    const int r8 = q & 7, c = (q >> 3) % KC, g = (q >> 3) / KC;
-    const int row = g * 8 + r8, r = r0 + row, t = t0 + c * 4;
-    float x[4];
-    if (vec) {
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (r < nr && t < d) v = __ldg(reinterpret_cast<const float4 *>(a + (size_t)r * d + t));
-      x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
-    } else {
-#pragma unroll
-      for (int j = 0; j < 4; ++j) x[j] = (r < nr && t + j < d) ? __ldg(a + (size_t)r * d + t + j) : 0.f;
-    }
-    float h[4], l[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      h[j] = tf32_round(x[j]);
-      l[j] = tf32_round(x[j] - h[j]);
-    }
-    const int o = (g * KC + c) * CORE + r8 * 4;
-    *reinterpret_cast<float4 *>(hi + o) = make_float4(h[0], h[1], h[2], h[3]);
-    *reinterpret_cast<float4 *>(lo + o) = make_float4(l[0], l[1], l[2], l[3]);
-  }
-}
-
 }  // namespace tc
 
+// Split a row-major FP32 matrix (R x d) into the blocked TF32 hi / lo layout:
+// dst[((rt * nkb + kb) * 2 + hl) * BR * 32 + core-matrix offset], rows padded to
+// a multiple of BR and K to nkb * 32 with zeros.  One thread per 16-byte chunk.
+__global__ void tf32_split_kernel(const float *__restrict__ src, int R, int d, int BR, int nrt,
+                                  int nkb, float *__restrict__ dst) {
+  using namespace tc;
+  const size_t n = (size_t)nrt * BR * nkb * KC;
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int per_row = nkb * KC;
+  const int row = (int)(i / per_row), ci = (int)(i - (size_t)row * per_row);
+  const int kb = ci / KC, ch = ci - kb * KC;
+  const int rt = row / BR, r = row - rt * BR;
+  const int t0 = kb * TKB + ch * 4;
+  float x[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) x[j] = (row < R && t0 + j < d) ? __ldg(src + (size_t)row * d + t0 + j) : 0.f;
+  float h[4], l[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    h[j] = tf32_round(x[j]);
+    l[j] = tf32_round(x[j] - h[j]);
+  }
+  const size_t blk = ((size_t)rt * nkb + kb) * 2 * (size_t)BR * TKB;
+  const int off = ((r >> 3) * KC + ch) * CORE + (r & 7) * 4;
+  *reinterpret_cast<float4 *>(dst + blk + off) = make_float4(h[0], h[1], h[2], h[3]);
+  *reinterpret_cast<float4 *>(dst + blk + (size_t)BR * TKB + off) = make_float4(l[0], l[1], l[2], l[3]);
+}
+
 __global__ void __launch_bounds__(128, 1)
-    cost_table_tc_kernel(const float *__restrict__ cs, int nrows, const float *__restrict__ vocab,
-                         int V, int d, const float *__restrict__ cnorm,
+    cost_table_tc_kernel(const float *__restrict__ asplit, int nrows, const float *__restrict__ bsplit,
+                         int V, int nkb, const float *__restrict__ cnorm,
                          const float *__restrict__ vnorm, int m, int MP, float *__restrict__ T,
                          int *__restrict__ err) {
   using namespace tc;
   extern __shared__ __align__(1024) float sm[];
-  float *Ahi = sm, *Alo = Ahi + TM * TKB, *Bhi = Alo + TM * TKB, *Blo = Bhi + TN * TKB;
-  __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t full[2], empty[2];
   __shared__ uint32_t tmem_base;
   __shared__ int fail;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int r0 = blockIdx.y * TM, v0 = blockIdx.x * TN;
+  const float *ablk = asplit + (size_t)blockIdx.y * nkb * 2 * SA;  // [kb][hi, lo][SA]
+  const float *bblk = bsplit + (size_t)blockIdx.x * nkb * 2 * SB;  // [kb][hi, lo][SB]
 
   if (warp == 0) {  // tensor-memory accumulator: 128 lanes x 256 FP32 columns
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -151,7 +172,11 @@ __global__ void __launch_bounds__(128, 1)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    mbar_init1(&mbar);
+    mbar_init1(&full[0]);
+    mbar_init1(&full[1]);
+    mbar_init1(&empty[0]);
+    mbar_init1(&empty[1]);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     fail = 0;
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -159,39 +184,60 @@ __global__ void __launch_bounds__(128, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base;
 
-  const int nkb = (d + TKB - 1) / TKB;
-  const bool vec = (d & 3) == 0;
-  for (int kb = 0; kb < nkb; ++kb) {
-    const int t0 = kb * TKB;
-    // Staging: lanes 8j..8j+7 of a warp take the 8 rows of one core matrix at
-    // K chunk c+j, so each 8-lane phase stores 128 contiguous bytes and a warp
-    // reads 64 contiguous bytes from each of 8 rows.
-    stage_split(cs, nrows, d, r0, t0, TM, vec, Ahi, Alo);
-    stage_split(vocab, V, d, v0, t0, TN, vec, Bhi, Blo);
-    // generic-proxy stores must be visible to the tensor core's async proxy
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (tid == 0) {
+  if (tid == 0) {
+    auto load = [&](int kb, int s) {
+      float *st = sm + s * STAGE;
+      mbar_expect(&full[s], (uint32_t)STAGE * 4u);
+      bulk_load(st, ablk + (size_t)kb * 2 * SA, 2u * SA * 4u, &full[s]);
+      bulk_load(st + 2 * SA, bblk + (size_t)kb * 2 * SB, 2u * SB * 4u, &full[s]);
+    };
+    load(0, 0);
+    if (nkb > 1) load(1, 1);
+    int issued = nkb > 1 ? 2 : 1;  // K blocks whose copies were issued
+    bool ok = true;
+    for (int kb = 0; kb < nkb; ++kb) {
+      const int s = kb & 1;
+      const uint32_t par = (uint32_t)(kb >> 1) & 1u;
+      if (!mbar_wait_bounded(&full[s], par)) {
+        ok = false;
+        break;
+      }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const float *Ah = sm + s * STAGE, *Al = Ah + SA, *Bh = Al + SA, *Bl = Bh + SB;
 #pragma unroll
-      for (int s = 0; s < TKB / 8; ++s) {  // one MMA k-step = 8 TF32 = two 16-byte chunks
-        const int off = s * 2 * CORE;
-        const uint64_t ah = smem_desc(Ahi + off), al = smem_desc(Alo + off);
-        const uint64_t bh = smem_desc(Bhi + off), bl = smem_desc(Blo + off);
-        mma_tf32(tmem, ah, bh, (kb > 0 || s > 0) ? 1u : 0u);
+      for (int ks = 0; ks < TKB / 8; ++ks) {  // one MMA k-step = 8 TF32 = two 16-byte chunks
+        const int off = ks * 2 * CORE;
+        const uint64_t ah = smem_desc(Ah + off), al = smem_desc(Al + off);
+        const uint64_t bh = smem_desc(Bh + off), bl = smem_desc(Bl + off);
+        mma_tf32(tmem, ah, bh, (kb > 0 || ks > 0) ? 1u : 0u);
         mma_tf32(tmem, ah, bl, 1u);
         mma_tf32(tmem, al, bh, 1u);
       }
       asm volatile(
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-              smem_addr(&mbar))
+              smem_addr(&empty[s]))
           : "memory");
+      if (kb + 2 < nkb) {  // refill this stage once its MMAs have read it
+        if (!mbar_wait_bounded(&empty[s], par)) {
+          ok = false;
+          break;
+        }
+        load(kb + 2, s);
+        ++issued;
+      }
     }
-    // the MMAs have read the block once the commit arrives
-    if (!tc::mbar_wait_bounded(&mbar, kb & 1)) fail = 1;
-    __syncthreads();
-    if (fail) break;
+    if (!ok) {
+      fail = 1;
+      // let the copies in flight land (bounded) before the CTA leaves
+      for (int kb = 0; kb < issued; ++kb) mbar_wait_bounded(&full[kb & 1], (uint32_t)(kb >> 1) & 1u);
+    }
   }
+  // the last commit completes after every MMA of the tile
+  {
+    const int last = nkb - 1;
+    if (!mbar_wait_bounded(&empty[last & 1], (uint32_t)(last >> 1) & 1u)) fail = 1;
+  }
+  __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
   if (!fail) {
@@ -229,9 +275,24 @@ __global__ void __launch_bounds__(128, 1)
                  : "memory");
 }
 
-cudaError_t launch_cost_table_tc(const float *cs, int nrows, const float *vocab, int V, int d,
+size_t tf32_split_floats(int R, int d, int BR) {
+  const size_t nrt = (size_t)(R + BR - 1) / BR, nkb = (size_t)(d + tc::TKB - 1) / tc::TKB;
+  return nrt * nkb * 2 * (size_t)BR * tc::TKB;
+}
+
+cudaError_t launch_tf32_split(const float *src, int R, int d, int BR, float *dst, cudaStream_t st) {
+  const int nrt = (R + BR - 1) / BR, nkb = (d + tc::TKB - 1) / tc::TKB;
+  const size_t n = (size_t)nrt * BR * nkb * tc::KC;
+  if (n == 0) return cudaSuccess;
+  tf32_split_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(src, R, d, BR, nrt, nkb, dst);
+  return cudaGetLastError();
+}
+
+// csplit: the centroids' split buffer (tf32_split_floats(nrows, d, 128) floats);
+// vsplit: the vocabulary split once with launch_tf32_split(vocab, V, d, 256, ...)
+cudaError_t launch_cost_table_tc(const float *cs, int nrows, const float *vsplit, int V, int d,
                                  const float *cnorm, const float *vnorm, int m, int MP, float *T,
-                                 int *err, cudaStream_t st) {
+                                 float *csplit, int *err, cudaStream_t st) {
   if (nrows <= 0) return cudaSuccess;
   // per device; the first call for a device comes before any graph capture
   static bool configured[64] = {};
@@ -245,9 +306,12 @@ cudaError_t launch_cost_table_tc(const float *cs, int nrows, const float *vocab,
     if (e != cudaSuccess) return e;
     configured[dev] = true;
   }
+  e = launch_tf32_split(cs, nrows, d, tc::TM, csplit, st);
+  if (e != cudaSuccess) return e;
+  const int nkb = (d + tc::TKB - 1) / tc::TKB;
   dim3 grid((V + tc::TN - 1) / tc::TN, (nrows + tc::TM - 1) / tc::TM);
-  cost_table_tc_kernel<<<grid, 128, tc::kSmemBytes, st>>>(cs, nrows, vocab, V, d, cnorm, vnorm, m,
-                                                          MP, T, err);
+  cost_table_tc_kernel<<<grid, 128, tc::kSmemBytes, st>>>(csplit, nrows, vsplit, V, nkb, cnorm, vnorm,
+                                                          m, MP, T, err);
   return cudaGetLastError();
 }
 
