@@ -258,11 +258,11 @@ static bool batched_supported(const d2g_phase_desc *d, std::string *why) {
 //   - units: every range above of at most G groups, at most one wide slice
 //     per unit and at its start (deferred iterations, one plain launch).
 static int build_packing(d2g_phase *ph, bool with_units) {
-  const int G = ph->geo.G;
+  const int G = ph->geo.G, S = ph->geo.S;
   const size_t n = ph->size;
   std::vector<int> ng(n), csz(n);
   for (size_t i = 0; i < n; ++i) {
-    ng[i] = (ph->p_str[i] + kS - 1) / kS;
+    ng[i] = (ph->p_str[i] + S - 1) / S;
     int c = (ng[i] + G - 1) / G;
     c = next_pow2(c);
     if (c > kMaxCluster) return fail(D2G_E_UNSUPPORTED, "instance support size exceeds 8 CTAs");
@@ -325,7 +325,7 @@ static int build_packing(d2g_phase *ph, bool with_units) {
     h_plan_ng.push_back(ng[i]);
     h_plan_cum.push_back(ph->cum[i]);
     for (int q = 0; q < ng[i]; ++q) {
-      const int nv = std::min(kS, ph->p_str[i] - q * kS);
+      const int nv = std::min(S, ph->p_str[i] - q * S);
       h_meta.push_back((p << 4) | nv);
       ph->h_grp_rec.push_back(make_int4(p, g, 0, (ng[i] << 4) | nv));
       ph->h_grp_plan.push_back(p);
@@ -385,7 +385,7 @@ static int build_packing(d2g_phase *ph, bool with_units) {
   ph->total_blocks = blocks;
   ph->ngroups = g;
   ph->nplans = (int)n;
-  ph->ncols_packed = (long long)g * kS;
+  ph->ncols_packed = (long long)g * S;
   if (ph->ncols_packed * ph->MP > (1LL << 40)) return fail(D2G_E_UNSUPPORTED, "phase too large");
 
   D2G_CUDA(ph->grp_meta.alloc(h_meta.size()));
@@ -493,7 +493,7 @@ static int set_labels_impl(d2g_phase *ph, const int *label) {
       std::vector<int4> wl(ph->nwide);
       for (int q = 0; q < ph->nwide; ++q) {
         const int p = ph->h_wide_plans[q];
-        const int ngp = (ph->p_str[ph->plan_inst[p]] + kS - 1) / kS;
+        const int ngp = (ph->p_str[ph->plan_inst[p]] + ph->geo.S - 1) / ph->geo.S;
         wl[q] = make_int4(slot[p], (ngp + ph->geo.G - 1) / ph->geo.G, pl[p], 0);
       }
       D2G_CUDA(ph->wide.alloc(ph->nwide));
@@ -509,10 +509,10 @@ static int set_labels_impl(d2g_phase *ph, const int *label) {
       for (size_t gi = 0; gi < ph->h_grp_rec.size(); ++gi) {
         const int p = gplan[gi];
         const int nv = ph->h_grp_rec[gi].w & 15;
-        const int jj0 = (int)(gi - ph->h_grp_rec[gi].y) * kS;
+        const int jj0 = (int)(gi - ph->h_grp_rec[gi].y) * ph->geo.S;
         const long long c0 = ph->cum[ph->plan_inst[p]];
         for (int s2 = 0; s2 < nv; ++s2)
-          key_of[gi * kS + s2] = pl[p] * V + ph->h_sym[c0 + jj0 + s2];
+          key_of[gi * ph->geo.S + s2] = pl[p] * V + ph->h_sym[c0 + jj0 + s2];
       }
       std::vector<int> cnt((size_t)ph->K * V + 1, 0);
       for (int k2 : key_of)
@@ -934,7 +934,7 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
         if (b.cs > 1) {
           D2G_CUDA(launch_plan_finalize(ph->Z.p, ph->Y.p, ph->item_g0.p + b.item_off,
                                         ph->item_ng.p + b.item_off, b.nitems, b.cs, ph->geo.G,
-                                        ph->MP, ph->grp_rec.p, ph->rowsc.p, ph->def_iter.p,
+                                        ph->geo.S, ph->MP, ph->grp_rec.p, ph->rowsc.p, ph->def_iter.p,
                                         ph->ctl.p, ph->st));
           ++nl;
         }

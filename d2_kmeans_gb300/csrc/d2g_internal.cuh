@@ -40,8 +40,12 @@
 
 namespace d2g {
 
-constexpr int kS = 4;         // columns per thread (one column group)
-constexpr int kThreads = 256; // threads per plan-update CTA
+// Plan-update CTA shape per padded support size MP: S columns per thread (one
+// column group), NT threads.  (512 threads of 2 columns for MP = 256 -- the same
+// 32 columns per CTA with twice the warps -- measured 15-20 % slower than 256
+// threads of 4 columns: the column shuffles and row-partial sums double.)
+__host__ __device__ constexpr int plan_cols_per_thread(int /*MP*/) { return 4; }
+__host__ __device__ constexpr int plan_threads(int /*MP*/) { return 256; }
 constexpr int kMaxCluster = 8;
 constexpr float kRoundoff = 1e-9f;  // ROUNDOFF, src/d2/centroid_Bregman.c:20
 
@@ -96,7 +100,7 @@ struct PlanArgs {
 
 // per-MP launch geometry
 struct Geo {
-  int MP, RPT, TPC, G, JC;
+  int MP, RPT, TPC, G, JC, S, NT;
 };
 Geo geo_for(int MP);
 
@@ -121,7 +125,7 @@ cudaError_t launch_rowsum_combine(const int4 *wide, int nwide, const float *rowp
                                   const float *cw32, int MP, int m, float *rowsum_out,
                                   float *rowsc, const Ctl *ctl, int iter, cudaStream_t st);
 cudaError_t launch_plan_finalize(float *Z, float *Y, const int *item_g0, const int *item_ng,
-                                 int nitems, int cs, int G, int MP, const int4 *grp_rec,
+                                 int nitems, int cs, int G, int S, int MP, const int4 *grp_rec,
                                  const float *rowsc, const unsigned char *def_iter, const Ctl *ctl,
                                  cudaStream_t st);
 

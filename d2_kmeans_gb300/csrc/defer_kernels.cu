@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(256) plan_finalize_kernel(float *__restrict__ 
                                                             float *__restrict__ Y,
                                                             const int *__restrict__ item_g0,
                                                             const int *__restrict__ item_ng, int cs,
-                                                            int G, int MP,
+                                                            int G, int S, int MP,
                                                             const int4 *__restrict__ grp_rec,
                                                             const float *__restrict__ rowsc,
                                                             const unsigned char *__restrict__ def_iter,
@@ -64,8 +64,8 @@ __global__ void __launch_bounds__(256) plan_finalize_kernel(float *__restrict__ 
   if (ng <= 0) return;
   const int slot = grp_rec[g0].x;
   const float *sc = rowsc + (size_t)slot * MP;
-  const size_t base = (size_t)g0 * kS * MP;
-  const int n = ng * kS * MP;
+  const size_t base = (size_t)g0 * S * MP;
+  const int n = ng * S * MP;
   for (int e = threadIdx.x; e < n; e += blockDim.x) {
     const float z = Z[base + e] * sc[e & (MP - 1)];
     Z[base + e] = z;
@@ -84,11 +84,11 @@ cudaError_t launch_rowsum_combine(const int4 *wide, int nwide, const float *rowp
 }
 
 cudaError_t launch_plan_finalize(float *Z, float *Y, const int *item_g0, const int *item_ng,
-                                 int nitems, int cs, int G, int MP, const int4 *grp_rec,
+                                 int nitems, int cs, int G, int S, int MP, const int4 *grp_rec,
                                  const float *rowsc, const unsigned char *def_iter, const Ctl *ctl,
                                  cudaStream_t st) {
   if (nitems <= 0) return cudaSuccess;
-  plan_finalize_kernel<<<nitems * cs, 256, 0, st>>>(Z, Y, item_g0, item_ng, cs, G, MP, grp_rec,
+  plan_finalize_kernel<<<nitems * cs, 256, 0, st>>>(Z, Y, item_g0, item_ng, cs, G, S, MP, grp_rec,
                                                     rowsc, def_iter, ctl);
   return cudaGetLastError();
 }

@@ -35,8 +35,10 @@ Geo geo_for(int MP) {
   g.MP = MP;
   g.RPT = MP >= 256 ? 8 : 4;
   g.TPC = MP / g.RPT;
-  g.G = kThreads / g.TPC;
-  g.JC = g.G * kS;
+  g.S = plan_cols_per_thread(MP);
+  g.NT = plan_threads(MP);
+  g.G = g.NT / g.TPC;
+  g.JC = g.G * g.S;
   return g;
 }
 

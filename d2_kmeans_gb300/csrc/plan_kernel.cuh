@@ -18,7 +18,7 @@
 // (step 5), and on check iterations per-CTA partials of <C,X>, |X-Z|, |Z-Z0|
 // (step 6).
 //
-// Thread mapping: a CTA of kThreads threads owns JC = G*S columns; TPC
+// Thread mapping: a CTA of NT threads owns JC = G*S columns; TPC
 // threads share one column (RPT rows each, MP = TPC*RPT), each thread holds S
 // consecutive columns.  Plans start on S-column group boundaries, so a thread
 // never straddles two plans.
@@ -38,8 +38,10 @@ template <int MP>
 struct GeoT {
   static constexpr int RPT = MP >= 256 ? 8 : 4;
   static constexpr int TPC = MP / RPT;
-  static constexpr int G = kThreads / TPC;
-  static constexpr int JC = G * kS;
+  static constexpr int NT = plan_threads(MP);        // threads per CTA
+  static constexpr int S = plan_cols_per_thread(MP); // columns per thread
+  static constexpr int G = NT / TPC;
+  static constexpr int JC = G * S;
   static_assert(TPC >= 1 && TPC <= 32 && (32 % TPC) == 0, "TPC must divide a warp");
 };
 
@@ -105,7 +107,7 @@ __device__ __forceinline__ void block_sum3(double v0, double v1, double v2, doub
 template <int MP, int MODE>
 struct Tile {
   using Gm = GeoT<MP>;
-  static constexpr int RPT = Gm::RPT, TPC = Gm::TPC, G = Gm::G, S = kS;
+  static constexpr int RPT = Gm::RPT, TPC = Gm::TPC, G = Gm::G, S = Gm::S;
   static constexpr bool EUC = MODE != COST_TABLE;
   static constexpr int DS = MODE == COST_EUCLID8 ? 8 : 4;
 
@@ -300,9 +302,9 @@ __device__ __forceinline__ void st_rows_sm(float *p, const float (&v)[N]) {
 }
 
 template <int MP, int MODE, bool CHECK>
-__global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2) plan_kernel(const PlanArgs a) {
+__global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2) plan_kernel(const PlanArgs a) {
   using T = Tile<MP, MODE>;
-  constexpr int RPT = T::RPT, TPC = T::TPC, G = T::G, S = kS;
+  constexpr int RPT = T::RPT, TPC = T::TPC, G = T::G, S = T::S;
   extern __shared__ __align__(16) float smem[];
   float *sm_rs = smem;              // [G][MP] per-group row partials of Z'
   float *sm_tot = sm_rs + G * MP;   // [MP] CTA partial row sums (cluster exchange)
@@ -523,15 +525,15 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2) plan_kernel(const
     }
   }
   if constexpr (CHECK) {
-    block_sum3<kThreads>(s_obj, s_pr, s_dr, a.resid_part + (size_t)(a.resid_off + blockIdx.x) * 4);
+    block_sum3<GeoT<MP>::NT>(s_obj, s_pr, s_dr, a.resid_part + (size_t)(a.resid_off + blockIdx.x) * 4);
   }
 }
 
 // Sum of the initial ground costs (for rho), FP32 costs accumulated in FP64.
 template <int MP, int MODE>
-__global__ void __launch_bounds__(kThreads) rho_partial_kernel(const PlanArgs a, double *part) {
+__global__ void __launch_bounds__(GeoT<MP>::NT) rho_partial_kernel(const PlanArgs a, double *part) {
   using T = Tile<MP, MODE>;
-  constexpr int RPT = T::RPT, S = kS;
+  constexpr int RPT = T::RPT, S = T::S;
   T t;
   t.init(a);
   t.load_costs(a);
@@ -545,7 +547,7 @@ __global__ void __launch_bounds__(kThreads) rho_partial_kernel(const PlanArgs a,
       if (s < t.nvalid && t.k0 + q < a.m) acc += (double)c[q];
   }
   __shared__ double res[3];
-  block_sum3<kThreads>(acc, 0.0, 0.0, res);
+  block_sum3<GeoT<MP>::NT>(acc, 0.0, 0.0, res);
   if (threadIdx.x == 0) part[blockIdx.x] = res[0];
 }
 
@@ -557,13 +559,13 @@ __global__ void __launch_bounds__(kThreads) rho_partial_kernel(const PlanArgs a,
 //          (src/d2/centroid_Bregman.c:116-124); other plans are left as they are
 //   dir 3: as dir 1, times ln(2) (Y is stored scaled by log2(e))
 template <int MP>
-__global__ void __launch_bounds__(kThreads) pack_convert_kernel(const PlanArgs a, int dir,
+__global__ void __launch_bounds__(GeoT<MP>::NT) pack_convert_kernel(const PlanArgs a, int dir,
                                                                 double *ref,
                                                                 const long long *plan_refcol,
                                                                 const char *reinit,
                                                                 const double *cw64, int str) {
   using T = Tile<MP, COST_TABLE>;
-  constexpr int RPT = T::RPT, S = kS;
+  constexpr int RPT = T::RPT, S = T::S;
   T t;
   t.init(a);
   if (!t.active) return;
@@ -600,7 +602,7 @@ __global__ void __launch_bounds__(kThreads) pack_convert_kernel(const PlanArgs a
 // j for dense histograms, the vocabulary / bin id otherwise).  Pad columns get
 // zeros.
 template <int MP>
-__global__ void __launch_bounds__(kThreads) pack_columns_kernel(
+__global__ void __launch_bounds__(GeoT<MP>::NT) pack_columns_kernel(
     const PlanArgs a, const long long *plan_cum, const double *w_ref, const double *supp_ref,
     const int *sym_ref, float *col_w, float *col_supp, int *col_sym, int dim, int DS,
     int dense_hist) {
@@ -609,8 +611,8 @@ __global__ void __launch_bounds__(kThreads) pack_columns_kernel(
   t.init(a);
   if (!t.active || t.r != 0) return;
   const long long cum = plan_cum[t.p];
-  const int jj0 = (t.cta_g0 + t.g - t.pl_g0) * kS;
-  for (int s = 0; s < kS; ++s) {
+  const int jj0 = (t.cta_g0 + t.g - t.pl_g0) * T::S;
+  for (int s = 0; s < T::S; ++s) {
     const size_t pc = t.colbase + s;
     const bool ok = s < t.nvalid;
     const long long rc = cum + jj0 + s;
@@ -626,9 +628,9 @@ __global__ void __launch_bounds__(kThreads) pack_columns_kernel(
 // the residual check of an iteration that also moved the supports (the
 // reference evaluates obj after step 5, :301).  Partial per CTA into slot 3.
 template <int MP, int MODE>
-__global__ void __launch_bounds__(kThreads) obj_kernel(const PlanArgs a) {
+__global__ void __launch_bounds__(GeoT<MP>::NT) obj_kernel(const PlanArgs a) {
   using T = Tile<MP, MODE>;
-  constexpr int RPT = T::RPT, S = kS;
+  constexpr int RPT = T::RPT, S = T::S;
   if (a.iter >= a.ctl->stop_iter) return;
   T t;
   t.init(a);
@@ -645,7 +647,7 @@ __global__ void __launch_bounds__(kThreads) obj_kernel(const PlanArgs a) {
       if (s < t.nvalid && t.k0 + q < a.m) acc = fmaf(c[q] * inv_rho, x[q], acc);
   }
   __shared__ double res[3];
-  block_sum3<kThreads>((double)acc, 0.0, 0.0, res);
+  block_sum3<GeoT<MP>::NT>((double)acc, 0.0, 0.0, res);
   if (threadIdx.x == 0) a.resid_part[(size_t)(a.resid_off + blockIdx.x) * 4 + 3] = res[0];
 }
 
@@ -706,7 +708,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *b, unsigned parity
 
 template <int MP>
 __host__ __device__ constexpr int tma_tile_floats() {
-  return GeoT<MP>::G * kS * MP;
+  return GeoT<MP>::JC * MP;
 }
 
 // table costs staged in shared memory by bulk copies (one table row per column)
@@ -717,10 +719,10 @@ __host__ __device__ constexpr bool plan_stages_costs(int MP, int MODE) {
 // WIDE: the phase has plans wider than one CTA (cluster launches, deferred
 // units); without them the exchange machinery compiles out.
 template <int MP, int MODE, bool CHECK, bool FULL, bool WIDE>
-__global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
+__global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
     plan_kernel_tma(const PlanArgs a, int nitems) {
   using T = Tile<MP, MODE>;
-  constexpr int RPT = T::RPT, TPC = T::TPC, G = T::G, S = kS;
+  constexpr int RPT = T::RPT, TPC = T::TPC, G = T::G, S = T::S;
   constexpr int TILE = tma_tile_floats<MP>();
   constexpr int JC = G * S;
   constexpr int CW = T::EUC ? T::DS : 1;  // staged column data: supports or table row
@@ -729,7 +731,8 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
   // table rows with cp.async (TILE / 4 pieces per unit, PPT per thread)
   constexpr bool SCC = plan_stages_costs(MP, MODE);
   constexpr int CPR = MP / 4;                                  // pieces per table row
-  constexpr int PPT = SCC ? TILE / 4 / kThreads : 1;
+  constexpr int NT = GeoT<MP>::NT;
+  constexpr int PPT = SCC ? TILE / 4 / NT : 1;
   const bool SC = SCC && a.stage_costs;
   extern __shared__ __align__(128) float smem[];
   float *stZ = smem;                                  // [2][TILE]
@@ -802,14 +805,14 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
   auto load_rows_idx = [&](int g0, int ng) {
 #pragma unroll
     for (int j = 0; j < PPT; ++j) {
-      const int c = (tid + kThreads * j) / CPR;
+      const int c = (tid + NT * j) / CPR;
       crow_p[j] = c < ng * S ? __ldg(a.col_crow + (size_t)g0 * S + c) : -1;
     }
   };
   auto issue_rows = [&](int stg) {
 #pragma unroll
     for (int j = 0; j < PPT; ++j) {
-      const int i = tid + kThreads * j, c = i / CPR, part = i - c * CPR;
+      const int i = tid + NT * j, c = i / CPR, part = i - c * CPR;
       if (crow_p[j] >= 0)
         asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
                          smem_u32(stK + stg * TILE + c * MP + part * 4)),
@@ -1185,7 +1188,7 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
   if constexpr (CHECK) {
     // one partial per CTA in the slot of its first (item, rank); its other slots get zeros
     __shared__ double res[3];
-    block_sum3<kThreads>(s_obj, s_pr, s_dr, res);
+    block_sum3<GeoT<MP>::NT>(s_obj, s_pr, s_dr, res);
     // (check iterations never run deferred: a unit is an item, the rank is crank)
     if (tid == 0 && u0 < nitems) {
       double *pp = a.resid_part + (size_t)(a.resid_off + u0 * CS + crank) * 4;
@@ -1200,11 +1203,11 @@ __global__ void __launch_bounds__(kThreads, MP >= 256 ? 1 : 2)
   }
 }
 
-static inline cudaLaunchConfig_t plan_cfg(int nblocks, size_t smem, cudaStream_t st,
+static inline cudaLaunchConfig_t plan_cfg(int nblocks, int threads, size_t smem, cudaStream_t st,
                                           cudaLaunchAttribute *attr, int cs) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nblocks, 1, 1);
-  cfg.blockDim = dim3(kThreads, 1, 1);
+  cfg.blockDim = dim3(threads, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   if (cs > 1) {
@@ -1222,7 +1225,7 @@ template <int MP, int MODE, bool CHECK, bool FULL, bool WIDE>
 cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaStream_t st) {
   // persistent grid: as many clusters of a.cs CTAs as are resident at once
   static int grid[kMaxCluster + 1] = {0};
-  constexpr int JC = GeoT<MP>::G * kS;
+  constexpr int JC = GeoT<MP>::JC;
   constexpr int CW = MODE == COST_EUCLID8 ? 8 : (MODE == COST_EUCLID4 ? 4 : 1);
   const size_t sm = smem + (size_t)4 * tma_tile_floats<MP>() * sizeof(float) +
                     2 * (size_t)GeoT<MP>::G * 16 + 2 * (size_t)JC * 4 * (1 + CW) + (size_t)2 * MP * 4 +
@@ -1242,7 +1245,7 @@ cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaSt
   if (grid[cs] == 0) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(cs * 1024, 1, 1);
-    cfg.blockDim = dim3(kThreads, 1, 1);
+    cfg.blockDim = dim3(GeoT<MP>::NT, 1, 1);
     cfg.dynamicSmemBytes = sm;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -1261,7 +1264,8 @@ cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaSt
     int dev = 0, per = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kThreads, sm);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, GeoT<MP>::NT, sm);
     if (e != cudaSuccess) return e;
     grid[0] = (per > 0 ? per : 1) * nsm;
   }
@@ -1272,7 +1276,7 @@ cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaSt
   if (plain && a.ctas_per_sm > 0) cap = std::min(cap, a.ctas_per_sm * nsm);
   const int g = units < cap ? (int)units : cap;
   cudaLaunchAttribute attr[1];
-  cudaLaunchConfig_t cfg = plan_cfg(g, sm, st, attr, plain ? 1 : cs);
+  cudaLaunchConfig_t cfg = plan_cfg(g, GeoT<MP>::NT, sm, st, attr, plain ? 1 : cs);
   return cudaLaunchKernelEx(&cfg, kern, a, nitems);
 }
 
@@ -1297,7 +1301,7 @@ cudaError_t launch_plan_t(const PlanArgs &a, int nitems, size_t smem, cudaStream
   }
   if (nitems <= 0) return cudaSuccess;
   cudaLaunchAttribute attr[1];
-  cudaLaunchConfig_t cfg = plan_cfg(nitems * a.cs, smem, st, attr, a.cs);
+  cudaLaunchConfig_t cfg = plan_cfg(nitems * a.cs, GeoT<MP>::NT, smem, st, attr, a.cs);
   return cudaLaunchKernelEx(&cfg, plan_kernel<MP, MODE, CHECK>, a);
 }
 
@@ -1316,7 +1320,7 @@ cudaError_t launch_plan_mp(int mode, bool check, const PlanArgs &a, int nitems, 
 
 template <int MP>
 cudaError_t launch_rho_mp(int mode, const PlanArgs &a, int nitems, double *part, cudaStream_t st) {
-  const dim3 grid(nitems * a.cs), block(kThreads);
+  const dim3 grid(nitems * a.cs), block(GeoT<MP>::NT);
   if (mode == COST_EUCLID4)
     rho_partial_kernel<MP, COST_EUCLID4><<<grid, block, 0, st>>>(a, part);
   else if (mode == COST_EUCLID8)
@@ -1330,7 +1334,7 @@ template <int MP>
 cudaError_t launch_convert_mp(int dir, const PlanArgs &a, int nitems, double *ref,
                               const long long *plan_refcol, const char *reinit,
                               const double *cw64, int str, cudaStream_t st) {
-  pack_convert_kernel<MP><<<nitems * a.cs, kThreads, 0, st>>>(a, dir, ref, plan_refcol, reinit,
+  pack_convert_kernel<MP><<<nitems * a.cs, GeoT<MP>::NT, 0, st>>>(a, dir, ref, plan_refcol, reinit,
                                                               cw64, str);
   return cudaGetLastError();
 }
@@ -1340,7 +1344,7 @@ cudaError_t launch_pack_columns_mp(const PlanArgs &a, int nitems, const long lon
                                    const double *w_ref, const double *supp_ref, const int *sym_ref,
                                    float *col_w, float *col_supp, int *col_sym, int dim, int DS,
                                    int dense_hist, cudaStream_t st) {
-  pack_columns_kernel<MP><<<nitems * a.cs, kThreads, 0, st>>>(a, plan_cum, w_ref, supp_ref, sym_ref,
+  pack_columns_kernel<MP><<<nitems * a.cs, GeoT<MP>::NT, 0, st>>>(a, plan_cum, w_ref, supp_ref, sym_ref,
                                                               col_w, col_supp, col_sym, dim, DS,
                                                               dense_hist);
   return cudaGetLastError();
@@ -1349,11 +1353,11 @@ cudaError_t launch_pack_columns_mp(const PlanArgs &a, int nitems, const long lon
 template <int MP>
 cudaError_t launch_obj_mp(int mode, const PlanArgs &a, int nitems, cudaStream_t st) {
   if (mode == COST_EUCLID4)
-    obj_kernel<MP, COST_EUCLID4><<<nitems * a.cs, kThreads, 0, st>>>(a);
+    obj_kernel<MP, COST_EUCLID4><<<nitems * a.cs, GeoT<MP>::NT, 0, st>>>(a);
   else if (mode == COST_EUCLID8)
-    obj_kernel<MP, COST_EUCLID8><<<nitems * a.cs, kThreads, 0, st>>>(a);
+    obj_kernel<MP, COST_EUCLID8><<<nitems * a.cs, GeoT<MP>::NT, 0, st>>>(a);
   else
-    obj_kernel<MP, COST_TABLE><<<nitems * a.cs, kThreads, 0, st>>>(a);
+    obj_kernel<MP, COST_TABLE><<<nitems * a.cs, GeoT<MP>::NT, 0, st>>>(a);
   return cudaGetLastError();
 }
 

@@ -32,6 +32,8 @@ def main(argv=None):
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--requests", type=int, default=64)
     ap.add_argument("--cost-gemm", type=int, default=0)
+    ap.add_argument("--batch-entries", type=int, default=0,
+                    help="serving: plan entries per device batch (0 = library default)")
     args = ap.parse_args(argv)
     badmm.set_config(verbose=0, cost_gemm=args.cost_gemm)
     if args.workload == "serve":
@@ -39,7 +41,7 @@ def main(argv=None):
 
         from . import serve
         c_w, c_supp, means = synth.serving_centroids(k=256, m=64, dim=64, n_comp=32, seed=args.seed)
-        S = serve.Server(c_w, c_supp, iters=args.iters or 200)
+        S = serve.Server(c_w, c_supp, iters=args.iters or 200, max_batch_entries=args.batch_entries)
         qs = synth.serving_queries(args.requests, means, sizes=(4, 512), seed=args.seed + 1)
         t = time.perf_counter()
         out = serve.poisson_run(S, qs, rate=1e9, seed=0)
