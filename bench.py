@@ -19,6 +19,7 @@ Prints one JSON line:
   workloads  the word-embedding, 256-bin histogram and two-phase Euclidean
              workloads: plan-updates/s and the plan kernel against the HBM peak
   tuning     the launch shape the autotuner picked for the headline phase
+  io         d2 text input: d2g_read MB/s against the reference's fscanf reader
 
 --impl reference times the reference algorithm's CPU implementation (the
 oracle port; the reference tree itself is not on the GPU host) with every
@@ -296,6 +297,41 @@ def workload_leg(name, steps, hbm, tf32_peak):
     return out
 
 
+IO_WORKLOAD = ("d2 text file of 20 000 instances of the batched workload (d = 3, m_i log-uniform 8-128), "
+               "parsed into the reference's mph")
+
+
+def io_leg():
+    """d2g_read (parallel, every host core) against the oracle's restatement of
+    the reference's fscanf reader (one core) on the same file; the arrays must
+    be identical."""
+    import numpy as np
+    import oracle
+    from d2_kmeans_gb300 import d2io, synth
+    ph, _, _ = synth.workload("batched", seed=0, scale=0.1)
+    n = len(ph["p_str"])
+    with tempfile.TemporaryDirectory() as td:
+        f = os.path.join(td, "batched.d2")
+        d2io.write(f, [dict(metric=d2io.EUCLIDEAN, dim=3, p_str=ph["p_str"], p_w=ph["p_w"],
+                            p_supp=ph["p_supp"])])
+        mb = os.path.getsize(f) / 1e6
+        d2io.read(f, n, [3], [0], avg_strides=[43])  # page cache warm
+        t = time.perf_counter()
+        ours = d2io.read(f, n, [3], [0], avg_strides=[43])
+        t_ours = time.perf_counter() - t
+        ensure_oracle()
+        t = time.perf_counter()
+        rc, port = oracle.read("port", f, n, [3], [0], avg_strides=[43])
+        t_port = time.perf_counter() - t
+    same = rc == 0 and all(np.array_equal(ours["phases"][0][k], port["phases"][0][k])
+                           for k in ("p_str", "p_str_cum", "p_w", "p_supp"))
+    return {"workload": IO_WORKLOAD, "file_mb": mb, "value": mb / t_ours, "unit": "MB/s",
+            "threads": os.cpu_count(), "seconds": t_ours,
+            "cpu_baseline": {"value": mb / t_port, "unit": "MB/s", "cores": 1, "kind": "port",
+                             "sample": "the oracle's restatement of d2_read (fscanf per token)"},
+            "identical_arrays": bool(same)}
+
+
 SERVE_WORKLOAD = ("serving: k=256 resident centroids, m=64, d=64; queries with m_q log-uniform 4-512, "
                   "GMM supports, Dirichlet(1) weights; 200 B-ADMM iterations per solve against all "
                   "centroids + argmin; Poisson arrivals")
@@ -325,7 +361,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip", default="",
-                    help="comma list of legs to skip: e2e,plain,cpu,profile,serve,workloads,fp64")
+                    help="comma list of legs to skip: e2e,plain,cpu,profile,serve,workloads,fp64,io")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -420,6 +456,8 @@ def main():
                       "api": "d2_centroid_sphBregman (reference structs, host buffers)"}
     if "serve" not in skip and rank == 0:
         out["serve"] = serve_leg()
+    if "io" not in skip and rank == 0:
+        out["io"] = io_leg()
     if "workloads" not in skip and rank == 0:
         tf32 = bf16_peak() / 2
         out["workloads"] = {w: workload_leg(w, 2, hbm, tf32) for w in OTHER_WORKLOADS}

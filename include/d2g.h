@@ -253,6 +253,24 @@ void *d2g_phase_stream(d2g_phase *ph);
  * reference leaves it), Y and C (divided by rho), reference layout, FP64 */
 int d2g_phase_get_scratch(d2g_phase *ph, double *X, double *Y, double *C);
 
+/* ------------------------------------------------------------ d2 input files
+ * Replaces d2_read, src/d2/clustering_io.c:14-201 (declared
+ * include/d2/clustering.h:144), with the same signature and result: reads the
+ * reference's d2 text formats (.d2 multi-phase Euclidean; dense histograms
+ * with a .histN cost file; .d2s symbolic supports with a .vocabN embedding
+ * file; sparse histograms) into an mph allocated by the reference's
+ * d2_allocate (or by d2g_mph_alloc), growing its arrays when needed.  The
+ * file is parsed in parallel (D2G_IO_THREADS threads, default all cores).
+ * Malformed input returns D2G_E_INVAL (the reference asserts). */
+int d2g_read(const char *filename, const char *meta_filename, mph *p_data);
+/* The data part of d2_allocate (src/d2/clustering_util.c:93-130): phases,
+ * labels (-1), per-phase arrays for size objects of avg_strides[n] + 0.6
+ * support points on average.  d2g_mph_free releases it (and the cost /
+ * vocabulary arrays d2g_read attached). */
+int d2g_mph_alloc(int s_ph, size_t size, const int *avg_strides, const int *dims,
+                  const int *types, mph **out);
+int d2g_mph_free(mph *p_data);
+
 /* ------------------------------------------------------------- autotuning
  * Launch-shape choices of the batched form.  All choices compute the same
  * B-ADMM iteration; they differ in speed (and, for exchange, in the rounding

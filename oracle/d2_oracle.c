@@ -315,3 +315,180 @@ out:
   free(C); free(X); free(Y); free(Z); free(rs);
   return best;
 }
+
+/* ------------------------------------------------------------ d2 input files
+ * Restatement of d2_allocate's data part (src/d2/clustering_util.c:18-59,
+ * 93-130) and of d2_read (src/d2/clustering_io.c:14-201): the same fscanf
+ * token reads, weight checks and renormalisation, id shift and array growth.
+ * Deviation: where the reference assert()s (missing file, dimension mismatch,
+ * weight <= 1e-9) this returns -1. */
+#include <stdio.h>
+
+#include "d2g.h"
+
+static int o_alloc_sph(sph *ph, int d, int stride, size_t num, double semicol, int type) {
+  const size_t m = (size_t)(num * (stride + semicol));
+  ph->max_col = m;
+  ph->dim = d;
+  ph->str = stride;
+  ph->max_str = stride;
+  ph->p_str = (int *)calloc(num, sizeof(int));
+  ph->p_str_cum = (size_t *)calloc(num, sizeof(size_t));
+  ph->p_w = (double *)malloc((m ? m : 1) * sizeof(double));
+  ph->metric_type = type;
+  ph->p_supp = NULL;
+  ph->p_supp_sym = NULL;
+  if (type == D2O_EUCLIDEAN_L2) ph->p_supp = (double *)malloc((m * d > 0 ? m * d : 1) * sizeof(double));
+  if (type == D2O_WORD_EMBED || type == D2O_SPARSE_HISTOGRAM) ph->p_supp_sym = (int *)malloc((m ? m : 1) * sizeof(int));
+  ph->is_meta_allocated = 0;
+  return 0;
+}
+
+int d2o_mph_free(void *pv) {
+  mph *p = (mph *)pv;
+  if (!p) return -1;
+  for (int n = 0; n < p->s_ph; ++n) {
+    sph *ph = p->ph + n;
+    free(ph->p_str);
+    free(ph->p_str_cum);
+    free(ph->p_w);
+    free(ph->p_supp);
+    free(ph->p_supp_sym);
+    if (ph->is_meta_allocated) {
+      free(ph->dist_mat);
+      free(ph->vocab_vec);
+    }
+  }
+  free(p->ph);
+  free(p->label);
+  free(p);
+  return 0;
+}
+
+int d2o_read(const char *filename, const char *meta_filename, int s_ph, size_t size,
+             const int *avg_strides, const int *dims, const int *types, void **out) {
+  mph *p = (mph *)calloc(1, sizeof(mph));
+  p->s_ph = s_ph;
+  p->size = size;
+  p->ph = (sph *)calloc((size_t)s_ph, sizeof(sph));
+  p->label = (int *)malloc(size * sizeof(int));
+  for (size_t i = 0; i < size; ++i) p->label[i] = -1;
+  for (int n = 0; n < s_ph; ++n) o_alloc_sph(p->ph + n, dims[n], avg_strides[n], size, 0.6, types[n]);
+  *out = p;
+
+  int **p_str = (int **)malloc(s_ph * sizeof(int *));
+  int **p_sym = (int **)malloc(s_ph * sizeof(int *));
+  double **p_supp = (double **)malloc(s_ph * sizeof(double *));
+  double **p_w = (double **)malloc(s_ph * sizeof(double *));
+  for (int n = 0; n < s_ph; ++n) {
+    p_str[n] = p->ph[n].p_str;
+    p_sym[n] = p->ph[n].p_supp_sym;
+    p_supp[n] = p->ph[n].p_supp;
+    p_w[n] = p->ph[n].p_w;
+    p->ph[n].col = 0;
+  }
+  int rc = 0;
+  /* meta files (:55-89) */
+  for (int n = 0; n < s_ph && !rc; ++n) {
+    sph *ph = p->ph + n;
+    char extra[1024];
+    const int hist = ph->metric_type == D2O_HISTOGRAM || ph->metric_type == D2O_SPARSE_HISTOGRAM;
+    if (!hist && ph->metric_type != D2O_WORD_EMBED) continue;
+    if (meta_filename && s_ph == 1)
+      snprintf(extra, sizeof extra, "%s", meta_filename);
+    else
+      snprintf(extra, sizeof extra, "%s.%s%d", filename, hist ? "hist" : "vocab", n);
+    FILE *fm = fopen(extra, "r");
+    if (!fm) { rc = -1; break; }
+    if (hist) {
+      int str = 0;
+      if (fscanf(fm, "%d", &str) != 1 || str <= 0) { fclose(fm); rc = -1; break; }
+      ph->dist_mat = (double *)malloc((size_t)str * str * sizeof(double));
+      for (size_t i = 0; i < (size_t)str * str; ++i)
+        if (fscanf(fm, "%lf", &ph->dist_mat[i]) != 1) rc = -1;
+      ph->vocab_size = str;
+    } else {
+      int dim = 0;
+      if (fscanf(fm, "%d", &dim) != 1 || dim != ph->dim) { fclose(fm); rc = -1; break; }
+      if (fscanf(fm, "%d", &ph->vocab_size) != 1) { fclose(fm); rc = -1; break; }
+      ph->vocab_vec = (double *)malloc((size_t)dim * ph->vocab_size * sizeof(double));
+      for (size_t i = 0; i < (size_t)ph->vocab_size * dim; ++i)
+        if (fscanf(fm, "%lf", &ph->vocab_vec[i]) != 1) rc = -1;
+    }
+    ph->is_meta_allocated = 1;
+    fclose(fm);
+  }
+  FILE *fp = rc ? NULL : fopen(filename, "r");
+  if (!fp) rc = -1;
+  /* main file (:91-176) */
+  for (size_t i = 0; !rc && i < size; ++i) {
+    for (int n = 0; n < s_ph; ++n) {
+      sph *ph = p->ph + n;
+      int dim, str;
+      if (fscanf(fp, "%d", &dim) != 1) {
+        fprintf(stderr, "rank 0 warning: only read %zd d2!\n", i);
+        p->size = i;
+        size = i;
+        break;
+      }
+      if (dim != ph->dim) { rc = -1; break; }
+      if (fscanf(fp, "%d", &str) != 1 || str < 0) { rc = -1; break; }
+      if (str == 0) continue;
+      *p_str[n] = str;
+      if (str > ph->max_str) ph->max_str = str;
+      if (ph->col + str > ph->max_col) { /* grow as the reference does (:110-135) */
+        const size_t cap = 2 * ph->max_col > ph->col + str ? 2 * ph->max_col : ph->col + str;
+        ph->p_w = (double *)realloc(ph->p_w, cap * sizeof(double));
+        p_w[n] = ph->p_w + ph->col;
+        if (ph->metric_type == D2O_EUCLIDEAN_L2) {
+          ph->p_supp = (double *)realloc(ph->p_supp, cap * dim * sizeof(double));
+          p_supp[n] = ph->p_supp + ph->col * dim;
+        } else if (ph->metric_type == D2O_WORD_EMBED || ph->metric_type == D2O_SPARSE_HISTOGRAM) {
+          ph->p_supp_sym = (int *)realloc(ph->p_supp_sym, cap * sizeof(int));
+          p_sym[n] = ph->p_supp_sym + ph->col;
+        }
+        ph->max_col = cap;
+      }
+      ph->col += str;
+      double *w = p_w[n], wsum = 0.;
+      for (int j = 0; j < str; ++j) {
+        if (fscanf(fp, "%lf", &w[j]) != 1) { rc = -1; break; }
+        if (ph->metric_type != D2O_HISTOGRAM && !(w[j] > 1E-9)) { rc = -1; break; }
+        wsum += w[j];
+      }
+      if (rc) break;
+      for (int j = 0; j < str; ++j) w[j] /= wsum;
+      p_w[n] += str;
+      if (ph->metric_type == D2O_EUCLIDEAN_L2) {
+        for (int j = 0; j < str * dim; ++j)
+          if (fscanf(fp, "%lf", &p_supp[n][j]) != 1) rc = -1;
+        p_supp[n] += str * dim;
+      } else if (ph->metric_type == D2O_WORD_EMBED || ph->metric_type == D2O_SPARSE_HISTOGRAM) {
+        for (int j = 0; j < str; ++j) {
+          if (fscanf(fp, "%d", &p_sym[n][j]) != 1) rc = -1;
+          p_sym[n][j]--; /* ids start at one */
+          if (p_sym[n][j] < 0) p_sym[n][j] = ph->vocab_size - 1;
+        }
+        p_sym[n] += str;
+      }
+      p_str[n]++;
+    }
+  }
+  if (fp) fclose(fp);
+  /* cumulative sizes (:178-190) */
+  for (int n = 0; !rc && n < s_ph; ++n) {
+    sph *ph = p->ph + n;
+    if (ph->col > 0) {
+      ph->p_str_cum[0] = 0;
+      for (size_t i = 1; i < size; ++i) ph->p_str_cum[i] = ph->p_str_cum[i - 1] + ph->p_str[i - 1];
+      if (ph->metric_type == D2O_SPARSE_HISTOGRAM) ph->str = ph->vocab_size;
+    }
+  }
+  p->global_size = p->size;
+  free(p_w);
+  free(p_supp);
+  free(p_str);
+  free(p_sym);
+  return rc;
+}
+

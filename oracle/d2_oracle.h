@@ -88,6 +88,21 @@ int d2o_serve_query(int dim, int str, int k, const double *c_w, const double *c_
                     int m_q, const double *w_q, const double *supp_q, int iters,
                     double rhoCoeff, double *cost_out);
 
+/*
+ * d2 input files (the reference's d2_read, src/d2/clustering_io.c:14-201,
+ * into the mph of its d2_allocate, src/d2/clustering_util.c:93-130).  The
+ * mph is returned as an opaque pointer with the reference's layout
+ * (include/d2/clustering.h:14-51); free it with the matching *_mph_free.
+ *   d2o_read - d2_oracle.c, a restatement (token by token with fscanf).
+ *   d2r_read - ref_harness.c, the reference's own d2_allocate + d2_read.
+ */
+int d2o_read(const char *filename, const char *meta_filename, int s_ph, size_t size,
+             const int *avg_strides, const int *dims, const int *types, void **out_mph);
+int d2o_mph_free(void *p_mph);
+int d2r_read(const char *filename, const char *meta_filename, int s_ph, size_t size,
+             const int *avg_strides, const int *dims, const int *types, void **out_mph);
+int d2r_mph_free(void *p_mph);
+
 #ifdef __cplusplus
 }
 #endif

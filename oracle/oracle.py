@@ -171,3 +171,33 @@ def serve_query(c_w, c_supp, w_q, supp_q, iters=200, rho_coeff=2.0):
                                w_q.ctypes.data, supp_q.ctypes.data, int(iters),
                                float(rho_coeff), cost.ctypes.data)
     return best, cost
+
+
+def read(kind: str, filename: str, size: int, dims, types, avg_strides=None, meta_filename=None):
+    """d2 input file through the restatement (``port``: d2o_read) or the
+    reference's own d2_allocate + d2_read (``ref``); returns the mph's arrays
+    (d2_kmeans_gb300.d2io.mph_arrays layout) and the call's return code."""
+    import numpy as np
+    from d2_kmeans_gb300 import _lib as L
+    from d2_kmeans_gb300.d2io import mph_arrays
+    lib = _lib(kind)
+    fn = lib.d2o_read if kind == "port" else lib.d2r_read
+    free = lib.d2o_mph_free if kind == "port" else lib.d2r_mph_free
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_size_t] + [C.c_void_p] * 3 + \
+        [C.POINTER(C.c_void_p)]
+    free.restype = C.c_int
+    free.argtypes = [C.c_void_p]
+    s_ph = len(dims)
+    avg = np.ascontiguousarray(avg_strides if avg_strides is not None else [8] * s_ph, np.int32)
+    dims = np.ascontiguousarray(dims, np.int32)
+    types = np.ascontiguousarray(types, np.int32)
+    out = C.c_void_p()
+    rc = fn(filename.encode(), meta_filename.encode() if meta_filename else None, s_ph, int(size),
+            avg.ctypes.data, dims.ctypes.data, types.ctypes.data, C.byref(out))
+    try:
+        arrays = mph_arrays(C.cast(out, C.POINTER(L.mph))) if out.value else None
+    finally:
+        if out.value:
+            free(out)
+    return rc, arrays

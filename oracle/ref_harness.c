@@ -150,3 +150,38 @@ int d2r_badmm(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_s
   free(data.p_str_cum);
   return rc;
 }
+
+/* the reference's own d2_allocate + d2_read (src/d2/clustering_util.c:93-130,
+ * src/d2/clustering_io.c:14-201) into a heap mph */
+int d2_alg_type = 0; /* src/d2/clustering.c:24; clustering_util.c reads it */
+
+int d2r_read(const char *filename, const char *meta_filename, int s_ph, size_t size,
+             const int *avg_strides, const int *dims, const int *types, void **out) {
+  mph *p = (mph *)calloc(1, sizeof(mph));
+  if (d2_allocate(p, s_ph, size, avg_strides, dims, types)) return -1;
+  *out = p;
+  return d2_read(filename, meta_filename, p);
+}
+
+int d2r_mph_free(void *pv) {
+  /* d2_allocate leaves the pointers a metric does not use unset: free by type */
+  mph *p = (mph *)pv;
+  for (int n = 0; n < p->s_ph; ++n) {
+    sph *ph = p->ph + n;
+    const int mt = ph->metric_type;
+    free(ph->p_str);
+    free(ph->p_str_cum);
+    free(ph->p_w);
+    if (mt == D2_EUCLIDEAN_L2) free(ph->p_supp);
+    if (mt == D2_WORD_EMBED || mt == D2_SPARSE_HISTOGRAM) free(ph->p_supp_sym);
+    if (ph->is_meta_allocated) {
+      if (mt == D2_HISTOGRAM || mt == D2_SPARSE_HISTOGRAM) free(ph->dist_mat);
+      if (mt == D2_WORD_EMBED) free(ph->vocab_vec);
+    }
+  }
+  free(p->ph);
+  free(p->label);
+  free(p);
+  return 0;
+}
+

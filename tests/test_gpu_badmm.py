@@ -345,3 +345,42 @@ def test_autotune_times_every_candidate_and_keeps_results(d2g, oracle_mod, tmp_p
     Q = d2g.Phase(ph, 0)
     assert Q.tuning() == fastest
     Q.close()
+
+
+@pytest.mark.parametrize("exchange", EXCHANGES)
+def test_widest_packable_plan_and_one_more(d2g, oracle_mod, monkeypatch, exchange):
+    """m = 32 packs 128 columns per CTA and a plan over at most 8 CTAs: a
+    1024-column plan runs batched (8 slices); a 1025-column plan runs on the
+    FP64 form.  Both match the oracle."""
+    _exchange(monkeypatch, exchange)
+    for width, path in ((1024, 0), (1025, 1)):
+        ph, c = synth.euclidean_phase(6, 2, 32, 3, (4, 40), False, 5, 1.0, seed=71)
+        ph["p_str"][0] = width
+        rng = np.random.default_rng(72)
+        cum = np.concatenate([[0], np.cumsum(ph["p_str"])])
+        ph["p_w"] = np.concatenate([rng.dirichlet(np.ones(s)) for s in ph["p_str"]])
+        ph["p_supp"] = rng.normal(size=(int(cum[-1]), 3)).reshape(-1) * 3.0
+        opts = dict(maxIters=20, rhoCoeff=2.0, updatePerLoops=10)
+        ref = _port(oracle_mod, ph, c, opts)
+        P = d2g.Phase(ph, 0)
+        r = P.run(c, opts)
+        assert r["stats"]["path"] == path
+        assert_close(r, ref, 2, 32, fp64=path == 1)
+        P.close()
+
+
+def test_read_file_then_update(d2g, oracle_mod, tmp_path):
+    """A d2 file read by d2g_read feeds the batched centroid update; the result
+    matches the oracle on the same arrays."""
+    from d2_kmeans_gb300 import d2io
+    ph, c = synth.euclidean_phase(300, 5, 16, 3, (4, 30), False, 8, 1.0, seed=81)
+    f = str(tmp_path / "p.d2")
+    d2io.write(f, [dict(metric=d2io.EUCLIDEAN, dim=3, p_str=ph["p_str"], p_w=ph["p_w"], p_supp=ph["p_supp"])])
+    data = d2io.read(f, 300, [3], [d2io.EUCLIDEAN], avg_strides=[17])
+    rd = d2io.phase_dict(data, 0, 16, ph["label"], 5)
+    np.testing.assert_array_equal(rd["p_str"], ph["p_str"])
+    opts = dict(maxIters=30, rhoCoeff=2.0, updatePerLoops=10)
+    ref = _port(oracle_mod, rd, c, opts)
+    P = d2g.Phase(rd, 0)
+    assert_close(P.run(c, opts), ref, 5, 16)
+    P.close()
