@@ -69,10 +69,20 @@ void parallel_for(int nt, F f) {
 bool load_text(const char *path, Text &tx) {
   FILE *f = fopen(path, "rb");
   if (!f) return false;
+  // one read of the whole file (its size from the end offset; a stream that
+  // cannot seek is read in pieces)
   std::vector<char> buf;
-  char tmp[1 << 16];
-  size_t r;
-  while ((r = fread(tmp, 1, sizeof tmp, f)) > 0) buf.insert(buf.end(), tmp, tmp + r);
+  long sz = -1;
+  if (fseek(f, 0, SEEK_END) == 0) sz = ftell(f);
+  if (sz >= 0 && fseek(f, 0, SEEK_SET) == 0) {
+    buf.resize((size_t)sz + 1);
+    const size_t r = fread(buf.data(), 1, (size_t)sz, f);
+    buf.resize(r);
+  } else {
+    char tmp[1 << 16];
+    size_t r;
+    while ((r = fread(tmp, 1, sizeof tmp, f)) > 0) buf.insert(buf.end(), tmp, tmp + r);
+  }
   fclose(f);
   tx.len = buf.size();
   buf.push_back(0);
