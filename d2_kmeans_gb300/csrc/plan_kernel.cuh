@@ -928,7 +928,7 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
         csum += v;
       }
       csum = seg_sum<TPC>(csum);
-      const float f = colok ? w[s] / csum : 0.f;
+      const float f = colok ? __fdividef(w[s], csum) : 0.f;  // (column sum > 0: ROUNDOFF)
 #pragma unroll
       for (int q = 0; q < RPT; ++q) {
         const bool ok = colok && (FULL || t.k0 + q < m);
@@ -1118,7 +1118,7 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
 #pragma unroll
     for (int q = 0; q < RPT; ++q) {
       const bool ok = t.active && (FULL || t.k0 + q < m) && !def_out;
-      sc[q] = ok ? __ldg(a.cw32 + (size_t)t.lab * MP + t.k0 + q) / tot[q] : 0.f;
+      sc[q] = ok ? __fdividef(__ldg(a.cw32 + (size_t)t.lab * MP + t.k0 + q), tot[q]) : 0.f;
     }
     float i_obj = 0.f, i_pr = 0.f, i_dr = 0.f;
 #pragma unroll
