@@ -605,7 +605,7 @@ static int create_batched(d2g_phase *ph, const d2g_phase_desc *d) {
   ph->MP = std::max(4, next_pow2(ph->str));
   ph->geo = geo_for(ph->MP);
   if (ph->metric == D2_EUCLIDEAN_L2) {
-    ph->mode = ph->dim <= 4 ? COST_EUCLID4 : COST_EUCLID8;
+    ph->mode = ph->dim == 3 ? COST_EUCLID3 : (ph->dim <= 4 ? COST_EUCLID4 : COST_EUCLID8);
     ph->DS = ph->dim <= 4 ? 4 : 8;
   } else {
     ph->mode = COST_TABLE;

@@ -49,7 +49,9 @@ __host__ __device__ constexpr int plan_threads(int /*MP*/) { return 256; }
 constexpr int kMaxCluster = 8;
 constexpr float kRoundoff = 1e-9f;  // ROUNDOFF, src/d2/centroid_Bregman.c:20
 
-enum CostMode { COST_EUCLID4 = 0, COST_EUCLID8 = 1, COST_TABLE = 2 };
+// Euclidean costs from supports padded to 4 or 8 coordinates (EUCLID3: d = 3,
+// stored padded to 4, summed over 3), or read from a cost table
+enum CostMode { COST_EUCLID4 = 0, COST_EUCLID8 = 1, COST_TABLE = 2, COST_EUCLID3 = 3 };
 
 enum PlanFlags {
   PF_UPDATE = 1,   // support-update iteration: emit X moments (Euclidean)

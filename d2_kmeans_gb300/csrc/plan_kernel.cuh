@@ -109,7 +109,8 @@ struct Tile {
   using Gm = GeoT<MP>;
   static constexpr int RPT = Gm::RPT, TPC = Gm::TPC, G = Gm::G, S = Gm::S;
   static constexpr bool EUC = MODE != COST_TABLE;
-  static constexpr int DS = MODE == COST_EUCLID8 ? 8 : 4;
+  static constexpr int DS = MODE == COST_EUCLID8 ? 8 : 4;        // stored coordinates
+  static constexpr int NDIM = MODE == COST_EUCLID3 ? 3 : DS;     // coordinates summed
 
   int g, r, k0, rank, cta_g0, cta_ng, p, nvalid, pl_g0, pl_ng, lab;
   bool active;
@@ -252,7 +253,7 @@ struct Tile {
       for (int q = 0; q < RPT; ++q) {
         float acc = 0.f;
 #pragma unroll
-        for (int t = 0; t < DS; ++t) {
+        for (int t = 0; t < NDIM; ++t) {  // (padded coordinates are 0 on both sides)
           const float d = cc[q][t] - sp[s][t];
           acc = fmaf(d, d, acc);
         }
@@ -922,18 +923,32 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
       float csum = 0.f;
 #pragma unroll
       for (int q = 0; q < RPT; ++q) {
-        const bool ok = colok && (FULL || t.k0 + q < m);
-        const float v = ok ? fmaf(z[q], ex2f(-fmaf(c[q], ir2, y[q])), kRoundoff) : 0.f;
+        // Full height (m == MP): a padded column holds Z = Y = 0 and weight 0,
+        // so its X comes out 0 through the column scale and no mask is needed
+        // (its column sum is ROUNDOFF-positive); step 2 adds ROUNDOFF to
+        // valid columns only.
+        float v;
+        if constexpr (FULL) {
+          v = fmaf(z[q], ex2f(-fmaf(c[q], ir2, y[q])), kRoundoff);
+        } else {
+          const bool ok = colok && t.k0 + q < m;
+          v = ok ? fmaf(z[q], ex2f(-fmaf(c[q], ir2, y[q])), kRoundoff) : 0.f;
+        }
         x[s][q] = v;
         csum += v;
       }
       csum = seg_sum<TPC>(csum);
-      const float f = colok ? __fdividef(w[s], csum) : 0.f;  // (column sum > 0: ROUNDOFF)
+      const float f = (FULL || colok) ? __fdividef(w[s], csum) : 0.f;  // (column sum > 0)
+      const float eps2 = colok ? kRoundoff : 0.f;
 #pragma unroll
       for (int q = 0; q < RPT; ++q) {
-        const bool ok = colok && (FULL || t.k0 + q < m);
         x[s][q] *= f;
-        zp[s][q] = ok ? fmaf(x[s][q], ex2f(y[q]), kRoundoff) : 0.f;
+        if constexpr (FULL) {
+          zp[s][q] = fmaf(x[s][q], ex2f(y[q]), eps2);
+        } else {
+          const bool ok = colok && t.k0 + q < m;
+          zp[s][q] = ok ? fmaf(x[s][q], ex2f(y[q]), kRoundoff) : 0.f;
+        }
       }
     }
     {
@@ -1226,7 +1241,7 @@ cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaSt
   // persistent grid: as many clusters of a.cs CTAs as are resident at once
   static int grid[kMaxCluster + 1] = {0};
   constexpr int JC = GeoT<MP>::JC;
-  constexpr int CW = MODE == COST_EUCLID8 ? 8 : (MODE == COST_EUCLID4 ? 4 : 1);
+  constexpr int CW = MODE == COST_TABLE ? 1 : (MODE == COST_EUCLID8 ? 8 : 4);
   const size_t sm = smem + (size_t)4 * tma_tile_floats<MP>() * sizeof(float) +
                     2 * (size_t)GeoT<MP>::G * 16 + 2 * (size_t)JC * 4 * (1 + CW) + (size_t)2 * MP * 4 +
                     (plan_stages_costs(MP, MODE) ? (size_t)2 * tma_tile_floats<MP>() * 4 : 0) +
@@ -1308,6 +1323,9 @@ cudaError_t launch_plan_t(const PlanArgs &a, int nitems, size_t smem, cudaStream
 template <int MP>
 cudaError_t launch_plan_mp(int mode, bool check, const PlanArgs &a, int nitems, size_t smem,
                            cudaStream_t st) {
+  if (mode == COST_EUCLID3)
+    return check ? launch_plan_t<MP, COST_EUCLID3, true>(a, nitems, smem, st)
+                 : launch_plan_t<MP, COST_EUCLID3, false>(a, nitems, smem, st);
   if (mode == COST_EUCLID4)
     return check ? launch_plan_t<MP, COST_EUCLID4, true>(a, nitems, smem, st)
                  : launch_plan_t<MP, COST_EUCLID4, false>(a, nitems, smem, st);
@@ -1321,7 +1339,7 @@ cudaError_t launch_plan_mp(int mode, bool check, const PlanArgs &a, int nitems, 
 template <int MP>
 cudaError_t launch_rho_mp(int mode, const PlanArgs &a, int nitems, double *part, cudaStream_t st) {
   const dim3 grid(nitems * a.cs), block(GeoT<MP>::NT);
-  if (mode == COST_EUCLID4)
+  if (mode == COST_EUCLID4 || mode == COST_EUCLID3)  // (d = 3: the same costs, bit for bit)
     rho_partial_kernel<MP, COST_EUCLID4><<<grid, block, 0, st>>>(a, part);
   else if (mode == COST_EUCLID8)
     rho_partial_kernel<MP, COST_EUCLID8><<<grid, block, 0, st>>>(a, part);
@@ -1352,7 +1370,7 @@ cudaError_t launch_pack_columns_mp(const PlanArgs &a, int nitems, const long lon
 
 template <int MP>
 cudaError_t launch_obj_mp(int mode, const PlanArgs &a, int nitems, cudaStream_t st) {
-  if (mode == COST_EUCLID4)
+  if (mode == COST_EUCLID4 || mode == COST_EUCLID3)
     obj_kernel<MP, COST_EUCLID4><<<nitems * a.cs, GeoT<MP>::NT, 0, st>>>(a);
   else if (mode == COST_EUCLID8)
     obj_kernel<MP, COST_EUCLID8><<<nitems * a.cs, GeoT<MP>::NT, 0, st>>>(a);
