@@ -55,15 +55,32 @@ __global__ void __launch_bounds__(kRedThreads) cluster_partial_kernel(const Clus
   for (int i = 0; i < NK; ++i) acc[i] = 0.0;
   const bool weights = plane == a.dim + 1;
   const bool slotted = a.cl_plans == nullptr;  // batched form: already normalised, in slot order
-  for (int ii = pb + warp; ii < pe; ii += kRedWarps) {
-    const int p = slotted ? ii : a.cl_plans[ii];
-    if (weights && slotted) {
+  if (weights && slotted) {
+    // Each warp takes GP consecutive plans at a time: their FP32 row sums are
+    // added pairwise in FP32 (at most log2(GP) roundings of terms <= 1), the
+    // group total in FP64.  GB300's FP64 pipe is narrow; this keeps the long
+    // accumulation (up to 10^5-10^6 plans per cluster) in FP64 with GP times
+    // fewer FP64 operations.
+    constexpr int GP = NK <= 2 ? 16 : (NK == 4 ? 8 : 4);
+    for (int i0 = pb + warp * GP; i0 < pe; i0 += kRedWarps * GP) {
 #pragma unroll
       for (int i = 0; i < NK; ++i) {
         const int k = lane + 32 * i;
-        if (k < m) acc[i] += (double)a.rowsum32[(size_t)p * a.rstride + k];
+        float v[GP];
+#pragma unroll
+        for (int j = 0; j < GP; ++j)
+          v[j] = (i0 + j < pe && k < m) ? a.rowsum32[(size_t)(i0 + j) * a.rstride + k] : 0.f;
+#pragma unroll
+        for (int w = GP / 2; w >= 1; w >>= 1)
+#pragma unroll
+          for (int j = 0; j < w; ++j) v[j] += v[j + w];
+        acc[i] += (double)v[0];
       }
-    } else if (weights) {
+    }
+  }
+  for (int ii = pb + warp; ii < pe && !(weights && slotted); ii += kRedWarps) {
+    const int p = slotted ? ii : a.cl_plans[ii];
+    if (weights) {
       double v[NK], s = 0.0;
 #pragma unroll
       for (int i = 0; i < NK; ++i) {
