@@ -538,15 +538,21 @@ __global__ void __launch_bounds__(GeoT<MP>::NT) rho_partial_kernel(const PlanArg
   T t;
   t.init(a);
   t.load_costs(a);
-  double acc = 0.0;
+  // the thread's S x RPT costs added pairwise in FP32 (a few roundings), the
+  // thread totals in FP64 (GB300's FP64 pipe is narrow)
+  float v[S * RPT];
 #pragma unroll
   for (int s = 0; s < S; ++s) {
     float c[RPT];
     t.costs(s, c);
 #pragma unroll
-    for (int q = 0; q < RPT; ++q)
-      if (s < t.nvalid && t.k0 + q < a.m) acc += (double)c[q];
+    for (int q = 0; q < RPT; ++q) v[s * RPT + q] = (s < t.nvalid && t.k0 + q < a.m) ? c[q] : 0.f;
   }
+#pragma unroll
+  for (int w = S * RPT / 2; w >= 1; w >>= 1)
+#pragma unroll
+    for (int j = 0; j < w; ++j) v[j] += v[j + w];
+  const double acc = (double)v[0];
   __shared__ double res[3];
   block_sum3<GeoT<MP>::NT>(acc, 0.0, 0.0, res);
   if (threadIdx.x == 0) part[blockIdx.x] = res[0];
@@ -577,14 +583,19 @@ __global__ void __launch_bounds__(GeoT<MP>::NT) pack_convert_kernel(const PlanAr
     const size_t off = (t.colbase + s) * MP + t.k0;
     const long long rc = base + (long long)(jj0 + s) * str;
     float v[RPT];
-    if (dir == 0 || dir == 2) {
-      const double wj = (double)a.col_w[t.colbase + s];
+    if (dir == 2) {  // re-initialised plan Z = w (x) c_w, in FP32 (GB300's FP64 pipe is narrow)
+      const float wj = a.col_w[t.colbase + s];
 #pragma unroll
       for (int q = 0; q < RPT; ++q) {
         const int k = t.k0 + q;
-        double val = 0.0;
-        if (k < str) val = dir == 2 ? wj * cw64[(size_t)t.lab * str + k] : ref[rc + k];
-        v[q] = (float)val;
+        v[q] = k < str ? wj * a.cw32[(size_t)t.lab * MP + k] : 0.f;
+      }
+      st_rows(a.Z + off, v);
+    } else if (dir == 0) {
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        const int k = t.k0 + q;
+        v[q] = k < str ? (float)ref[rc + k] : 0.f;
       }
       st_rows(a.Z + off, v);
     } else {
