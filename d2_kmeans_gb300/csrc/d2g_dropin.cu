@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <mutex>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "d2g_internal.cuh"
@@ -46,6 +47,34 @@ struct DropinState {
 
 std::mutex g_mu;
 std::unordered_map<const var_sphBregman *, DropinState> g_states;
+// host work arrays allocated page-locked (cudaMallocHost), freed accordingly
+std::unordered_set<void *> g_pinned;
+
+// Z is copied back after every call: page-locked, the copy runs at the
+// host link's full rate.  Falls back to malloc where pinning is refused.
+void *alloc_pinned(size_t bytes) {
+  void *p = nullptr;
+  if (cudaMallocHost(&p, bytes) == cudaSuccess) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_pinned.insert(p);
+    return p;
+  }
+  cudaGetLastError();
+  return malloc(bytes);
+}
+
+void free_host(void *p) {
+  if (!p) return;
+  bool pinned = false;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    pinned = g_pinned.erase(p) > 0;
+  }
+  if (pinned)
+    cudaFreeHost(p);
+  else
+    free(p);
+}
 
 int err(int code, const char *msg) {
   d2g::set_error(msg);
@@ -59,7 +88,7 @@ extern "C" int d2_allocate_work_sphBregman(sph *ph, size_t size, var_sphBregman 
   if (!ph || !w || ph->str <= 0 || ph->col == 0 || size == 0) return err(D2G_E_INVAL, "bad work shape");
   const size_t nent = (size_t)ph->str * ph->col;
   w->X = (double *)malloc(nent * sizeof(double));
-  w->Z = (double *)malloc(nent * sizeof(double));
+  w->Z = (double *)alloc_pinned(nent * sizeof(double));
   w->Xc = (double *)malloc(ph->col * sizeof(double));
   w->Zr = (double *)malloc((size_t)ph->str * size * sizeof(double));
   w->Y = (double *)malloc(nent * sizeof(double));
@@ -78,7 +107,7 @@ extern "C" int d2_free_work_sphBregman(var_sphBregman *w) {
     }
   }
   free(w->X);
-  free(w->Z);
+  free_host(w->Z);
   free(w->Y);
   free(w->Xc);
   free(w->Zr);
