@@ -121,7 +121,6 @@ struct d2g_phase {
   std::vector<int> h_grp_plan;  // plan of each group
   DBuf<double> resid_part, rho_part;
   size_t smem_plan = 0, smem_plan_upd = 0;
-  int use_tma = 1;  // persistent TMA-pipelined kernel for single-CTA items (D2G_PLAN_KERNEL=v1 turns it off)
   // plans wider than one CTA: deferred row normalisation
   std::vector<int> h_wide_plans;  // packed ids
   Bucket units{1, 0, 0, 0};       // units of the deferred iterations
@@ -174,8 +173,8 @@ namespace d2g {
 // record: key exchange stage_costs ctas_per_sm cost_gemm; later lines win).
 static std::string tune_key(const d2g_phase *ph) {
   char b[256];
-  snprintf(b, sizeof b, "m%d.s%d.d%d.n%zu.c%zu.k%d.v%d.t%d", ph->metric, ph->str, ph->dim, ph->size,
-           ph->col, ph->K, ph->vocab_size, ph->use_tma);
+  snprintf(b, sizeof b, "m%d.s%d.d%d.n%zu.c%zu.k%d.v%d", ph->metric, ph->str, ph->dim, ph->size,
+           ph->col, ph->K, ph->vocab_size);
   return b;
 }
 static std::mutex g_tune_mu;
@@ -218,7 +217,7 @@ static void tune_cache_put(const std::string &key, const d2g_tuning &t) {
 
 // the run-time switches that follow from the phase's tuning
 static void apply_tuning(d2g_phase *ph) {
-  ph->defer = ph->path == 0 && ph->use_tma && ph->nwide > 0 && ph->units.nitems > 0 &&
+  ph->defer = ph->path == 0 && ph->nwide > 0 && ph->units.nitems > 0 &&
               ph->tune.exchange == 0;
   ph->stage_costs = ph->tune.stage_costs;
   ph->cost_gemm = ph->tune.cost_gemm;
@@ -428,7 +427,6 @@ static PlanArgs base_args(d2g_phase *ph) {
   a.ctas_per_sm = ph->tune.ctas_per_sm;
   a.m = ph->str;
   a.dim = ph->metric == D2_EUCLIDEAN_L2 ? ph->dim : 0;
-  a.use_tma = ph->use_tma;
   a.grp_rec = ph->grp_rec.p;
   a.plan_slot = ph->plan_slot.p;
   a.rowpart = ph->rowpart.p;
@@ -611,9 +609,7 @@ static int create_batched(d2g_phase *ph, const d2g_phase_desc *d) {
     ph->mode = COST_TABLE;
     ph->DS = 4;
   }
-  const char *pk = getenv("D2G_PLAN_KERNEL");
-  ph->use_tma = !(pk && std::string(pk) == "v1");
-  int rc = build_packing(ph, ph->use_tma != 0);
+  int rc = build_packing(ph, true);
   if (rc) return rc;
   const size_t nz = (size_t)ph->ncols_packed * ph->MP;
   D2G_CUDA(ph->Z.alloc(nz));
@@ -1441,9 +1437,9 @@ int d2g_phase_autotune(d2g_phase *ph, const d2g_badmm_opts *opt, const double *c
   // candidates: every combination of the choices that apply to this phase
   const d2g_tuning base = ph->tune;
   std::vector<int> ex = {base.exchange}, sc = {0}, cp = {0}, cg = {base.cost_gemm};
-  if (ph->use_tma && ph->nwide > 0 && ph->units.nitems > 0) ex = {0, 1};
-  if (ph->use_tma && ph->mode == COST_TABLE && ph->MP >= 16 && ph->MP <= 128) sc = {0, 1};
-  if (ph->use_tma && ph->MP < 256) cp = {0, 1};
+  if (ph->nwide > 0 && ph->units.nitems > 0) ex = {0, 1};
+  if (ph->mode == COST_TABLE && ph->MP >= 16 && ph->MP <= 128) sc = {0, 1};
+  if (ph->MP < 256) cp = {0, 1};
   if (emb) cg = {0, 1};
   std::vector<d2g_tuning> cand;
   for (int e : ex)

@@ -89,7 +89,6 @@ struct PlanArgs {
   double *resid_part;       // 4 doubles per CTA (obj, primres, dualres, -)
   Ctl *ctl;
   int m, dim, flags, cs, iter, resid_off;
-  int use_tma;              // single-CTA items: persistent TMA-pipelined kernel
   const int4 *grp_rec;      // per group {plan slot, plan first group, label, plan groups << 4 | valid}
   const int *plan_slot;     // plan -> slot: position in cluster-sorted order (row-sum outputs)
   float *rowpart;           // [slot][8][MP] per-slice row sums of Z' (deferred wide plans)

@@ -302,235 +302,6 @@ __device__ __forceinline__ void st_rows_sm(float *p, const float (&v)[N]) {
     ((float4 *)p)[q4] = make_float4(v[4 * q4], v[4 * q4 + 1], v[4 * q4 + 2], v[4 * q4 + 3]);
 }
 
-template <int MP, int MODE, bool CHECK>
-__global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2) plan_kernel(const PlanArgs a) {
-  using T = Tile<MP, MODE>;
-  constexpr int RPT = T::RPT, TPC = T::TPC, G = T::G, S = T::S;
-  extern __shared__ __align__(16) float smem[];
-  float *sm_rs = smem;              // [G][MP] per-group row partials of Z'
-  float *sm_tot = sm_rs + G * MP;   // [MP] CTA partial row sums (cluster exchange)
-
-  if (a.iter >= a.ctl->stop_iter) return;  // time budget hit in an earlier iteration
-  if (a.iter == 0 && a.resid_off == 0 && blockIdx.x == 0 && threadIdx.x == 0)
-    a.ctl->t_start_ns = global_ns();
-
-  T t;
-  t.init(a);
-  const int m = a.m;
-  const float inv_rho = a.ctl->inv_rho;
-  const float ir2 = a.ctl->inv_rho_l2;  // Y is kept scaled by log2(e): base-2 exponents
-  const bool update = a.flags & PF_UPDATE;
-
-  float z[S][RPT], y[S][RPT], x[S][RPT];
-  float zold[CHECK ? S : 1][RPT];
-  float w[S];
-#pragma unroll
-  for (int s = 0; s < S; ++s) {
-    const size_t off = (t.colbase + s) * MP + t.k0;
-    ld_rows(a.Z + off, z[s], s < t.nvalid);
-    ld_rows(a.Y + off, y[s], s < t.nvalid);
-    w[s] = s < t.nvalid ? __ldg(a.col_w + t.colbase + s) : 0.f;
-  }
-  t.load_costs(a);
-
-  // step 1: X = Z exp(-(C+Y)) + ROUNDOFF, column-normalised, times w_j
-#pragma unroll
-  for (int s = 0; s < S; ++s) {
-    float c[RPT];
-    t.costs(s, c);
-    float csum = 0.f;
-#pragma unroll
-    for (int q = 0; q < RPT; ++q) {
-      const bool ok = s < t.nvalid && t.k0 + q < m;
-      const float v = ok ? fmaf(z[s][q], ex2f(-fmaf(c[q], ir2, y[s][q])), kRoundoff) : 0.f;
-      x[s][q] = v;
-      csum += v;
-    }
-    csum = seg_sum<TPC>(csum);
-    const float f = s < t.nvalid ? w[s] / csum : 0.f;
-#pragma unroll
-    for (int q = 0; q < RPT; ++q) x[s][q] *= f;
-  }
-
-  // step 2 (first half): Z' = X exp(Y) + ROUNDOFF, row partials
-  float rp[RPT];
-#pragma unroll
-  for (int q = 0; q < RPT; ++q) rp[q] = 0.f;
-#pragma unroll
-  for (int s = 0; s < S; ++s)
-#pragma unroll
-    for (int q = 0; q < RPT; ++q) {
-      const bool ok = s < t.nvalid && t.k0 + q < m;
-      if constexpr (CHECK) zold[s][q] = z[s][q];
-      const float v = ok ? fmaf(x[s][q], ex2f(y[s][q]), kRoundoff) : 0.f;
-      z[s][q] = v;
-      rp[q] += v;
-    }
-  st_rows_sm(sm_rs + t.g * MP + t.k0, rp);
-
-  // step 5 inputs: per-group X moments sum_j X[k,j]*(s_j[0..dim), 1)
-  float *sm_mom = sm_tot + MP;             // [dim+1][G][MP]
-  float *sm_momx = sm_mom + (a.dim + 1) * G * MP;  // [dim+1][MP] cluster exchange
-  if constexpr (T::EUC) {
-    if (update) {
-      for (int d = 0; d <= a.dim; ++d) {
-        float mv[RPT];
-#pragma unroll
-        for (int q = 0; q < RPT; ++q) {
-          float acc = 0.f;
-#pragma unroll
-          for (int s = 0; s < S; ++s) {
-            float sv = 1.f;  // plane dim: the X row sum (denominator)
-            if (d < a.dim) {
-#pragma unroll
-              for (int tt = 0; tt < T::DS; ++tt)
-                if (tt == d) sv = t.sp[s][tt];
-            }
-            acc = fmaf(x[s][q], sv, acc);
-          }
-          mv[q] = acc;
-        }
-        st_rows_sm(sm_mom + (d * G + t.g) * MP + t.k0, mv);
-      }
-    }
-  }
-  __syncthreads();
-
-  // plan totals over this CTA's groups of the plan
-  int lo = 0, hi = 0;
-  if (t.active) {
-    lo = max(t.pl_g0, t.cta_g0) - t.cta_g0;
-    hi = min(t.pl_g0 + t.pl_ng, t.cta_g0 + t.cta_ng) - t.cta_g0;
-  }
-  float tot[RPT];
-#pragma unroll
-  for (int q = 0; q < RPT; ++q) tot[q] = 0.f;
-  for (int j = lo; j < hi; ++j) {
-    float v[RPT];
-#pragma unroll
-    for (int q4 = 0; q4 < RPT / 4; ++q4) {
-      const float4 u = *((const float4 *)(sm_rs + j * MP + t.k0) + q4);
-      v[4 * q4] = u.x;
-      v[4 * q4 + 1] = u.y;
-      v[4 * q4 + 2] = u.z;
-      v[4 * q4 + 3] = u.w;
-    }
-#pragma unroll
-    for (int q = 0; q < RPT; ++q) tot[q] += v[q];
-  }
-  // the thread set that owns the plan's output rows: first group of the plan
-  const bool writer = t.active && (t.cta_g0 + t.g) == t.pl_g0;
-  const bool upd_euc = T::EUC && update;
-
-  if (a.cs > 1) {
-    // one plan spans the cluster: exchange CTA partials through DSMEM
-    cg::cluster_group cl = cg::this_cluster();
-    if (t.g == 0) {
-      st_rows_sm(sm_tot + t.k0, tot);
-      if (upd_euc) {
-        for (int d = 0; d <= a.dim; ++d) {
-          float mv[RPT];
-#pragma unroll
-          for (int q = 0; q < RPT; ++q) mv[q] = 0.f;
-          for (int j = lo; j < hi; ++j)
-#pragma unroll
-            for (int q = 0; q < RPT; ++q) mv[q] += sm_mom[(d * G + j) * MP + t.k0 + q];
-          st_rows_sm(sm_momx + d * MP + t.k0, mv);
-        }
-      }
-    }
-    cl.sync();
-    float sum[RPT];
-#pragma unroll
-    for (int q = 0; q < RPT; ++q) sum[q] = 0.f;
-    for (int rk = 0; rk < a.cs; ++rk) {
-      const float *rem = cl.map_shared_rank(sm_tot, rk);
-#pragma unroll
-      for (int q = 0; q < RPT; ++q) sum[q] += rem[t.k0 + q];
-    }
-#pragma unroll
-    for (int q = 0; q < RPT; ++q) tot[q] = sum[q];
-    if (upd_euc && writer) {
-      float *xo = a.xmom_out + (size_t)a.plan_slot[t.p] * (a.dim + 1) * MP;
-      for (int d = 0; d <= a.dim; ++d) {
-        float mv[RPT];
-#pragma unroll
-        for (int q = 0; q < RPT; ++q) mv[q] = 0.f;
-        for (int rk = 0; rk < a.cs; ++rk) {
-          const float *rem = cl.map_shared_rank(sm_momx, rk);
-#pragma unroll
-          for (int q = 0; q < RPT; ++q) mv[q] += rem[d * MP + t.k0 + q];
-        }
-        st_rows(xo + d * MP + t.k0, mv);
-      }
-    }
-    cl.sync();  // no CTA leaves while a peer still reads its shared memory
-  } else if (upd_euc && writer) {
-    float *xo = a.xmom_out + (size_t)a.plan_slot[t.p] * (a.dim + 1) * MP;
-    for (int d = 0; d <= a.dim; ++d) {
-      float mv[RPT];
-#pragma unroll
-      for (int q = 0; q < RPT; ++q) mv[q] = 0.f;
-      for (int j = lo; j < hi; ++j)
-#pragma unroll
-        for (int q = 0; q < RPT; ++q) mv[q] += sm_mom[(d * G + j) * MP + t.k0 + q];
-      st_rows(xo + d * MP + t.k0, mv);
-    }
-  }
-  {  // step 4's per-instance normalisation of Zr (:180), by slot
-    float rs = 0.f;
-#pragma unroll
-    for (int q = 0; q < RPT; ++q) rs += t.k0 + q < m ? tot[q] : 0.f;
-    rs = seg_sum<TPC>(rs);
-    if (writer) {
-      float zr[RPT];
-      const float inv = 1.f / rs;
-#pragma unroll
-      for (int q = 0; q < RPT; ++q) zr[q] = tot[q] * inv;
-      st_rows(a.rowsum_out + (size_t)a.plan_slot[t.p] * MP + t.k0, zr);
-    }
-  }
-
-  // step 2 (second half) and step 3
-  float sc[RPT];
-#pragma unroll
-  for (int q = 0; q < RPT; ++q) {
-    const bool ok = t.active && t.k0 + q < m;
-    sc[q] = ok ? __ldg(a.cw32 + (size_t)t.lab * MP + t.k0 + q) / tot[q] : 0.f;
-  }
-  float s_obj = 0.f, s_pr = 0.f, s_dr = 0.f;
-  const bool write_x = a.flags & PF_WRITE_X;
-#pragma unroll
-  for (int s = 0; s < S; ++s) {
-    if (s < t.nvalid) {
-      float zn[RPT], yn[RPT];
-#pragma unroll
-      for (int q = 0; q < RPT; ++q) {
-        zn[q] = z[s][q] * sc[q];
-        yn[q] = fmaf(kLog2e, x[s][q] - zn[q], y[s][q]);
-      }
-      if constexpr (CHECK) {
-        float c[RPT];
-        t.costs(s, c);
-#pragma unroll
-        for (int q = 0; q < RPT; ++q) {
-          s_obj = fmaf(c[q] * inv_rho, x[s][q], s_obj);
-          s_pr += fabsf(x[s][q] - zn[q]);
-          s_dr += fabsf(zn[q] - zold[s][q]);
-        }
-      }
-      const size_t off = (t.colbase + s) * MP + t.k0;
-      st_rows(a.Z + off, zn);
-      st_rows(a.Y + off, yn);
-      if (write_x) st_rows(a.X_out + off, x[s]);
-    }
-  }
-  if constexpr (CHECK) {
-    block_sum3<GeoT<MP>::NT>(s_obj, s_pr, s_dr, a.resid_part + (size_t)(a.resid_off + blockIdx.x) * 4);
-  }
-}
-
-// Sum of the initial ground costs (for rho), FP32 costs accumulated in FP64.
 template <int MP, int MODE>
 __global__ void __launch_bounds__(GeoT<MP>::NT) rho_partial_kernel(const PlanArgs a, double *part) {
   using T = Tile<MP, MODE>;
@@ -664,16 +435,19 @@ __global__ void __launch_bounds__(GeoT<MP>::NT) obj_kernel(const PlanArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// Persistent, TMA-pipelined form of the plan update for single-CTA items.
+// Persistent, TMA-pipelined form of the plan update (the production kernel).
 //
-// Each CTA walks items blockIdx.x, +gridDim.x, ...  The item's Z and Y tiles
-// (contiguous in the packed layout) arrive in shared memory by bulk async copy
+// Each CTA (or each cluster, for plans wider than one CTA exchanged
+// synchronously) walks its units blockIdx.x, +gridDim.x, ...  A unit's Z and
+// Y tiles (contiguous in the packed layout), group records, weights and
+// supports or table rows arrive in shared memory by bulk async copy
 // (cp.async.bulk + mbarrier transaction count) into one of two stages; the
-// copy of the next item is issued as soon as the current one has landed, so
-// HBM reads overlap the exp / normalisation work of the current item.  Results
-// go back with streaming 128-bit stores from registers.  Z and Y are read from
-// shared memory twice (step 1 and the final step 2/3), which keeps only X and
-// Z' in registers.
+// copy of the next unit is issued as soon as the current one has landed, so
+// HBM reads overlap the exp / normalisation work of the current unit.  Table
+// costs of 16 <= MP <= 128 can be staged too (cp.async of the next unit's
+// rows).  Results go back with streaming 128-bit stores from registers.  Z
+// and Y are read from shared memory twice (step 1 and the final step 2/3),
+// which keeps only X and Z' in registers.
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -1308,27 +1082,12 @@ cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaSt
 
 template <int MP, int MODE, bool CHECK>
 cudaError_t launch_plan_t(const PlanArgs &a, int nitems, size_t smem, cudaStream_t st) {
-  if (a.use_tma) {
-    if (a.wide) {
-      if (a.m == MP) return launch_plan_tma_t<MP, MODE, CHECK, true, true>(a, nitems, smem, st);
-      return launch_plan_tma_t<MP, MODE, CHECK, false, true>(a, nitems, smem, st);
-    }
-    if (a.m == MP) return launch_plan_tma_t<MP, MODE, CHECK, true, false>(a, nitems, smem, st);
-    return launch_plan_tma_t<MP, MODE, CHECK, false, false>(a, nitems, smem, st);
+  if (a.wide) {
+    if (a.m == MP) return launch_plan_tma_t<MP, MODE, CHECK, true, true>(a, nitems, smem, st);
+    return launch_plan_tma_t<MP, MODE, CHECK, false, true>(a, nitems, smem, st);
   }
-  // the dynamic shared-memory limit is raised once per kernel, before any
-  // stream capture (launch_plan is first called with nitems == 0 for that)
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(plan_kernel<MP, MODE, CHECK>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
-  if (nitems <= 0) return cudaSuccess;
-  cudaLaunchAttribute attr[1];
-  cudaLaunchConfig_t cfg = plan_cfg(nitems * a.cs, GeoT<MP>::NT, smem, st, attr, a.cs);
-  return cudaLaunchKernelEx(&cfg, plan_kernel<MP, MODE, CHECK>, a);
+  if (a.m == MP) return launch_plan_tma_t<MP, MODE, CHECK, true, false>(a, nitems, smem, st);
+  return launch_plan_tma_t<MP, MODE, CHECK, false, false>(a, nitems, smem, st);
 }
 
 template <int MP>
