@@ -288,8 +288,9 @@ class DropIn:
     def Y(self) -> np.ndarray:
         return np.ctypeslib.as_array(self.bw.Y, shape=(self.m * self.col,)).copy()
 
-    def call(self, opts: dict, label_switch=None, labels=None) -> int:
-        """One d2_centroid_sphBregman call with the given BADMM options."""
+    def call(self, opts: dict, label_switch=None, labels=None, random_init=False) -> int:
+        """One d2_centroid_sphBregman call with the given BADMM options;
+        ``random_init`` passes c0 = NULL (centroid_Bregman.c:95-98)."""
         if label_switch is not None:
             self.ls[:] = np.asarray(label_switch, np.int8)
         if labels is not None:
@@ -301,7 +302,7 @@ class DropIn:
         C.c_double.in_dll(self.lib, "time_budget").value = float(opts.get("time_budget", 1e300))
         c = self.c
         return self.lib.d2_centroid_sphBregman(C.byref(self.mph), C.byref(self.vw), 0,
-                                               C.byref(c), C.byref(c))
+                                               None if random_init else C.byref(c), C.byref(c))
 
     def close(self):
         if getattr(self, "bw", None) is not None:

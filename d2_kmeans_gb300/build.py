@@ -62,7 +62,7 @@ def build(verbose: bool = False, ptxas_info: bool = False, jobs: int | None = No
     if failed:
         raise RuntimeError(f"nvcc failed for {failed}")
     if cmds or _stale(LIB, objs):
-        link = [nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        link = [nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-ldl"]
         r = subprocess.run(link, capture_output=True, text=True)
         if r.returncode:
             raise RuntimeError("link failed:\n" + r.stdout + r.stderr)

@@ -8,6 +8,7 @@
 // the phase's shape and support sizes stay the same; weights, supports,
 // labels and the warm-start plans are re-sent on every call, so a caller
 // that edits its host arrays in place sees the same results as the reference.
+#include <dlfcn.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -118,9 +119,20 @@ extern "C" int d2_free_work_sphBregman(var_sphBregman *w) {
 extern "C" int d2_centroid_sphBregman(mph *p_data, var_mph *var_work, int idx_ph, sph *c0, sph *c) {
   if (!p_data || !var_work || !c || idx_ph < 0 || idx_ph >= p_data->s_ph || !var_work->l_var_sphBregman)
     return err(D2G_E_INVAL, "bad arguments");
-  if (!c0)  // :95-98 initialises at random; callers of the drop-in pass c0
-    return err(D2G_E_UNSUPPORTED, "c0 == NULL (random initialisation) is not part of the drop-in");
-  *c = *c0;  // :100 warm start
+  if (!c0) {
+    // :95-98 initialises c at random with the reference's own d2_centroid_rands
+    // (src/d2/centroid_rand.c:161-295), which stays in a program that links
+    // this library in place of centroid_Bregman.c.  One process: there is no
+    // broadcast_centroids step.
+    typedef int (*rands_fn)(mph *, int, sph *);
+    const rands_fn rands = (rands_fn)dlsym(RTLD_DEFAULT, "d2_centroid_rands");
+    if (!rands)
+      return err(D2G_E_UNSUPPORTED, "c0 == NULL needs d2_centroid_rands (src/d2/centroid_rand.c) linked");
+    if (c->str != p_data->ph[idx_ph].str) return err(D2G_E_INVAL, "c->str differs from the phase's str");
+    rands(p_data, idx_ph, c);
+  } else {
+    *c = *c0;  // :100 warm start
+  }
   sph *dp = p_data->ph + idx_ph;
   var_sphBregman *bw = var_work->l_var_sphBregman + idx_ph;
   const BADMM_options *o = p_badmm_options;

@@ -127,7 +127,10 @@ int d2_free_work_sphBregman(var_sphBregman *var_phwork);
  * for the next call's warm start.  Honours p_badmm_options (maxIters+1
  * iterations, rhoCoeff, updatePerLoops) and the global time_budget.
  * Metric types: D2_EUCLIDEAN_L2, D2_WORD_EMBED, D2_HISTOGRAM,
- * D2_SPARSE_HISTOGRAM; D2_N_GRAM returns D2G_E_UNSUPPORTED.  The host X, Y
+ * D2_SPARSE_HISTOGRAM; D2_N_GRAM returns D2G_E_UNSUPPORTED.  c0 == NULL
+ * (:95-98) initialises c with d2_centroid_rands when the program links it
+ * (src/d2/centroid_rand.c:161-295, found by dlsym), else returns
+ * D2G_E_UNSUPPORTED.  The host X, Y
  * and C buffers are scratch for the reference's callers and are only written
  * back when d2g_config.sync_scratch is set. */
 int d2_centroid_sphBregman(mph *p_data, var_mph *var_work, int idx_ph, sph *c0, sph *c);

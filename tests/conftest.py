@@ -57,3 +57,54 @@ def load_golden(name):
 def digest(zv):
     from golden.make_golden import digest as d
     return d(zv)
+
+
+# A stand-in for the reference's d2_centroid_rands (src/d2/centroid_rand.c:161-295)
+# with a fixed, easily restated choice: the first num_of_labels instances whose
+# support size equals the centroid's, copied in order.  The drop-in finds it by
+# dlsym once it is loaded into the global scope.
+RANDS_STUB = r"""
+#include "d2g.h"
+int d2_centroid_rands(mph *p, int idx, sph *c) {
+  sph *ph = p->ph + idx;
+  int K = p->num_of_labels, m = c->str, d = ph->dim, j = 0;
+  for (size_t i = 0; i < p->size && j < K; ++i) {
+    if (ph->p_str[i] != m) continue;
+    size_t o = ph->p_str_cum[i];
+    for (int k = 0; k < m; ++k) {
+      c->p_w[j * m + k] = ph->p_w[o + k];
+      for (int t = 0; t < d; ++t) c->p_supp[(j * m + k) * d + t] = ph->p_supp[(o + k) * d + t];
+    }
+    ++j;
+  }
+  return 0;
+}
+"""
+
+
+def rands_stub_init(ph, k, m):
+    """What RANDS_STUB writes into c (numpy)."""
+    p_str = np.asarray(ph["p_str"])
+    cum = np.concatenate([[0], np.cumsum(p_str)])
+    d = int(ph["dim"])
+    sel = np.nonzero(p_str == m)[0][:k]
+    assert sel.size == k
+    w = np.concatenate([ph["p_w"][cum[i]:cum[i] + m] for i in sel])
+    s = np.concatenate([np.asarray(ph["p_supp"]).reshape(-1, d)[cum[i]:cum[i] + m] for i in sel])
+    return {"c_w": w, "c_supp": s.reshape(-1)}
+
+
+@pytest.fixture(scope="session")
+def rands_stub(tmp_path_factory):
+    """RANDS_STUB compiled with gcc and loaded with RTLD_GLOBAL."""
+    import ctypes
+    import shutil
+    import subprocess
+    if not shutil.which("gcc"):
+        pytest.skip("gcc is not present")
+    d = tmp_path_factory.mktemp("rands")
+    src, so = d / "rands.c", d / "librands.so"
+    src.write_text(RANDS_STUB)
+    subprocess.run(["gcc", "-O2", "-shared", "-fPIC", "-I", os.path.join(ROOT, "include"), "-o", str(so),
+                    str(src)], check=True)
+    return ctypes.CDLL(str(so), mode=ctypes.RTLD_GLOBAL)

@@ -7,6 +7,7 @@ import os
 import re
 import subprocess
 
+import numpy as np
 import pytest
 
 from d2_kmeans_gb300 import _lib as L
@@ -127,3 +128,39 @@ def test_python_struct_mirror_sizes():
     assert C.sizeof(L.sph) == C.sizeof(C.c_void_p) * 11 + 16 + 8  # 104 on LP64
     assert C.sizeof(L.mph) == 48
     assert C.sizeof(L.var_sphBregman) == 40
+
+
+def _small_dropin():
+    from d2_kmeans_gb300 import badmm, synth
+    ph, c = synth.euclidean_phase(60, 3, 8, 3, (4, 12), False, 5, 1.0, seed=5)
+    return ph, badmm.DropIn(ph, c)
+
+
+def test_random_init_without_rands_is_unsupported(lib):
+    """c0 == NULL with no d2_centroid_rands in the program: D2G_E_UNSUPPORTED,
+    before any device work."""
+    if hasattr(C.CDLL(None), "d2_centroid_rands"):
+        pytest.skip("a d2_centroid_rands is already loaded into this process")
+    _, d = _small_dropin()
+    c_w = d.c_w.copy()
+    assert d.call({}, random_init=True) == L.D2G_E_UNSUPPORTED
+    assert np.array_equal(d.c_w, c_w)
+    d.close()
+
+
+def test_random_init_calls_the_programs_rands(lib, rands_stub):
+    """With d2_centroid_rands loaded, c0 == NULL fills c through it first
+    (centroid_Bregman.c:95-98).  Without a GPU the update itself then fails
+    with a device error, leaving the initialisation in c."""
+    import torch
+    from conftest import rands_stub_init
+    if torch.cuda.is_available():
+        pytest.skip("covered with the update by the GPU tests")
+    ph, d = _small_dropin()
+    d.c_w[:] = -1.0
+    d.c_supp[:] = -1.0
+    rc = d.call({}, random_init=True)
+    assert rc not in (0, L.D2G_E_UNSUPPORTED, L.D2G_E_INVAL)
+    exp = rands_stub_init(ph, 3, 8)
+    assert np.array_equal(d.c_w, exp["c_w"]) and np.array_equal(d.c_supp, exp["c_supp"])
+    d.close()

@@ -384,3 +384,19 @@ def test_read_file_then_update(d2g, oracle_mod, tmp_path):
     P = d2g.Phase(rd, 0)
     assert_close(P.run(c, opts), ref, 5, 16)
     P.close()
+
+
+def test_dropin_random_init_uses_the_programs_rands(d2g, rands_stub):
+    """c0 == NULL initialises c with the program's d2_centroid_rands, then runs
+    the same update as a call whose c0 holds that initialisation."""
+    from conftest import rands_stub_init
+    ph, c = synth.euclidean_phase(400, 4, 8, 3, (4, 12), False, 6, 1.0, seed=91)
+    opts = dict(maxIters=40, rhoCoeff=2.0, updatePerLoops=10)
+    a = d2g.DropIn(ph, c)
+    assert a.call(opts, random_init=True) == 0
+    b = d2g.DropIn(ph, rands_stub_init(ph, 4, 8))
+    assert b.call(opts) == 0
+    assert np.array_equal(a.c_w, b.c_w) and np.array_equal(a.c_supp, b.c_supp)
+    assert np.array_equal(a.Z(), b.Z())
+    a.close()
+    b.close()
