@@ -432,7 +432,7 @@ def main():
                 traffic = json.load(f).get("traffic_bytes_per_launch")
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
-                "kernel": "plan_kernel_tma<32, EUCLID4>",
+                "kernel": "plan_kernel_tma<32, EUCLID3>",
                 "algo_bytes_per_launch": ps["plan_bytes"], "ms_per_launch": ps["plan_ms_avg"]}
     trace_b = r["trace"]
     cw_b = r["c_w"].copy()
