@@ -91,6 +91,11 @@ class d2g_tuning(C.Structure):
                 ("cost_gemm", C.c_int)]
 
 
+class d2g_dists(C.Structure):
+    _fields_ = [("size", C.c_size_t), ("str", C.c_int), ("p_str", C.c_void_p), ("p_w", C.c_void_p),
+                ("p_supp", C.c_void_p), ("p_supp_sym", C.c_void_p)]
+
+
 class d2g_server_desc(C.Structure):
     _fields_ = [("num_of_labels", C.c_int), ("str", C.c_int), ("dim", C.c_int),
                 ("c_w", C.c_void_p), ("c_supp", C.c_void_p), ("iters", C.c_int),
@@ -127,6 +132,8 @@ SIGNATURES = {
     "d2g_read": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(mph)]),
     "d2g_mph_alloc": (C.c_int, [C.c_int, C.c_size_t, ip, ip, ip, C.POINTER(C.POINTER(mph))]),
     "d2g_mph_free": (C.c_int, [C.POINTER(mph)]),
+    "d2g_emd_pairs": (C.c_int, [C.c_int, C.c_int, C.POINTER(d2g_dists), C.POINTER(d2g_dists),
+                                C.c_void_p, C.c_int, C.c_size_t] + [C.c_void_p] * 4),
     "d2g_phase_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(d2g_tuning)]),
     "d2g_phase_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(d2g_tuning)]),
     "d2g_phase_autotune": (C.c_int, [C.c_void_p, C.POINTER(d2g_badmm_opts), C.c_void_p, C.c_void_p,

@@ -240,6 +240,39 @@ int distmat_fp64(int dim, int str, size_t size, const int *p_str, int metric, co
 void set_error(const std::string &msg);
 int cuda_fail(cudaError_t e, const char *what);
 
+// exact transport (emd_kernel.cu): one warp per (row object, column object) pair
+enum EmdMode { EMD_EUCLID = 0, EMD_TABLE = 1 };
+struct EmdArgs {
+  int mode, dim;
+  // rows: weights, first support and support count per object (cum/str may
+  // be null: every object has rfix supports), FP64 supports or table keys
+  const double *rw;
+  const size_t *rcum;
+  const int *rstr;
+  int rfix;
+  const double *rsupp;
+  const int *rsym;
+  // columns, the same
+  const double *cw;
+  const size_t *ccum;
+  const int *cstr;
+  int cfix;
+  const double *csupp;
+  const int *csym;
+  // table costs T[key_row * V + key_col] (EMD_TABLE)
+  const float *T32;
+  const double *T64;
+  int V;
+  const int *prow, *pcol;  // the pairs
+  long long npairs;
+  double *out;             // exact cost per pair
+  int *piv;                // pivots per pair; -1: no optimum within max_piv
+  int nmax;                // >= n + m of every pair, multiple of 32
+  int max_piv;
+};
+size_t emd_slice(int nmax, int mode, int dim);
+cudaError_t launch_emd(const EmdArgs &a, cudaStream_t st);
+
 }  // namespace d2g
 
 #define D2G_CUDA(call)                                     \

@@ -274,6 +274,33 @@ int d2g_mph_alloc(int s_ph, size_t size, const int *avg_strides, const int *dims
                   const int *types, mph **out);
 int d2g_mph_free(mph *p_data);
 
+/* ------------------------------------------- exact transport (assignment)
+ * The assignment step's distances: the exact optimal transport cost of
+ * d2_match_by_distmat (src/d2/solver_mosek.cc:61-226, a MOSEK network
+ * simplex in the reference), computed on the GPU by a transportation simplex
+ * (one warp per pair, FP32 pricing, FP64 optimality check and cost). */
+typedef struct {
+  size_t size;           /* objects */
+  int str;               /* support count of every object when p_str is NULL */
+  const int *p_str;      /* [size] support counts, or NULL */
+  const double *p_w;     /* weights, object after object (each sums to 1) */
+  const double *p_supp;  /* [.. * dim] Euclidean supports (D2_EUCLIDEAN_L2) */
+  const int *p_supp_sym; /* bin ids (D2_SPARSE_HISTOGRAM); NULL: bin = support index */
+} d2g_dists;
+
+/* Exact transport cost of each pair (rows object pair_row[p], cols object
+ * pair_col[p]) for metric D2_EUCLIDEAN_L2 (dim 1..7, squared Euclidean
+ * ground cost in the difference form of _dpdist2, blas_like64.c:199-208),
+ * D2_HISTOGRAM or D2_SPARSE_HISTOGRAM (ground cost dist_mat, vocab_size^2,
+ * row-major by row bin).  Row sums are fixed to the row weights, column sums
+ * to the column weights except the last column's, as in the reference's
+ * program (solver_mosek.cc:64, :134-140).  cost[npairs]; pivots[npairs]
+ * (optional): simplex pivots per pair.  D2G_E_NUMERIC if a pair did not
+ * reach an optimal basis within 64 * (n + m rounded to 32) + 1024 pivots. */
+int d2g_emd_pairs(int metric_type, int dim, const d2g_dists *rows, const d2g_dists *cols,
+                  const double *dist_mat, int vocab_size, size_t npairs, const int *pair_row,
+                  const int *pair_col, double *cost, int *pivots);
+
 /* ------------------------------------------------------------- autotuning
  * Launch-shape choices of the batched form.  All choices compute the same
  * B-ADMM iteration; they differ in speed (and, for exchange, in the rounding

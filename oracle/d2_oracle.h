@@ -99,6 +99,13 @@ int d2o_serve_query(int dim, int str, int k, const double *c_w, const double *c_
 int d2o_read(const char *filename, const char *meta_filename, int s_ph, size_t size,
              const int *avg_strides, const int *dims, const int *types, void **out_mph);
 int d2o_mph_free(void *p_mph);
+
+/* Exact transport cost between a row distribution wX[n] and a column
+ * distribution wY[m] under C (column-major, C[i + j*n]), the linear program
+ * of d2_match_by_distmat (src/d2/solver_mosek.cc:61-226) with the last column
+ * constraint left free.  Successive shortest paths in FP64 (emd_oracle.c).
+ * x_out (optional): the n*m plan, column-major. */
+double d2o_emd(int n, int m, const double *C, const double *wX, const double *wY, double *x_out);
 int d2r_read(const char *filename, const char *meta_filename, int s_ph, size_t size,
              const int *avg_strides, const int *dims, const int *types, void **out_mph);
 int d2r_mph_free(void *p_mph);

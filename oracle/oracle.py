@@ -201,3 +201,21 @@ def read(kind: str, filename: str, size: int, dims, types, avg_strides=None, met
         if out.value:
             free(out)
     return rc, arrays
+
+
+def emd(C_nm, wX, wY, want_plan=False):
+    """Exact transport cost (d2o_emd) between wX (rows) and wY (columns) under
+    the n x m cost matrix C_nm (row i, column j); the last column's constraint
+    is left free, as in the reference's d2_match_by_distmat."""
+    import numpy as np
+    lib = _lib("port")
+    lib.d2o_emd.restype = C.c_double
+    lib.d2o_emd.argtypes = [C.c_int, C.c_int] + [C.c_void_p] * 4
+    Cc = np.asfortranarray(C_nm, dtype=np.float64)  # column-major, C[i + j*n]
+    n, m = Cc.shape
+    wX = np.ascontiguousarray(wX, np.float64)
+    wY = np.ascontiguousarray(wY, np.float64)
+    x = np.zeros((n, m), order="F") if want_plan else None
+    v = lib.d2o_emd(n, m, Cc.ctypes.data, wX.ctypes.data, wY.ctypes.data,
+                    x.ctypes.data if want_plan else None)
+    return (v, x) if want_plan else v
