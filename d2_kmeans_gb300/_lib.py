@@ -134,6 +134,20 @@ SIGNATURES = {
     "d2g_mph_free": (C.c_int, [C.POINTER(mph)]),
     "d2g_emd_pairs": (C.c_int, [C.c_int, C.c_int, C.POINTER(d2g_dists), C.POINTER(d2g_dists),
                                 C.c_void_p, C.c_int, C.c_size_t] + [C.c_void_p] * 4),
+    "d2g_compute_distances": (C.c_int, [C.POINTER(mph), C.POINTER(mph), C.c_int, C.c_size_t,
+                                        C.c_void_p, C.c_void_p, C.c_void_p]),
+    "d2g_labeling": (C.c_int, [C.POINTER(mph), C.POINTER(mph), C.POINTER(var_mph), C.c_int,
+                               C.POINTER(C.c_size_t), C.POINTER(C.c_double)]),
+    "d2g_labeling_prep": (C.c_int, [C.POINTER(mph), C.POINTER(mph), C.POINTER(var_mph), C.c_int,
+                                    C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+    "d2g_labeling_post": (C.c_int, [C.POINTER(mph), C.POINTER(mph), C.POINTER(mph),
+                                    C.POINTER(var_mph), C.c_int]),
+    "d2_compute_distance": (C.c_double, [C.POINTER(mph), C.c_size_t, C.POINTER(mph), C.c_size_t,
+                                         C.c_int, C.POINTER(var_mph), C.c_size_t]),
+    "d2_labeling": (C.c_size_t, [C.POINTER(mph), C.POINTER(mph), C.POINTER(var_mph), C.c_int]),
+    "d2_labeling_prep": (C.c_size_t, [C.POINTER(mph), C.POINTER(mph), C.POINTER(var_mph), C.c_int]),
+    "d2_labeling_post": (C.c_size_t, [C.POINTER(mph), C.POINTER(mph), C.POINTER(mph),
+                                      C.POINTER(var_mph), C.c_int]),
     "d2g_phase_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(d2g_tuning)]),
     "d2g_phase_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(d2g_tuning)]),
     "d2g_phase_autotune": (C.c_int, [C.c_void_p, C.POINTER(d2g_badmm_opts), C.c_void_p, C.c_void_p,
@@ -146,7 +160,8 @@ SIGNATURES = {
     "d2g_server_result": (C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(C.c_int), C.c_void_p,
                                     C.POINTER(C.c_double)]),
 }
-DATA_SYMBOLS = ("badmm_clu_options", "badmm_cen_options", "p_badmm_options", "time_budget")
+DATA_SYMBOLS = ("badmm_clu_options", "badmm_cen_options", "p_badmm_options", "time_budget",
+                "d2_alg_type")
 
 _lib = None
 

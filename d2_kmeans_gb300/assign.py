@@ -51,3 +51,128 @@ def emd_pairs(metric: int, rows: dict, cols: dict, pair_row, pair_col, dim: int 
                               None if dm is None else dm.ctypes.data, V, npairs, pr.ctypes.data,
                               pc.ctypes.data, cost.ctypes.data, piv.ctypes.data), "d2g_emd_pairs")
     return (cost, piv) if with_pivots else cost
+
+
+# ---------------------------------------------------------------------------
+# the reference's structures for the assignment step (include/d2g.h, the
+# layout of include/d2/clustering.h)
+
+class Mph:
+    """An mph (instances or centroids) built from per-phase dicts: ``metric``,
+    ``dim``, ``str``, ``p_w`` and ``p_str`` (or every object ``str``
+    supports), plus ``p_supp`` / ``p_supp_sym`` / ``dist_mat`` +
+    ``vocab_size`` as the metric needs."""
+
+    def __init__(self, phases, size: int, label=None, num_of_labels: int = 0):
+        self.keep = []
+        self.size = int(size)
+        sphs = (L.sph * len(phases))()
+        for n, ph in enumerate(phases):
+            s = sphs[n]
+            p_str = np.ascontiguousarray(ph["p_str"] if ph.get("p_str") is not None
+                                         else np.full(self.size, ph["str"]), np.int32)
+            cum = np.zeros(self.size, np.uint64)
+            cum[1:] = np.cumsum(p_str[:-1])
+            s.dim = int(ph.get("dim", 0))
+            s.str = int(ph["str"])
+            s.max_str = int(p_str.max()) if p_str.size else 0
+            s.col = int(p_str.sum())
+            s.max_col = s.col
+            s.p_str = self._ptr(p_str, C.c_int)
+            s.p_str_cum = self._ptr(cum, C.c_size_t)
+            s.p_w = self._ptr(np.ascontiguousarray(ph["p_w"], np.float64), C.c_double)
+            s.metric_type = int(ph["metric"])
+            if ph.get("p_supp") is not None:
+                s.p_supp = self._ptr(np.ascontiguousarray(ph["p_supp"], np.float64), C.c_double)
+            if ph.get("p_supp_sym") is not None:
+                s.p_supp_sym = self._ptr(np.ascontiguousarray(ph["p_supp_sym"], np.int32), C.c_int)
+            if ph.get("dist_mat") is not None:
+                s.dist_mat = self._ptr(np.ascontiguousarray(ph["dist_mat"], np.float64), C.c_double)
+            s.vocab_size = int(ph.get("vocab_size", 0))
+        self.sphs = sphs
+        self.label = np.ascontiguousarray(label if label is not None else np.full(self.size, -1),
+                                          np.int32)
+        m = L.mph()
+        m.s_ph = len(phases)
+        m.size = self.size
+        m.global_size = self.size
+        m.label = self.label.ctypes.data_as(C.POINTER(C.c_int))
+        m.num_of_labels = int(num_of_labels)
+        m.ph = C.cast(sphs, C.POINTER(L.sph))
+        self.mph = m
+
+    def _ptr(self, a, t):
+        self.keep.append(a)
+        return a.ctypes.data_as(C.POINTER(t))
+
+
+class Work:
+    """A var_mph holding what the assignment step reads and writes:
+    label_switch and the triangle-inequality bounds (tr), initialised as
+    d2_allocate_work does (clustering_util.c:218-228)."""
+
+    def __init__(self, size: int, k: int, s_ph: int, cost_scratch=None):
+        """``cost_scratch``: per phase, the g_var[n].C array the reference's
+        own d2_compute_distance writes its cost blocks into (and reads the
+        precomputed sparse-histogram costs from); this library needs none."""
+        self.label_switch = np.zeros(size, np.int8)
+        self.l = np.zeros(size * k)
+        self.u = np.full(size, np.finfo(np.float64).max)
+        self.s = np.zeros(k)
+        self.c = np.zeros(k * k)
+        self.r = np.ones(size, np.int8)
+        w = L.var_mph()
+        w.s_ph = s_ph
+        w.label_switch = self.label_switch.ctypes.data_as(C.POINTER(C.c_char))
+        w.tr.l = self.l.ctypes.data_as(C.POINTER(C.c_double))
+        w.tr.u = self.u.ctypes.data_as(C.POINTER(C.c_double))
+        w.tr.s = self.s.ctypes.data_as(C.POINTER(C.c_double))
+        w.tr.c = self.c.ctypes.data_as(C.POINTER(C.c_double))
+        w.tr.r = C.cast(self.r.ctypes.data, C.c_char_p)
+        if cost_scratch is not None:
+            self.scratch = [np.ascontiguousarray(a, np.float64) for a in cost_scratch]
+            gv = (L.var_sph * s_ph)()
+            for n, a in enumerate(self.scratch):
+                gv[n].C = a.ctypes.data_as(C.POINTER(C.c_double))
+            self.gv = gv
+            w.g_var = C.cast(gv, C.POINTER(L.var_sph))
+        self.var = w
+
+    def state(self):
+        return {k: getattr(self, k).copy() for k in ("label_switch", "l", "u", "s", "c", "r")}
+
+
+def labeling(data: Mph, cents: Mph, work: Work, selected_phase: int = -1):
+    """d2g_labeling: returns (labels changed, sum of squared nearest distances)."""
+    lib = L.load()
+    cnt, cost = C.c_size_t(), C.c_double()
+    L.check(lib.d2g_labeling(C.byref(data.mph), C.byref(cents.mph), C.byref(work.var),
+                             int(selected_phase), C.byref(cnt), C.byref(cost)), "d2g_labeling")
+    return cnt.value, cost.value
+
+
+def labeling_prep(data: Mph, cents: Mph, work: Work, selected_phase: int = -1):
+    """d2g_labeling_prep: returns (labels changed, distances computed)."""
+    lib = L.load()
+    cnt, dc = C.c_size_t(), C.c_size_t()
+    L.check(lib.d2g_labeling_prep(C.byref(data.mph), C.byref(cents.mph), C.byref(work.var),
+                                  int(selected_phase), C.byref(cnt), C.byref(dc)),
+            "d2g_labeling_prep")
+    return cnt.value, dc.value
+
+
+def labeling_post(data: Mph, c_old: Mph, c_new: Mph, work: Work, selected_phase: int = -1):
+    lib = L.load()
+    L.check(lib.d2g_labeling_post(C.byref(data.mph), C.byref(c_old.mph), C.byref(c_new.mph),
+                                  C.byref(work.var), int(selected_phase)), "d2g_labeling_post")
+
+
+def compute_distances(a: Mph, b: Mph, ia, jb, selected_phase: int = -1):
+    lib = L.load()
+    ia = np.ascontiguousarray(ia, np.int32)
+    jb = np.ascontiguousarray(jb, np.int32)
+    out = np.zeros(ia.size)
+    L.check(lib.d2g_compute_distances(C.byref(a.mph), C.byref(b.mph), int(selected_phase), ia.size,
+                                      ia.ctypes.data, jb.ctypes.data, out.ctypes.data),
+            "d2g_compute_distances")
+    return out

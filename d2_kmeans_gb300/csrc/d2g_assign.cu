@@ -9,9 +9,13 @@
 // for the phase's metric: squared Euclidean distances of the supports
 // (_dpdist2, src/utils/blas_like64.c:199-208) or the phase's bin-to-bin
 // cost matrix (histograms, sparse histograms).
+#include <float.h>
+#include <math.h>
 #include <string.h>
+#include <time.h>
 
 #include <algorithm>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -181,4 +185,489 @@ extern "C" int d2g_emd_pairs(int metric_type, int dim, const d2g_dists *rows, co
       return D2G_E_NUMERIC;
     }
   return D2G_OK;
+}
+
+// ------------------------------------------------------------------------
+// The assignment step on the reference's structures: d2_compute_distance,
+// d2_labeling, d2_labeling_prep (Elkan's triangle-inequality pruning) and
+// d2_labeling_post (src/d2/clustering.c:33-376), every distance an exact
+// transport cost from emd_kernel.cu.  Distances are batched: d2_labeling
+// sends all size x k pairs at once; the pruned labeling keeps the
+// reference's per-instance order of decisions (which distances it computes,
+// the bounds it writes) and runs it in waves - each instance advances
+// through its centroid loop until it needs a distance, the wave's pairs go
+// to the GPU together, and the results let every instance continue.
+
+namespace d2g {
+namespace {
+
+// one phase of one mph, on the device (weights, prefix sums, counts,
+// supports or bin ids)
+struct DevPhase {
+  DevMem w, cum, str, supp, sym;
+  // what the copy was made from
+  const void *kw = nullptr, *ks = nullptr, *ky = nullptr;
+  size_t size = 0, col = 0;
+  int max_str = 0, dim = 0, metric = -1;
+  std::vector<int> h_str;
+};
+
+int upload_phase(const sph *s, size_t size, DevPhase &d, cudaStream_t st) {
+  d = DevPhase();
+  std::vector<size_t> cum(size);
+  d.h_str.resize(size);
+  size_t c = 0;
+  int mx = 0;
+  for (size_t i = 0; i < size; ++i) {
+    const int k = s->p_str ? s->p_str[i] : s->str;
+    if (k < 0) return D2G_E_INVAL;
+    cum[i] = s->p_str_cum ? s->p_str_cum[i] : c;
+    d.h_str[i] = k;
+    c = cum[i] + (size_t)k;
+    mx = std::max(mx, k);
+  }
+  d.size = size;
+  d.col = c;
+  d.max_str = mx;
+  d.dim = s->dim;
+  d.metric = s->metric_type;
+  int rc = upload(d.w, s->p_w, c, st);
+  if (!rc) rc = upload(d.cum, cum.data(), size, st);
+  if (!rc) rc = upload(d.str, d.h_str.data(), size, st);
+  if (!rc && s->metric_type == D2_EUCLIDEAN_L2) rc = upload(d.supp, s->p_supp, c * (size_t)s->dim, st);
+  if (!rc && s->metric_type == D2_SPARSE_HISTOGRAM) rc = upload(d.sym, s->p_supp_sym, c, st);
+  if (!rc) D2G_CUDA(cudaStreamSynchronize(st));
+  d.kw = s->p_w;
+  d.ks = s->p_supp;
+  d.ky = s->p_supp_sym;
+  return rc;
+}
+
+bool same_source(const DevPhase &d, const sph *s, size_t size) {
+  if (d.kw != s->p_w || d.ks != s->p_supp || d.ky != s->p_supp_sym || d.size != size ||
+      d.metric != s->metric_type || d.dim != s->dim)
+    return false;
+  for (size_t i = 0; i < size; ++i)
+    if (d.h_str[i] != (s->p_str ? s->p_str[i] : s->str)) return false;
+  return true;
+}
+
+// the ground-cost table of a histogram phase: cost(row bin r, column bin c)
+// = dist_mat[c * V + r], the reference's column-major use of dist_mat
+// (clustering.c:88-95, blas_like64.c:222-230)
+struct DevTable {
+  DevMem T32, T64;
+  const double *src = nullptr;
+  int V = 0;
+};
+
+int upload_table(const double *dm, int V, DevTable &t, cudaStream_t st) {
+  if (t.src == dm && t.V == V) return D2G_OK;
+  t = DevTable();
+  const size_t vv = (size_t)V * V;
+  std::vector<double> t64(vv);
+  std::vector<float> t32(vv);
+  for (int r = 0; r < V; ++r)
+    for (int c = 0; c < V; ++c) {
+      t64[(size_t)r * V + c] = dm[(size_t)c * V + r];
+      t32[(size_t)r * V + c] = (float)dm[(size_t)c * V + r];
+    }
+  int rc = upload(t.T64, t64.data(), vv, st);
+  if (!rc) rc = upload(t.T32, t32.data(), vv, st);
+  if (!rc) D2G_CUDA(cudaStreamSynchronize(st));
+  if (rc) return rc;
+  t.src = dm;
+  t.V = V;
+  return D2G_OK;
+}
+
+struct AssignCache {
+  std::mutex mu;
+  std::vector<DevPhase> data;  // per phase of the instance mph
+  std::vector<DevTable> tables;
+};
+AssignCache g_assign;
+
+// exact transport of (rows: B object pb[p], columns: A object pa[p]) for
+// phase n, added to d[p]
+int phase_pairs(const sph *sa, const DevPhase &A, const sph *sb, const DevPhase &B, DevTable *tab,
+                const std::vector<int> &pa, const std::vector<int> &pb, std::vector<double> &d,
+                cudaStream_t st) {
+  const size_t np = pa.size();
+  if (np == 0) return D2G_OK;
+  const int metric = sa->metric_type;
+  EmdArgs a{};
+  if (metric == D2_EUCLIDEAN_L2) {
+    if (sa->dim < 1 || sa->dim > 7 || sb->dim != sa->dim) {
+      set_error("labeling: Euclidean supports of dimension 1..7");
+      return D2G_E_UNSUPPORTED;
+    }
+    a.mode = EMD_EUCLID;
+  } else if (metric == D2_HISTOGRAM || metric == D2_SPARSE_HISTOGRAM) {
+    if (!sa->dist_mat || sa->vocab_size <= 0) return D2G_E_INVAL;
+    int rc = upload_table(sa->dist_mat, sa->vocab_size, *tab, st);
+    if (rc) return rc;
+    a.mode = EMD_TABLE;
+    a.T32 = tab->T32.get<float>();
+    a.T64 = tab->T64.get<double>();
+    a.V = sa->vocab_size;
+    if (B.max_str > a.V || (metric == D2_HISTOGRAM && A.max_str > a.V)) {
+      set_error("labeling: a histogram with more bins than the cost matrix");
+      return D2G_E_INVAL;
+    }
+  } else {
+    set_error("labeling: metric type without an exact-transport path (word embeddings, n-grams)");
+    return D2G_E_UNSUPPORTED;
+  }
+  a.dim = sa->dim;
+  a.rw = B.w.get<double>();
+  a.rcum = B.cum.get<size_t>();
+  a.rstr = B.str.get<int>();
+  a.rsupp = B.supp.get<double>();
+  a.rsym = nullptr;  // centroids of histogram phases are dense
+  a.cw = A.w.get<double>();
+  a.ccum = A.cum.get<size_t>();
+  a.cstr = A.str.get<int>();
+  a.csupp = A.supp.get<double>();
+  a.csym = metric == D2_SPARSE_HISTOGRAM ? A.sym.get<int>() : nullptr;
+  a.nmax = ((A.max_str + B.max_str + 31) / 32) * 32;
+  if (a.nmax > 8192 || emd_slice(a.nmax, a.mode, a.dim) > 220 * 1024) {
+    set_error("labeling: a pair too large for one warp's shared memory");
+    return D2G_E_UNSUPPORTED;
+  }
+  a.max_piv = 64 * a.nmax + 1024;
+  DevMem dpa, dpb, out, piv;
+  int rc = upload(dpa, pa.data(), np, st);
+  if (!rc) rc = upload(dpb, pb.data(), np, st);
+  if (rc) return rc;
+  D2G_CUDA(cudaMalloc(&out.p, np * sizeof(double)));
+  D2G_CUDA(cudaMalloc(&piv.p, np * sizeof(int)));
+  a.prow = dpb.get<int>();
+  a.pcol = dpa.get<int>();
+  a.npairs = (long long)np;
+  a.out = out.get<double>();
+  a.piv = piv.get<int>();
+  D2G_CUDA(launch_emd(a, st));
+  std::vector<double> h(np);
+  std::vector<int> hp(np);
+  D2G_CUDA(cudaMemcpyAsync(h.data(), out.p, np * sizeof(double), cudaMemcpyDeviceToHost, st));
+  D2G_CUDA(cudaMemcpyAsync(hp.data(), piv.p, np * sizeof(int), cudaMemcpyDeviceToHost, st));
+  D2G_CUDA(cudaStreamSynchronize(st));
+  for (size_t p = 0; p < np; ++p) {
+    if (hp[p] < 0) {
+      set_error("labeling: a transport problem did not reach an optimal basis");
+      return D2G_E_NUMERIC;
+    }
+    d[p] += h[p];
+  }
+  return D2G_OK;
+}
+
+// distances of pairs (A object pa[p], B object pb[p]) as d2_compute_distance
+// returns them: sqrt of the phase costs' sum (phases in order), 0 if <= 0.
+// A = the instances when cache_a (their device copy is kept across calls).
+int pair_distances(mph *A, mph *B, int selected_phase, const std::vector<int> &pa,
+                   const std::vector<int> &pb, std::vector<double> &out, bool cache_a) {
+  const size_t np = pa.size();
+  out.assign(np, 0.0);
+  if (np == 0) return D2G_OK;
+  if (A->s_ph != B->s_ph) return D2G_E_INVAL;
+  cudaStream_t st = 0;
+  std::lock_guard<std::mutex> lk(g_assign.mu);
+  if (cache_a && g_assign.data.size() < (size_t)A->s_ph) g_assign.data.resize(A->s_ph);
+  if (g_assign.tables.size() < (size_t)A->s_ph) g_assign.tables.resize(A->s_ph);
+  for (int n = 0; n < A->s_ph; ++n) {
+    if (selected_phase >= 0 && n != selected_phase) continue;
+    const sph *sa = A->ph + n, *sb = B->ph + n;
+    DevPhase localA, devB;
+    DevPhase *dA = &localA;
+    int rc;
+    if (cache_a) {
+      dA = &g_assign.data[n];
+      rc = same_source(*dA, sa, A->size) ? D2G_OK : upload_phase(sa, A->size, *dA, st);
+    } else {
+      rc = upload_phase(sa, A->size, localA, st);
+    }
+    if (!rc) rc = upload_phase(sb, B->size, devB, st);
+    if (!rc) rc = phase_pairs(sa, *dA, sb, devB, &g_assign.tables[n], pa, pb, out, st);
+    if (rc) return rc;
+  }
+  for (size_t p = 0; p < np; ++p) out[p] = out[p] <= 0.0 ? 0.0 : sqrt(out[p]);
+  return D2G_OK;
+}
+
+double wall_seconds() {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+// Elkan's per-instance loop (clustering.c:177-224) as a resumable state:
+// advance() runs the reference's decisions until the next distance it needs
+struct ElkanInst {
+  int i, init_label, jj, j, stage;  // stage 0: test j; 1: 3a pending; 2: 3b test; 3: 3b pending
+  double minv;
+  int need;
+};
+
+}  // namespace
+}  // namespace d2g
+
+extern "C" {
+// The reference's driver owns these (src/d2/clustering.c:21-24); the weak
+// definitions let libd2g.so load without it.
+__attribute__((weak)) int d2_alg_type = 0;  // D2_CENTROID_BADMM
+}
+
+namespace d2g {
+namespace {
+constexpr double kTimeBudgetRatio = 2000.0;  // clustering.c:20
+
+bool elkan_advance(ElkanInst &s, int k, const double *L, const double *U, const double *c,
+                   const char *r) {
+  while (s.j < k) {
+    if (s.stage == 0) {
+      const int j = s.j;
+      if (!((j != s.jj || s.init_label < 0) && *U > L[j] && *U > c[(size_t)j * k + s.jj] / 2.)) {
+        ++s.j;
+        continue;
+      }
+      if (*r == 1) {  // 3a: the bound is stale, compute d(i, jj)
+        s.need = s.jj;
+        s.stage = 1;
+        return true;
+      }
+      s.minv = *U;
+      s.stage = 2;
+    }
+    if (s.stage == 2) {  // 3b
+      const int j = s.j;
+      if ((s.minv > L[j] || s.minv > c[(size_t)j * k + s.jj] / 2.) && j != s.jj) {
+        s.need = j;
+        s.stage = 3;
+        return true;
+      }
+      s.stage = 0;
+      ++s.j;
+      continue;
+    }
+    return false;  // stages 1 and 3 are resolved by elkan_apply
+  }
+  return false;
+}
+
+void elkan_apply(ElkanInst &s, double d, double *L, double *U, char *r) {
+  if (s.stage == 1) {
+    L[s.jj] = d;
+    *U = d;
+    s.minv = d;
+    *r = 0;
+    s.stage = 2;
+  } else {  // stage 3
+    L[s.j] = d;
+    if (d < s.minv) {
+      s.jj = s.j;
+      s.minv = d;
+      *U = d;
+    }
+    s.stage = 0;
+    ++s.j;
+  }
+}
+
+}  // namespace
+}  // namespace d2g
+
+extern "C" int d2g_compute_distances(mph *a, mph *b, int selected_phase, size_t npairs,
+                                     const int *ia, const int *jb, double *out) {
+  if (!a || !b || (npairs && (!ia || !jb || !out))) return D2G_E_INVAL;
+  std::vector<int> pa(ia, ia + npairs), pb(jb, jb + npairs);
+  for (size_t p = 0; p < npairs; ++p)
+    if (pa[p] < 0 || (size_t)pa[p] >= a->size || pb[p] < 0 || (size_t)pb[p] >= b->size)
+      return D2G_E_INVAL;
+  std::vector<double> d;
+  int rc = pair_distances(a, b, selected_phase, pa, pb, d, false);
+  if (rc) return rc;
+  memcpy(out, d.data(), npairs * sizeof(double));
+  return D2G_OK;
+}
+
+extern "C" int d2g_labeling(mph *p_data, mph *centroids, var_mph *var_work, int selected_phase,
+                            size_t *count_out, double *cost_out) {
+  if (!p_data || !centroids || !var_work || !p_data->label) return D2G_E_INVAL;
+  const size_t size = p_data->size, k = centroids->size;
+  if (k == 0) return D2G_E_INVAL;
+  std::vector<int> pa(size * k), pb(size * k);
+  for (size_t i = 0; i < size; ++i)
+    for (size_t j = 0; j < k; ++j) {
+      pa[i * k + j] = (int)i;
+      pb[i * k + j] = (int)j;
+    }
+  std::vector<double> d;
+  int rc = pair_distances(p_data, centroids, selected_phase, pa, pb, d, true);
+  if (rc) return rc;
+  size_t count = 0;
+  double cost = 0.0;
+  int *label = p_data->label;
+  for (size_t i = 0; i < size; ++i) {  // clustering.c:341-365
+    double mind = -1;
+    int jj = label[i] >= 0 ? label[i] : 0;
+    for (size_t j = 0; j < k; ++j) {
+      const double v = d[i * k + j];
+      if (mind < 0 || v < mind) {
+        mind = v;
+        jj = (int)j;
+      }
+    }
+    cost += mind * mind;
+    if (label[i] == jj) {
+      if (d2_alg_type == 0 && var_work->label_switch) var_work->label_switch[i] = 0;
+    } else {
+      label[i] = jj;
+      if (d2_alg_type == 0 && var_work->label_switch) var_work->label_switch[i] = 1;
+      ++count;
+    }
+  }
+  if (count_out) *count_out = count;
+  if (cost_out) *cost_out = cost;
+  return D2G_OK;
+}
+
+extern "C" int d2g_labeling_prep(mph *p_data, mph *centroids, var_mph *var_work, int selected_phase,
+                                 size_t *count_out, size_t *dist_count_out) {
+  if (!p_data || !centroids || !var_work || !p_data->label) return D2G_E_INVAL;
+  trieq *tr = &var_work->tr;
+  if (!tr->l || !tr->u || !tr->s || !tr->c || !tr->r) return D2G_E_INVAL;
+  const size_t size = p_data->size;
+  const int k = (int)centroids->size;
+  if (k <= 0) return D2G_E_INVAL;
+  size_t count = 0, dist_count = 0;
+  // step 1 (clustering.c:148-172): pairwise centroid distances, s = half the nearest
+  for (int i = 0; i < k; ++i) tr->s[i] = DBL_MAX;
+  for (size_t e = 0; e < (size_t)k * k; ++e) tr->c[e] = 0;
+  {
+    std::vector<int> pa, pb;
+    for (int i = 0; i < k; ++i)
+      for (int j = i + 1; j < k; ++j) {
+        pa.push_back(i);
+        pb.push_back(j);
+      }
+    std::vector<double> d;
+    int rc = pair_distances(centroids, centroids, selected_phase, pa, pb, d, false);
+    if (rc) return rc;
+    for (size_t p = 0; p < pa.size(); ++p) {  // in the reference's (i, j) order
+      const int i = pa[p], j = pb[p];
+      const double v = d[p];
+      ++dist_count;
+      tr->c[(size_t)i * k + j] = v;
+      tr->c[i + (size_t)j * k] = v;
+      if (tr->s[i] > v / 2.f) tr->s[i] = v / 2.f;
+      if (tr->s[j] > v / 2.f) tr->s[j] = v / 2.f;
+    }
+  }
+  if (d2_alg_type == 0 && var_work->label_switch)
+    for (size_t i = 0; i < size; ++i) var_work->label_switch[i] = 0;
+  // steps 2-3 in waves
+  int *label = p_data->label;
+  std::vector<ElkanInst> act;
+  for (size_t i = 0; i < size; ++i)
+    if (label[i] < 0 || tr->u[i] > tr->s[label[i]]) {
+      ElkanInst s{};
+      s.i = (int)i;
+      s.init_label = label[i];
+      s.jj = label[i] >= 0 ? label[i] : 0;
+      s.j = 0;
+      s.stage = 0;
+      act.push_back(s);
+    }
+  std::vector<ElkanInst> next;
+  std::vector<int> pa, pb;
+  std::vector<double> d;
+  while (!act.empty()) {
+    next.clear();
+    pa.clear();
+    pb.clear();
+    for (ElkanInst &s : act) {
+      double *L = tr->l + (size_t)s.i * k;
+      if (elkan_advance(s, k, L, tr->u + s.i, tr->c, tr->r + s.i)) {
+        pa.push_back(s.i);
+        pb.push_back(s.need);
+        next.push_back(s);
+      } else if (s.jj != s.init_label) {  // clustering.c:226-231
+        label[s.i] = s.jj;
+        if (d2_alg_type == 0 && var_work->label_switch) var_work->label_switch[s.i] = 1;
+        ++count;
+      }
+    }
+    if (next.empty()) break;
+    int rc = pair_distances(p_data, centroids, selected_phase, pa, pb, d, true);
+    if (rc) return rc;
+    dist_count += pa.size();
+    for (size_t p = 0; p < next.size(); ++p) {
+      ElkanInst &s = next[p];
+      elkan_apply(s, d[p], tr->l + (size_t)s.i * k, tr->u + s.i, tr->r + s.i);
+    }
+    act.swap(next);
+  }
+  if (count_out) *count_out = count;
+  if (dist_count_out) *dist_count_out = dist_count;
+  return D2G_OK;
+}
+
+extern "C" int d2g_labeling_post(mph *p_data, mph *c_old, mph *c_new, var_mph *var_work,
+                                 int selected_phase) {
+  if (!p_data || !c_old || !c_new || !var_work || !p_data->label) return D2G_E_INVAL;
+  trieq *tr = &var_work->tr;
+  if (!tr->l || !tr->u || !tr->r) return D2G_E_INVAL;
+  const int k = (int)c_old->size;
+  std::vector<int> idx(k);
+  for (int i = 0; i < k; ++i) idx[i] = i;
+  std::vector<double> dc;
+  // d_changes[i] = d2_compute_distance(c_new, i, c_old, i) (clustering.c:300-303)
+  int rc = pair_distances(c_new, c_old, selected_phase, idx, idx, dc, false);
+  if (rc) return rc;
+  for (size_t j = 0; j < p_data->size; ++j) {  // :305-310
+    double *L = tr->l + j * k;
+    for (int i = 0; i < k; ++i) L[i] = std::max(L[i] - dc[i], 0.0);
+    tr->u[j] += dc[p_data->label[j]];
+    tr->r[j] = 1;
+  }
+  return D2G_OK;
+}
+
+// The reference's own entry points (include/d2/clustering.h), same
+// signatures; a failure is reported through d2g_last_error and, for the
+// counting functions, a return of (size_t)-1.  Like the reference, the
+// labelings set the global time_budget for the next centroid update from
+// their own wall time (clustering.c:245, :372).
+extern "C" double d2_compute_distance(mph *a, size_t i, mph *b, size_t j, int selected_phase,
+                                      var_mph *var_work, size_t index_task) {
+  (void)var_work;
+  (void)index_task;
+  const int ia = (int)i, jb = (int)j;
+  double out = 0.0;
+  return d2g_compute_distances(a, b, selected_phase, 1, &ia, &jb, &out) ? NAN : out;
+}
+
+extern "C" size_t d2_labeling(mph *p_data, mph *centroids, var_mph *var_work, int selected_phase) {
+  size_t count = 0;
+  const double t0 = wall_seconds();
+  if (d2g_labeling(p_data, centroids, var_work, selected_phase, &count, nullptr)) return (size_t)-1;
+  time_budget = kTimeBudgetRatio * (wall_seconds() - t0) / p_data->num_of_labels;
+  return count;
+}
+
+extern "C" size_t d2_labeling_prep(mph *p_data, mph *centroids, var_mph *var_work,
+                                   int selected_phase) {
+  size_t count = 0;
+  const double t0 = wall_seconds();
+  if (d2g_labeling_prep(p_data, centroids, var_work, selected_phase, &count, nullptr))
+    return (size_t)-1;
+  time_budget = kTimeBudgetRatio * (wall_seconds() - t0);
+  return count;
+}
+
+extern "C" size_t d2_labeling_post(mph *p_data, mph *c_old, mph *c_new, var_mph *var_work,
+                                   int selected_phase) {
+  return d2g_labeling_post(p_data, c_old, c_new, var_work, selected_phase) ? (size_t)-1 : 0;
 }

@@ -301,6 +301,39 @@ int d2g_emd_pairs(int metric_type, int dim, const d2g_dists *rows, const d2g_dis
                   const double *dist_mat, int vocab_size, size_t npairs, const int *pair_row,
                   const int *pair_col, double *cost, int *pivots);
 
+/* The assignment step on the reference's structures (src/d2/clustering.c:
+ * 33-376); every distance is the square root of the phases' summed exact
+ * transport costs, as d2_compute_distance returns it.  Metric types:
+ * D2_EUCLIDEAN_L2 (dim 1..7), D2_HISTOGRAM, D2_SPARSE_HISTOGRAM; word
+ * embeddings and n-grams return D2G_E_UNSUPPORTED.  The instances' device
+ * copy is kept across calls while their arrays stay the same. */
+
+/* out[p] = d2_compute_distance(a, ia[p], b, jb[p], selected_phase, ...) */
+int d2g_compute_distances(mph *a, mph *b, int selected_phase, size_t npairs, const int *ia,
+                          const int *jb, double *out);
+/* d2_labeling (clustering.c:327-376): every instance to its nearest
+ * centroid (first of equals), label_switch as the reference sets it;
+ * *count = labels changed, *cost = sum of squared nearest distances. */
+int d2g_labeling(mph *p_data, mph *centroids, var_mph *var_work, int selected_phase,
+                 size_t *count, double *cost);
+/* d2_labeling_prep (clustering.c:134-248), Elkan's pruning with the bounds in
+ * var_work->tr: the same distances computed, bounds written and labels as
+ * the reference's loop; *dist_count = distances computed. */
+int d2g_labeling_prep(mph *p_data, mph *centroids, var_mph *var_work, int selected_phase,
+                      size_t *count, size_t *dist_count);
+/* d2_labeling_post (clustering.c:287-318): bounds after a centroid update */
+int d2g_labeling_post(mph *p_data, mph *c_old, mph *c_new, var_mph *var_work, int selected_phase);
+
+/* The reference's own entry points with its signatures (clustering.h); a
+ * failure returns NaN / (size_t)-1 with the message in d2g_last_error.  The
+ * labelings set time_budget as the reference does (clustering.c:245, :372). */
+double d2_compute_distance(mph *a, size_t i, mph *b, size_t j, int selected_phase,
+                           var_mph *var_work, size_t index_task);
+size_t d2_labeling(mph *p_data, mph *centroids, var_mph *var_work, int selected_phase);
+size_t d2_labeling_prep(mph *p_data, mph *centroids, var_mph *var_work, int selected_phase);
+size_t d2_labeling_post(mph *p_data, mph *c_old, mph *c_new, var_mph *var_work, int selected_phase);
+extern int d2_alg_type; /* clustering.c:24; label_switch is written when 0 (B-ADMM) */
+
 /* ------------------------------------------------------------- autotuning
  * Launch-shape choices of the batched form.  All choices compute the same
  * B-ADMM iteration; they differ in speed (and, for exchange, in the rounding

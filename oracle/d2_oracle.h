@@ -106,6 +106,17 @@ int d2o_mph_free(void *p_mph);
  * constraint left free.  Successive shortest paths in FP64 (emd_oracle.c).
  * x_out (optional): the n*m plan, column-major. */
 double d2o_emd(int n, int m, const double *C, const double *wX, const double *wY, double *x_out);
+
+/* The assignment step restated (labeling_oracle.c, src/d2/clustering.c:33-376)
+ * on the reference's structures (include/d2g.h); the mph / var_mph pointers
+ * are passed as void * here so this header stays free of those types. */
+double d2o_compute_distance(const void *a, size_t i, const void *b, size_t j, int selected_phase);
+size_t d2o_labeling_prep(void *p_data, const void *centroids, void *var_work, int selected_phase,
+                         size_t *dist_count);
+void d2o_labeling_post(void *p_data, const void *c_old, const void *c_new, void *var_work,
+                       int selected_phase);
+size_t d2o_labeling(void *p_data, const void *centroids, void *var_work, int selected_phase,
+                    double *cost);
 int d2r_read(const char *filename, const char *meta_filename, int s_ph, size_t size,
              const int *avg_strides, const int *dims, const int *types, void **out_mph);
 int d2r_mph_free(void *p_mph);

@@ -219,3 +219,66 @@ def emd(C_nm, wX, wY, want_plan=False):
     v = lib.d2o_emd(n, m, Cc.ctypes.data, wX.ctypes.data, wY.ctypes.data,
                     x.ctypes.data if want_plan else None)
     return (v, x) if want_plan else v
+
+
+class Labeling:
+    """The assignment step on the reference's structures (mph / var_mph built
+    by d2_kmeans_gb300.assign.Mph / Work): ``port`` = the oracle's
+    restatement (labeling_oracle.c), ``ref`` = the reference's own
+    clustering.c functions compiled into oracle/_ref with the oracle's exact
+    transport under d2_match_by_distmat (ref_solver.c)."""
+
+    def __init__(self, kind: str):
+        self.kind = kind
+        lib = _lib(kind)
+        vp, sz = C.c_void_p, C.c_size_t
+        if kind == "port":
+            self._lab = lib.d2o_labeling
+            self._lab.restype, self._lab.argtypes = sz, [vp, vp, vp, C.c_int, C.POINTER(C.c_double)]
+            self._prep = lib.d2o_labeling_prep
+            self._prep.restype, self._prep.argtypes = sz, [vp, vp, vp, C.c_int, C.POINTER(sz)]
+            self._post = lib.d2o_labeling_post
+            self._post.restype, self._post.argtypes = None, [vp, vp, vp, vp, C.c_int]
+            self._dist = lib.d2o_compute_distance
+            self._dist.restype, self._dist.argtypes = C.c_double, [vp, sz, vp, sz, C.c_int]
+        else:
+            self._lab = lib.d2_labeling
+            self._lab.restype, self._lab.argtypes = sz, [vp, vp, vp, C.c_int]
+            self._prep = lib.d2_labeling_prep
+            self._prep.restype, self._prep.argtypes = sz, [vp, vp, vp, C.c_int]
+            self._post = lib.d2_labeling_post
+            self._post.restype, self._post.argtypes = sz, [vp, vp, vp, vp, C.c_int]
+            self._dist = lib.d2_compute_distance
+            self._dist.restype, self._dist.argtypes = C.c_double, [vp, sz, vp, sz, C.c_int, vp, sz]
+
+    @staticmethod
+    def _p(x):
+        return C.cast(C.pointer(x), C.c_void_p)
+
+    def labeling(self, data, cents, work, selected_phase=-1):
+        """(labels changed, sum of squared nearest distances or None)"""
+        if self.kind == "port":
+            cost = C.c_double()
+            n = self._lab(self._p(data.mph), self._p(cents.mph), self._p(work.var), selected_phase,
+                          C.byref(cost))
+            return n, cost.value
+        return self._lab(self._p(data.mph), self._p(cents.mph), self._p(work.var), selected_phase), None
+
+    def labeling_prep(self, data, cents, work, selected_phase=-1):
+        """(labels changed, distances computed or None)"""
+        if self.kind == "port":
+            dc = C.c_size_t()
+            n = self._prep(self._p(data.mph), self._p(cents.mph), self._p(work.var), selected_phase,
+                           C.byref(dc))
+            return n, dc.value
+        return self._prep(self._p(data.mph), self._p(cents.mph), self._p(work.var),
+                          selected_phase), None
+
+    def labeling_post(self, data, c_old, c_new, work, selected_phase=-1):
+        self._post(self._p(data.mph), self._p(c_old.mph), self._p(c_new.mph), self._p(work.var),
+                   selected_phase)
+
+    def distance(self, a, i, b, j, selected_phase=-1):
+        if self.kind == "port":
+            return self._dist(self._p(a.mph), i, self._p(b.mph), j, selected_phase)
+        return self._dist(self._p(a.mph), i, self._p(b.mph), j, selected_phase, None, 0)

@@ -24,10 +24,9 @@
 #include "d2/param.h"
 #include "d2_oracle.h"
 
-/* globals the reference's hot-path objects expect from src/d2/clustering.c:21-26 */
-double time_budget = 1e300;
-int world_rank = 0;
-int nprocs = 1;
+/* time_budget, world_rank, nprocs and d2_alg_type come from the reference's
+ * own src/d2/clustering.c:21-26, compiled into the same library */
+extern double time_budget;
 
 extern BADMM_options *p_badmm_options;
 
@@ -153,7 +152,6 @@ int d2r_badmm(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_s
 
 /* the reference's own d2_allocate + d2_read (src/d2/clustering_util.c:93-130,
  * src/d2/clustering_io.c:14-201) into a heap mph */
-int d2_alg_type = 0; /* src/d2/clustering.c:24; clustering_util.c reads it */
 
 int d2r_read(const char *filename, const char *meta_filename, int s_ph, size_t size,
              const int *avg_strides, const int *dims, const int *types, void **out) {

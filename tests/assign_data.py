@@ -1,0 +1,93 @@
+"""Seeded assignment-step problems (instances + centroids in the reference's
+structures) shared by the oracle and GPU tests of the assignment step."""
+import numpy as np
+
+from d2_kmeans_gb300.assign import EUCLIDEAN, HISTOGRAM, SPARSE_HISTOGRAM, Mph, Work
+
+
+def euclid_phase(rng, n, dim, lo, hi, k, m, spread=3.0):
+    """instances: supports around k cluster means; centroids: m supports near each mean"""
+    means = rng.normal(size=(k, dim)) * spread
+    lab = rng.integers(0, k, size=n)
+    p_str = rng.integers(lo, hi + 1, size=n).astype(np.int32)
+    supp = np.concatenate([means[lab[i]] + rng.normal(size=(s, dim)) for i, s in enumerate(p_str)])
+    w = np.concatenate([rng.dirichlet(np.full(s, 0.8)) for s in p_str])
+    c_supp = np.concatenate([means[j] + rng.normal(size=(m, dim)) * 0.8 for j in range(k)])
+    c_w = np.concatenate([rng.dirichlet(np.ones(m)) for _ in range(k)])
+    data = dict(metric=EUCLIDEAN, dim=dim, str=m, p_str=p_str, p_w=w, p_supp=supp.reshape(-1))
+    cent = dict(metric=EUCLIDEAN, dim=dim, str=m, p_w=c_w, p_supp=c_supp.reshape(-1))
+    return data, cent
+
+
+def grid_costs(side):
+    g = np.stack(np.meshgrid(np.arange(side), np.arange(side), indexing="ij"), -1).reshape(-1, 2)
+    return ((g[:, None, :] - g[None, :, :]) ** 2).sum(-1).astype(float)
+
+
+def hist_phase(rng, n, k, side, sparse=False, asym=False):
+    V = side * side
+    dm = grid_costs(side)
+    if asym:
+        dm = dm * (1.0 + 0.3 * rng.random((V, V)))
+    protos = rng.dirichlet(np.full(V, 0.3), size=k)
+    lab = rng.integers(0, k, size=n)
+    c_w = np.concatenate([rng.dirichlet(protos[j] * 50 + 0.05) for j in range(k)])
+    cent = dict(metric=HISTOGRAM, dim=0, str=V, p_w=c_w, dist_mat=dm, vocab_size=V)
+    if not sparse:
+        w = np.stack([rng.dirichlet(protos[lab[i]] * 40 + 0.05) for i in range(n)])
+        w[w < 1e-4] = 0.0
+        w /= w.sum(1, keepdims=True)
+        data = dict(metric=HISTOGRAM, dim=0, str=V, p_str=np.full(n, V, np.int32),
+                    p_w=w.reshape(-1), dist_mat=dm, vocab_size=V)
+    else:
+        p_str = rng.integers(3, V // 2, size=n).astype(np.int32)
+        sym, w = [], []
+        for i, s in enumerate(p_str):
+            p = protos[lab[i]] + 1e-3
+            ids = np.sort(rng.choice(V, s, replace=False, p=p / p.sum()))
+            sym.append(ids)
+            w.append(rng.dirichlet(np.ones(s)))
+        data = dict(metric=SPARSE_HISTOGRAM, dim=0, str=V, p_str=p_str, p_w=np.concatenate(w),
+                    p_supp_sym=np.concatenate(sym).astype(np.int32), dist_mat=dm, vocab_size=V)
+    return data, cent
+
+
+def build(data_phases, cent_phases, n, k, label):
+    data = Mph(data_phases, n, label=label, num_of_labels=k)
+    cents = Mph(cent_phases, k, num_of_labels=k)
+    return data, cents
+
+
+def ref_scratch(data_phases, n, k):
+    """The g_var[n].C arrays the reference's d2_compute_distance needs
+    (clustering_util.c:178-197): str * (col + k * str) doubles per phase, with
+    the sparse-histogram cost blocks precomputed as _dpdist2_submat does."""
+    out = []
+    for ph in data_phases:
+        p_str = np.asarray(ph["p_str"])
+        col = int(p_str.sum())
+        m = int(ph["str"])
+        C = np.zeros(m * (col + k * m))
+        if ph["metric"] == SPARSE_HISTOGRAM:
+            V = ph["vocab_size"]
+            dm = np.asarray(ph["dist_mat"]).reshape(V, V)
+            cum = np.concatenate([[0], np.cumsum(p_str)])
+            for i in range(p_str.size):
+                sym = ph["p_supp_sym"][cum[i]:cum[i + 1]]
+                C[m * cum[i]: m * cum[i + 1]] = dm[sym, :].reshape(-1)
+        out.append(C)
+    return out
+
+
+def perturb(cent_phases, rng, scale):
+    """new centroids near the old ones (weights renormalised)"""
+    out = []
+    for ph in cent_phases:
+        ph = dict(ph)
+        w = np.asarray(ph["p_w"]).reshape(-1, ph["str"])
+        w = w * np.exp(rng.normal(size=w.shape) * scale)
+        ph["p_w"] = (w / w.sum(1, keepdims=True)).reshape(-1)
+        if ph.get("p_supp") is not None:
+            ph["p_supp"] = np.asarray(ph["p_supp"]) + rng.normal(size=len(ph["p_supp"])) * scale
+        out.append(ph)
+    return out
