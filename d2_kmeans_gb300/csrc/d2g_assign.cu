@@ -123,6 +123,7 @@ extern "C" int d2g_emd_pairs(int metric_type, int dim, const d2g_dists *rows, co
   }
 
   cudaStream_t st = 0;
+  float tscale = 0.f;
   DevMem rw, rcum, rstr, rsupp, rsym, cw, ccum, cstr, csupp, csym, T64, T32, pr, pc, out, piv;
   rc = upload(rw, rows->p_w, R.col, st);
   if (!rc) rc = upload(rcum, R.cum.data(), R.cum.size(), st);
@@ -137,7 +138,12 @@ extern "C" int d2g_emd_pairs(int metric_type, int dim, const d2g_dists *rows, co
   if (!rc && table) {
     const size_t vv = (size_t)vocab_size * vocab_size;
     std::vector<float> t32(vv);
-    for (size_t e = 0; e < vv; ++e) t32[e] = (float)dist_mat[e];
+    double mx = 0.0;
+    for (size_t e = 0; e < vv; ++e) {
+      t32[e] = (float)dist_mat[e];
+      mx = std::max(mx, fabs(dist_mat[e]));
+    }
+    tscale = (float)mx;
     rc = upload(T64, dist_mat, vv, st);
     if (!rc) rc = upload(T32, t32.data(), vv, st);
     if (!rc) D2G_CUDA(cudaStreamSynchronize(st));  // t32 leaves scope
@@ -166,6 +172,7 @@ extern "C" int d2g_emd_pairs(int metric_type, int dim, const d2g_dists *rows, co
   a.T32 = T32.get<float>();
   a.T64 = T64.get<double>();
   a.V = vocab_size;
+  a.tscale = tscale;
   a.prow = pr.get<int>();
   a.pcol = pc.get<int>();
   a.npairs = (long long)npairs;
@@ -259,6 +266,7 @@ struct DevTable {
   DevMem T32, T64;
   const double *src = nullptr;
   int V = 0;
+  float scale = 0.f;
 };
 
 int upload_table(const double *dm, int V, DevTable &t, cudaStream_t st) {
@@ -267,11 +275,14 @@ int upload_table(const double *dm, int V, DevTable &t, cudaStream_t st) {
   const size_t vv = (size_t)V * V;
   std::vector<double> t64(vv);
   std::vector<float> t32(vv);
+  double mx = 0.0;
   for (int r = 0; r < V; ++r)
     for (int c = 0; c < V; ++c) {
       t64[(size_t)r * V + c] = dm[(size_t)c * V + r];
       t32[(size_t)r * V + c] = (float)dm[(size_t)c * V + r];
+      mx = std::max(mx, fabs(dm[(size_t)c * V + r]));
     }
+  t.scale = (float)mx;
   int rc = upload(t.T64, t64.data(), vv, st);
   if (!rc) rc = upload(t.T32, t32.data(), vv, st);
   if (!rc) D2G_CUDA(cudaStreamSynchronize(st));
@@ -311,6 +322,7 @@ int phase_pairs(const sph *sa, const DevPhase &A, const sph *sb, const DevPhase 
     a.T32 = tab->T32.get<float>();
     a.T64 = tab->T64.get<double>();
     a.V = sa->vocab_size;
+    a.tscale = tab->scale;
     if (B.max_str > a.V || (metric == D2_HISTOGRAM && A.max_str > a.V)) {
       set_error("labeling: a histogram with more bins than the cost matrix");
       return D2G_E_INVAL;

@@ -259,10 +259,11 @@ struct EmdArgs {
   int cfix;
   const double *csupp;
   const int *csym;
-  // table costs T[key_row * V + key_col] (EMD_TABLE)
+  // table costs T[key_row * V + key_col] (EMD_TABLE); tscale >= every |T|
   const float *T32;
   const double *T64;
   int V;
+  float tscale;
   const int *prow, *pcol;  // the pairs
   long long npairs;
   double *out;             // exact cost per pair

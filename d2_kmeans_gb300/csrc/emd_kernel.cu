@@ -17,22 +17,26 @@
 //    last column takes whatever the rows still hold: its constraint is the
 //    dropped one);
 //  * node potentials (u_i + v_j = C_ij on tree arcs) by pointer jumping over
-//    the parent array: log2(depth) rounds, all lanes, no traversal order to
-//    maintain; depths come out of the same rounds;
-//  * pricing: every cell's reduced cost C_ij - u_i - v_j, spread over the
-//    warp's lanes, warp argmin (ties to the lowest cell index); FP32 costs
-//    from supports staged in shared memory;
-//  * pivot (lane 0): walk both ends of the entering cell up to their common
-//    ancestor, ratio test over the arcs that lose flow (ties: the last
-//    blocking arc met going round the cycle from the apex, the
-//    strongly-feasible-tree choice that avoids cycling), update the flows,
-//    re-hang the cut-off subtree by reversing the parent pointers from the
-//    entering node to the leaving arc;
-//  * exactness: when FP32 pricing finds no cell below -1e-5 of the cost
-//    scale, the potentials are recomputed in FP64 from FP64 costs and every
-//    cell is priced again in FP64; pivots continue in FP64 until no reduced
-//    cost is below -1e-12 of the scale.  The cost is then sum x_ij C_ij over
-//    the tree arcs in FP64, in a fixed order.
+//    the parent array: log2(depth) rounds over all lanes, no traversal order
+//    to maintain; depths come out of the same rounds;
+//  * pricing: every cell's reduced cost, the lanes spread over rows, columns
+//    or cells (whichever keeps more lanes busy), warp argmin (ties to the
+//    lowest cell index).  Euclidean costs in the norm form
+//    |x|^2 + |y|^2 - 2 x.y with the potentials folded into the norms, so a
+//    cell is one dot product; supports are centred on the rows' mean (FP64)
+//    before they are rounded to FP32 to keep the norms small;
+//  * pivot: lane 0 walks both ends of the entering cell up to their common
+//    ancestor and records the path; the ratio test (ties: the last blocking
+//    arc met going round the cycle from the apex, the strongly-feasible-tree
+//    choice that avoids cycling), the flow update and the re-hanging of the
+//    cut-off subtree (parent pointers reversed from the entering node to the
+//    leaving arc) run over the recorded path on all lanes;
+//  * exactness: FP32 pricing enters only cells below -1e-5 of the cost
+//    scale; when none is left the potentials are recomputed in FP64 from
+//    FP64 costs (the reference's difference form) and every cell is priced
+//    again in FP64; pivots continue in FP64 until no reduced cost is below
+//    -1e-12 of the scale.  The cost is then sum x_ij C_ij over the tree arcs
+//    in FP64, in a fixed order.
 //
 // A pair that has not reached optimality after max_piv pivots reports -1
 // pivots and a NaN cost (-3: a tree walk ran past the node count, which a
@@ -47,13 +51,14 @@ namespace {
 
 constexpr int kEmdWarps = 8;               // warps per block at most (fewer when the slices are large)
 constexpr int kEmdSmemLimit = 220 * 1024;  // dynamic shared memory per block
+constexpr int kSideJ = 1 << 20;            // ratio-test keys of the j side sort after the i side's
 
-// per-node bytes of the shared-memory slice of one warp
+// per-node bytes of one warp's shared-memory slice: node data (DP floats:
+// centred support + folded potential, or key + potential for tables), flow
+// and FP64 potential (doubles), two FP32 jump accumulators (one FP64 buffer
+// in the FP64 phase), two packed jump states, arc cost, parent, depth, path
 __host__ __device__ constexpr int emd_node_bytes(int DP) {
-  // flow, pot64 (weights first), acc64 second buffer: 3 doubles
-  // acost, jacc[2]: 3 floats; jan[2], jdep[2], parent, depth: 6 shorts
-  // data: DP floats (supports + potential), or key + potential for tables
-  return 3 * 8 + 3 * 4 + 6 * 2 + (DP > 0 ? DP * 4 : 8);
+  return (DP > 0 ? DP * 4 : 8) + 8 + 8 + 8 + 8 + 4 + 2 + 2 + 4;
 }
 
 __host__ __device__ inline size_t emd_slice_bytes(int nmax, int DP) {
@@ -61,10 +66,13 @@ __host__ __device__ inline size_t emd_slice_bytes(int nmax, int DP) {
 }
 
 struct EmdWarp {
-  double *flow, *p64, *q64;
-  float *acost, *jacc0, *jacc1;
-  short *jan0, *jan1, *jdep0, *jdep1, *parent, *depth;
-  float *dat;  // DP floats per node (EUCLID) or {key bits, pot} (TABLE)
+  float *dat;
+  double *flow, *p64;
+  float *jacc;   // [2][NM] FP32 accumulators; as double[NM]: the FP64 second buffer
+  int *jad;      // [2][NM] packed (anc + 1) | dep << 16
+  float *acost;
+  short *parent, *depth, *path;
+  int *stage;    // [NM] re-hang staging (aliases jad[0..NM))
 };
 
 __device__ inline EmdWarp carve(unsigned char *p, int NM, int DP) {
@@ -75,39 +83,30 @@ __device__ inline EmdWarp carve(unsigned char *p, int NM, int DP) {
   p += (size_t)NM * 8;
   w.p64 = (double *)p;
   p += (size_t)NM * 8;
-  w.q64 = (double *)p;
+  w.jacc = (float *)p;
+  p += (size_t)NM * 8;
+  w.jad = (int *)p;
+  w.stage = (int *)p;
   p += (size_t)NM * 8;
   w.acost = (float *)p;
   p += (size_t)NM * 4;
-  w.jacc0 = (float *)p;
-  p += (size_t)NM * 4;
-  w.jacc1 = (float *)p;
-  p += (size_t)NM * 4;
-  w.jan0 = (short *)p;
-  p += (size_t)NM * 2;
-  w.jan1 = (short *)p;
-  p += (size_t)NM * 2;
-  w.jdep0 = (short *)p;
-  p += (size_t)NM * 2;
-  w.jdep1 = (short *)p;
-  p += (size_t)NM * 2;
   w.parent = (short *)p;
   p += (size_t)NM * 2;
   w.depth = (short *)p;
+  p += (size_t)NM * 2;
+  w.path = (short *)p;
   return w;
 }
 
-// cost access for one problem
+// one problem: sizes, where its supports live, and the staged node data
 template <int MODE, int DP>
-struct Costs {
+struct Prob {
   const EmdArgs *a;
   EmdWarp w;
-  int n;
+  int n, m, N, NM;
   size_t r0, c0;  // first support of the row / column object
-  const float *T32;
-  const double *T64;
 
-  // FP32 cost from the staged node data
+  // FP32 cost in the difference form, from the staged (centred) supports
   __device__ inline float c32(int i, int j) const {
     if constexpr (MODE == EMD_EUCLID) {
       const float *x = w.dat + (size_t)i * DP, *y = w.dat + (size_t)(n + j) * DP;
@@ -120,7 +119,7 @@ struct Costs {
       return s;
     } else {
       const int ki = __float_as_int(w.dat[2 * i]), kj = __float_as_int(w.dat[2 * (n + j)]);
-      return __ldg(T32 + (size_t)ki * a->V + kj);
+      return __ldg(a->T32 + (size_t)ki * a->V + kj);
     }
   }
   // FP64 cost, the reference's difference form (_dpdist2, blas_like64.c:199-208)
@@ -136,91 +135,91 @@ struct Costs {
       return s;
     } else {
       const int ki = __float_as_int(w.dat[2 * i]), kj = __float_as_int(w.dat[2 * (n + j)]);
-      return __ldg(T64 + (size_t)ki * a->V + kj);
+      return __ldg(a->T64 + (size_t)ki * a->V + kj);
     }
   }
-  __device__ inline void set_pot(int x, float p) const {
-    if constexpr (MODE == EMD_EUCLID)
-      w.dat[(size_t)x * DP + DP - 1] = p;
-    else
-      w.dat[2 * x + 1] = p;
+  __device__ inline double arc_c64(int x, int px) const {
+    return x < n ? c64(x, px - n) : c64(px, x - n);
   }
-  __device__ inline float pot(int x) const {
-    if constexpr (MODE == EMD_EUCLID)
-      return w.dat[(size_t)x * DP + DP - 1];
-    else
-      return w.dat[2 * x + 1];
+  // store node x's FP32 potential: folded into the norm (Euclidean) or kept
+  __device__ inline void set_pot(int x, float p) const {
+    if constexpr (MODE == EMD_EUCLID) {
+      const float *v = w.dat + (size_t)x * DP;
+      float nrm = 0.f;
+#pragma unroll
+      for (int t = 0; t < DP - 1; ++t) nrm = fmaf(v[t], v[t], nrm);
+      w.dat[(size_t)x * DP + DP - 1] = nrm - p;
+    } else {
+      w.dat[2 * x + 1] = p;
+    }
   }
 };
 
-// cost of node x's tree arc (x and its parent: one row, one column)
-template <int MODE, int DP>
-__device__ inline double arc_c64(const Costs<MODE, DP> &cs, int x, int px) {
-  const int n = cs.n;
-  return x < n ? cs.c64(x, px - n) : cs.c64(px, x - n);
-}
-
 // Potentials by pointer jumping: pot[x] = acc + (-1)^dep * pot[anc] until
-// every anc is the root's -1.  FP32 (acc in jacc, costs from acost) or FP64
-// (acc in p64 / q64, costs recomputed).  Leaves depths in w.depth.
+// every anc is past the root.  FP32 (accumulators in jacc, arc costs from
+// acost) or FP64 (p64 and jacc as double, arc costs recomputed).  Leaves the
+// depths in w.depth and the potentials in the node data (FP32) or p64.
 template <int MODE, int DP, bool F64>
-__device__ void potentials(const Costs<MODE, DP> &cs, int N, int lane) {
-  const EmdWarp &w = cs.w;
+__device__ void potentials(const Prob<MODE, DP> &P, int lane) {
+  const EmdWarp &w = P.w;
+  const int N = P.N, NM = P.NM;
+  double *const a64_0 = w.p64, *const a64_1 = (double *)w.jacc;
+  float *const a32_0 = w.jacc, *const a32_1 = w.jacc + NM;
+  int *const jad0 = w.jad, *const jad1 = w.jad + NM;
   for (int x = lane; x < N; x += 32) {
     const int px = w.parent[x];
-    w.jan0[x] = (short)px;
-    w.jdep0[x] = px < 0 ? 0 : 1;
+    jad0[x] = (px + 1) | ((px < 0 ? 0 : 1) << 16);
     if (F64)
-      w.p64[x] = px < 0 ? 0.0 : arc_c64(cs, x, px);
+      a64_0[x] = px < 0 ? 0.0 : P.arc_c64(x, px);
     else
-      w.jacc0[x] = px < 0 ? 0.f : w.acost[x];
+      a32_0[x] = px < 0 ? 0.f : w.acost[x];
   }
   __syncwarp();
   int cur = 0;
   for (int round = 0; round < 16; ++round) {
-    const short *an = cur ? w.jan1 : w.jan0;
-    const short *dp = cur ? w.jdep1 : w.jdep0;
-    short *an2 = cur ? w.jan0 : w.jan1;
-    short *dp2 = cur ? w.jdep0 : w.jdep1;
+    const int *s = cur ? jad1 : jad0;
+    int *d = cur ? jad0 : jad1;
+    const double *s64 = cur ? a64_1 : a64_0;
+    double *d64 = cur ? a64_0 : a64_1;
+    const float *s32 = cur ? a32_1 : a32_0;
+    float *d32 = cur ? a32_0 : a32_1;
     bool more = false;
     for (int x = lane; x < N; x += 32) {
-      const int a0 = an[x];
-      const int d0 = dp[x];
-      if (a0 < 0) {
-        an2[x] = -1;
-        dp2[x] = (short)d0;
+      const int v = s[x];
+      const int A = v & 0xffff;
+      if (A == 0) {
+        d[x] = v;
         if (F64)
-          (cur ? w.p64 : w.q64)[x] = (cur ? w.q64 : w.p64)[x];
+          d64[x] = s64[x];
         else
-          (cur ? w.jacc0 : w.jacc1)[x] = (cur ? w.jacc1 : w.jacc0)[x];
+          d32[x] = s32[x];
         continue;
       }
-      const int a1 = an[a0];
+      const int u = s[A - 1];
+      const bool odd = (v >> 16) & 1;
       if (F64) {
-        const double *ac = cur ? w.q64 : w.p64;
-        double *ac2 = cur ? w.p64 : w.q64;
-        ac2[x] = (d0 & 1) ? ac[x] - ac[a0] : ac[x] + ac[a0];
+        const double q = s64[A - 1];
+        d64[x] = odd ? s64[x] - q : s64[x] + q;
       } else {
-        const float *ac = cur ? w.jacc1 : w.jacc0;
-        float *ac2 = cur ? w.jacc0 : w.jacc1;
-        ac2[x] = (d0 & 1) ? ac[x] - ac[a0] : ac[x] + ac[a0];
+        const float q = s32[A - 1];
+        d32[x] = odd ? s32[x] - q : s32[x] + q;
       }
-      an2[x] = (short)a1;
-      dp2[x] = (short)(d0 + dp[a0]);
-      more |= a1 >= 0;
+      const int A2 = u & 0xffff;
+      d[x] = A2 | (((v >> 16) + (u >> 16)) << 16);
+      more |= A2 != 0;
     }
     __syncwarp();
     cur ^= 1;
     if (!__any_sync(0xffffffffu, more)) break;
   }
-  // results in buffer `cur`
-  const short *dp = cur ? w.jdep1 : w.jdep0;
+  const int *fin = cur ? jad1 : jad0;
+  const float *f32 = cur ? a32_1 : a32_0;
   for (int x = lane; x < N; x += 32) {
-    w.depth[x] = dp[x];
+    w.depth[x] = (short)(fin[x] >> 16);
     if (F64) {
-      if (cur) w.p64[x] = w.q64[x];
+      if (cur) w.p64[x] = a64_1[x];
     } else {
-      cs.set_pot(x, cur ? w.jacc1[x] : w.jacc0[x]);
+      P.set_pot(x, f32[x]);
     }
   }
   __syncwarp();
@@ -248,76 +247,128 @@ __device__ inline Best warp_best(Best b) {
   return b;
 }
 
-// FP32 pricing: the cell with the most negative reduced cost
+// node data as registers: Euclidean (DP = 4: x, y, z, folded potential;
+// DP = 8: two float4) or table (key, potential)
+struct NodeV {
+  float4 a, b;
+};
+
 template <int MODE, int DP>
-__device__ Best price32(const Costs<MODE, DP> &cs, int n, int m, int lane) {
+__device__ inline NodeV load_node(const float *dat, int x) {
+  NodeV v;
+  if constexpr (MODE == EMD_EUCLID) {
+    v.a = *(const float4 *)(dat + (size_t)x * DP);
+    if constexpr (DP == 8) v.b = *(const float4 *)(dat + (size_t)x * DP + 4);
+  } else {
+    const float2 t = *(const float2 *)(dat + 2 * (size_t)x);
+    v.a = make_float4(t.x, t.y, 0.f, 0.f);
+  }
+  return v;
+}
+
+// reduced cost of the cell (row node data r, column node data c)
+template <int MODE, int DP>
+__device__ inline float rcost(const NodeV &r, const NodeV &c, const EmdArgs *a) {
+  if constexpr (MODE == EMD_EUCLID) {
+    if constexpr (DP == 4) {
+      const float dot = fmaf(r.a.x, c.a.x, fmaf(r.a.y, c.a.y, r.a.z * c.a.z));
+      return fmaf(-2.f, dot, r.a.w + c.a.w);
+    } else {
+      float dot = r.a.x * c.a.x;
+      dot = fmaf(r.a.y, c.a.y, dot);
+      dot = fmaf(r.a.z, c.a.z, dot);
+      dot = fmaf(r.a.w, c.a.w, dot);
+      dot = fmaf(r.b.x, c.b.x, dot);
+      dot = fmaf(r.b.y, c.b.y, dot);
+      dot = fmaf(r.b.z, c.b.z, dot);
+      return fmaf(-2.f, dot, r.b.w + c.b.w);
+    }
+  } else {
+    const float t = __ldg(a->T32 + (size_t)__float_as_int(r.a.x) * a->V + __float_as_int(c.a.x));
+    return t - r.a.y - c.a.y;
+  }
+}
+
+// FP32 pricing: the cell with the most negative reduced cost.  map 0:
+// lanes over rows, 1: over columns, 2: over cells.
+template <int MODE, int DP>
+__device__ Best price32(const Prob<MODE, DP> &P, int lane, int map) {
+  const int n = P.n, m = P.m;
+  const float *dat = P.w.dat;
   Best b{INFINITY, 0x7fffffff};
-  if (m <= 32) {
-    const int mp = m <= 1 ? 1 : 1 << (32 - __clz(m - 1));
-    const int R = 32 / mp;
-    const int j = lane & (mp - 1);
-    if (j < m) {
-      const float vj = cs.pot(n + j);
-      for (int i = lane / mp; i < n; i += R) {
-        const float r = cs.c32(i, j) - cs.pot(i) - vj;
-        better(b, r, i * m + j);
+  if (map == 0) {
+    for (int i = lane; i - lane < n; i += 32) {
+      const bool ok = i < n;
+      const NodeV r = load_node<MODE, DP>(dat, ok ? i : 0);
+      for (int j = 0; j < m; ++j) {
+        const float v = rcost<MODE, DP>(r, load_node<MODE, DP>(dat, n + j), P.a);
+        if (ok && v < b.v) {
+          b.v = v;
+          b.idx = i * m + j;
+        }
+      }
+    }
+  } else if (map == 1) {
+    for (int j = lane; j - lane < m; j += 32) {
+      const bool ok = j < m;
+      const NodeV c = load_node<MODE, DP>(dat, n + (ok ? j : 0));
+      for (int i = 0; i < n; ++i) {
+        const float v = rcost<MODE, DP>(load_node<MODE, DP>(dat, i), c, P.a);
+        if (ok) better(b, v, i * m + j);
       }
     }
   } else {
-    for (int j = lane; j < m; j += 32) {
-      const float vj = cs.pot(n + j);
-      for (int i = 0; i < n; ++i) {
-        const float r = cs.c32(i, j) - cs.pot(i) - vj;
-        better(b, r, i * m + j);
+    int i = lane / m, j = lane - (lane / m) * m;
+    const int di = 32 / m, dj = 32 - di * m;
+    while (i < n) {
+      const float v = rcost<MODE, DP>(load_node<MODE, DP>(dat, i), load_node<MODE, DP>(dat, n + j), P.a);
+      if (v < b.v) {
+        b.v = v;
+        b.idx = i * m + j;
+      }
+      i += di;
+      j += dj;
+      if (j >= m) {
+        j -= m;
+        ++i;
       }
     }
   }
   return warp_best(b);
 }
 
-// FP64 pricing, potentials in p64
+// FP64 pricing, potentials in p64: the most negative reduced cost below -tol
 template <int MODE, int DP>
-__device__ Best price64(const Costs<MODE, DP> &cs, int n, int m, int lane, double tol) {
+__device__ Best price64(const Prob<MODE, DP> &P, int lane, double tol) {
+  const int n = P.n, m = P.m;
   double bv = INFINITY;
   int bi = 0x7fffffff;
   const int cells = n * m;
   for (int c = lane; c < cells; c += 32) {
     const int i = c / m, j = c - i * m;
-    const double r = cs.c64(i, j) - cs.w.p64[i] - cs.w.p64[n + j];
+    const double r = P.c64(i, j) - P.w.p64[i] - P.w.p64[n + j];
     if (r < bv) {
       bv = r;
       bi = c;
     }
   }
+  // rank by the value in units of tol (ties to the lowest index)
   Best b{bv < -tol ? (float)(bv / tol) : INFINITY, bv < -tol ? bi : 0x7fffffff};
-  // ties on the scaled value fall to the lowest index
   return warp_best(b);
-}
-
-// the maximum FP32 cost (tolerance scale)
-template <int MODE, int DP>
-__device__ float cost_scale(const Costs<MODE, DP> &cs, int n, int m, int lane) {
-  float s = 0.f;
-  for (int c = lane; c < n * m; c += 32) {
-    const int i = c / m, j = c - i * m;
-    s = fmaxf(s, fabsf(cs.c32(i, j)));
-  }
-#pragma unroll
-  for (int o = 16; o >= 1; o >>= 1) s = fmaxf(s, __shfl_xor_sync(0xffffffffu, s, o));
-  return s;
 }
 
 // north-west corner start (lane 0); weights staged in p64
 template <int MODE, int DP>
-__device__ void nw_corner(const Costs<MODE, DP> &cs, int n, int m) {
-  const EmdWarp &w = cs.w;
+__device__ void nw_corner(const Prob<MODE, DP> &P) {
+  const EmdWarp &w = P.w;
+  const int n = P.n, m = P.m;
   w.parent[0] = -1;
   w.flow[0] = 0.0;
   w.acost[0] = 0.f;
   int r = 0, c = 0, cur = n;  // node holding the current cell's arc
   double s = w.p64[0], d = m == 1 ? INFINITY : w.p64[n];
   w.parent[n] = 0;
-  w.acost[n] = cs.c32(0, 0);
+  w.acost[n] = P.c32(0, 0);
   for (;;) {
     const double f = fmin(s, d);
     w.flow[cur] = f;
@@ -328,111 +379,121 @@ __device__ void nw_corner(const Costs<MODE, DP> &cs, int n, int m) {
       ++r;
       s = w.p64[r];
       w.parent[r] = (short)(n + c);
-      w.acost[r] = cs.c32(r, c);
+      w.acost[r] = P.c32(r, c);
       cur = r;
     } else {
       ++c;
       d = c == m - 1 ? INFINITY : w.p64[n + c];
       w.parent[n + c] = (short)r;
-      w.acost[n + c] = cs.c32(r, c);
+      w.acost[n + c] = P.c32(r, c);
       cur = n + c;
     }
   }
 }
 
-// one pivot on cell (ei, ej) (lane 0); false if a walk outgrows the tree
-// (a broken tree: every walk is bounded by the node count)
+// One pivot on cell (ei, ej).  Lane 0 records the cycle's tree path (i side
+// at path[0..ta), j side at path[N-1], path[N-2], ...); the ratio test, flow
+// update and re-hang run on all lanes.  Returns false if a walk outgrows the
+// tree (every walk is bounded by the node count).
 template <int MODE, int DP>
-__device__ bool pivot(const Costs<MODE, DP> &cs, int n, int N, int ei, int ej) {
-  const EmdWarp &w = cs.w;
+__device__ bool pivot(const Prob<MODE, DP> &P, int lane, int ei, int ej) {
+  const EmdWarp &w = P.w;
+  const int n = P.n, N = P.N;
   const int ni = ei, nj = n + ej;
-  // ratio test: arcs at even positions from either end lose flow
+  int packed = 0;
+  if (lane == 0) {
+    int a = ni, b = nj, ta = 0, tb = 0;
+    int da = w.depth[a], db = w.depth[b];
+    bool ok = da < N && db < N;
+    while (ok && da > db) {
+      w.path[ta++] = (short)a;
+      a = w.parent[a];
+      --da;
+    }
+    while (ok && db > da) {
+      w.path[N - 1 - tb++] = (short)b;
+      b = w.parent[b];
+      --db;
+    }
+    while (ok && a != b) {
+      if (a < 0 || b < 0 || ta + tb + 2 > N) {
+        ok = false;
+        break;
+      }
+      w.path[ta++] = (short)a;
+      a = w.parent[a];
+      w.path[N - 1 - tb++] = (short)b;
+      b = w.parent[b];
+    }
+    packed = ok ? (ta | (tb << 16)) : -1;
+  }
+  __syncwarp();
+  packed = __shfl_sync(0xffffffffu, packed, 0);
+  if (packed < 0) return false;
+  const int ta = packed & 0xffff, tb = packed >> 16;
+  // ratio test over the arcs at even positions (they lose flow)
   double theta = INFINITY;
-  int q = -1, qkey = -2147483647;
-  {
-    int a = ni, b = nj, ta = 0, tb = 0;
-    int da = w.depth[a], db = w.depth[b];
-    auto visit_i = [&](int x, int t) {  // i side, position t from ei
-      if (t & 1) return;
-      const double f = w.flow[x];
-      const int key = -t;  // nearest ei is last on this side
-      if (f < theta || (f == theta && key > qkey)) {
-        theta = f;
-        q = x;
-        qkey = key;
-      }
-    };
-    auto visit_j = [&](int x, int t) {  // j side, position t from ej
-      if (t & 1) return;
-      const double f = w.flow[x];
-      const int key = 1000000 + t;  // j side after i side, nearest the apex last
-      if (f < theta || (f == theta && key > qkey)) {
-        theta = f;
-        q = x;
-        qkey = key;
-      }
-    };
-    if (da >= N || db >= N) return false;
-    while (da > db) {
-      visit_i(a, ta++);
-      a = w.parent[a];
-      --da;
+  int qkey = -0x7fffffff;
+  for (int t = lane; t < ta + tb; t += 32) {
+    const bool iside = t < ta;
+    const int pos = iside ? t : t - ta;
+    if (pos & 1) continue;
+    const int x = iside ? w.path[t] : w.path[N - 1 - pos];
+    const double f = w.flow[x];
+    const int key = iside ? -pos : kSideJ + pos;
+    if (f < theta || (f == theta && key > qkey)) {
+      theta = f;
+      qkey = key;
     }
-    while (db > da) {
-      visit_j(b, tb++);
-      b = w.parent[b];
-      --db;
-    }
-    while (a != b) {
-      if (a < 0 || b < 0 || ta + tb > N) return false;
-      visit_i(a, ta++);
-      a = w.parent[a];
-      visit_j(b, tb++);
-      b = w.parent[b];
-    }
-    if (q < 0) return false;
   }
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    const double f = __shfl_xor_sync(0xffffffffu, theta, o);
+    const int k = __shfl_xor_sync(0xffffffffu, qkey, o);
+    if (f < theta || (f == theta && k > qkey)) {
+      theta = f;
+      qkey = k;
+    }
+  }
+  if (qkey == -0x7fffffff) return false;
   // flows along the cycle
-  {
-    int a = ni, b = nj, ta = 0, tb = 0;
-    int da = w.depth[a], db = w.depth[b];
-    while (da > db) {
-      w.flow[a] += (ta++ & 1) ? theta : -theta;
-      a = w.parent[a];
-      --da;
-    }
-    while (db > da) {
-      w.flow[b] += (tb++ & 1) ? theta : -theta;
-      b = w.parent[b];
-      --db;
-    }
-    while (a != b) {
-      w.flow[a] += (ta++ & 1) ? theta : -theta;
-      a = w.parent[a];
-      w.flow[b] += (tb++ & 1) ? theta : -theta;
-      b = w.parent[b];
-    }
+  for (int t = lane; t < ta + tb; t += 32) {
+    const bool iside = t < ta;
+    const int pos = iside ? t : t - ta;
+    const int x = iside ? w.path[t] : w.path[N - 1 - pos];
+    w.flow[x] += (pos & 1) ? theta : -theta;
   }
-  // q's arc leaves; the endpoint below it is re-hung from the other endpoint
-  const bool jside = qkey >= 1000000;
+  __syncwarp();
+  // the leaving arc's lower node q is at position tq on its side; the
+  // endpoint e on that side is re-hung from the other endpoint o and the
+  // parent pointers from e to q reversed (arc data move one node down)
+  const bool jside = qkey >= kSideJ;
+  const int tq = jside ? qkey - kSideJ : -qkey;
   const int e = jside ? nj : ni, o = jside ? ni : nj;
-  double pf = theta;
-  float pc = cs.c32(ei, ej);
-  int px = o, x = e;
-  for (int step = 0;; ++step) {
-    if (x < 0 || step > N) return false;
-    const int nx = w.parent[x];
-    const double tf = w.flow[x];
-    const float tc = w.acost[x];
-    w.parent[x] = (short)px;
-    w.flow[x] = pf;
-    w.acost[x] = pc;
-    if (x == q) break;
-    px = x;
-    pf = tf;
-    pc = tc;
-    x = nx;
+  auto node_at = [&](int t) -> int { return jside ? w.path[N - 1 - t] : w.path[t]; };
+  // stage the new (parent, flow, cost) of every reversed node
+  double *sflow = (double *)w.jacc;
+  float *scost = (float *)(w.stage + P.NM);
+  for (int t = lane; t <= tq; t += 32) {
+    if (t == 0) {
+      w.stage[0] = o;
+      sflow[0] = theta;
+      scost[0] = P.c32(ei, ej);
+    } else {
+      const int prev = node_at(t - 1);
+      w.stage[t] = prev;
+      sflow[t] = w.flow[prev];
+      scost[t] = w.acost[prev];
+    }
   }
+  __syncwarp();
+  for (int t = lane; t <= tq; t += 32) {
+    const int x = t == 0 ? e : node_at(t);
+    w.parent[x] = (short)w.stage[t];
+    w.flow[x] = sflow[t];
+    w.acost[x] = scost[t];
+  }
+  __syncwarp();
   return true;
 }
 
@@ -441,12 +502,11 @@ __global__ void __launch_bounds__(kEmdWarps * 32) emd_kernel(const __grid_consta
   extern __shared__ __align__(16) unsigned char emd_smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   const int NM = a.nmax;
-  Costs<MODE, DP> cs;
-  cs.a = &a;
-  cs.w = carve(emd_smem + (size_t)wib * emd_slice_bytes(NM, DP), NM, DP);
-  cs.T32 = a.T32;
-  cs.T64 = a.T64;
-  const EmdWarp &w = cs.w;
+  Prob<MODE, DP> P;
+  P.a = &a;
+  P.w = carve(emd_smem + (size_t)wib * emd_slice_bytes(NM, DP), NM, DP);
+  P.NM = NM;
+  const EmdWarp &w = P.w;
   for (long long p = (long long)blockIdx.x * wpb + wib; p < a.npairs; p += (long long)gridDim.x * wpb) {
     const int ro = __ldg(a.prow + p), co = __ldg(a.pcol + p);
     const int n = a.rstr ? __ldg(a.rstr + ro) : a.rfix;
@@ -461,58 +521,98 @@ __global__ void __launch_bounds__(kEmdWarps * 32) emd_kernel(const __grid_consta
       }
       continue;
     }
-    cs.n = n;
-    cs.r0 = r0;
-    cs.c0 = c0;
-    // stage weights (p64) and FP32 supports / table keys
-    for (int x = lane; x < N; x += 32) {
-      const bool row = x < n;
-      const size_t g = row ? r0 + x : c0 + (x - n);
-      w.p64[x] = __ldg((row ? a.rw : a.cw) + g);
-      if constexpr (MODE == EMD_EUCLID) {
-        const double *s = (row ? a.rsupp : a.csupp) + g * a.dim;
-        float *dst = w.dat + (size_t)x * DP;
+    P.n = n;
+    P.m = m;
+    P.N = N;
+    P.r0 = r0;
+    P.c0 = c0;
+    // stage weights (p64) and supports (centred on the rows' mean, FP32) or
+    // table keys; the cost scale bounds every cell's cost
+    float scale;
+    if constexpr (MODE == EMD_EUCLID) {
+      const int d = a.dim;
+      double ctr[DP - 1];
 #pragma unroll
-        for (int t = 0; t < DP - 1; ++t) dst[t] = t < a.dim ? (float)__ldg(s + t) : 0.f;
+      for (int t = 0; t < DP - 1; ++t) ctr[t] = 0.0;
+      for (int x = lane; x < n; x += 32)
+#pragma unroll
+        for (int t = 0; t < DP - 1; ++t)
+          if (t < d) ctr[t] += __ldg(a.rsupp + (r0 + x) * d + t);
+#pragma unroll
+      for (int t = 0; t < DP - 1; ++t) {
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) ctr[t] += __shfl_xor_sync(0xffffffffu, ctr[t], o);
+        ctr[t] /= n;
+      }
+      float nr = 0.f, nc = 0.f;
+      for (int x = lane; x < N; x += 32) {
+        const bool row = x < n;
+        const size_t g = row ? r0 + x : c0 + (x - n);
+        w.p64[x] = __ldg((row ? a.rw : a.cw) + g);
+        const double *s = (row ? a.rsupp : a.csupp) + g * d;
+        float *dst = w.dat + (size_t)x * DP;
+        float nrm = 0.f;
+#pragma unroll
+        for (int t = 0; t < DP - 1; ++t) {
+          const float v = t < d ? (float)(__ldg(s + t) - ctr[t]) : 0.f;
+          dst[t] = v;
+          nrm = fmaf(v, v, nrm);
+        }
         dst[DP - 1] = 0.f;
-      } else {
+        if (row)
+          nr = fmaxf(nr, nrm);
+        else
+          nc = fmaxf(nc, nrm);
+      }
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) {
+        nr = fmaxf(nr, __shfl_xor_sync(0xffffffffu, nr, o));
+        nc = fmaxf(nc, __shfl_xor_sync(0xffffffffu, nc, o));
+      }
+      const float rad = sqrtf(nr) + sqrtf(nc);
+      scale = rad * rad;
+    } else {
+      for (int x = lane; x < N; x += 32) {
+        const bool row = x < n;
+        const size_t g = row ? r0 + x : c0 + (x - n);
+        w.p64[x] = __ldg((row ? a.rw : a.cw) + g);
         const int *sym = row ? a.rsym : a.csym;
         const int key = sym ? __ldg(sym + g) : (row ? x : x - n);
         w.dat[2 * x] = __int_as_float(key);
         w.dat[2 * x + 1] = 0.f;
       }
+      scale = a.tscale;
     }
     __syncwarp();
-    if (lane == 0) nw_corner(cs, n, m);
+    if (lane == 0) nw_corner(P);
     __syncwarp();
-    const float scale = fmaxf(cost_scale(cs, n, m, lane), 1e-30f);
+    scale = fmaxf(scale, 1e-30f);
     const float tol32 = 1e-5f * scale;
     const double tol64 = 1e-12 * (double)scale;
+    // lanes over rows, columns or cells: whichever keeps more lanes busy
+    const float ur = (float)n / (32 * ((n + 31) / 32)), uc = (float)m / (32 * ((m + 31) / 32));
+    const int map = fmaxf(ur, uc) < 0.7f ? 2 : (ur >= uc ? 0 : 1);
     int piv = 0, status = 0;
     bool f64 = false;
     for (;;) {
       Best b;
       if (!f64) {
-        potentials<MODE, DP, false>(cs, N, lane);
-        b = price32(cs, n, m, lane);
+        potentials<MODE, DP, false>(P, lane);
+        b = price32(P, lane, map);
         if (!(b.v < -tol32)) {
           f64 = true;
           continue;
         }
       } else {
-        potentials<MODE, DP, true>(cs, N, lane);
-        b = price64(cs, n, m, lane, tol64);
+        potentials<MODE, DP, true>(P, lane);
+        b = price64(P, lane, tol64);
         if (b.idx == 0x7fffffff) break;
       }
       if (++piv > a.max_piv) {
         status = -1;
         break;
       }
-      int ok = 1;
-      if (lane == 0) ok = pivot(cs, n, N, b.idx / m, b.idx % m);
-      __syncwarp();
-      ok = __shfl_sync(0xffffffffu, ok, 0);
-      if (!ok) {
+      if (!pivot(P, lane, b.idx / m, b.idx % m)) {
         status = -3;
         break;
       }
@@ -522,7 +622,7 @@ __global__ void __launch_bounds__(kEmdWarps * 32) emd_kernel(const __grid_consta
     if (status == 0) {
       for (int x = lane; x < N; x += 32) {
         const int px = w.parent[x];
-        if (px >= 0) obj += w.flow[x] * arc_c64(cs, x, px);
+        if (px >= 0) obj += w.flow[x] * P.arc_c64(x, px);
       }
 #pragma unroll
       for (int o = 16; o >= 1; o >>= 1) obj += __shfl_xor_sync(0xffffffffu, obj, o);
@@ -538,11 +638,25 @@ __global__ void __launch_bounds__(kEmdWarps * 32) emd_kernel(const __grid_consta
 template <int MODE, int DP>
 cudaError_t launch_emd_t(const EmdArgs &a, cudaStream_t st) {
   const size_t slice = emd_slice_bytes(a.nmax, DP);
-  int wpb = (int)((size_t)kEmdSmemLimit / slice);
-  if (wpb > kEmdWarps) wpb = kEmdWarps;
+  auto kern = emd_kernel<MODE, DP>;
+  int dev = 0, sms = 0, smem_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  // warps per block: the most warps per SM that the shared memory holds
+  int best_w = 0, wpb = 0;
+  for (int cand = kEmdWarps; cand >= 1; --cand) {
+    const size_t smem = (size_t)cand * slice;
+    if (smem > (size_t)kEmdSmemLimit) continue;
+    const int blocks = (int)((size_t)smem_sm / (smem + 1024));
+    const int warps = blocks * cand > 64 ? 64 : blocks * cand;
+    if (warps > best_w) {
+      best_w = warps;
+      wpb = cand;
+    }
+  }
   if (wpb < 1) return cudaErrorInvalidValue;
   const size_t smem = (size_t)wpb * slice;
-  auto kern = emd_kernel<MODE, DP>;
   static size_t configured = 0;
   if (smem > configured) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -553,9 +667,6 @@ cudaError_t launch_emd_t(const EmdArgs &a, cudaStream_t st) {
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, wpb * 32, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const long long need = (a.npairs + wpb - 1) / wpb;
   const long long grid = need < (long long)per_sm * sms ? need : (long long)per_sm * sms;
   if (grid <= 0) return cudaSuccess;
