@@ -13,9 +13,9 @@
 //
 //  * basis = spanning tree over the n + m row and column nodes, stored as a
 //    parent array rooted at row 0 with the flow and FP32 cost of each node's
-//    arc to its parent; initial tree from the north-west corner rule (the
-//    last column takes whatever the rows still hold: its constraint is the
-//    dropped one);
+//    arc to its parent; initial tree from the row-minimum rule (the last
+//    column's demand is what the rows supply beyond the other columns: its
+//    constraint is the dropped one);
 //  * node potentials (u_i + v_j = C_ij on tree arcs) by pointer jumping over
 //    the parent array: log2(depth) rounds over all lanes, no traversal order
 //    to maintain; depths come out of the same rounds;
@@ -33,10 +33,11 @@
 //    leaving arc) run over the recorded path on all lanes;
 //  * exactness: FP32 pricing enters only cells below -1e-5 of the cost
 //    scale; when none is left the potentials are recomputed in FP64 from
-//    FP64 costs (the reference's difference form) and every cell is priced
-//    again in FP64; pivots continue in FP64 until no reduced cost is below
-//    -1e-12 of the scale.  The cost is then sum x_ij C_ij over the tree arcs
-//    in FP64, in a fixed order.
+//    FP64 costs (the reference's difference form) and every cell whose FP32
+//    reduced cost is within a safe margin of zero is priced again in FP64;
+//    pivots continue in FP64 until no reduced cost is below -1e-12 of the
+//    scale.  The cost is then sum x_ij C_ij over the tree arcs in FP64, in a
+//    fixed order.
 //
 // A pair that has not reached optimality after max_piv pivots reports -1
 // pivots and a NaN cost (-3: a tree walk ran past the node count, which a
@@ -337,19 +338,44 @@ __device__ Best price32(const Prob<MODE, DP> &P, int lane, int map) {
   return warp_best(b);
 }
 
-// FP64 pricing, potentials in p64: the most negative reduced cost below -tol
+// FP64 pricing, potentials in p64: the most negative reduced cost below
+// -tol.  The potentials are folded into the FP32 node data too; a cell whose
+// FP32 reduced cost is above thr (far above the FP32 rounding error of the
+// norms, dot products and potentials) is nonnegative in exact arithmetic and
+// is not evaluated in FP64.
 template <int MODE, int DP>
-__device__ Best price64(const Prob<MODE, DP> &P, int lane, double tol) {
-  const int n = P.n, m = P.m;
+__device__ Best price64(const Prob<MODE, DP> &P, int lane, double tol, float scale) {
+  const int n = P.n, m = P.m, N = P.N;
+  float pmax = 0.f;
+  for (int x = lane; x < N; x += 32) {
+    const float pv = (float)P.w.p64[x];
+    P.set_pot(x, pv);
+    pmax = fmaxf(pmax, fabsf(pv));
+  }
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) pmax = fmaxf(pmax, __shfl_xor_sync(0xffffffffu, pmax, o));
+  __syncwarp();
+  const float thr = 1e-3f * scale + 1e-5f * pmax;
+  const float *dat = P.w.dat;
   double bv = INFINITY;
   int bi = 0x7fffffff;
-  const int cells = n * m;
-  for (int c = lane; c < cells; c += 32) {
-    const int i = c / m, j = c - i * m;
-    const double r = P.c64(i, j) - P.w.p64[i] - P.w.p64[n + j];
-    if (r < bv) {
-      bv = r;
-      bi = c;
+  int i = lane / m, j = lane - (lane / m) * m;
+  const int di = 32 / m, dj = 32 - di * m;
+  while (i < n) {
+    const float r32 = rcost<MODE, DP>(load_node<MODE, DP>(dat, i), load_node<MODE, DP>(dat, n + j), P.a);
+    if (r32 < thr) {
+      const double r = P.c64(i, j) - P.w.p64[i] - P.w.p64[n + j];
+      const int c = i * m + j;
+      if (r < bv || (r == bv && c < bi)) {
+        bv = r;
+        bi = c;
+      }
+    }
+    i += di;
+    j += dj;
+    if (j >= m) {
+      j -= m;
+      ++i;
     }
   }
   // rank by the value in units of tol (ties to the lowest index)
@@ -357,38 +383,131 @@ __device__ Best price64(const Prob<MODE, DP> &P, int lane, double tol) {
   return warp_best(b);
 }
 
-// north-west corner start (lane 0); weights staged in p64
+// Starting basis by the row-minimum rule (Dantzig 1963, ch. 18): rows in
+// order, each ships to its cheapest open column until the row or the column
+// is used up, crossing out exactly one line per cell (never the last open
+// row or column), which gives n + m - 1 cells forming a spanning tree.  It
+// needs about half the pivots of the north-west corner on Euclidean costs.
+// The last column's demand is what the rows supply beyond the other columns
+// (its constraint is the dropped one).  Weights staged in p64; the cells go
+// to scratch (rows, columns in jad, flows in jacc), then lane 0 roots the
+// tree at row 0 by a breadth-first walk over an adjacency list.  False if
+// the cells do not span every node (not for a correct allocation).
 template <int MODE, int DP>
-__device__ void nw_corner(const Prob<MODE, DP> &P) {
+__device__ bool row_min_start(const Prob<MODE, DP> &P, int lane) {
   const EmdWarp &w = P.w;
-  const int n = P.n, m = P.m;
-  w.parent[0] = -1;
-  w.flow[0] = 0.0;
-  w.acost[0] = 0.f;
-  int r = 0, c = 0, cur = n;  // node holding the current cell's arc
-  double s = w.p64[0], d = m == 1 ? INFINITY : w.p64[n];
-  w.parent[n] = 0;
-  w.acost[n] = P.c32(0, 0);
-  for (;;) {
-    const double f = fmin(s, d);
-    w.flow[cur] = f;
-    s -= f;
-    d -= f;
-    if (r == n - 1 && c == m - 1) break;
-    if (c == m - 1 || (r < n - 1 && s <= d)) {
-      ++r;
-      s = w.p64[r];
-      w.parent[r] = (short)(n + c);
-      w.acost[r] = P.c32(r, c);
-      cur = r;
-    } else {
-      ++c;
-      d = c == m - 1 ? INFINITY : w.p64[n + c];
-      w.parent[n + c] = (short)r;
-      w.acost[n + c] = P.c32(r, c);
-      cur = n + c;
+  const int n = P.n, m = P.m, N = P.N, NM = P.NM;
+  int *const crow = w.jad, *const ccol = w.jad + NM;
+  double *const cflow = (double *)w.jacc;
+  short *const coldone = w.parent + n;
+  // last column's demand: total supply minus the other columns' demands
+  double tot = 0.0;
+  for (int x = lane; x < N - 1; x += 32) tot += x < n ? w.p64[x] : -w.p64[x];
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+  for (int j = lane; j < m; j += 32) coldone[j] = 0;
+  __syncwarp();
+  if (lane == 0) w.p64[N - 1] = fmax(tot, 0.0);
+  __syncwarp();
+  int count = 0, nr = n, nc = m;
+  for (int i = 0; i < n && count < N - 1; ++i) {
+    double si = w.p64[i];
+    for (;;) {
+      float bv = INFINITY;
+      int bj = 0x7fffffff;
+      for (int j = lane; j < m; j += 32)
+        if (!coldone[j]) {
+          const float c = P.c32(i, j);
+          if (c < bv) {
+            bv = c;
+            bj = j;
+          }
+        }
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) {
+        const float v = __shfl_xor_sync(0xffffffffu, bv, o);
+        const int jj = __shfl_xor_sync(0xffffffffu, bj, o);
+        if (v < bv || (v == bv && jj < bj)) {
+          bv = v;
+          bj = jj;
+        }
+      }
+      if (bj >= m) return false;  // no open column: not for a correct allocation
+      const int j = bj;
+      double dj = w.p64[n + j];
+      const double f = fmin(si, dj);
+      si -= f;
+      dj -= f;
+      __syncwarp();
+      if (lane == 0) {
+        crow[count] = i;
+        ccol[count] = j;
+        cflow[count] = f;
+        w.p64[n + j] = dj;
+      }
+      ++count;
+      bool row_done = false;
+      if (count == N - 1) {
+        row_done = true;
+      } else if (si <= dj && nr > 1) {
+        --nr;
+        row_done = true;
+      } else if (nc > 1) {
+        if (lane == 0) coldone[j] = 1;
+        --nc;
+      } else {
+        --nr;
+        row_done = true;
+      }
+      __syncwarp();
+      if (row_done) break;
     }
   }
+  // root the tree at row 0: adjacency list (degrees in acost as ints,
+  // offsets in depth, entries in p64 as ints), then a breadth-first walk
+  int spanned = 0;
+  if (lane == 0 && count == N - 1) {
+    int *const deg = (int *)w.acost;
+    short *const off = w.depth;
+    int *const adj = (int *)w.p64;
+    for (int x = 0; x < N; ++x) deg[x] = 0;
+    for (int k = 0; k < N - 1; ++k) {
+      ++deg[crow[k]];
+      ++deg[n + ccol[k]];
+    }
+    int acc = 0;
+    for (int x = 0; x < N; ++x) {
+      off[x] = (short)acc;
+      acc += deg[x];
+      deg[x] = off[x];  // fill cursor
+    }
+    for (int k = 0; k < N - 1; ++k) {
+      const int r = crow[k], c = n + ccol[k];
+      adj[deg[r]++] = c | (k << 16);
+      adj[deg[c]++] = r | (k << 16);
+    }
+    for (int x = 0; x < N; ++x) w.parent[x] = -2;
+    w.parent[0] = -1;
+    w.flow[0] = 0.0;
+    w.acost[0] = 0.f;
+    int head = 0, tail = 0;
+    w.path[tail++] = 0;
+    while (head < tail) {
+      const int u = w.path[head++];
+      const int end = u + 1 < N ? off[u + 1] : 2 * (N - 1);
+      for (int e = off[u]; e < end; ++e) {
+        const int v = adj[e] & 0xffff, k = adj[e] >> 16;
+        if (w.parent[v] != -2) continue;
+        w.parent[v] = (short)u;
+        w.flow[v] = cflow[k];
+        w.acost[v] = P.c32(crow[k], ccol[k]);
+        if (tail < N) w.path[tail++] = (short)v;
+      }
+    }
+    spanned = tail == N;
+  }
+  __syncwarp();
+  return __shfl_sync(0xffffffffu, spanned, 0) != 0;
 }
 
 // One pivot on cell (ei, ej).  Lane 0 records the cycle's tree path (i side
@@ -498,7 +617,7 @@ __device__ bool pivot(const Prob<MODE, DP> &P, int lane, int ei, int ej) {
 }
 
 template <int MODE, int DP>
-__global__ void __launch_bounds__(kEmdWarps * 32) emd_kernel(const __grid_constant__ EmdArgs a) {
+__global__ void __launch_bounds__(kEmdWarps * 32, 2) emd_kernel(const __grid_constant__ EmdArgs a) {
   extern __shared__ __align__(16) unsigned char emd_smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   const int NM = a.nmax;
@@ -584,17 +703,15 @@ __global__ void __launch_bounds__(kEmdWarps * 32) emd_kernel(const __grid_consta
       scale = a.tscale;
     }
     __syncwarp();
-    if (lane == 0) nw_corner(P);
-    __syncwarp();
+    int piv = 0, status = row_min_start(P, lane) ? 0 : -3;
     scale = fmaxf(scale, 1e-30f);
     const float tol32 = 1e-5f * scale;
     const double tol64 = 1e-12 * (double)scale;
     // lanes over rows, columns or cells: whichever keeps more lanes busy
     const float ur = (float)n / (32 * ((n + 31) / 32)), uc = (float)m / (32 * ((m + 31) / 32));
     const int map = fmaxf(ur, uc) < 0.7f ? 2 : (ur >= uc ? 0 : 1);
-    int piv = 0, status = 0;
     bool f64 = false;
-    for (;;) {
+    while (status == 0) {
       Best b;
       if (!f64) {
         potentials<MODE, DP, false>(P, lane);
@@ -605,7 +722,7 @@ __global__ void __launch_bounds__(kEmdWarps * 32) emd_kernel(const __grid_consta
         }
       } else {
         potentials<MODE, DP, true>(P, lane);
-        b = price64(P, lane, tol64);
+        b = price64(P, lane, tol64, scale);
         if (b.idx == 0x7fffffff) break;
       }
       if (++piv > a.max_piv) {
