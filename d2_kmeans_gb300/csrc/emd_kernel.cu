@@ -617,7 +617,7 @@ __device__ bool pivot(const Prob<MODE, DP> &P, int lane, int ei, int ej) {
 }
 
 template <int MODE, int DP>
-__global__ void __launch_bounds__(kEmdWarps * 32, 2) emd_kernel(const __grid_constant__ EmdArgs a) {
+__global__ void __launch_bounds__(kEmdWarps * 32, 3) emd_kernel(const __grid_constant__ EmdArgs a) {
   extern __shared__ __align__(16) unsigned char emd_smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   const int NM = a.nmax;
