@@ -20,6 +20,9 @@ Prints one JSON line:
              workloads: plan-updates/s and the plan kernel against the HBM peak
   tuning     the launch shape the autotuner picked for the headline phase
   io         d2 text input: d2g_read MB/s against the reference's fscanf reader
+  assign     the assignment step (d2_labeling, exact transport on the GPU):
+             transport problems/s, the pruned labeling, a sample checked
+             against the oracle's exact solver, which is also timed
 
 --impl reference times the reference algorithm's CPU implementation (the
 oracle port; the reference tree itself is not on the GPU host) with every
@@ -347,6 +350,78 @@ def io_leg():
             "identical_arrays": bool(same)}
 
 
+ASSIGN_WORKLOAD = ("assignment step: exact transport distances of the batched workload's n=200000 "
+                   "instances (d=3, m_i 8-128) to its k=64 centroids (m=32), 12.8 M transport "
+                   "problems per d2_labeling; d2_labeling_prep (Elkan) after a small centroid move")
+
+
+def assign_leg():
+    """d2_labeling / d2_labeling_prep / d2_labeling_post on the GPU (exact
+    transport, transportation simplex) over the headline workload, its
+    distances checked against the oracle's exact solver on a sample, and the
+    oracle timed on that sample as the CPU baseline."""
+    import numpy as np
+    import oracle
+    from d2_kmeans_gb300 import assign, synth
+    from d2_kmeans_gb300.assign import Mph, Work
+    ph, c, _ = synth.workload("batched", seed=0)
+    n, k, m = len(ph["p_str"]), int(ph["num_of_labels"]), int(ph["str"])
+
+    def data_mph(cnt):
+        col = int(ph["p_str"][:cnt].sum())
+        return Mph([dict(metric=0, dim=3, str=m, p_str=ph["p_str"][:cnt], p_w=ph["p_w"][:col],
+                         p_supp=ph["p_supp"][:col * 3])], cnt, label=ph["label"][:cnt].copy(),
+                   num_of_labels=k)
+
+    def cent_mph(c_w, c_supp):
+        return Mph([dict(metric=0, dim=3, str=m, p_w=c_w, p_supp=c_supp)], k, num_of_labels=k)
+
+    data = data_mph(n)
+    cents = cent_mph(c["c_w"], c["c_supp"])
+    w = Work(n, k, 1)
+    t = time.perf_counter()
+    assign.labeling(data, cents, w)  # uploads the instances (kept for later calls)
+    first = time.perf_counter() - t
+    data.label[:] = ph["label"]
+    t = time.perf_counter()
+    changed, cost = assign.labeling(data, cents, w)
+    t_lab = time.perf_counter() - t
+    # pruned labeling, the steady state of the k-means rounds: bounds from a
+    # first round, centroids moved a little, bounds updated, labeling again
+    w2 = Work(n, k, 1)
+    data.label[:] = ph["label"]
+    assign.labeling_prep(data, cents, w2)
+    rng = np.random.default_rng(7)
+    cw2 = c["c_w"].reshape(k, m) * np.exp(rng.normal(size=(k, m)) * 0.02)
+    cw2 = (cw2 / cw2.sum(1, keepdims=True)).reshape(-1)
+    cents2 = cent_mph(cw2, c["c_supp"] + rng.normal(size=c["c_supp"].size) * 0.02)
+    assign.labeling_post(data, cents, cents2, w2)
+    t = time.perf_counter()
+    changed2, dist2 = assign.labeling_prep(data, cents2, w2)
+    t_prep = time.perf_counter() - t
+    # distances of a sample against the oracle; the oracle timed on it
+    sample = 200
+    ds = data_mph(sample)
+    ia, jb = np.meshgrid(np.arange(sample), np.arange(k), indexing="ij")
+    ours = assign.compute_distances(ds, cents, ia.reshape(-1), jb.reshape(-1))
+    ensure_oracle()
+    lab = oracle.Labeling("port")
+    t = time.perf_counter()
+    ref = np.array([lab.distance(ds, i, cents, j) for i, j in zip(ia.reshape(-1), jb.reshape(-1))])
+    t_cpu = time.perf_counter() - t
+    rel = float(np.max(np.abs(ours - ref) / np.maximum(np.abs(ref), 1e-300)))
+    return {"workload": ASSIGN_WORKLOAD, "value": n * k / t_lab, "unit": "transport problems/s",
+            "labeling_s": t_lab, "first_call_s": first, "labels_changed": int(changed),
+            "mean_cost": cost / n,
+            "prep": {"seconds": t_prep, "distances": int(dist2), "labels_changed": int(changed2),
+                     "problems_per_s": dist2 / t_prep},
+            "check": {"pairs": int(ours.size), "max_rel_err_vs_oracle": rel},
+            "cpu_baseline": {"value": ref.size / t_cpu, "unit": "transport problems/s", "cores": 1,
+                             "kind": "port",
+                             "sample": f"{sample} instances x {k} centroids with the oracle's exact "
+                                       "solver (successive shortest paths, FP64)"}}
+
+
 SERVE_WORKLOAD = ("serving: k=256 resident centroids, m=64, d=64; queries with m_q log-uniform 4-512, "
                   "GMM supports, Dirichlet(1) weights; 200 B-ADMM iterations per solve against all "
                   "centroids + argmin; Poisson arrivals")
@@ -376,7 +451,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip", default="",
-                    help="comma list of legs to skip: e2e,plain,cpu,profile,serve,workloads,fp64,io")
+                    help="comma list of legs to skip: e2e,plain,cpu,profile,serve,workloads,fp64,io,"
+                         "assign")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -471,6 +547,8 @@ def main():
         out["serve"] = serve_leg()
     if "io" not in skip and rank == 0:
         out["io"] = io_leg()
+    if "assign" not in skip and rank == 0:
+        out["assign"] = assign_leg()
     if "workloads" not in skip and rank == 0:
         tf32 = bf16_peak() / 2
         out["workloads"] = {w: workload_leg(w, 2, hbm, tf32) for w in OTHER_WORKLOADS}

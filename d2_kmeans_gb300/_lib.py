@@ -145,6 +145,12 @@ SIGNATURES = {
     "d2_compute_distance": (C.c_double, [C.POINTER(mph), C.c_size_t, C.POINTER(mph), C.c_size_t,
                                          C.c_int, C.POINTER(var_mph), C.c_size_t]),
     "d2_labeling": (C.c_size_t, [C.POINTER(mph), C.POINTER(mph), C.POINTER(var_mph), C.c_int]),
+    "d2g_clustering": (C.c_int, [C.c_int, C.c_int, C.POINTER(mph), C.POINTER(mph), C.c_int, C.c_int,
+                                 C.c_char_p, C.POINTER(C.c_int)]),
+    "d2g_assignment": (C.c_int, [C.c_int, C.POINTER(mph), C.POINTER(mph), C.c_int,
+                                 C.POINTER(C.c_size_t)]),
+    "d2_clustering": (C.c_int, [C.c_int, C.c_int, C.POINTER(mph), C.POINTER(mph), C.c_int, C.c_char,
+                                C.c_char_p]),
     "d2_labeling_prep": (C.c_size_t, [C.POINTER(mph), C.POINTER(mph), C.POINTER(var_mph), C.c_int]),
     "d2_labeling_post": (C.c_size_t, [C.POINTER(mph), C.POINTER(mph), C.POINTER(mph),
                                       C.POINTER(var_mph), C.c_int]),

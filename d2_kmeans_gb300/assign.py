@@ -66,9 +66,12 @@ class Mph:
     def __init__(self, phases, size: int, label=None, num_of_labels: int = 0):
         self.keep = []
         self.size = int(size)
+        self.arrays = []  # per phase: the numpy arrays the mph points into
         sphs = (L.sph * len(phases))()
         for n, ph in enumerate(phases):
             s = sphs[n]
+            arrs = {}
+            self.arrays.append(arrs)
             p_str = np.ascontiguousarray(ph["p_str"] if ph.get("p_str") is not None
                                          else np.full(self.size, ph["str"]), np.int32)
             cum = np.zeros(self.size, np.uint64)
@@ -80,10 +83,12 @@ class Mph:
             s.max_col = s.col
             s.p_str = self._ptr(p_str, C.c_int)
             s.p_str_cum = self._ptr(cum, C.c_size_t)
-            s.p_w = self._ptr(np.ascontiguousarray(ph["p_w"], np.float64), C.c_double)
+            arrs["p_w"] = np.array(ph["p_w"], np.float64)
+            s.p_w = self._ptr(arrs["p_w"], C.c_double)
             s.metric_type = int(ph["metric"])
             if ph.get("p_supp") is not None:
-                s.p_supp = self._ptr(np.ascontiguousarray(ph["p_supp"], np.float64), C.c_double)
+                arrs["p_supp"] = np.array(ph["p_supp"], np.float64)
+                s.p_supp = self._ptr(arrs["p_supp"], C.c_double)
             if ph.get("p_supp_sym") is not None:
                 s.p_supp_sym = self._ptr(np.ascontiguousarray(ph["p_supp_sym"], np.int32), C.c_int)
             if ph.get("dist_mat") is not None:
@@ -176,3 +181,17 @@ def compute_distances(a: Mph, b: Mph, ia, jb, selected_phase: int = -1):
                                       ia.ctypes.data, jb.ctypes.data, out.ctypes.data),
             "d2g_compute_distances")
     return out
+
+
+def clustering(data: Mph, cents: Mph, k: int, max_iter: int, use_triangle: bool = True,
+               selected_phase: int = -1, log_file: str | None = None) -> int:
+    """d2g_clustering (the reference's d2_clustering loop) on the GPU; the
+    centroids' arrays and the instances' labels are updated in place.
+    Returns the number of rounds run."""
+    lib = L.load()
+    rounds = C.c_int()
+    L.check(lib.d2g_clustering(int(k), int(max_iter), C.byref(data.mph), C.byref(cents.mph),
+                               int(selected_phase), int(bool(use_triangle)),
+                               log_file.encode() if log_file else None, C.byref(rounds)),
+            "d2g_clustering")
+    return rounds.value

@@ -84,7 +84,12 @@ int err(int code, const char *msg) {
 
 }  // namespace
 
-extern "C" int d2_allocate_work_sphBregman(sph *ph, size_t size, var_sphBregman *w) {
+// The implementations live in namespace d2g so that this library's own outer
+// loop (d2g_cluster.cu) reaches them directly, not through the exported
+// names a program may define for itself.
+namespace d2g {
+
+int work_alloc_bregman(sph *ph, size_t size, var_sphBregman *w) {
   // centroid_Bregman.c:26-35: same host buffers and sizes
   if (!ph || !w || ph->str <= 0 || ph->col == 0 || size == 0) return err(D2G_E_INVAL, "bad work shape");
   const size_t nent = (size_t)ph->str * ph->col;
@@ -97,7 +102,7 @@ extern "C" int d2_allocate_work_sphBregman(sph *ph, size_t size, var_sphBregman 
   return D2G_OK;
 }
 
-extern "C" int d2_free_work_sphBregman(var_sphBregman *w) {
+int work_free_bregman(var_sphBregman *w) {
   if (!w) return D2G_E_INVAL;
   {
     std::lock_guard<std::mutex> lk(g_mu);
@@ -116,7 +121,7 @@ extern "C" int d2_free_work_sphBregman(var_sphBregman *w) {
   return D2G_OK;
 }
 
-extern "C" int d2_centroid_sphBregman(mph *p_data, var_mph *var_work, int idx_ph, sph *c0, sph *c) {
+int centroid_update(mph *p_data, var_mph *var_work, int idx_ph, sph *c0, sph *c) {
   if (!p_data || !var_work || !c || idx_ph < 0 || idx_ph >= p_data->s_ph || !var_work->l_var_sphBregman)
     return err(D2G_E_INVAL, "bad arguments");
   if (!c0) {
@@ -237,6 +242,18 @@ extern "C" int d2_centroid_sphBregman(mph *p_data, var_mph *var_work, int idx_ph
     fflush(stdout);
   }
   return D2G_OK;
+}
+
+}  // namespace d2g
+
+extern "C" int d2_allocate_work_sphBregman(sph *ph, size_t size, var_sphBregman *w) {
+  return d2g::work_alloc_bregman(ph, size, w);
+}
+
+extern "C" int d2_free_work_sphBregman(var_sphBregman *w) { return d2g::work_free_bregman(w); }
+
+extern "C" int d2_centroid_sphBregman(mph *p_data, var_mph *var_work, int idx_ph, sph *c0, sph *c) {
+  return d2g::centroid_update(p_data, var_work, idx_ph, c0, c);
 }
 
 extern "C" void calculate_distmat(sph *data_ph, int *label, size_t size, sph *c, double *C) {

@@ -334,6 +334,22 @@ size_t d2_labeling_prep(mph *p_data, mph *centroids, var_mph *var_work, int sele
 size_t d2_labeling_post(mph *p_data, mph *c_old, mph *c_new, var_mph *var_work, int selected_phase);
 extern int d2_alg_type; /* clustering.c:24; label_switch is written when 0 (B-ADMM) */
 
+/* The outer loop, d2_clustering (src/d2/clustering.c:409-525): rounds of
+ * labeling (Elkan's pruning when use_triangle) and B-ADMM centroid updates
+ * (p_badmm_options) until fewer than 0.1 % of the instances change label or
+ * max_iter rounds; centroids->ph == NULL initialises them with the program's
+ * d2_centroid_rands.  Log files <log_file>_c.d2 / <log_file>.label every
+ * tenth round when log_file is given.  *rounds (optional): rounds run. */
+int d2g_clustering(int num_of_clusters, int max_iter, mph *p_data, mph *centroids,
+                   int selected_phase, int use_triangle, const char *log_file, int *rounds);
+/* One labeling against given centroids (the labeling of d2_assignment,
+ * clustering.c:528-548); *count = labels changed. */
+int d2g_assignment(int num_of_clusters, mph *p_data, mph *centroids, int selected_phase,
+                   size_t *count);
+/* The reference's signature; returns 0 or a negative D2G_E* code. */
+int d2_clustering(int num_of_clusters, int max_iter, mph *p_data, mph *centroids,
+                  int selected_phase, char use_triangle, const char *log_file);
+
 /* ------------------------------------------------------------- autotuning
  * Launch-shape choices of the batched form.  All choices compute the same
  * B-ADMM iteration; they differ in speed (and, for exchange, in the rounding

@@ -91,3 +91,46 @@ def perturb(cent_phases, rng, scale):
             ph["p_supp"] = np.asarray(ph["p_supp"]) + rng.normal(size=len(ph["p_supp"])) * scale
         out.append(ph)
     return out
+
+
+def oracle_clustering(oracle_mod, data_phases, cent_phases, n, k, label, max_iter, use_triangle,
+                      opts=None):
+    """The reference's d2_clustering loop (src/d2/clustering.c:409-525) composed
+    from the oracle's labeling restatement and its B-ADMM restatement (both
+    bit-identical to the reference's own functions), no time budget.  Returns
+    (labels, centroid Mph, rounds)."""
+    opts = opts or dict(maxIters=100, rhoCoeff=2.0, updatePerLoops=10)
+    lab = oracle_mod.Labeling("port")
+    data = Mph(data_phases, n, label=np.asarray(label).copy(), num_of_labels=k)
+    cents = Mph(cent_phases, k, num_of_labels=k)
+    work = Work(n, k, len(data_phases))
+    Z = [None] * len(data_phases)
+    it = 0
+    while it < max_iter:
+        if use_triangle:
+            changed = lab.labeling_prep(data, cents, work)[0]
+        else:
+            changed = lab.labeling(data, cents, work)[0]
+        if changed < 0.001 * n:
+            break
+        old = Mph([dict(ph, p_w=cents.arrays[i]["p_w"].copy(),
+                        p_supp=None if "p_supp" not in cents.arrays[i] else cents.arrays[i]["p_supp"].copy())
+                   for i, ph in enumerate(cent_phases)], k, num_of_labels=k)
+        for i, ph in enumerate(data_phases):
+            phase = dict(ph, label=data.label.copy(), num_of_labels=k,
+                         label_switch=work.label_switch.copy())
+            cw = {"c_w": cents.arrays[i]["p_w"], "c_supp": cents.arrays[i].get("p_supp")}
+            if Z[i] is not None:
+                cw["Z"] = Z[i]
+            r = oracle_mod.badmm(phase, cw, opts, "port", want=())
+            assert r["rc"] == 0
+            cents.arrays[i]["p_w"][:] = r["c_w"]
+            if "p_supp" in cents.arrays[i]:
+                cents.arrays[i]["p_supp"][:] = r["c_supp"][:cents.arrays[i]["p_supp"].size]
+            Z[i] = r["Z"]
+        if use_triangle:
+            lab.labeling_post(data, old, cents, work)
+        it += 1
+    if use_triangle:
+        lab.labeling(data, cents, work)
+    return data.label.copy(), cents, it
