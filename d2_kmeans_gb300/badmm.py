@@ -30,7 +30,8 @@ def _arr(a, dtype):
 
 def set_config(**kw) -> dict:
     """Update the library configuration (precision, verbose, use_graph,
-    sync_scratch, profile, cost_gemm); returns the previous values."""
+    sync_scratch, profile, cost_gemm, keep_time_budget); returns the previous
+    values."""
     lib = L.load()
     cfg = L.d2g_config()
     L.check(lib.d2g_get_config(C.byref(cfg)), "d2g_get_config")
@@ -254,6 +255,9 @@ class DropIn:
         c.str = m
         c.max_str = m
         c.col = k * m
+        # strides as d2_allocate_sph + d2_centroid_rands leave them
+        c.p_str = ptr(np.full(k, m, np.int32), C.c_int)
+        c.p_str_cum = ptr(np.arange(k, dtype=np.uint64) * m, C.c_size_t)
         c.p_w = self.c_w.ctypes.data_as(C.POINTER(C.c_double))
         c.p_supp = (None if self.c_supp is None
                     else self.c_supp.ctypes.data_as(C.POINTER(C.c_double)))

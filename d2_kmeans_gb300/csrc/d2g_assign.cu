@@ -22,6 +22,7 @@
 #include "d2g_internal.cuh"
 
 namespace d2g {
+d2g_config cfg_snapshot();
 namespace {
 
 // a device allocation released on scope exit
@@ -665,7 +666,8 @@ extern "C" size_t d2_labeling(mph *p_data, mph *centroids, var_mph *var_work, in
   size_t count = 0;
   const double t0 = wall_seconds();
   if (d2g_labeling(p_data, centroids, var_work, selected_phase, &count, nullptr)) return (size_t)-1;
-  time_budget = kTimeBudgetRatio * (wall_seconds() - t0) / p_data->num_of_labels;
+  if (!cfg_snapshot().keep_time_budget)
+    time_budget = kTimeBudgetRatio * (wall_seconds() - t0) / p_data->num_of_labels;
   return count;
 }
 
@@ -675,7 +677,7 @@ extern "C" size_t d2_labeling_prep(mph *p_data, mph *centroids, var_mph *var_wor
   const double t0 = wall_seconds();
   if (d2g_labeling_prep(p_data, centroids, var_work, selected_phase, &count, nullptr))
     return (size_t)-1;
-  time_budget = kTimeBudgetRatio * (wall_seconds() - t0);
+  if (!cfg_snapshot().keep_time_budget) time_budget = kTimeBudgetRatio * (wall_seconds() - t0);
   return count;
 }
 

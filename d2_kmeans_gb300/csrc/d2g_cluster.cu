@@ -8,7 +8,10 @@
 // 0.1 % of the instances changed label, copy the centroids (pruned form),
 // update every selected phase's centroids, update the bounds; after the
 // loop the pruned form labels once more without pruning.  The labelings set
-// time_budget for the next update as the reference's do.
+// time_budget for the next update as the reference's do (clustering.c:245,
+// :372) unless d2g_config.keep_time_budget is set; that rule makes the
+// update depend on the labeling's wall time, so runs that must repeat bit
+// for bit keep the budget fixed.
 //
 // Work arrays are this library's own: label_switch, the triangle bounds and
 // one var_sphBregman per phase (the reference's d2_allocate_work also
@@ -30,6 +33,7 @@
 #include "d2g_internal.cuh"
 
 namespace d2g {
+d2g_config cfg_snapshot();
 int work_alloc_bregman(sph *ph, size_t size, var_sphBregman *w);
 int work_free_bregman(var_sphBregman *w);
 int centroid_update(mph *p_data, var_mph *var_work, int idx_ph, sph *c0, sph *c);
@@ -216,6 +220,7 @@ extern "C" int d2g_clustering(int num_of_clusters, int max_iter, mph *p_data, mp
   if (rc) return rc;
   if (centroids->s_ph != p_data->s_ph || centroids->size != (size_t)num_of_clusters) return D2G_E_INVAL;
   const bool tri = use_triangle != 0;
+  const bool set_budget = !d2g::cfg_snapshot().keep_time_budget;
   LoopWork w;
   rc = work_alloc(p_data, w, tri, selected_phase);
   CentroidCopy copy;
@@ -225,10 +230,10 @@ extern "C" int d2g_clustering(int num_of_clusters, int max_iter, mph *p_data, mp
     const double t0 = now_s();
     if (tri) {
       rc = d2g_labeling_prep(p_data, centroids, &w.vw, selected_phase, &changed, nullptr);
-      if (!rc) time_budget = kTimeBudgetRatio * (now_s() - t0);
+      if (!rc && set_budget) time_budget = kTimeBudgetRatio * (now_s() - t0);
     } else {
       rc = d2g_labeling(p_data, centroids, &w.vw, selected_phase, &changed, nullptr);
-      if (!rc) time_budget = kTimeBudgetRatio * (now_s() - t0) / num_of_clusters;
+      if (!rc && set_budget) time_budget = kTimeBudgetRatio * (now_s() - t0) / num_of_clusters;
     }
     if (rc) break;
     if (log_file && (iter + 1) % 10 == 0) write_log(log_file, centroids, p_data);
@@ -242,7 +247,7 @@ extern "C" int d2g_clustering(int num_of_clusters, int max_iter, mph *p_data, mp
   if (!rc && tri) {  // clustering.c:509
     const double t0 = now_s();
     rc = d2g_labeling(p_data, centroids, &w.vw, selected_phase, nullptr, nullptr);
-    if (!rc) time_budget = kTimeBudgetRatio * (now_s() - t0) / num_of_clusters;
+    if (!rc && set_budget) time_budget = kTimeBudgetRatio * (now_s() - t0) / num_of_clusters;
   }
   work_free(w);
   if (rounds) *rounds = iter;

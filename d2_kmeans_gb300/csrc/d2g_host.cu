@@ -35,7 +35,7 @@ static int fail(int code, const std::string &msg) {
 }
 
 std::mutex g_cfg_mu;
-d2g_config g_cfg = {0, 1, 1, 0, 0, 0};
+d2g_config g_cfg = {0, 1, 1, 0, 0, 0, 0};
 d2g_config cfg_snapshot() {
   std::lock_guard<std::mutex> lk(g_cfg_mu);
   return g_cfg;
@@ -1230,7 +1230,8 @@ int d2g_get_config(d2g_config *cfg) {
 }
 
 int d2g_set_config(const d2g_config *cfg) {
-  if (!cfg || cfg->precision < 0 || cfg->precision > 1 || cfg->cost_gemm < 0 || cfg->cost_gemm > 1)
+  if (!cfg || cfg->precision < 0 || cfg->precision > 1 || cfg->cost_gemm < 0 || cfg->cost_gemm > 1 ||
+      cfg->keep_time_budget < 0 || cfg->keep_time_budget > 1)
     return D2G_E_INVAL;
   std::lock_guard<std::mutex> lk(g_cfg_mu);
   g_cfg = *cfg;

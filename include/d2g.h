@@ -181,6 +181,8 @@ typedef struct {
   int profile;      /* 1: time every plan-update launch with CUDA events (no graph) */
   int cost_gemm;    /* word-embedding cost table of phases created afterwards:
                        0 tensor cores, 3xTF32 (default); 1 FP32 CUDA cores */
+  int keep_time_budget; /* 0: the labelings set time_budget from their wall time as
+                           the reference's do (default); 1: they leave it as it is */
 } d2g_config;
 
 int d2g_get_config(d2g_config *cfg);

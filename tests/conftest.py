@@ -61,13 +61,19 @@ def digest(zv):
 
 # A stand-in for the reference's d2_centroid_rands (src/d2/centroid_rand.c:161-295)
 # with a fixed, easily restated choice: the first num_of_labels instances whose
-# support size equals the centroid's, copied in order.  The drop-in finds it by
-# dlsym once it is loaded into the global scope.
+# support size equals the centroid's, copied in order; like the reference it
+# also sets the centroids' strides and column count (:176-182).  The drop-in
+# finds it by dlsym once it is loaded into the global scope.
 RANDS_STUB = r"""
 #include "d2g.h"
 int d2_centroid_rands(mph *p, int idx, sph *c) {
   sph *ph = p->ph + idx;
   int K = p->num_of_labels, m = c->str, d = ph->dim, j = 0;
+  for (int l = 0; l < K; ++l) {
+    c->p_str[l] = m;
+    c->p_str_cum[l] = (size_t)l * m;
+  }
+  c->col = (size_t)m * K;
   for (size_t i = 0; i < p->size && j < K; ++i) {
     if (ph->p_str[i] != m) continue;
     size_t o = ph->p_str_cum[i];

@@ -23,8 +23,20 @@ def lib(oracle_mod):
     from d2_kmeans_gb300 import badmm
     from d2_kmeans_gb300.build import build
     build()
-    badmm.set_config(verbose=0, precision=0, use_graph=1, profile=0, sync_scratch=0, cost_gemm=0)
-    return L.load()
+    # the reference's rule ties the update's time budget to the labeling's
+    # wall time; keep it fixed so that the runs repeat
+    badmm.set_config(verbose=0, precision=0, use_graph=1, profile=0, sync_scratch=0, cost_gemm=0,
+                     keep_time_budget=1)
+    lib = L.load()
+    C.c_double.in_dll(lib, "time_budget").value = 1e300
+    # the update runs with p_badmm_options -> badmm_clu_options, the
+    # reference's defaults {100, 2.0, 10} (centroid_Bregman.c:17), which other
+    # tests may have changed
+    opt = L.BADMM_options.in_dll(lib, "badmm_clu_options")
+    opt.maxIters, opt.rhoCoeff, opt.updatePerLoops = 100, 2.0, 10
+    C.c_void_p.in_dll(lib, "p_badmm_options").value = C.addressof(opt)
+    yield lib
+    badmm.set_config(keep_time_budget=0)
 
 
 def case(seed, n, k, dims=(2,)):
