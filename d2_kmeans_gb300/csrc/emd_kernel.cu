@@ -157,73 +157,94 @@ struct Prob {
 };
 
 // Potentials by pointer jumping: pot[x] = acc + (-1)^dep * pot[anc] until
-// every anc is past the root.  FP32 (accumulators in jacc, arc costs from
-// acost) or FP64 (p64 and jacc as double, arc costs recomputed).  Leaves the
-// depths in w.depth and the potentials in the node data (FP32) or p64.
+// every anc is past the root.  FP32: the state of a node is one 8-byte word
+// {acc, (anc + 1) | dep << 16} (two buffers: the jacc and jad regions), arc
+// costs from acost.  FP64: acc in p64 and the jacc region as double, the
+// packed anc/dep in the jad region, arc costs recomputed.  Leaves the depths
+// in w.depth and the potentials in the node data (FP32) or p64.
 template <int MODE, int DP, bool F64>
 __device__ void potentials(const Prob<MODE, DP> &P, int lane) {
   const EmdWarp &w = P.w;
   const int N = P.N, NM = P.NM;
-  double *const a64_0 = w.p64, *const a64_1 = (double *)w.jacc;
-  float *const a32_0 = w.jacc, *const a32_1 = w.jacc + NM;
-  int *const jad0 = w.jad, *const jad1 = w.jad + NM;
-  for (int x = lane; x < N; x += 32) {
-    const int px = w.parent[x];
-    jad0[x] = (px + 1) | ((px < 0 ? 0 : 1) << 16);
-    if (F64)
-      a64_0[x] = px < 0 ? 0.0 : P.arc_c64(x, px);
-    else
-      a32_0[x] = px < 0 ? 0.f : w.acost[x];
-  }
-  __syncwarp();
-  int cur = 0;
-  for (int round = 0; round < 16; ++round) {
-    const int *s = cur ? jad1 : jad0;
-    int *d = cur ? jad0 : jad1;
-    const double *s64 = cur ? a64_1 : a64_0;
-    double *d64 = cur ? a64_0 : a64_1;
-    const float *s32 = cur ? a32_1 : a32_0;
-    float *d32 = cur ? a32_0 : a32_1;
-    bool more = false;
+  if constexpr (!F64) {
+    int2 *const b0 = (int2 *)w.jacc, *const b1 = (int2 *)w.jad;
     for (int x = lane; x < N; x += 32) {
-      const int v = s[x];
-      const int A = v & 0xffff;
-      if (A == 0) {
-        d[x] = v;
-        if (F64)
-          d64[x] = s64[x];
-        else
-          d32[x] = s32[x];
-        continue;
-      }
-      const int u = s[A - 1];
-      const bool odd = (v >> 16) & 1;
-      if (F64) {
-        const double q = s64[A - 1];
-        d64[x] = odd ? s64[x] - q : s64[x] + q;
-      } else {
-        const float q = s32[A - 1];
-        d32[x] = odd ? s32[x] - q : s32[x] + q;
-      }
-      const int A2 = u & 0xffff;
-      d[x] = A2 | (((v >> 16) + (u >> 16)) << 16);
-      more |= A2 != 0;
+      const int px = w.parent[x];
+      b0[x] = make_int2(__float_as_int(px < 0 ? 0.f : w.acost[x]), (px + 1) | ((px < 0 ? 0 : 1) << 16));
     }
     __syncwarp();
-    cur ^= 1;
-    if (!__any_sync(0xffffffffu, more)) break;
-  }
-  const int *fin = cur ? jad1 : jad0;
-  const float *f32 = cur ? a32_1 : a32_0;
-  for (int x = lane; x < N; x += 32) {
-    w.depth[x] = (short)(fin[x] >> 16);
-    if (F64) {
-      if (cur) w.p64[x] = a64_1[x];
-    } else {
-      P.set_pot(x, f32[x]);
+    int cur = 0;
+    for (int round = 0; round < 16; ++round) {
+      const int2 *s = cur ? b1 : b0;
+      int2 *d = cur ? b0 : b1;
+      bool more = false;
+      for (int x = lane; x < N; x += 32) {
+        const int2 v = s[x];
+        const int A = v.y & 0xffff;
+        if (A == 0) {
+          d[x] = v;
+          continue;
+        }
+        const int2 u = s[A - 1];
+        const float acc = (v.y >> 16) & 1 ? __int_as_float(v.x) - __int_as_float(u.x)
+                                           : __int_as_float(v.x) + __int_as_float(u.x);
+        const int A2 = u.y & 0xffff;
+        d[x] = make_int2(__float_as_int(acc), A2 | (((v.y >> 16) + (u.y >> 16)) << 16));
+        more |= A2 != 0;
+      }
+      __syncwarp();
+      cur ^= 1;
+      if (!__any_sync(0xffffffffu, more)) break;
     }
+    const int2 *fin = cur ? b1 : b0;
+    for (int x = lane; x < N; x += 32) {
+      const int2 v = fin[x];
+      w.depth[x] = (short)(v.y >> 16);
+      P.set_pot(x, __int_as_float(v.x));
+    }
+    __syncwarp();
+  } else {
+    double *const a0 = w.p64, *const a1 = (double *)w.jacc;
+    int *const j0 = w.jad, *const j1 = w.jad + NM;
+    for (int x = lane; x < N; x += 32) {
+      const int px = w.parent[x];
+      j0[x] = (px + 1) | ((px < 0 ? 0 : 1) << 16);
+      a0[x] = px < 0 ? 0.0 : P.arc_c64(x, px);
+    }
+    __syncwarp();
+    int cur = 0;
+    for (int round = 0; round < 16; ++round) {
+      const int *s = cur ? j1 : j0;
+      int *d = cur ? j0 : j1;
+      const double *sa = cur ? a1 : a0;
+      double *da = cur ? a0 : a1;
+      bool more = false;
+      for (int x = lane; x < N; x += 32) {
+        const int v = s[x];
+        const int A = v & 0xffff;
+        if (A == 0) {
+          d[x] = v;
+          da[x] = sa[x];
+          continue;
+        }
+        const int u = s[A - 1];
+        const double q = sa[A - 1];
+        da[x] = (v >> 16) & 1 ? sa[x] - q : sa[x] + q;
+        const int A2 = u & 0xffff;
+        d[x] = A2 | (((v >> 16) + (u >> 16)) << 16);
+        more |= A2 != 0;
+      }
+      __syncwarp();
+      cur ^= 1;
+      if (!__any_sync(0xffffffffu, more)) break;
+    }
+    const int *fin = cur ? j1 : j0;
+    for (int x = lane; x < N; x += 32) {
+      w.depth[x] = (short)(fin[x] >> 16);
+      if (cur) w.p64[x] = a1[x];
+    }
+    __syncwarp();
   }
-  __syncwarp();
 }
 
 struct Best {
@@ -550,31 +571,34 @@ __device__ bool pivot(const Prob<MODE, DP> &P, int lane, int ei, int ej) {
   packed = __shfl_sync(0xffffffffu, packed, 0);
   if (packed < 0) return false;
   const int ta = packed & 0xffff, tb = packed >> 16;
-  // ratio test over the arcs at even positions (they lose flow)
-  double theta = INFINITY;
+  // ratio test over the arcs at even positions (they lose flow).  Flows are
+  // nonnegative, so they order like their bit patterns (sign bit cleared for
+  // -0): integer compares, off the narrow FP64 pipe.
+  unsigned long long tbits = 0x7ff0000000000000ull;  // +inf
   int qkey = -0x7fffffff;
   for (int t = lane; t < ta + tb; t += 32) {
     const bool iside = t < ta;
     const int pos = iside ? t : t - ta;
     if (pos & 1) continue;
     const int x = iside ? w.path[t] : w.path[N - 1 - pos];
-    const double f = w.flow[x];
+    const unsigned long long f = (unsigned long long)__double_as_longlong(w.flow[x]) & 0x7fffffffffffffffull;
     const int key = iside ? -pos : kSideJ + pos;
-    if (f < theta || (f == theta && key > qkey)) {
-      theta = f;
+    if (f < tbits || (f == tbits && key > qkey)) {
+      tbits = f;
       qkey = key;
     }
   }
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) {
-    const double f = __shfl_xor_sync(0xffffffffu, theta, o);
+    const unsigned long long f = __shfl_xor_sync(0xffffffffu, tbits, o);
     const int k = __shfl_xor_sync(0xffffffffu, qkey, o);
-    if (f < theta || (f == theta && k > qkey)) {
-      theta = f;
+    if (f < tbits || (f == tbits && k > qkey)) {
+      tbits = f;
       qkey = k;
     }
   }
   if (qkey == -0x7fffffff) return false;
+  const double theta = __longlong_as_double((long long)tbits);
   // flows along the cycle
   for (int t = lane; t < ta + tb; t += 32) {
     const bool iside = t < ta;
