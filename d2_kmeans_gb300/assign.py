@@ -93,6 +93,8 @@ class Mph:
                 s.p_supp_sym = self._ptr(np.ascontiguousarray(ph["p_supp_sym"], np.int32), C.c_int)
             if ph.get("dist_mat") is not None:
                 s.dist_mat = self._ptr(np.ascontiguousarray(ph["dist_mat"], np.float64), C.c_double)
+            if ph.get("vocab_vec") is not None:
+                s.vocab_vec = self._ptr(np.ascontiguousarray(ph["vocab_vec"], np.float64), C.c_double)
             s.vocab_size = int(ph.get("vocab_size", 0))
         self.sphs = sphs
         self.label = np.ascontiguousarray(label if label is not None else np.full(self.size, -1),

@@ -218,6 +218,7 @@ struct DevPhase {
   size_t size = 0, col = 0;
   int max_str = 0, dim = 0, metric = -1;
   std::vector<int> h_str;
+  std::vector<size_t> h_cum;
 };
 
 int upload_phase(const sph *s, size_t size, DevPhase &d, cudaStream_t st) {
@@ -237,13 +238,23 @@ int upload_phase(const sph *s, size_t size, DevPhase &d, cudaStream_t st) {
   d.size = size;
   d.col = c;
   d.max_str = mx;
+  d.h_cum = cum;
   d.dim = s->dim;
   d.metric = s->metric_type;
   int rc = upload(d.w, s->p_w, c, st);
   if (!rc) rc = upload(d.cum, cum.data(), size, st);
   if (!rc) rc = upload(d.str, d.h_str.data(), size, st);
   if (!rc && s->metric_type == D2_EUCLIDEAN_L2) rc = upload(d.supp, s->p_supp, c * (size_t)s->dim, st);
-  if (!rc && s->metric_type == D2_SPARSE_HISTOGRAM) rc = upload(d.sym, s->p_supp_sym, c, st);
+  const bool symbolic = s->metric_type == D2_SPARSE_HISTOGRAM || s->metric_type == D2_WORD_EMBED;
+  if (!rc && symbolic) {
+    if (!s->p_supp_sym || s->vocab_size <= 0) return D2G_E_INVAL;
+    for (size_t e = 0; e < c; ++e)
+      if (s->p_supp_sym[e] < 0 || s->p_supp_sym[e] >= s->vocab_size) {
+        set_error("labeling: a word or bin id outside the vocabulary");
+        return D2G_E_INVAL;
+      }
+    rc = upload(d.sym, s->p_supp_sym, c, st);
+  }
   if (!rc) D2G_CUDA(cudaStreamSynchronize(st));
   d.kw = s->p_w;
   d.ks = s->p_supp;
@@ -293,65 +304,92 @@ int upload_table(const double *dm, int V, DevTable &t, cudaStream_t st) {
   return D2G_OK;
 }
 
+// the FP64 vocabulary of a word-embedding phase on the device, and the FP32
+// cost table of the centroids of the current call (built once per call:
+// the centroids do not change between the waves of one labeling)
+struct DevVocab {
+  DevMem v;
+  const double *src = nullptr;
+  int V = 0, d = 0;
+  DevMem T;
+  unsigned long long tgen = 0;
+  const double *tsrc = nullptr;
+  float tscale = 0.f;
+};
+
+// T[(l * V + v) * m + k] = |c_{l,k} - vocab_v|^2 in FP32, difference form:
+// the FP32 costs the simplex prices with for word-embedding phases (the FP64
+// check recomputes the cells near zero from the FP64 data).  64 x 64 tiles
+// of (support, word), 32 dimensions per step.
+__global__ void __launch_bounds__(256) embed_label_table(const double *__restrict__ c, int m,
+                                                         const double *__restrict__ vocab, int V,
+                                                         int d, float *__restrict__ T) {
+  __shared__ float cs[64][33], vs[64][33];
+  const int l = blockIdx.z, k0 = blockIdx.y * 64, v0 = blockIdx.x * 64;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  float acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+  for (int t0 = 0; t0 < d; t0 += 32) {
+    for (int e = threadIdx.x; e < 64 * 32; e += 256) {
+      const int r = e >> 5, t = e & 31, tt = t0 + t;
+      const int k = k0 + r, v = v0 + r;
+      cs[r][t] = (k < m && tt < d) ? (float)c[((size_t)l * m + k) * d + tt] : 0.f;
+      vs[r][t] = (v < V && tt < d) ? (float)vocab[(size_t)v * d + tt] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int t = 0; t < 32; ++t) {
+      float a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        a[i] = cs[ty + 16 * i][t];
+        b[i] = vs[tx + 16 * i][t];
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float df = a[i] - b[j];
+          acc[i][j] = fmaf(df, df, acc[i][j]);
+        }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int k = k0 + ty + 16 * i, v = v0 + tx + 16 * j;
+      if (k < m && v < V) T[((size_t)l * V + v) * m + k] = acc[i][j];
+    }
+}
+
 struct AssignCache {
   std::mutex mu;
   std::vector<DevPhase> data;  // per phase of the instance mph
   std::vector<DevTable> tables;
+  std::vector<DevVocab> vocab;
+  unsigned long long gen = 0;  // advanced by every public call
 };
 AssignCache g_assign;
 
-// exact transport of (rows: B object pb[p], columns: A object pa[p]) for
-// phase n, added to d[p]
-int phase_pairs(const sph *sa, const DevPhase &A, const sph *sb, const DevPhase &B, DevTable *tab,
-                const std::vector<int> &pa, const std::vector<int> &pb, std::vector<double> &d,
-                cudaStream_t st) {
-  const size_t np = pa.size();
+// launch the pairs sel[] (indices into pa / pb) with the arguments a and add
+// their costs to d[]
+int run_pairs(EmdArgs a, const std::vector<int> &pa, const std::vector<int> &pb,
+              const std::vector<size_t> &sel, std::vector<double> &d, cudaStream_t st) {
+  const size_t np = sel.size();
   if (np == 0) return D2G_OK;
-  const int metric = sa->metric_type;
-  EmdArgs a{};
-  if (metric == D2_EUCLIDEAN_L2) {
-    if (sa->dim < 1 || sa->dim > 7 || sb->dim != sa->dim) {
-      set_error("labeling: Euclidean supports of dimension 1..7");
-      return D2G_E_UNSUPPORTED;
-    }
-    a.mode = EMD_EUCLID;
-  } else if (metric == D2_HISTOGRAM || metric == D2_SPARSE_HISTOGRAM) {
-    if (!sa->dist_mat || sa->vocab_size <= 0) return D2G_E_INVAL;
-    int rc = upload_table(sa->dist_mat, sa->vocab_size, *tab, st);
-    if (rc) return rc;
-    a.mode = EMD_TABLE;
-    a.T32 = tab->T32.get<float>();
-    a.T64 = tab->T64.get<double>();
-    a.V = sa->vocab_size;
-    a.tscale = tab->scale;
-    if (B.max_str > a.V || (metric == D2_HISTOGRAM && A.max_str > a.V)) {
-      set_error("labeling: a histogram with more bins than the cost matrix");
-      return D2G_E_INVAL;
-    }
-  } else {
-    set_error("labeling: metric type without an exact-transport path (word embeddings, n-grams)");
-    return D2G_E_UNSUPPORTED;
+  std::vector<int> qa(np), qb(np);
+  for (size_t p = 0; p < np; ++p) {
+    qa[p] = pa[sel[p]];
+    qb[p] = pb[sel[p]];
   }
-  a.dim = sa->dim;
-  a.rw = B.w.get<double>();
-  a.rcum = B.cum.get<size_t>();
-  a.rstr = B.str.get<int>();
-  a.rsupp = B.supp.get<double>();
-  a.rsym = nullptr;  // centroids of histogram phases are dense
-  a.cw = A.w.get<double>();
-  a.ccum = A.cum.get<size_t>();
-  a.cstr = A.str.get<int>();
-  a.csupp = A.supp.get<double>();
-  a.csym = metric == D2_SPARSE_HISTOGRAM ? A.sym.get<int>() : nullptr;
-  a.nmax = ((A.max_str + B.max_str + 31) / 32) * 32;
-  if (a.nmax > 8192 || emd_slice(a.nmax, a.mode, a.dim) > 220 * 1024) {
-    set_error("labeling: a pair too large for one warp's shared memory");
-    return D2G_E_UNSUPPORTED;
-  }
-  a.max_piv = 64 * a.nmax + 1024;
   DevMem dpa, dpb, out, piv;
-  int rc = upload(dpa, pa.data(), np, st);
-  if (!rc) rc = upload(dpb, pb.data(), np, st);
+  int rc = upload(dpa, qa.data(), np, st);
+  if (!rc) rc = upload(dpb, qb.data(), np, st);
   if (rc) return rc;
   D2G_CUDA(cudaMalloc(&out.p, np * sizeof(double)));
   D2G_CUDA(cudaMalloc(&piv.p, np * sizeof(int)));
@@ -371,9 +409,154 @@ int phase_pairs(const sph *sa, const DevPhase &A, const sph *sb, const DevPhase 
       set_error("labeling: a transport problem did not reach an optimal basis");
       return D2G_E_NUMERIC;
     }
-    d[p] += h[p];
+    d[sel[p]] += h[p];
   }
   return D2G_OK;
+}
+
+double max_sq_norm(const double *x, size_t count, int dim) {
+  double mx = 0.0;
+  for (size_t e = 0; e < count; ++e) {
+    double s = 0.0;
+    for (int t = 0; t < dim; ++t) s += x[e * dim + t] * x[e * dim + t];
+    mx = std::max(mx, s);
+  }
+  return mx;
+}
+
+constexpr size_t kTableBytes = (size_t)2 << 30;  // FP32 cost table per launch, at most
+
+// exact transport of (rows: B object pb[p], columns: A object pa[p]) for
+// phase n, added to d[p]
+int phase_pairs(const sph *sa, const DevPhase &A, const sph *sb, const DevPhase &B, DevTable *tab,
+                DevVocab *voc, const std::vector<int> &pa, const std::vector<int> &pb,
+                std::vector<double> &d, cudaStream_t st) {
+  const size_t np = pa.size();
+  if (np == 0) return D2G_OK;
+  const int metric = sa->metric_type;
+  EmdArgs a{};
+  a.dim = sa->dim;
+  a.rw = B.w.get<double>();
+  a.rcum = B.cum.get<size_t>();
+  a.rstr = B.str.get<int>();
+  a.rsupp = B.supp.get<double>();
+  a.rsym = nullptr;  // centroids of histogram phases are dense
+  a.cw = A.w.get<double>();
+  a.ccum = A.cum.get<size_t>();
+  a.cstr = A.str.get<int>();
+  a.csupp = A.supp.get<double>();
+  a.nmax = ((A.max_str + B.max_str + 31) / 32) * 32;
+  std::vector<size_t> all(np);
+  for (size_t p = 0; p < np; ++p) all[p] = p;
+  const bool big_euclid = metric == D2_EUCLIDEAN_L2 && sa->dim > 7;
+  if (metric == D2_EUCLIDEAN_L2 && !big_euclid) {
+    if (sa->dim < 1 || sb->dim != sa->dim) return D2G_E_INVAL;
+    a.mode = EMD_EUCLID;
+  } else if (metric == D2_HISTOGRAM || metric == D2_SPARSE_HISTOGRAM) {
+    if (!sa->dist_mat || sa->vocab_size <= 0) return D2G_E_INVAL;
+    int rc = upload_table(sa->dist_mat, sa->vocab_size, *tab, st);
+    if (rc) return rc;
+    a.mode = EMD_TABLE;
+    a.T32 = tab->T32.get<float>();
+    a.T64 = tab->T64.get<double>();
+    a.V = sa->vocab_size;
+    a.tscale = tab->scale;
+    a.csym = metric == D2_SPARSE_HISTOGRAM ? A.sym.get<int>() : nullptr;
+    if (B.max_str > a.V || (metric == D2_HISTOGRAM && A.max_str > a.V)) {
+      set_error("labeling: a histogram with more bins than the cost matrix");
+      return D2G_E_INVAL;
+    }
+  } else if (metric == D2_WORD_EMBED || big_euclid) {
+    // rows: R^d supports; columns: word ids into vocab_vec (_dpdist2_sym,
+    // blas_like64.c:210-220) or, for Euclidean supports of d > 7, the column
+    // supports themselves taken as the vocabulary
+    const int dim = sa->dim, m = B.max_str;
+    if (dim < 1 || sb->dim != dim || sb->metric_type != D2_EUCLIDEAN_L2 || !sb->p_supp) return D2G_E_INVAL;
+    if (metric == D2_WORD_EMBED && (!sa->vocab_vec || sa->vocab_size <= 0)) return D2G_E_INVAL;
+    for (size_t i = 0; i < B.size; ++i)
+      if (B.h_str[i] != m) {
+        set_error("labeling: row objects of unequal support sizes in a table-cost phase");
+        return D2G_E_UNSUPPORTED;
+      }
+    a.mode = EMD_EMBED;
+    a.tm = m;
+    const double cn = max_sq_norm(sb->p_supp, B.col, dim);
+    if (metric == D2_WORD_EMBED) {
+      const int V = sa->vocab_size;
+      if (voc->src != sa->vocab_vec || voc->V != V || voc->d != dim) {
+        *voc = DevVocab();
+        int rc = upload(voc->v, sa->vocab_vec, (size_t)V * dim, st);
+        if (rc) return rc;
+        voc->src = sa->vocab_vec;
+        voc->V = V;
+        voc->d = dim;
+      }
+      if (voc->tgen != g_assign.gen || voc->tsrc != sb->p_supp) {
+        voc->T = DevMem();
+        D2G_CUDA(cudaMalloc(&voc->T.p, B.size * (size_t)V * m * sizeof(float)));
+        dim3 grid((V + 63) / 64, (m + 63) / 64, (unsigned)B.size);
+        embed_label_table<<<grid, 256, 0, st>>>(B.supp.get<double>(), m, voc->v.get<double>(), V, dim,
+                                                voc->T.get<float>());
+        D2G_CUDA(cudaGetLastError());
+        const double vn = max_sq_norm(sa->vocab_vec, V, dim);
+        voc->tscale = (float)((sqrt(cn) + sqrt(vn)) * (sqrt(cn) + sqrt(vn)));
+        voc->tgen = g_assign.gen;
+        voc->tsrc = sb->p_supp;
+      }
+      a.T32 = voc->T.get<float>();
+      a.V = V;
+      a.vocab = voc->v.get<double>();
+      a.tscale = voc->tscale;
+      a.csym = A.sym.get<int>();
+    } else {
+      // chunks of instances whose supports' table fits kTableBytes
+      const double vn = max_sq_norm(sa->p_supp, A.col, dim);
+      a.tscale = (float)((sqrt(cn) + sqrt(vn)) * (sqrt(cn) + sqrt(vn)));
+      a.csym = nullptr;
+      const std::vector<size_t> &cum = A.h_cum;
+      std::vector<size_t> order(all);
+      std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return pa[x] < pa[y]; });
+      const size_t vmax = std::max<size_t>(kTableBytes / (B.size * (size_t)m * sizeof(float)), (size_t)A.max_str);
+      size_t i = 0;
+      while (i < order.size()) {
+        const size_t base = cum[pa[order[i]]];
+        size_t j = i;
+        while (j < order.size() && cum[pa[order[j]]] + A.h_str[pa[order[j]]] - base <= vmax) ++j;
+        const size_t last = pa[order[j - 1]];
+        const int V = (int)(cum[last] + A.h_str[last] - base);
+        DevMem T;
+        D2G_CUDA(cudaMalloc(&T.p, B.size * (size_t)V * m * sizeof(float)));
+        dim3 grid((V + 63) / 64, (m + 63) / 64, (unsigned)B.size);
+        embed_label_table<<<grid, 256, 0, st>>>(B.supp.get<double>(), m, A.supp.get<double>() + base * dim,
+                                                V, dim, T.get<float>());
+        D2G_CUDA(cudaGetLastError());
+        EmdArgs c = a;
+        c.T32 = T.get<float>();
+        c.V = V;
+        c.vocab = A.supp.get<double>() + base * dim;
+        c.key_off = base;
+        if (c.nmax > 8192 || emd_slice(c.nmax, c.mode, c.dim) > 220 * 1024) {
+          set_error("labeling: a pair too large for one warp's shared memory");
+          return D2G_E_UNSUPPORTED;
+        }
+        c.max_piv = 64 * c.nmax + 1024;
+        std::vector<size_t> sel(order.begin() + i, order.begin() + j);
+        int rc = run_pairs(c, pa, pb, sel, d, st);
+        if (rc) return rc;
+        i = j;
+      }
+      return D2G_OK;
+    }
+  } else {
+    set_error("labeling: metric type without an exact-transport path (n-grams)");
+    return D2G_E_UNSUPPORTED;
+  }
+  if (a.nmax > 8192 || emd_slice(a.nmax, a.mode, a.dim) > 220 * 1024) {
+    set_error("labeling: a pair too large for one warp's shared memory");
+    return D2G_E_UNSUPPORTED;
+  }
+  a.max_piv = 64 * a.nmax + 1024;
+  return run_pairs(a, pa, pb, all, d, st);
 }
 
 // distances of pairs (A object pa[p], B object pb[p]) as d2_compute_distance
@@ -389,6 +572,7 @@ int pair_distances(mph *A, mph *B, int selected_phase, const std::vector<int> &p
   std::lock_guard<std::mutex> lk(g_assign.mu);
   if (cache_a && g_assign.data.size() < (size_t)A->s_ph) g_assign.data.resize(A->s_ph);
   if (g_assign.tables.size() < (size_t)A->s_ph) g_assign.tables.resize(A->s_ph);
+  if (g_assign.vocab.size() < (size_t)A->s_ph) g_assign.vocab.resize(A->s_ph);
   for (int n = 0; n < A->s_ph; ++n) {
     if (selected_phase >= 0 && n != selected_phase) continue;
     const sph *sa = A->ph + n, *sb = B->ph + n;
@@ -402,11 +586,17 @@ int pair_distances(mph *A, mph *B, int selected_phase, const std::vector<int> &p
       rc = upload_phase(sa, A->size, localA, st);
     }
     if (!rc) rc = upload_phase(sb, B->size, devB, st);
-    if (!rc) rc = phase_pairs(sa, *dA, sb, devB, &g_assign.tables[n], pa, pb, out, st);
+    if (!rc) rc = phase_pairs(sa, *dA, sb, devB, &g_assign.tables[n], &g_assign.vocab[n], pa, pb, out, st);
     if (rc) return rc;
   }
   for (size_t p = 0; p < np; ++p) out[p] = out[p] <= 0.0 ? 0.0 : sqrt(out[p]);
   return D2G_OK;
+}
+
+// a public call starts: tables built for earlier centroids are stale
+void new_call() {
+  std::lock_guard<std::mutex> lk(g_assign.mu);
+  ++g_assign.gen;
 }
 
 double wall_seconds() {
@@ -493,6 +683,7 @@ void elkan_apply(ElkanInst &s, double d, double *L, double *U, char *r) {
 
 extern "C" int d2g_compute_distances(mph *a, mph *b, int selected_phase, size_t npairs,
                                      const int *ia, const int *jb, double *out) {
+  new_call();
   if (!a || !b || (npairs && (!ia || !jb || !out))) return D2G_E_INVAL;
   std::vector<int> pa(ia, ia + npairs), pb(jb, jb + npairs);
   for (size_t p = 0; p < npairs; ++p)
@@ -507,6 +698,7 @@ extern "C" int d2g_compute_distances(mph *a, mph *b, int selected_phase, size_t 
 
 extern "C" int d2g_labeling(mph *p_data, mph *centroids, var_mph *var_work, int selected_phase,
                             size_t *count_out, double *cost_out) {
+  new_call();
   if (!p_data || !centroids || !var_work || !p_data->label) return D2G_E_INVAL;
   const size_t size = p_data->size, k = centroids->size;
   if (k == 0) return D2G_E_INVAL;
@@ -548,6 +740,7 @@ extern "C" int d2g_labeling(mph *p_data, mph *centroids, var_mph *var_work, int 
 
 extern "C" int d2g_labeling_prep(mph *p_data, mph *centroids, var_mph *var_work, int selected_phase,
                                  size_t *count_out, size_t *dist_count_out) {
+  new_call();
   if (!p_data || !centroids || !var_work || !p_data->label) return D2G_E_INVAL;
   trieq *tr = &var_work->tr;
   if (!tr->l || !tr->u || !tr->s || !tr->c || !tr->r) return D2G_E_INVAL;
@@ -629,6 +822,7 @@ extern "C" int d2g_labeling_prep(mph *p_data, mph *centroids, var_mph *var_work,
 
 extern "C" int d2g_labeling_post(mph *p_data, mph *c_old, mph *c_new, var_mph *var_work,
                                  int selected_phase) {
+  new_call();
   if (!p_data || !c_old || !c_new || !var_work || !p_data->label) return D2G_E_INVAL;
   trieq *tr = &var_work->tr;
   if (!tr->l || !tr->u || !tr->r) return D2G_E_INVAL;

@@ -241,7 +241,7 @@ void set_error(const std::string &msg);
 int cuda_fail(cudaError_t e, const char *what);
 
 // exact transport (emd_kernel.cu): one warp per (row object, column object) pair
-enum EmdMode { EMD_EUCLID = 0, EMD_TABLE = 1 };
+enum EmdMode { EMD_EUCLID = 0, EMD_TABLE = 1, EMD_EMBED = 2 };
 struct EmdArgs {
   int mode, dim;
   // rows: weights, first support and support count per object (cum/str may
@@ -259,11 +259,17 @@ struct EmdArgs {
   int cfix;
   const double *csupp;
   const int *csym;
-  // table costs T[key_row * V + key_col] (EMD_TABLE); tscale >= every |T|
+  // table costs T[key_row * V + key_col] (EMD_TABLE); tscale >= every |T|.
+  // EMD_EMBED: row objects are Euclidean (rsupp), column objects word ids
+  // (csym) into vocab [V * dim]; FP32 costs T32[row object][word][row support]
+  // with row-support stride tm
   const float *T32;
   const double *T64;
   int V;
   float tscale;
+  const double *vocab;
+  int tm;
+  size_t key_off;  // EMD_EMBED without csym: column key = global support index - key_off
   const int *prow, *pcol;  // the pairs
   long long npairs;
   double *out;             // exact cost per pair

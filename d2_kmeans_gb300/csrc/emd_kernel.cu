@@ -106,6 +106,9 @@ struct Prob {
   EmdWarp w;
   int n, m, N, NM;
   size_t r0, c0;  // first support of the row / column object
+  // FP32 table view (tables, embeddings): cost(key_i, key_j) = tb[key_i * sR + key_j * sC]
+  const float *tb;
+  int sR, sC;
 
   // FP32 cost in the difference form, from the staged (centred) supports
   __device__ inline float c32(int i, int j) const {
@@ -120,14 +123,18 @@ struct Prob {
       return s;
     } else {
       const int ki = __float_as_int(w.dat[2 * i]), kj = __float_as_int(w.dat[2 * (n + j)]);
-      return __ldg(a->T32 + (size_t)ki * a->V + kj);
+      return __ldg(tb + (size_t)ki * sR + (size_t)kj * sC);
     }
   }
-  // FP64 cost, the reference's difference form (_dpdist2, blas_like64.c:199-208)
+  // FP64 cost, the reference's difference form (_dpdist2 / _dpdist2_sym,
+  // blas_like64.c:199-220)
   __device__ inline double c64(int i, int j) const {
-    if constexpr (MODE == EMD_EUCLID) {
+    if constexpr (MODE == EMD_EUCLID || MODE == EMD_EMBED) {
       const int d = a->dim;
-      const double *x = a->rsupp + (r0 + i) * d, *y = a->csupp + (c0 + j) * d;
+      const double *x = a->rsupp + (r0 + i) * d;
+      const double *y = MODE == EMD_EUCLID
+                            ? a->csupp + (c0 + j) * d
+                            : a->vocab + (size_t)__float_as_int(w.dat[2 * (n + j)]) * d;
       double s = 0.0;
       for (int t = 0; t < d; ++t) {
         const double v = __ldg(x + t) - __ldg(y + t);
@@ -290,7 +297,7 @@ __device__ inline NodeV load_node(const float *dat, int x) {
 
 // reduced cost of the cell (row node data r, column node data c)
 template <int MODE, int DP>
-__device__ inline float rcost(const NodeV &r, const NodeV &c, const EmdArgs *a) {
+__device__ inline float rcost(const NodeV &r, const NodeV &c, const Prob<MODE, DP> &P) {
   if constexpr (MODE == EMD_EUCLID) {
     if constexpr (DP == 4) {
       const float dot = fmaf(r.a.x, c.a.x, fmaf(r.a.y, c.a.y, r.a.z * c.a.z));
@@ -306,7 +313,7 @@ __device__ inline float rcost(const NodeV &r, const NodeV &c, const EmdArgs *a) 
       return fmaf(-2.f, dot, r.b.w + c.b.w);
     }
   } else {
-    const float t = __ldg(a->T32 + (size_t)__float_as_int(r.a.x) * a->V + __float_as_int(c.a.x));
+    const float t = __ldg(P.tb + (size_t)__float_as_int(r.a.x) * P.sR + (size_t)__float_as_int(c.a.x) * P.sC);
     return t - r.a.y - c.a.y;
   }
 }
@@ -323,7 +330,7 @@ __device__ Best price32(const Prob<MODE, DP> &P, int lane, int map) {
       const bool ok = i < n;
       const NodeV r = load_node<MODE, DP>(dat, ok ? i : 0);
       for (int j = 0; j < m; ++j) {
-        const float v = rcost<MODE, DP>(r, load_node<MODE, DP>(dat, n + j), P.a);
+        const float v = rcost<MODE, DP>(r, load_node<MODE, DP>(dat, n + j), P);
         if (ok && v < b.v) {
           b.v = v;
           b.idx = i * m + j;
@@ -335,7 +342,7 @@ __device__ Best price32(const Prob<MODE, DP> &P, int lane, int map) {
       const bool ok = j < m;
       const NodeV c = load_node<MODE, DP>(dat, n + (ok ? j : 0));
       for (int i = 0; i < n; ++i) {
-        const float v = rcost<MODE, DP>(load_node<MODE, DP>(dat, i), c, P.a);
+        const float v = rcost<MODE, DP>(load_node<MODE, DP>(dat, i), c, P);
         if (ok) better(b, v, i * m + j);
       }
     }
@@ -343,7 +350,7 @@ __device__ Best price32(const Prob<MODE, DP> &P, int lane, int map) {
     int i = lane / m, j = lane - (lane / m) * m;
     const int di = 32 / m, dj = 32 - di * m;
     while (i < n) {
-      const float v = rcost<MODE, DP>(load_node<MODE, DP>(dat, i), load_node<MODE, DP>(dat, n + j), P.a);
+      const float v = rcost<MODE, DP>(load_node<MODE, DP>(dat, i), load_node<MODE, DP>(dat, n + j), P);
       if (v < b.v) {
         b.v = v;
         b.idx = i * m + j;
@@ -383,7 +390,7 @@ __device__ Best price64(const Prob<MODE, DP> &P, int lane, double tol, float sca
   int i = lane / m, j = lane - (lane / m) * m;
   const int di = 32 / m, dj = 32 - di * m;
   while (i < n) {
-    const float r32 = rcost<MODE, DP>(load_node<MODE, DP>(dat, i), load_node<MODE, DP>(dat, n + j), P.a);
+    const float r32 = rcost<MODE, DP>(load_node<MODE, DP>(dat, i), load_node<MODE, DP>(dat, n + j), P);
     if (r32 < thr) {
       const double r = P.c64(i, j) - P.w.p64[i] - P.w.p64[n + j];
       const int c = i * m + j;
@@ -669,6 +676,15 @@ __global__ void __launch_bounds__(kEmdWarps * 32, 3) emd_kernel(const __grid_con
     P.N = N;
     P.r0 = r0;
     P.c0 = c0;
+    if constexpr (MODE == EMD_TABLE) {
+      P.tb = a.T32;
+      P.sR = a.V;
+      P.sC = 1;
+    } else if constexpr (MODE == EMD_EMBED) {  // T[row object][word][row support]
+      P.tb = a.T32 + (size_t)ro * a.V * a.tm;
+      P.sR = 1;
+      P.sC = a.tm;
+    }
     // stage weights (p64) and supports (centred on the rows' mean, FP32) or
     // table keys; the cost scale bounds every cell's cost
     float scale;
@@ -720,7 +736,10 @@ __global__ void __launch_bounds__(kEmdWarps * 32, 3) emd_kernel(const __grid_con
         const size_t g = row ? r0 + x : c0 + (x - n);
         w.p64[x] = __ldg((row ? a.rw : a.cw) + g);
         const int *sym = row ? a.rsym : a.csym;
-        const int key = sym ? __ldg(sym + g) : (row ? x : x - n);
+        // keys: bin / word ids, else the support's index in its object (rows,
+        // tables) or its global index less key_off (embedding-mode columns)
+        const int key = sym ? __ldg(sym + g)
+                            : (row ? x : (MODE == EMD_EMBED ? (int)(g - a.key_off) : x - n));
         w.dat[2 * x] = __int_as_float(key);
         w.dat[2 * x + 1] = 0.f;
       }
@@ -829,6 +848,7 @@ cudaError_t launch_emd(const EmdArgs &a, cudaStream_t st) {
     if (a.dim <= 7) return launch_emd_t<EMD_EUCLID, 8>(a, st);
     return cudaErrorInvalidValue;
   }
+  if (a.mode == EMD_EMBED) return launch_emd_t<EMD_EMBED, 0>(a, st);
   return launch_emd_t<EMD_TABLE, 0>(a, st);
 }
 

@@ -7,7 +7,7 @@
  * with every transport cost from d2o_emd (emd_oracle.c) where the reference
  * calls MOSEK through d2_match_by_distmat.  Same loops, same order, same
  * comparisons; the printing and the time_budget side effect are left out.
- * Metric types: Euclidean, histogram, sparse histogram.
+ * Metric types: Euclidean, histogram, sparse histogram, word embeddings.
  */
 #include <float.h>
 #include <math.h>
@@ -40,6 +40,22 @@ static double distance(const mph *a, size_t i, const mph *b, size_t j, int selec
         break;
       case D2_HISTOGRAM: /* the phase's dist_mat, as is (:88-95) */
         for (size_t e = 0; e < (size_t)nr * nc; ++e) C[e] = as->dist_mat[e];
+        break;
+      case D2_WORD_EMBED: /* _dpdist2_sym (blas_like64.c:210-220) */
+        for (int c = 0; c < nc; ++c) {
+          const int sym = as->p_supp_sym[ca + c];
+          for (int r = 0; r < nr; ++r) {
+            double s = 0.0;
+            for (int t = 0; t < dim; ++t) {
+              const double b = bs->p_supp[(rb + r) * dim + t];
+              if (sym < 0)
+                s += b * b;
+              else
+                s += (b - as->vocab_vec[(size_t)sym * dim + t]) * (b - as->vocab_vec[(size_t)sym * dim + t]);
+            }
+            C[(size_t)c * nr + r] = s;
+          }
+        }
         break;
       case D2_SPARSE_HISTOGRAM: /* _dpdist2_submat (blas_like64.c:222-230) */
         for (int c = 0; c < nc; ++c)

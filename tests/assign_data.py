@@ -4,6 +4,8 @@ import numpy as np
 
 from d2_kmeans_gb300.assign import EUCLIDEAN, HISTOGRAM, SPARSE_HISTOGRAM, Mph, Work
 
+WORD_EMBED = 7
+
 
 def euclid_phase(rng, n, dim, lo, hi, k, m, spread=3.0):
     """instances: supports around k cluster means; centroids: m supports near each mean"""
@@ -134,3 +136,25 @@ def oracle_clustering(oracle_mod, data_phases, cent_phases, n, k, label, max_ite
     if use_triangle:
         lab.labeling(data, cents, work)
     return data.label.copy(), cents, it
+
+
+def embed_phase(rng, n, k, V, dim, m, lo=3, hi=30):
+    """word-embedding instances (distinct word ids, Dirichlet weights) over a
+    Gaussian vocabulary; centroids with m supports in R^dim near topic words"""
+    vocab = rng.normal(size=(V, dim))
+    topics = [rng.choice(V, V // k, replace=False) for _ in range(k)]
+    p_str = rng.integers(lo, hi + 1, size=n).astype(np.int32)
+    lab = rng.integers(0, k, size=n)
+    sym, w = [], []
+    for i, s in enumerate(p_str):
+        pool = topics[lab[i]] if rng.random() < 0.8 and s <= V // k else np.arange(V)
+        sym.append(rng.choice(pool, s, replace=False))
+        w.append(rng.dirichlet(np.ones(s)))
+    data = dict(metric=WORD_EMBED, dim=dim, str=m, p_str=p_str, p_w=np.concatenate(w),
+                p_supp_sym=np.concatenate(sym).astype(np.int32), vocab_vec=vocab.reshape(-1),
+                vocab_size=V)
+    c_supp = np.concatenate([vocab[rng.choice(topics[j], m, replace=False)] + rng.normal(size=(m, dim)) * 0.3
+                             for j in range(k)])
+    c_w = np.concatenate([rng.dirichlet(np.ones(m)) for _ in range(k)])
+    cent = dict(metric=EUCLIDEAN, dim=dim, str=m, p_w=c_w, p_supp=c_supp.reshape(-1))
+    return data, cent

@@ -104,6 +104,25 @@ def test_histograms(port, sparse):
     rounds(port, [dph], [cph], 80, 4, label, 2, rng, prep=True)
 
 
+def test_word_embeddings(port):
+    """word-embedding phases: FP32 costs from the (centroid, word) table, FP64
+    check against the vocabulary"""
+    rng = np.random.default_rng(12)
+    dph, cph = AD.embed_phase(rng, 120, 5, 300, 24, 8, lo=3, hi=60)
+    label = rng.integers(-1, 5, size=120)
+    rounds(port, [dph], [cph], 120, 5, label, 3, rng, prep=True)
+    rounds(port, [dph], [cph], 120, 5, label, 1, rng, prep=False)
+
+
+def test_high_dimensional_euclidean(port):
+    """Euclidean supports of d = 12 (beyond the direct-cost kernel's 7): costs
+    through a (centroid support, instance support) table"""
+    rng = np.random.default_rng(13)
+    d0, c0 = AD.euclid_phase(rng, 100, 12, 2, 20, 4, 6)
+    label = rng.integers(-1, 4, size=100)
+    rounds(port, [d0], [c0], 100, 4, label, 3, rng, prep=True)
+
+
 def test_plain_config_shape(port):
     """n = 2 000 instances, d = 3, m_i 4-16, k = 10, m = 16: every label and
     the cost against the oracle."""
@@ -143,7 +162,7 @@ def test_unsupported_metric_is_refused(port):
     from d2_kmeans_gb300._lib import D2GError
     rng = np.random.default_rng(8)
     d0, c0 = AD.euclid_phase(rng, 10, 3, 2, 5, 2, 3)
-    d0 = dict(d0, metric=7)  # word embeddings: no exact-transport path here
+    d0 = dict(d0, metric=6)  # n-grams: no exact-transport path here
     dg, cg = AD.build([d0], [c0], 10, 2, np.zeros(10, int))
     with pytest.raises(D2GError):
         assign.labeling(dg, cg, Work(10, 2, 1))

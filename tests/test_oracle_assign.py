@@ -87,6 +87,13 @@ def test_selected_phase(both):
     run_both(both, dph, cph, 120, 5, label, rounds=2, rng=rng, selected_phase=1)
 
 
+def test_word_embeddings(both):
+    rng = np.random.default_rng(6)
+    dph, cph = AD.embed_phase(rng, 60, 4, 80, 6, 5)
+    label = rng.integers(-1, 4, size=60)
+    run_both(both, [dph], [cph], 60, 4, label, rounds=2, rng=rng, prep=True)
+
+
 @pytest.mark.parametrize("sparse", [False, True])
 def test_histograms(both, sparse):
     rng = np.random.default_rng(5)
