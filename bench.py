@@ -410,12 +410,44 @@ def assign_leg():
     ref = np.array([lab.distance(ds, i, cents, j) for i, j in zip(ia.reshape(-1), jb.reshape(-1))])
     t_cpu = time.perf_counter() - t
     rel = float(np.max(np.abs(ours - ref) / np.maximum(np.abs(ref), 1e-300)))
+    # word embeddings: the embedding workload's shape at 1/10 (2 000 documents
+    # of 20-400 words x 20 centroids of m = 64 in R^300)
+    pe, ce, _ = synth.workload("embed", seed=0, scale=0.1)
+    ne, ke, me, de, V = len(pe["p_str"]), int(pe["num_of_labels"]), int(pe["str"]), int(pe["dim"]), int(pe["vocab_size"])
+
+    def emb_mph(cnt):
+        col = int(pe["p_str"][:cnt].sum())
+        return Mph([dict(metric=7, dim=de, str=me, p_str=pe["p_str"][:cnt], p_w=pe["p_w"][:col],
+                         p_supp_sym=pe["p_supp_sym"][:col], vocab_vec=pe["vocab_vec"], vocab_size=V)],
+                   cnt, label=pe["label"][:cnt].copy(), num_of_labels=ke)
+
+    de_m = emb_mph(ne)
+    ce_m = Mph([dict(metric=0, dim=de, str=me, p_w=ce["c_w"], p_supp=ce["c_supp"])], ke, num_of_labels=ke)
+    assign.labeling(de_m, ce_m, Work(ne, ke, 1))
+    de_m.label[:] = pe["label"]
+    t = time.perf_counter()
+    assign.labeling(de_m, ce_m, Work(ne, ke, 1))
+    t_emb = time.perf_counter() - t
+    es = emb_mph(5)
+    ia, jb = np.meshgrid(np.arange(5), np.arange(ke), indexing="ij")
+    ours_e = assign.compute_distances(es, ce_m, ia.reshape(-1), jb.reshape(-1))
+    t = time.perf_counter()
+    ref_e = np.array([lab.distance(es, i, ce_m, j) for i, j in zip(ia.reshape(-1), jb.reshape(-1))])
+    t_cpu_e = time.perf_counter() - t
+    embed = {"workload": "word embeddings: 2000 documents (20-400 Zipf(1.1) words of V=20000 x 300) x "
+                         "20 centroids (m=64)",
+             "value": ne * ke / t_emb, "unit": "transport problems/s", "seconds": t_emb,
+             "check": {"pairs": int(ref_e.size),
+                       "max_rel_err_vs_oracle": float(np.max(np.abs(ours_e - ref_e) / np.abs(ref_e)))},
+             "cpu_baseline": {"value": ref_e.size / t_cpu_e, "unit": "transport problems/s", "cores": 1,
+                              "kind": "port", "sample": f"5 documents x {ke} centroids, oracle exact solver"}}
     return {"workload": ASSIGN_WORKLOAD, "value": n * k / t_lab, "unit": "transport problems/s",
             "labeling_s": t_lab, "first_call_s": first, "labels_changed": int(changed),
             "mean_cost": cost / n,
             "prep": {"seconds": t_prep, "distances": int(dist2), "labels_changed": int(changed2),
                      "problems_per_s": dist2 / t_prep},
             "check": {"pairs": int(ours.size), "max_rel_err_vs_oracle": rel},
+            "embed": embed,
             "cpu_baseline": {"value": ref.size / t_cpu, "unit": "transport problems/s", "cores": 1,
                              "kind": "port",
                              "sample": f"{sample} instances x {k} centroids with the oracle's exact "
