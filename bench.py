@@ -444,8 +444,14 @@ def assign_leg():
     # whole k-means rounds (d2g_clustering, pruned labeling + B-ADMM update
     # with the reference's options {100, 2.0, 10}) from the workload's
     # centroids; the update's time budget held fixed
+    import ctypes
+    from d2_kmeans_gb300 import _lib as L
     from d2_kmeans_gb300 import badmm
     old = badmm.set_config(keep_time_budget=1)
+    opt = L.BADMM_options.in_dll(L.load(), "badmm_clu_options")
+    opt.maxIters, opt.rhoCoeff, opt.updatePerLoops = 100, 2.0, 10
+    ctypes.c_void_p.in_dll(L.load(), "p_badmm_options").value = ctypes.addressof(opt)
+    ctypes.c_double.in_dll(L.load(), "time_budget").value = 1e300
     data_r = data_mph(n)
     cents_r = cent_mph(c["c_w"].copy(), c["c_supp"].copy())
     t = time.perf_counter()
