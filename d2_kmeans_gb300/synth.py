@@ -13,7 +13,7 @@ from __future__ import annotations
 
 import numpy as np
 
-EUCLIDEAN, HISTOGRAM, WORD_EMBED, SPARSE_HISTOGRAM = 0, 5, 7, 12
+EUCLIDEAN, HISTOGRAM, N_GRAM, WORD_EMBED, SPARSE_HISTOGRAM = 0, 5, 6, 7, 12
 
 # weights below this are lifted before re-normalising; the reference's reader
 # asserts w > 1e-9 for non-histogram phases (clustering_io.c:145)
@@ -135,6 +135,55 @@ def embed_phase(n, k, m, V=20000, dim=300, sizes=(20, 400), zipf=1.1, seed=0, vo
     return phase, dict(c_w=c_w.reshape(-1), c_supp=c_supp.reshape(-1))
 
 
+def symbol_cost(V=20, seed=0):
+    """Symmetric symbol-to-symbol cost with a zero diagonal, in half units like
+    a substitution-matrix distance: squared distances of V random points in R^5."""
+    rng = np.random.default_rng(seed)
+    p = rng.normal(size=(V, 5))
+    d = ((p[:, None, :] - p[None, :, :]) ** 2).sum(-1)
+    return np.round(2.0 * d) / 2.0
+
+
+def ngram_phase(n, k, m, dim=3, V=20, lengths=(30, 400), families=16, seed=0, dist=None):
+    """Sequences over V symbols as n-gram distributions (D2_N_GRAM).
+
+    Each sequence has a log-uniform length and draws its symbols i.i.d. from
+    one of ``families`` symbol distributions (Dirichlet(0.5)); its supports
+    are its distinct dim-grams (symbols in [0, V)) weighted by their counts,
+    normalised to 1, ordered by decreasing count like the reference's protein
+    n-gram files.  Centroid supports start at m n-grams drawn from the data.
+    """
+    rng = np.random.default_rng(seed)
+    if dist is None:
+        dist = symbol_cost(V, seed + 500)
+    fam = rng.dirichlet(np.full(V, 0.5), size=families)
+    lo, hi = lengths
+    L = np.clip(np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi + 1), size=n))), max(lo, dim), hi)
+    p_str, syms, ws = [], [], []
+    radix = V ** np.arange(dim - 1, -1, -1)
+    for i in range(n):
+        seq = rng.choice(V, size=int(L[i]), p=fam[rng.integers(families)])
+        grams = np.lib.stride_tricks.sliding_window_view(seq, dim)
+        code, cnt = np.unique(grams @ radix, return_counts=True)
+        order = np.argsort(-cnt, kind="stable")
+        code, cnt = code[order], cnt[order]
+        tup = (code[:, None] // radix[None, :]) % V
+        p_str.append(len(code))
+        syms.append(tup.reshape(-1))
+        ws.append(cnt / cnt.sum())
+    p_str = np.asarray(p_str, np.int32)
+    p_supp_sym = np.concatenate(syms).astype(np.int32)
+    p_w = np.concatenate(ws)
+    label = _labels(rng, n, k)
+    pick = rng.integers(0, int(p_str.sum()), size=k * m)
+    c_sym = p_supp_sym.reshape(-1, dim)[pick].reshape(-1)
+    c_w = rng.dirichlet(np.ones(m), size=k)
+    phase = dict(metric=N_GRAM, dim=dim, str=m, p_str=p_str, p_w=p_w, p_supp_sym=p_supp_sym,
+                 dist_mat=dist.reshape(-1), vocab_size=V, label=label, num_of_labels=k,
+                 label_switch=np.ones(n, np.int8))
+    return phase, dict(c_w=c_w.reshape(-1), c_supp=None, c_sym=c_sym.astype(np.int32))
+
+
 def serving_centroids(k=256, m=64, dim=64, n_comp=32, seed=0):
     rng = np.random.default_rng(seed)
     pts, means = _gmm(rng, k * m, dim, n_comp)
@@ -174,6 +223,9 @@ def workload(name: str, seed: int = 0, scale: float = 1.0):
         return ph, c, dict(maxIters=100, rhoCoeff=2.0, updatePerLoops=10)
     if name == "hist":           # phase 1 of the two-phase set: 256-bin histograms, k=32
         ph, c = histogram_phase(N(100000), 32, 16, 0.1, seed)
+        return ph, c, dict(maxIters=100, rhoCoeff=2.0, updatePerLoops=10)
+    if name == "ngram":          # sequences as 3-grams over 20 symbols, k=64, m=32
+        ph, c = ngram_phase(N(20000), 64, 32, 3, 20, (30, 400), 16, seed)
         return ph, c, dict(maxIters=100, rhoCoeff=2.0, updatePerLoops=10)
     if name == "twophase_euclid":  # phase 2: d=3, m_i 4..32, k=32, m=16
         ph, c = euclidean_phase(N(100000), 32, 16, 3, (4, 32), False, 10, 1.0, seed + 7)

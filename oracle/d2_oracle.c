@@ -11,7 +11,11 @@
  *   cnorm / rnorm / grms / gcms    src/utils/blas_like64.c:41-56,122-154
  *   irms / rsum2                   src/utils/blas_like64.c:69-77,113-119
  *   calculate_distmat              src/d2/centroid_util.c:8-36
- *   histogram cost layout          src/d2/clustering_util.c:183-198 (as intended:
+ *   pdist_symbolic (n-gram costs)  src/utils/blas_like64.c:232-242
+ *   n-gram support update          src/d2/centroid_Bregman.c:269-294 with
+ *                                  accumulate_symbolic / minimize_symbolic,
+ *                                  include/d2/centroid_util.h:15-37
+ *   histogram cost layout         src/d2/clustering_util.c:183-198 (as intended:
  *                                  the reference indexes ph[k] with an instance
  *                                  index there; this oracle uses the phase's own
  *                                  dist_mat)
@@ -22,6 +26,7 @@
 
 #include <math.h>
 #include <stdlib.h>
+#include <float.h>
 #include <string.h>
 #include <time.h>
 
@@ -65,6 +70,19 @@ static void cost_block(const d2o_phase *ph, size_t i, size_t cum, const double *
         Ci[(size_t)j * str + k] = s;
       }
     }
+  } else if (ph->metric == D2O_N_GRAM) {
+    /* centroid_util.c:31-33 -> _dpdist_symbolic, blas_like64.c:232-242: the
+     * cost of centroid support k against instance support j sums the symbol
+     * costs position by position, dist_mat[centroid symbol * V + instance symbol] */
+    const int *A = ph->c_sym + (size_t)l * str * d;
+    const int *B = ph->p_supp_sym + cum * d;
+    const int V = ph->vocab_size;
+    for (int j = 0; j < mi; ++j)
+      for (int k = 0; k < str; ++k) {
+        double s = 0;
+        for (int t = 0; t < d; ++t) s += ph->dist_mat[(size_t)A[k * d + t] * V + B[j * d + t]];
+        Ci[(size_t)j * str + k] = s;
+      }
   } else if (ph->metric == D2O_HISTOGRAM) {
     /* dense histogram: the plan's cost is the bin-to-bin matrix itself */
     for (size_t e = 0; e < (size_t)str * mi; ++e) Ci[e] = ph->dist_mat[e];
@@ -102,8 +120,10 @@ int d2o_badmm(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_s
   const int str = ph->str, dim = ph->dim, K = ph->num_of_labels;
   const size_t size = ph->size, col = ph->col, nent = (size_t)str * col;
   const int euclid = ph->metric == D2O_EUCLIDEAN_L2, embed = ph->metric == D2O_WORD_EMBED;
+  const int ngram = ph->metric == D2O_N_GRAM;
   int rc = 0, nt = 0, iter;
   if (str <= 0 || size == 0 || col == 0 || K <= 0) return -1;
+  if (ngram && (!ph->c_sym || !ph->dist_mat || ph->vocab_size < 1 || dim < 1)) return -1;
 
   size_t *cum = malloc(size * sizeof(size_t));
   double *C = malloc(nent * sizeof(double)), *X = malloc(nent * sizeof(double));
@@ -112,13 +132,19 @@ int d2o_badmm(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_s
   size_t zr_n = (size > (size_t)K ? size : (size_t)K) * str;
   double *Zr = malloc(zr_n * sizeof(double));
   size_t *count = calloc(K, sizeof(size_t));
-  if (!cum || !C || !X || !Y || !Z0 || !Xc || !Zr || !count) { rc = -1; goto done; }
+  /* n-gram support update scratch (the reference's Zr2, :127-130) */
+  double *zsym = ngram ? malloc((size_t)K * str * dim * ph->vocab_size * sizeof(double)) : NULL;
+  double *zbuf = ngram ? malloc((size_t)ph->vocab_size * sizeof(double)) : NULL;
+  if (!cum || !C || !X || !Y || !Z0 || !Xc || !Zr || !count || (ngram && (!zsym || !zbuf))) {
+    rc = -1;
+    goto done;
+  }
 
   cum[0] = 0; /* p_str_cum as built by d2_read, clustering_io.c:176-181 */
   for (size_t i = 1; i < size; ++i) cum[i] = cum[i - 1] + ph->p_str[i - 1];
 
   /* histograms: C is the cost filled by the caller at allocation (clustering_util.c:183-198) */
-  if (!euclid && !embed)
+  if (!euclid && !embed && !ngram)
     for (size_t i = 0; i < size; ++i) cost_block(ph, i, cum[i], c_supp, C + str * cum[i]);
   calc_distmat(ph, cum, c_supp, C); /* :106 */
 
@@ -221,6 +247,47 @@ int d2o_badmm(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_s
       calc_distmat(ph, cum, c_supp, C); /* :225-227 */
       for (size_t e = 0; e < nent; ++e) C[e] /= rho;
     }
+    if (iter % opt->updatePerLoops == 0 && ngram && iter > 0) { /* :269-294 */
+      /* weighted symbol counts per (cluster, support, position): the plan Z of
+       * this iteration, entries above 1e-10 only (accumulate_symbolic,
+       * include/d2/centroid_util.h:15-23), instances and supports in order */
+      const int V = ph->vocab_size;
+      const size_t sxdv = (size_t)str * dim * V;
+      for (size_t e = 0; e < sxdv * K; ++e) zsym[e] = 0;
+      for (size_t i = 0; i < size; ++i) {
+        const int mi = ph->p_str[i];
+        const int *si = ph->p_supp_sym + cum[i] * dim;
+        const double *zi = Z + str * cum[i];
+        double *z = zsym + (size_t)ph->label[i] * sxdv;
+        for (int j = 0; j < mi; ++j)
+          for (int k = 0; k < str; ++k) {
+            const double val = zi[(size_t)j * str + k];
+            if (val > 1E-10)
+              for (int t = 0; t < dim; ++t) z[(size_t)V * (dim * k + t) + si[j * dim + t]] += val;
+          }
+      }
+      /* each centroid symbol moves to the symbol of least expected cost
+       * (minimize_symbolic, centroid_util.h:25-37): zbuf = dist_mat * z as the
+       * column-major dgemm computes it (a running sum over u), first minimum */
+      for (int l = 0; l < K; ++l) {
+        const double *z = zsym + (size_t)l * sxdv;
+        for (int q = 0; q < str * dim; ++q) {
+          const double *zq = z + (size_t)q * V;
+          for (int r = 0; r < V; ++r) zbuf[r] = 0.0;
+          for (int u = 0; u < V; ++u) {
+            const double t = 1.0 * zq[u];
+            for (int r = 0; r < V; ++r) zbuf[r] += t * ph->dist_mat[(size_t)r + (size_t)u * V];
+          }
+          double mn = DBL_MAX;
+          int arg = 0;
+          for (int r = 0; r < V; ++r)
+            if (zbuf[r] < mn) { mn = zbuf[r]; arg = r; }
+          ph->c_sym[(size_t)l * str * dim + q] = arg;
+        }
+      }
+      calc_distmat(ph, cum, c_supp, C); /* :289-291 */
+      for (size_t e = 0; e < nent; ++e) C[e] /= rho;
+    }
 
     /* step 6, :300-316 */
     if ((iter % 100 == 99) || (iter < 100 && iter % 20 == 19)) {
@@ -251,6 +318,7 @@ int d2o_badmm(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_s
 done:
   if (ntrace) *ntrace = nt;
   free(cum); free(C); free(X); free(Y); free(Z0); free(Xc); free(Zr); free(count);
+  free(zsym); free(zbuf);
   return rc;
 }
 

@@ -29,6 +29,7 @@ extern "C" {
 /* metric codes are the reference's (include/d2/param.h:23-28) */
 #define D2O_EUCLIDEAN_L2 0
 #define D2O_HISTOGRAM 5
+#define D2O_N_GRAM 6
 #define D2O_WORD_EMBED 7
 #define D2O_SPARSE_HISTOGRAM 12
 
@@ -41,14 +42,18 @@ typedef struct {
   const int *p_str;      /* [size] support size of each instance */
   const double *p_w;     /* [col] instance weights (each instance sums to 1) */
   const double *p_supp;  /* [col*dim] Euclidean supports, row per support point */
-  const int *p_supp_sym; /* [col] 0-based vocabulary / bin ids (embedding, sparse histogram) */
+  const int *p_supp_sym; /* [col] 0-based vocabulary / bin ids (embedding, sparse histogram);
+                            [col*dim] symbols, dim per support point (n-gram) */
   const double *vocab_vec; /* [vocab_size*dim] embedding vectors */
   int vocab_size;        /* vocabulary size, or number of bins for histograms */
-  const double *dist_mat;  /* [vocab_size*vocab_size] bin-to-bin cost (histograms) */
+  const double *dist_mat;  /* [vocab_size*vocab_size] bin-to-bin cost (histograms) or
+                              symbol-to-symbol cost (n-gram) */
   const int *label;      /* [size] cluster of each instance */
   int num_of_labels;     /* k */
   const char *label_switch; /* [size] 1 = re-initialise this instance's plan */
   size_t global_size;    /* N used to normalise obj/primres/dualres */
+  int *c_sym;            /* n-gram only: [k*str*dim] centroid symbols, in/out (the
+                            reference's c->p_supp_sym); NULL for other metrics */
 } d2o_phase;
 
 typedef struct {

@@ -25,7 +25,7 @@ PORT_LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libd2ref.so")
 REF_TREE = "/root/reference"
 
-METRIC = {"euclidean": 0, "histogram": 5, "embed": 7, "sparse_histogram": 12}
+METRIC = {"euclidean": 0, "histogram": 5, "ngram": 6, "embed": 7, "sparse_histogram": 12}
 
 
 class _Phase(C.Structure):
@@ -35,7 +35,7 @@ class _Phase(C.Structure):
         ("p_str", C.c_void_p), ("p_w", C.c_void_p), ("p_supp", C.c_void_p),
         ("p_supp_sym", C.c_void_p), ("vocab_vec", C.c_void_p), ("vocab_size", C.c_int),
         ("dist_mat", C.c_void_p), ("label", C.c_void_p), ("num_of_labels", C.c_int),
-        ("label_switch", C.c_void_p), ("global_size", C.c_size_t),
+        ("label_switch", C.c_void_p), ("global_size", C.c_size_t), ("c_sym", C.c_void_p),
     ]
 
 
@@ -89,7 +89,8 @@ def badmm(phase: dict, centroids: dict, opts: dict, kind: str = "port",
     ``phase`` holds the reference's d2 arrays (``p_str``, ``p_w``, ``p_supp`` or
     ``p_supp_sym`` + ``vocab_vec`` or ``dist_mat``, ``label``, ``num_of_labels``,
     ``label_switch``, ``metric``, ``dim``, ``str``); ``centroids`` holds ``c_w``
-    (k*str) and ``c_supp`` (k*str*dim) plus optionally a warm-start ``Z``.
+    (k*str) and ``c_supp`` (k*str*dim) - or, for n-gram phases, the integer
+    symbols ``c_sym`` (k*str*dim) - plus optionally a warm-start ``Z``.
     Returns the updated centroids, Z, optional X/Y/C, the obj/primres/dualres
     trace and rho.
     """
@@ -138,6 +139,10 @@ def badmm(phase: dict, centroids: dict, opts: dict, kind: str = "port",
     cs = centroids.get("c_supp")
     c_supp = (np.zeros(max(k * m * dim, 1)) if cs is None
               else np.array(cs, dtype=np.float64, copy=True).reshape(-1))
+    c_sym = None
+    if centroids.get("c_sym") is not None:
+        c_sym = np.array(centroids["c_sym"], dtype=np.int32, copy=True).reshape(-1)
+        ph.c_sym = c_sym.ctypes.data
     Z = centroids.get("Z")
     Z = np.zeros(m * col) if Z is None else np.array(Z, dtype=np.float64, copy=True).reshape(-1)
     outs = {n: (np.empty(m * col) if n in want else None) for n in ("X", "Y", "C")}
@@ -150,7 +155,7 @@ def badmm(phase: dict, centroids: dict, opts: dict, kind: str = "port",
     rc = fn(C.byref(ph), C.byref(op), c_w.ctypes.data, c_supp.ctypes.data, Z.ctypes.data,
             _ptr(outs["X"]), _ptr(outs["Y"]), _ptr(outs["C"]), trace.ctypes.data,
             C.addressof(ntrace), C.addressof(rho), C.addressof(iters))
-    res = {"rc": rc, "c_w": c_w, "c_supp": c_supp, "Z": Z,
+    res = {"rc": rc, "c_w": c_w, "c_supp": c_supp, "c_sym": c_sym, "Z": Z,
            "trace": trace[: 4 * ntrace.value].reshape(-1, 4), "rho": rho.value,
            "iters": iters.value}
     res.update({n: v for n, v in outs.items() if v is not None})

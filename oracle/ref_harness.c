@@ -96,6 +96,7 @@ int d2r_badmm(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_s
   c.col = (size_t)K * str;
   c.p_w = c_w;
   c.p_supp = c_supp;
+  c.p_supp_sym = ph->c_sym; /* n-gram centroids: symbols, updated in place */
   c.metric_type = ph->metric % D2_GROUP_SIZE; /* clustering.c:390 */
   c.vocab_size = ph->vocab_size;
   c.vocab_vec = (double *)ph->vocab_vec;

@@ -48,6 +48,8 @@ def load_golden(name):
         elif k.startswith("meta_"):
             ph[k[5:]] = z[k].item()
     c0 = {"c_w": z["c0_w"], "c_supp": z["c0_supp"] if "c0_supp" in z.files else None}
+    if "c0_sym" in z.files:
+        c0["c_sym"] = z["c0_sym"]
     o = z["opts"]
     opts = dict(maxIters=int(o[0]), rhoCoeff=float(o[1]), updatePerLoops=int(o[2]))
     exp = {k: z[k] for k in z.files if k.startswith("out_") or k.startswith("first_")}

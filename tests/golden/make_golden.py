@@ -50,6 +50,41 @@ def read_simple():
     return np.array(w).reshape(-1, nb), np.array(h[1:1 + nb * nb]).reshape(nb, nb)
 
 
+def read_protein_1gram(limit):
+    """The first `limit` sequences of the reference's protein 1-gram file
+    (data/protein_seq/protein_1gram.dat) with its PAM250 symbol cost
+    (PAM250_distmat.dat), parsed as data/protein_seq/d2_protein_ngram.cc:71-150
+    reads them: letters keyed in the cost file's order, weights re-normalised.
+    Sequences holding a gap support ("--") are skipped: the reference's reader
+    drops the last weight slot for a gap and leaves the gap's symbol slot
+    unwritten, so those sequences have no well-defined input."""
+    base = os.path.join(REF_DATA, "protein_seq")
+    with open(os.path.join(base, "PAM250_distmat.dat")) as f:
+        head = f.readline()
+        keys = [ch for ch in head if "A" <= ch <= "Z"]
+        D = np.array(f.read().split()[: len(keys) ** 2], dtype=np.float64)
+    key = {ch: i for i, ch in enumerate(keys)}
+    toks = open(os.path.join(base, "protein_1gram.dat")).read().split()
+    pos = 6  # "Seq # N Class # C"
+    p_str, w, sym = [], [], []
+    while len(p_str) < limit:
+        pos += 2  # name, class
+        dim, n = int(toks[pos]), int(toks[pos + 1])
+        pos += 2
+        ww = np.array(toks[pos:pos + n], dtype=np.float64)
+        pos += n
+        grams = toks[pos:pos + n]
+        pos += n
+        if any("-" in g for g in grams):
+            continue
+        assert dim == 1 and all(len(g) == 1 and g in key for g in grams)
+        p_str.append(n)
+        w.extend(ww / ww.sum())
+        sym.extend(key[g] for g in grams)
+    return (np.array(p_str, np.int32), np.array(w), np.array(sym, np.int32),
+            D.reshape(len(keys), len(keys)))
+
+
 def cases():
     out = {}
     ph, c = synth.euclidean_phase(300, 6, 16, 3, (4, 16), False, 10, 1.0, seed=11)
@@ -69,6 +104,26 @@ def cases():
               num_of_labels=2, label_switch=np.ones(n, np.int8))
     c = dict(c_w=np.full(2 * nb, 1.0 / nb), c_supp=None)
     out["simple_kat"] = (ph, c, dict(maxIters=100, rhoCoeff=2.0, updatePerLoops=10))
+    # n-gram phases: synthetic 3-grams and 2-grams (support update / check collision)
+    ph, c = synth.ngram_phase(150, 5, 12, 3, 20, (20, 80), 6, seed=16)
+    out["ngram_small"] = (ph, c, dict(maxIters=60, rhoCoeff=2.0, updatePerLoops=10))
+    ph, c = synth.ngram_phase(100, 4, 8, 2, 12, (10, 50), 4, seed=17)
+    out["ngram_collide"] = (ph, c, dict(maxIters=40, rhoCoeff=2.0, updatePerLoops=3))
+    # the reference's protein 1-gram sequences with PAM250 costs, the protein
+    # app's B-ADMM options (d2_protein_ngram.cc:383-386) and centroid size 20
+    p_str, w, sym, D = read_protein_1gram(400)
+    rng = np.random.default_rng(18)
+    k, m = 8, 20
+    label = rng.integers(0, k, size=p_str.size).astype(np.int32)
+    label[:k] = np.arange(k)
+    ph = dict(metric=6, dim=1, str=m, p_str=p_str, p_w=w, p_supp_sym=sym, dist_mat=D.reshape(-1),
+              vocab_size=D.shape[0], label=label, num_of_labels=k,
+              label_switch=np.ones(p_str.size, np.int8))
+    c = dict(c_w=rng.dirichlet(np.ones(m), size=k).reshape(-1), c_supp=None,
+             c_sym=sym[rng.integers(0, sym.size, size=k * m)].astype(np.int32))
+    out["protein_kat"] = (ph, c, dict(maxIters=60, rhoCoeff=1.0, updatePerLoops=60))
+    ph2 = dict(ph)
+    out["protein_upd10"] = (ph2, c, dict(maxIters=40, rhoCoeff=1.0, updatePerLoops=10))
     return out
 
 
@@ -82,9 +137,13 @@ def pack(name, ph, c, opts, res, extra=None):
     d["c0_w"] = np.asarray(c["c_w"]).reshape(-1)
     if c.get("c_supp") is not None:
         d["c0_supp"] = np.asarray(c["c_supp"]).reshape(-1)
+    if c.get("c_sym") is not None:
+        d["c0_sym"] = np.asarray(c["c_sym"]).reshape(-1)
     d["out_c_w"] = res["c_w"]
     if c.get("c_supp") is not None:
         d["out_c_supp"] = res["c_supp"]
+    if c.get("c_sym") is not None:
+        d["out_c_sym"] = res["c_sym"]
     d["out_trace"] = res["trace"]
     d["out_Z_digest"] = digest(res["Z"])
     if extra:
@@ -100,6 +159,8 @@ def main():
         port = oracle.badmm(ph, c, opts, "port", want=())
         assert res["rc"] == 0 and port["rc"] == 0
         assert np.array_equal(res["c_w"], port["c_w"]) and np.array_equal(res["Z"], port["Z"])
+        if c.get("c_sym") is not None:
+            assert np.array_equal(res["c_sym"], port["c_sym"])
         pack(name, ph, c, opts, res)
         print(name, "col", int(np.sum(ph["p_str"])), "trace", res["trace"][:, 1])
     # warm start: second call after a k-means reassignment of ~10% of the instances

@@ -34,13 +34,15 @@ def test_port_matches_golden_bitwise(oracle_mod, name):
     np.testing.assert_array_equal(r["c_w"], exp["out_c_w"])
     if "out_c_supp" in exp:
         np.testing.assert_array_equal(r["c_supp"], exp["out_c_supp"])
+    if "out_c_sym" in exp:
+        np.testing.assert_array_equal(r["c_sym"], exp["out_c_sym"])
     np.testing.assert_array_equal(digest(r["Z"]), exp["out_Z_digest"])
     # the reference prints the trace with %f: 6 decimals
     np.testing.assert_allclose(r["trace"][:, 1:], exp["out_trace"][:, 1:], atol=5.1e-7, rtol=0)
     np.testing.assert_array_equal(r["trace"][:, 0], exp["out_trace"][:, 0])
 
 
-@pytest.mark.parametrize("metric", ["euclidean", "hist", "embed"])
+@pytest.mark.parametrize("metric", ["euclidean", "hist", "embed", "ngram"])
 def test_port_matches_reference_build(oracle_mod, metric):
     """Bit-identical to the reference's own d2_centroid_sphBregman, all outputs."""
     if not oracle_mod.available("reference"):
@@ -51,12 +53,18 @@ def test_port_matches_reference_build(oracle_mod, metric):
     elif metric == "hist":
         ph, c = synth.histogram_phase(40, 3, side=6, alpha=0.1, seed=4)
         opts = dict(maxIters=25, rhoCoeff=2.0, updatePerLoops=10)
-    else:
+    elif metric == "embed":
         ph, c = synth.embed_phase(30, 3, 8, V=500, dim=12, sizes=(5, 40), seed=5)
         opts = dict(maxIters=25, rhoCoeff=2.0, updatePerLoops=10)
+    else:
+        ph, c = synth.ngram_phase(60, 3, 10, 3, 9, (8, 60), 4, seed=6)
+        opts = dict(maxIters=45, rhoCoeff=2.0, updatePerLoops=4)
     a = oracle_mod.badmm(ph, c, opts, "port")
     b = oracle_mod.badmm(ph, c, opts, "reference")
     assert a["rc"] == 0 and b["rc"] == 0
+    if metric == "ngram":  # the symbols moved, identically
+        assert np.any(a["c_sym"] != c["c_sym"])
+        np.testing.assert_array_equal(a["c_sym"], b["c_sym"])
     for k in ("c_w", "c_supp", "Z", "X", "Y", "C"):
         np.testing.assert_array_equal(a[k], b[k], err_msg=k)
     np.testing.assert_allclose(a["trace"][:, 1:], b["trace"][:, 1:], atol=5.1e-7, rtol=0)
