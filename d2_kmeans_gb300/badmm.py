@@ -13,7 +13,8 @@ Two ways in, both through libd2g.so's C ABI:
 A phase is described by a dict with the reference's array names (``p_str``,
 ``p_w``, ``p_supp`` or ``p_supp_sym`` + ``vocab_vec``, ``dist_mat``,
 ``label``, ``num_of_labels``, ``metric``, ``dim``, ``str``); centroids by a
-dict with ``c_w`` (k*str) and ``c_supp`` (k*str*dim).
+dict with ``c_w`` (k*str) and ``c_supp`` (k*str*dim), or for n-gram phases
+the integer symbols ``c_sym`` (k*str*dim).
 """
 from __future__ import annotations
 
@@ -50,7 +51,7 @@ def get_config() -> dict:
 
 
 def _metric(v):
-    names = {"euclidean": 0, "histogram": 5, "embed": 7, "sparse_histogram": 12}
+    names = {"euclidean": 0, "histogram": 5, "ngram": 6, "embed": 7, "sparse_histogram": 12}
     return names[v] if isinstance(v, str) else int(v)
 
 
@@ -138,7 +139,8 @@ class Phase:
     def autotune(self, centroids: dict, opts: dict) -> dict:
         """Time every candidate tuning with short runs of ``opts`` (the plans
         are restored afterwards), keep the fastest; returns the chosen tuning
-        and the candidates with their loop times in ms."""
+        and the candidates with their loop times in ms.  An n-gram phase
+        starts every trial from the symbols of its last run."""
         o = L.d2g_badmm_opts()
         o.maxIters = int(opts.get("maxIters", 20))
         o.rhoCoeff = float(opts.get("rhoCoeff", 2.0))
@@ -188,6 +190,13 @@ class Phase:
             if c_supp_out is not None:
                 c_supp[:] = np.asarray(cs).reshape(-1)
         ls = None if label_switch is None else _arr(label_switch, np.int8)
+        if self.metric == 6:  # n-gram: integer centroid symbols
+            c_sym = np.array(centroids["c_sym"], np.int32).reshape(-1)
+            L.check(self.lib.d2g_badmm_run_sym(self.h, C.byref(o), c_w.ctypes.data, c_sym.ctypes.data,
+                                               None if ls is None else ls.ctypes.data),
+                    "d2g_badmm_run_sym")
+            return {"c_w": c_w, "c_supp": None, "c_sym": c_sym, "trace": self.trace(),
+                    "stats": self.stats()}
         L.check(self.lib.d2g_badmm_run(self.h, C.byref(o), c_w.ctypes.data,
                                        None if c_supp is None else c_supp.ctypes.data,
                                        None if ls is None else ls.ctypes.data), "d2g_badmm_run")
@@ -250,6 +259,8 @@ class DropIn:
         self.c_w = np.array(centroids["c_w"], np.float64).reshape(-1)
         cs = centroids.get("c_supp")
         self.c_supp = None if cs is None else np.array(cs, np.float64).reshape(-1)
+        sy = centroids.get("c_sym")
+        self.c_sym = None if sy is None else np.array(sy, np.int32).reshape(-1)
         c = L.sph()
         c.dim = dim
         c.str = m
@@ -261,6 +272,10 @@ class DropIn:
         c.p_w = self.c_w.ctypes.data_as(C.POINTER(C.c_double))
         c.p_supp = (None if self.c_supp is None
                     else self.c_supp.ctypes.data_as(C.POINTER(C.c_double)))
+        c.p_supp_sym = (None if self.c_sym is None
+                        else self.c_sym.ctypes.data_as(C.POINTER(C.c_int)))
+        c.vocab_size = ph.vocab_size
+        c.dist_mat = ph.dist_mat
         c.metric_type = ph.metric_type % 7
         self.c = c
         # work: C sized as d2_allocate_work does (clustering_util.c:179)
@@ -329,6 +344,6 @@ def centroid_sphBregman(phase: dict, centroids: dict, opts: dict, Z=None, label_
         rc = d.call(opts, label_switch)
         L.check(rc, "d2_centroid_sphBregman")
         return {"c_w": d.c_w.copy(), "c_supp": None if d.c_supp is None else d.c_supp.copy(),
-                "Z": d.Z()}
+                "c_sym": None if d.c_sym is None else d.c_sym.copy(), "Z": d.Z()}
     finally:
         d.close()

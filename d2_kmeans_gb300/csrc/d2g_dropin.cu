@@ -208,7 +208,8 @@ int centroid_update(mph *p_data, var_mph *var_work, int idx_ph, sph *c0, sph *c)
   bo.rhoCoeff = o->rhoCoeff;
   bo.updatePerLoops = o->updatePerLoops;
   bo.time_budget = time_budget;
-  rc = d2g_badmm_run(s.ph, &bo, c->p_w, c->p_supp, ls);
+  rc = dp->metric_type == D2_N_GRAM ? d2g_badmm_run_sym(s.ph, &bo, c->p_w, c->p_supp_sym, ls)
+                                    : d2g_badmm_run(s.ph, &bo, c->p_w, c->p_supp, ls);
   if (rc) return rc;
   rc = d2g_phase_get_plans(s.ph, bw->Z);
   if (rc) return rc;
@@ -257,14 +258,14 @@ extern "C" int d2_centroid_sphBregman(mph *p_data, var_mph *var_work, int idx_ph
 }
 
 extern "C" void calculate_distmat(sph *data_ph, int *label, size_t size, sph *c, double *C) {
-  // centroid_util.c:8-36: histogram costs are fixed (nothing to do), n-grams unsupported
+  // centroid_util.c:8-36: histogram costs are fixed (nothing to do)
   if (!data_ph || !label || !c || !C || size == 0) {
     d2g::set_error("calculate_distmat: bad arguments");
     return;
   }
   const int mt = data_ph->metric_type;
   if (mt == D2_HISTOGRAM || mt == D2_SPARSE_HISTOGRAM) return;
-  if (mt != D2_EUCLIDEAN_L2 && mt != D2_WORD_EMBED) {
+  if (mt != D2_EUCLIDEAN_L2 && mt != D2_WORD_EMBED && mt != D2_N_GRAM) {
     d2g::set_error("calculate_distmat: unsupported metric type");
     return;
   }
@@ -272,5 +273,5 @@ extern "C" void calculate_distmat(sph *data_ph, int *label, size_t size, sph *c,
   for (size_t i = 0; i < size; ++i) K = std::max(K, (size_t)(label[i] + 1));
   d2g::distmat_fp64(data_ph->dim, c->str, size, data_ph->p_str, mt, data_ph->p_supp,
                     data_ph->p_supp_sym, data_ph->vocab_vec, data_ph->vocab_size, label, c->p_supp,
-                    K, C);
+                    K, C, data_ph->dist_mat, c->p_supp_sym);
 }

@@ -14,8 +14,10 @@
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "d2g_internal.cuh"
@@ -133,12 +135,21 @@ struct d2g_phase {
   DBuf<unsigned char> def_iter;          // per iteration: 1 if it ran deferred
   std::vector<unsigned char> h_def_iter;
 
-  // ---- word-embedding phase (batched form)
-  std::vector<int> h_sym;  // token id per reference column
+  // ---- word-embedding and n-gram phases (batched form): per-cluster cost tables
+  int ntab = 0;            // table rows per cluster: vocabulary size, or distinct n-gram tuples
+  std::vector<int> h_sym;  // table row (token id / tuple id) per reference column
   DBuf<float> vocab32, vnorm, cnorm, cs32f, W, epart;
   DBuf<float> vsplit, csplit;  // TF32 hi / lo tiles of the vocabulary and of the centroids
   DBuf<int> pair_key, pair_ptr, occ_col;
   int npairs = 0, echunk = 0, enchunk = 0;
+
+  // ---- n-gram phase (both forms)
+  std::vector<int> h_nsym;        // [col*dim] instance symbols (host copy)
+  std::vector<int> h_tup;         // [U*dim] distinct instance tuples (batched)
+  std::vector<int> h_csym;        // centroid symbols of the last run (autotuner start point)
+  DBuf<int> ntup, csym, nkey, nptr, nocc;
+  DBuf<double> ndist, ncnt;
+  int nlists = 0;
 
   // ---- plain form
   DBuf<double> pC, pX, pY, pZ, pZ0, pw, psupp, pvocab, pdist, pzr, pxmom;
@@ -236,7 +247,7 @@ static bool batched_supported(const d2g_phase_desc *d, std::string *why) {
     return true;
   }
   if (d->metric_type == D2_HISTOGRAM || d->metric_type == D2_SPARSE_HISTOGRAM) return true;
-  if (d->metric_type == D2_WORD_EMBED) return d->dim >= 1;
+  if (d->metric_type == D2_WORD_EMBED || d->metric_type == D2_N_GRAM) return d->dim >= 1;
   *why = "metric type";
   return false;
 }
@@ -418,7 +429,8 @@ static PlanArgs base_args(d2g_phase *ph) {
   a.cw32 = ph->cw32.p;
   a.cs32 = ph->cs32.p;
   a.ctab = ph->ctab.p;
-  a.ctab_lstride = ph->metric == D2_WORD_EMBED ? (long long)ph->vocab_size * ph->MP : 0;
+  const bool tables = ph->metric == D2_WORD_EMBED || ph->metric == D2_N_GRAM;
+  a.ctab_lstride = tables ? (long long)ph->ntab * ph->MP : 0;
   a.rowsum_out = ph->rowsum.p;
   a.xmom_out = ph->xmom.p;
   a.X_out = ph->Xp.p;
@@ -431,7 +443,7 @@ static PlanArgs base_args(d2g_phase *ph) {
   a.plan_slot = ph->plan_slot.p;
   a.rowpart = ph->rowpart.p;
   a.rowsc = ph->rowsc.p;
-  a.col_crow = ph->metric == D2_WORD_EMBED ? ph->col_crow.p : ph->col_sym.p;
+  a.col_crow = tables ? ph->col_crow.p : ph->col_sym.p;
   a.stage_costs = ph->stage_costs;
   a.wide = ph->nwide > 0;
   return a;
@@ -447,6 +459,48 @@ static PlanArgs bucket_args(d2g_phase *ph, const PlanArgs &base, const d2g_phase
 }
 
 // ---------------------------------------------------------- labels / lists
+// Occurrence lists of an n-gram phase's support update: for every key
+// (label * dim + t) * V + v, the columns whose symbol at position t is v, in
+// increasing column order (packed columns in the batched form, reference
+// columns in the plain form, so that the plain form adds in the reference's
+// order).  col_label[c] < 0 marks a padding column; col_ref[c] is the column's
+// reference column (its symbols).
+static int build_ngram_lists(d2g_phase *ph, const std::vector<int> &col_label,
+                             const std::vector<long long> &col_ref) {
+  const int V = ph->vocab_size, dim = ph->dim;
+  const size_t nkeys = (size_t)ph->K * dim * V, nc = col_label.size();
+  if (nkeys >= (size_t)INT_MAX || nc * (size_t)dim >= (size_t)INT_MAX || nc >= (size_t)INT_MAX)
+    return fail(D2G_E_UNSUPPORTED, "n-gram phase too large for 32-bit occurrence lists");
+  std::vector<int> cnt(nkeys + 1, 0);
+  for (size_t c = 0; c < nc; ++c) {
+    if (col_label[c] < 0) continue;
+    const int *x = ph->h_nsym.data() + (size_t)col_ref[c] * dim;
+    for (int t = 0; t < dim; ++t) ++cnt[((size_t)col_label[c] * dim + t) * V + x[t] + 1];
+  }
+  std::vector<int> keys, ptr(1, 0);
+  for (size_t k = 0; k < nkeys; ++k)
+    if (cnt[k + 1]) {
+      keys.push_back((int)k);
+      ptr.push_back(ptr.back() + cnt[k + 1]);
+    }
+  for (size_t k = 1; k <= nkeys; ++k) cnt[k] += cnt[k - 1];
+  std::vector<int> occ(ptr.back());
+  for (size_t c = 0; c < nc; ++c) {
+    if (col_label[c] < 0) continue;
+    const int *x = ph->h_nsym.data() + (size_t)col_ref[c] * dim;
+    for (int t = 0; t < dim; ++t) occ[cnt[((size_t)col_label[c] * dim + t) * V + x[t]]++] = (int)c;
+  }
+  ph->nlists = (int)keys.size();
+  D2G_CUDA(ph->nkey.alloc(keys.size()));
+  D2G_CUDA(ph->nptr.alloc(ptr.size()));
+  D2G_CUDA(ph->nocc.alloc(occ.size()));
+  D2G_CUDA(cudaMemcpyAsync(ph->nkey.p, keys.data(), keys.size() * 4, cudaMemcpyHostToDevice, ph->st));
+  D2G_CUDA(cudaMemcpyAsync(ph->nptr.p, ptr.data(), ptr.size() * 4, cudaMemcpyHostToDevice, ph->st));
+  D2G_CUDA(cudaMemcpyAsync(ph->nocc.p, occ.data(), occ.size() * 4, cudaMemcpyHostToDevice, ph->st));
+  D2G_CUDA(cudaStreamSynchronize(ph->st));
+  return D2G_OK;
+}
+
 static int set_labels_impl(d2g_phase *ph, const int *label) {
   const size_t n = ph->size;
   for (size_t i = 0; i < n; ++i)
@@ -539,17 +593,82 @@ static int set_labels_impl(d2g_phase *ph, const int *label) {
       D2G_CUDA(cudaMemcpyAsync(ph->occ_col.p, occ.data(), occ.size() * 4, cudaMemcpyHostToDevice, ph->st));
       D2G_CUDA(cudaStreamSynchronize(ph->st));
     }
+    if (ph->metric == D2_N_GRAM) {
+      // per packed column: its cost-table row label * U + tuple (0 in pad
+      // columns), its label and reference column for the occurrence lists
+      const int U = ph->ntab;
+      std::vector<int> crow(ph->ncols_packed, 0), clab(ph->ncols_packed, -1);
+      std::vector<long long> cref(ph->ncols_packed, 0);
+      for (size_t gi = 0; gi < ph->h_grp_rec.size(); ++gi) {
+        const int p = gplan[gi];
+        const int nv = ph->h_grp_rec[gi].w & 15;
+        const int jj0 = (int)(gi - ph->h_grp_rec[gi].y) * ph->geo.S;
+        const long long c0 = ph->cum[ph->plan_inst[p]];
+        for (int s2 = 0; s2 < nv; ++s2) {
+          const size_t pc = gi * ph->geo.S + s2;
+          crow[pc] = pl[p] * U + ph->h_sym[c0 + jj0 + s2];
+          clab[pc] = pl[p];
+          cref[pc] = c0 + jj0 + s2;
+        }
+      }
+      if ((size_t)ph->K * U >= (size_t)INT_MAX) return fail(D2G_E_UNSUPPORTED, "n-gram table too large");
+      D2G_CUDA(ph->col_crow.alloc(crow.size()));
+      D2G_CUDA(cudaMemcpyAsync(ph->col_crow.p, crow.data(), crow.size() * 4, cudaMemcpyHostToDevice, ph->st));
+      int rc = build_ngram_lists(ph, clab, cref);
+      if (rc) return rc;
+    }
     D2G_CUDA(ph->grp_rec.alloc(ph->h_grp_rec.size()));
     D2G_CUDA(cudaMemcpyAsync(ph->grp_rec.p, ph->h_grp_rec.data(), ph->h_grp_rec.size() * sizeof(int4),
                              cudaMemcpyHostToDevice, ph->st));
   } else {
     D2G_CUDA(cudaMemcpyAsync(ph->plabel.p, label, n * 4, cudaMemcpyHostToDevice, ph->st));
+    if (ph->metric == D2_N_GRAM) {  // lists over the reference columns, in order
+      std::vector<int> clab(ph->col);
+      std::vector<long long> cref(ph->col);
+      for (size_t i = 0; i < n; ++i)
+        for (int j = 0; j < ph->p_str[i]; ++j) {
+          clab[ph->cum[i] + j] = label[i];
+          cref[ph->cum[i] + j] = ph->cum[i] + j;
+        }
+      int rc = build_ngram_lists(ph, clab, cref);
+      if (rc) return rc;
+    }
   }
   D2G_CUDA(cudaStreamSynchronize(ph->st));
   return D2G_OK;
 }
 
 // ------------------------------------------------------------------ create
+// n-gram phases: number the distinct instance tuples in order of first
+// appearance (h_tup), map every reference column to its tuple (h_sym)
+static void number_tuples(d2g_phase *ph) {
+  const int dim = ph->dim, V = ph->vocab_size;
+  const size_t col = ph->col;
+  ph->h_sym.resize(col);
+  ph->h_tup.clear();
+  const int *x = ph->h_nsym.data();
+  if (dim * std::log2((double)V) < 62.0) {  // tuples as base-V integers
+    std::unordered_map<unsigned long long, int> id;
+    id.reserve(1024);
+    for (size_t c = 0; c < col; ++c) {
+      unsigned long long code = 0;
+      for (int t = 0; t < dim; ++t) code = code * (unsigned long long)V + (unsigned long long)x[c * dim + t];
+      auto it = id.emplace(code, (int)id.size());
+      if (it.second) ph->h_tup.insert(ph->h_tup.end(), x + c * dim, x + c * dim + dim);
+      ph->h_sym[c] = it.first->second;
+    }
+  } else {
+    std::map<std::vector<int>, int> id;
+    for (size_t c = 0; c < col; ++c) {
+      std::vector<int> key(x + c * dim, x + c * dim + dim);
+      auto it = id.emplace(key, (int)id.size());
+      if (it.second) ph->h_tup.insert(ph->h_tup.end(), key.begin(), key.end());
+      ph->h_sym[c] = it.first->second;
+    }
+  }
+  ph->ntab = (int)(ph->h_tup.size() / dim);
+}
+
 // per-column data: reference layout -> staging -> packed FP32 (+ histogram cost table)
 static int upload_columns_batched(d2g_phase *ph, const d2g_phase_desc *d) {
   const bool euc = ph->metric == D2_EUCLIDEAN_L2;
@@ -563,6 +682,20 @@ static int upload_columns_batched(d2g_phase *ph, const d2g_phase_desc *d) {
   if (ph->metric == D2_SPARSE_HISTOGRAM || ph->metric == D2_WORD_EMBED) {
     D2G_CUDA(tsym.alloc(ph->col));
     D2G_CUDA(cudaMemcpyAsync(tsym.p, d->p_supp_sym, ph->col * 4, cudaMemcpyHostToDevice, ph->st));
+  }
+  if (ph->metric == D2_N_GRAM) {  // packed columns carry their tuple's table row
+    ph->h_nsym.assign(d->p_supp_sym, d->p_supp_sym + ph->col * ph->dim);
+    number_tuples(ph);
+    D2G_CUDA(tsym.alloc(ph->col));
+    D2G_CUDA(cudaMemcpyAsync(tsym.p, ph->h_sym.data(), ph->col * 4, cudaMemcpyHostToDevice, ph->st));
+    D2G_CUDA(ph->ntup.alloc(ph->h_tup.size()));
+    D2G_CUDA(cudaMemcpyAsync(ph->ntup.p, ph->h_tup.data(), ph->h_tup.size() * 4, cudaMemcpyHostToDevice,
+                             ph->st));
+    const size_t VV = (size_t)ph->vocab_size * ph->vocab_size;
+    D2G_CUDA(ph->ndist.alloc(VV));
+    D2G_CUDA(cudaMemcpyAsync(ph->ndist.p, d->dist_mat, VV * 8, cudaMemcpyHostToDevice, ph->st));
+    D2G_CUDA(ph->ctab.alloc((size_t)ph->K * ph->ntab * ph->MP));
+    D2G_CUDA(cudaStreamSynchronize(ph->st));
   }
   PlanArgs base = base_args(ph);
   for (auto &b : ph->buckets) {
@@ -586,7 +719,8 @@ static int upload_columns_batched(d2g_phase *ph, const d2g_phase_desc *d) {
     D2G_CUDA(ph->csplit.alloc(tf32_split_floats(ph->K * ph->str, ph->dim, 128)));
     ph->h_sym.assign(d->p_supp_sym, d->p_supp_sym + ph->col);
     D2G_CUDA(cudaStreamSynchronize(ph->st));
-  } else if (!euc) {  // histogram cost table: row v = cost from bin v to every centroid bin
+  } else if (ph->metric == D2_HISTOGRAM || ph->metric == D2_SPARSE_HISTOGRAM) {
+    // histogram cost table: row v = cost from bin v to every centroid bin
     const int V = ph->vocab_size;
     std::vector<float> t((size_t)V * ph->MP, 0.f);
     for (int v = 0; v < V; ++v)
@@ -628,6 +762,7 @@ static int create_batched(d2g_phase *ph, const d2g_phase_desc *d) {
   D2G_CUDA(ph->rho_part.alloc(ph->total_blocks));
   D2G_CUDA(ph->reinit.alloc(ph->size));
   if (ph->metric == D2_WORD_EMBED) {
+    ph->ntab = d->vocab_size;
     const size_t KV = (size_t)ph->K * d->vocab_size;
     D2G_CUDA(ph->ctab.alloc(KV * ph->MP));
     D2G_CUDA(cudaMemsetAsync(ph->ctab.p, 0, KV * ph->MP * 4, ph->st));  // padded rows stay 0
@@ -638,6 +773,10 @@ static int create_batched(d2g_phase *ph, const d2g_phase_desc *d) {
     ph->enchunk = std::max(1, std::min(64, (d->vocab_size + 511) / 512));
     ph->echunk = (d->vocab_size + ph->enchunk - 1) / ph->enchunk;
     D2G_CUDA(ph->epart.alloc((size_t)ph->enchunk * ph->K * ph->MP * (d->dim + 1)));
+  }
+  if (ph->metric == D2_N_GRAM) {
+    D2G_CUDA(ph->ncnt.alloc((size_t)ph->K * ph->str * ph->dim * ph->vocab_size));
+    D2G_CUDA(ph->csym.alloc((size_t)ph->K * ph->str * ph->dim));
   }
 
   int rc2 = upload_columns_batched(ph, d);
@@ -686,6 +825,16 @@ static int upload_columns_plain(d2g_phase *ph, const d2g_phase_desc *d) {
   if (emb || ph->metric == D2_SPARSE_HISTOGRAM) {
     D2G_CUDA(ph->psym.alloc(col));
     D2G_CUDA(cudaMemcpyAsync(ph->psym.p, d->p_supp_sym, col * 4, cudaMemcpyHostToDevice, ph->st));
+  }
+  if (ph->metric == D2_N_GRAM) {  // dim symbols per column, the symbol cost, counts, centroids
+    const size_t ns = col * (size_t)ph->dim, VV = (size_t)ph->vocab_size * ph->vocab_size;
+    ph->h_nsym.assign(d->p_supp_sym, d->p_supp_sym + ns);
+    D2G_CUDA(ph->psym.alloc(ns));
+    D2G_CUDA(cudaMemcpyAsync(ph->psym.p, d->p_supp_sym, ns * 4, cudaMemcpyHostToDevice, ph->st));
+    D2G_CUDA(ph->pdist.alloc(VV));
+    D2G_CUDA(cudaMemcpyAsync(ph->pdist.p, d->dist_mat, VV * 8, cudaMemcpyHostToDevice, ph->st));
+    D2G_CUDA(ph->ncnt.alloc((size_t)ph->K * ph->str * ph->dim * ph->vocab_size));
+    D2G_CUDA(ph->csym.alloc((size_t)ph->K * ph->str * ph->dim));
   }
   if (emb) {
     D2G_CUDA(ph->pvocab.alloc((size_t)ph->vocab_size * ph->dim));
@@ -743,6 +892,7 @@ static PlainArgs plain_args(d2g_phase *ph, int iter) {
   a.vocab = ph->pvocab.p;
   a.dist = ph->pdist.p;
   a.sym = ph->psym.p;
+  a.csym = ph->csym.p;
   a.col_inst = ph->pcol_inst.p;
   a.p_str = ph->pp_str.p;
   a.label = ph->plabel.p;
@@ -805,7 +955,9 @@ static std::vector<unsigned long long> loop_signature(d2g_phase *ph) {
           (unsigned long long)ph->global_size, (unsigned long long)ph->cost_gemm,
           u(ph->wide.p), u(ph->def_iter.p), u(ph->rowpart.p), u(ph->rowsc.p), u(ph->col_crow.p),
           (unsigned long long)ph->stage_costs, (unsigned long long)ph->tune.ctas_per_sm,
-          (unsigned long long)ph->defer};
+          (unsigned long long)ph->defer, u(ph->ncnt.p), u(ph->csym.p), u(ph->nkey.p), u(ph->nptr.p),
+          u(ph->nocc.p), (unsigned long long)ph->nlists, u(ph->ntup.p), u(ph->ndist.p),
+          (unsigned long long)ph->ntab};
 }
 
 static bool has_collision(int maxIters, int upl) {
@@ -844,17 +996,45 @@ static EmbedArgs embed_args(d2g_phase *ph, int iter) {
   return e;
 }
 
+static NgramArgs ngram_args(d2g_phase *ph, int iter) {
+  NgramArgs g{};
+  const bool b = ph->path == 0;
+  g.key = ph->nkey.p;
+  g.ptr = ph->nptr.p;
+  g.occ = ph->nocc.p;
+  g.nlists = ph->nlists;
+  g.Z32 = b ? ph->Z.p : nullptr;
+  g.Z64 = b ? nullptr : ph->pZ.p;
+  g.zstride = b ? ph->MP : ph->str;
+  g.cnt = ph->ncnt.p;
+  g.dist = b ? ph->ndist.p : ph->pdist.p;
+  g.csym = ph->csym.p;
+  g.tup = ph->ntup.p;
+  g.T = ph->ctab.p;
+  g.ctl = ph->ctl.p;
+  g.iter = iter;
+  g.K = ph->K;
+  g.m = ph->str;
+  g.dim = ph->dim;
+  g.V = ph->vocab_size;
+  g.U = ph->ntab;
+  g.MP = ph->MP;
+  return g;
+}
+
 // ------------------------------------------------------------- the loop
 static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long long *launches,
                         double *plan_ms, int *plan_timed) {
   const bool euc = ph->metric == D2_EUCLIDEAN_L2, emb = ph->metric == D2_WORD_EMBED;
+  const bool ng = ph->metric == D2_N_GRAM;
   int chk_idx = 0;
   long long nl = 0;
   std::vector<cudaEvent_t> evs, tevs;  // plan launches, cost-table launches (profile mode)
   if (ph->path == 0) {
     PlanArgs base = base_args(ph);
     for (int it = 0; it <= maxIters; ++it) {
-      const bool upd = (it % upl == 0) && (euc || emb);
+      // n-gram supports move from the second update iteration on (:270)
+      const bool upd = (it % upl == 0) && (euc || emb || (ng && it > 0));
       const bool chk = is_check_iter(it);
       const bool collide = upd && chk;
       int flags = (upd && euc ? PF_UPDATE : 0) | (chk ? PF_CHECK : 0) |
@@ -910,6 +1090,11 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
         }
         nl += 6;
       }
+      if (upd && ng) {  // step 5 of an n-gram phase from this iteration's Z, then the new table
+        D2G_CUDA(launch_ngram_support(ngram_args(ph, it), ph->st));
+        D2G_CUDA(launch_ngram_table(ngram_args(ph, it), ph->st));
+        nl += 3;
+      }
       if (collide) {
         for (auto &b : ph->buckets) {
           PlanArgs a = bucket_args(ph, base, b);
@@ -938,7 +1123,7 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
   } else {
     const unsigned nb = plain_check_blocks((long long)ph->col * ph->str);
     for (int it = 0; it <= maxIters; ++it) {
-      const bool upd = (it % upl == 0) && (euc || emb);
+      const bool upd = (it % upl == 0) && (euc || emb || (ng && it > 0));
       const bool chk = is_check_iter(it);
       PlainArgs a = plain_args(ph, it);
       if (profile) {
@@ -949,8 +1134,9 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
         evs.push_back(e1);
         cudaEventRecord(e0, ph->st);
       }
-      D2G_CUDA(plain_iter_steps(a, upd, ph->st));
-      D2G_CUDA(launch_cluster_reduce(cluster_args(ph, it, upd), ph->st));
+      D2G_CUDA(plain_iter_steps(a, upd && !ng, ph->st));
+      D2G_CUDA(launch_cluster_reduce(cluster_args(ph, it, upd && !ng), ph->st));
+      if (upd && ng) D2G_CUDA(launch_ngram_support(ngram_args(ph, it), ph->st));
       if (upd) D2G_CUDA(plain_cost(a, ph->st));
       if (chk) {
         D2G_CUDA(plain_check(a, ph->st));
@@ -959,7 +1145,7 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
         ++chk_idx;
       }
       if (profile) cudaEventRecord(evs.back(), ph->st);
-      nl += plain_launches_per_iter(upd, chk);
+      nl += ng ? plain_launches_per_iter(false, chk) + (upd ? 3 : 0) : plain_launches_per_iter(upd, chk);
     }
   }
   if (profile) {
@@ -988,15 +1174,21 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
 }
 
 static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, double *c_supp,
-                    const char *label_switch) {
+                    int *c_sym, const char *label_switch) {
   const d2g_config cfg = cfg_snapshot();
   apply_tuning(ph);
   if (!opt || opt->maxIters < 0 || opt->updatePerLoops <= 0 || !(opt->rhoCoeff > 0) || !c_w)
     return fail(D2G_E_INVAL, "bad B-ADMM options");
   const bool euc = ph->metric == D2_EUCLIDEAN_L2, emb = ph->metric == D2_WORD_EMBED;
+  const bool ng = ph->metric == D2_N_GRAM;
   if ((euc || emb) && !c_supp) return fail(D2G_E_INVAL, "c_supp required for this metric");
   const int K = ph->K, m = ph->str, dim = ph->dim;
   const size_t n = ph->size;
+  if (ng) {
+    if (!c_sym) return fail(D2G_E_INVAL, "centroid symbols required for an n-gram phase");
+    for (size_t q = 0; q < (size_t)K * m * dim; ++q)
+      if (c_sym[q] < 0 || c_sym[q] >= ph->vocab_size) return fail(D2G_E_INVAL, "centroid symbol out of range");
+  }
 
   // re-initialisation flags (per plan)
   std::vector<char> re(n, 1);
@@ -1018,6 +1210,8 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
     D2G_CUDA(ph->cs64.alloc((size_t)K * m * dim));
     D2G_CUDA(cudaMemcpyAsync(ph->cs64.p, c_supp, (size_t)K * m * dim * 8, cudaMemcpyHostToDevice, ph->st));
   }
+  if (ng)
+    D2G_CUDA(cudaMemcpyAsync(ph->csym.p, c_sym, (size_t)K * m * dim * 4, cudaMemcpyHostToDevice, ph->st));
   ph->max_checks = opt->maxIters / 20 + 8;
   D2G_CUDA(ph->trace.alloc((size_t)4 * ph->max_checks));
   D2G_CUDA(ph->ctl.alloc(1));
@@ -1030,7 +1224,7 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
   D2G_CUDA(cudaMemcpyAsync(ph->ctl.p, &h, sizeof h, cudaMemcpyHostToDevice, ph->st));
 
   long long launches = 0;
-  if (ph->path == 0 && (euc || emb) && has_collision(opt->maxIters, opt->updatePerLoops))
+  if (ph->path == 0 && (euc || emb || ng) && has_collision(opt->maxIters, opt->updatePerLoops))
     D2G_CUDA(ph->Xp.alloc((size_t)ph->ncols_packed * ph->MP));  // X kept for obj after step 5
   if (ph->path == 0) {
     D2G_CUDA(launch_centroid_to_f32(ph->cw64.p, euc ? ph->cs64.p : nullptr, ph->cw32.p,
@@ -1041,6 +1235,10 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
                                  ph->vnorm.p, ph->MP, ph->ctab.p, ph->cost_gemm, ph->vsplit.p,
                                  ph->csplit.p, &ph->ctl.p->err, ph->st));
       launches += 3;
+    }
+    if (ng) {  // the cost table of the initial centroid symbols
+      D2G_CUDA(launch_ngram_table(ngram_args(ph, -1), ph->st));
+      launches += 1;
     }
     PlanArgs base = base_args(ph);
     for (auto &b : ph->buckets) {
@@ -1068,7 +1266,9 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
   ph->h_def_iter.assign((size_t)opt->maxIters + 1, 0);
   if (ph->path == 0 && ph->defer) {
     for (int it = 0; it <= opt->maxIters; ++it) {
-      const bool upd = (it % opt->updatePerLoops == 0) && euc;
+      // Euclidean support updates need the moments of the same iteration, n-gram
+      // updates its final Z: those iterations exchange synchronously
+      const bool upd = (it % opt->updatePerLoops == 0) && (euc || (ng && it > 0));
       ph->h_def_iter[it] = !is_check_iter(it) && !upd;
     }
     if (ph->def_iter.n < ph->h_def_iter.size()) D2G_CUDA(ph->def_iter.alloc(ph->h_def_iter.size()));
@@ -1112,6 +1312,8 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
   D2G_CUDA(cudaMemcpyAsync(c_w, ph->cw64.p, (size_t)K * m * 8, cudaMemcpyDeviceToHost, ph->st));
   if (euc || emb)
     D2G_CUDA(cudaMemcpyAsync(c_supp, ph->cs64.p, (size_t)K * m * dim * 8, cudaMemcpyDeviceToHost, ph->st));
+  if (ng)
+    D2G_CUDA(cudaMemcpyAsync(c_sym, ph->csym.p, (size_t)K * m * dim * 4, cudaMemcpyDeviceToHost, ph->st));
   ph->h_trace.assign((size_t)4 * ph->max_checks, 0.0);
   D2G_CUDA(cudaMemcpyAsync(ph->h_trace.data(), ph->trace.p, ph->h_trace.size() * 8, cudaMemcpyDeviceToHost, ph->st));
   D2G_CUDA(cudaMemcpyAsync(&h, ph->ctl.p, sizeof h, cudaMemcpyDeviceToHost, ph->st));
@@ -1122,6 +1324,7 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
   for (int it = 0; it < h.iters_done; ++it) nchk += is_check_iter(it);
   ph->ntrace = nchk;
   ph->plans_valid = true;
+  if (ng) ph->h_csym.assign(c_sym, c_sym + (size_t)K * m * dim);
   ph->stats.iterations = h.iters_done;
   ph->stats.rho = h.rho;
   ph->stats.total_ms = ms;
@@ -1138,9 +1341,9 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
   {
     const double ent = (double)ph->col * m;
     const double colb = ph->path == 0 ? (double)ph->col * (euc ? 4.0 * (1 + dim) : 8.0) : 0.0;
-    // word-embedding costs stream from the per-cluster vocabulary table (4 B per
+    // word-embedding and n-gram costs stream from the per-cluster table (4 B per
     // entry); histogram costs come from one str x str table that stays in L2
-    ph->stats.plan_bytes = ph->path == 0 ? (emb ? 20.0 : 16.0) * ent + colb + 4.0 * m * (double)n
+    ph->stats.plan_bytes = ph->path == 0 ? ((emb || ng) ? 20.0 : 16.0) * ent + colb + 4.0 * m * (double)n
                                          : 136.0 * ent;
   }
   if (h.err == kErrTcTimeout)
@@ -1155,8 +1358,10 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
 // reference layout; backs the calculate_distmat drop-in.
 int distmat_fp64(int dim, int str, size_t size, const int *p_str, int metric, const double *supp,
                  const int *sym, const double *vocab, int V, const int *label, const double *c_supp,
-                 size_t K, double *C_host) {
-  if (dim < 1 || str < 1 || !p_str || !label || !c_supp || !C_host) return fail(D2G_E_INVAL, "distmat args");
+                 size_t K, double *C_host, const double *dist, const int *c_sym) {
+  const bool ng = metric == D2_N_GRAM;
+  if (dim < 1 || str < 1 || !p_str || !label || !C_host || (ng ? (!c_sym || !dist || !sym) : !c_supp))
+    return fail(D2G_E_INVAL, "distmat args");
   std::vector<long long> cum(size);
   long long col = 0;
   for (size_t i = 0; i < size; ++i) {
@@ -1174,20 +1379,29 @@ int distmat_fp64(int dim, int str, size_t size, const int *p_str, int metric, co
     ~Guard() { cudaStreamDestroy(s); }
   } guard{st};
   DBuf<double> dC, dS, dV, dCS;
-  DBuf<int> dSym, dCI, dL;
+  DBuf<int> dSym, dCI, dL, dCsym;
   DBuf<long long> dCum;
   const size_t nent = (size_t)col * str;
   D2G_CUDA(dC.alloc(nent));
-  D2G_CUDA(dCS.alloc(K * str * dim));
-  D2G_CUDA(cudaMemcpyAsync(dCS.p, c_supp, K * str * dim * 8, cudaMemcpyHostToDevice, st));
-  if (metric == D2_EUCLIDEAN_L2) {
-    D2G_CUDA(dS.alloc((size_t)col * dim));
-    D2G_CUDA(cudaMemcpyAsync(dS.p, supp, (size_t)col * dim * 8, cudaMemcpyHostToDevice, st));
+  if (ng) {  // symbols per column, centroid symbols, the symbol cost
+    D2G_CUDA(dSym.alloc((size_t)col * dim));
+    D2G_CUDA(cudaMemcpyAsync(dSym.p, sym, (size_t)col * dim * 4, cudaMemcpyHostToDevice, st));
+    D2G_CUDA(dCsym.alloc(K * str * dim));
+    D2G_CUDA(cudaMemcpyAsync(dCsym.p, c_sym, K * str * dim * 4, cudaMemcpyHostToDevice, st));
+    D2G_CUDA(dV.alloc((size_t)V * V));
+    D2G_CUDA(cudaMemcpyAsync(dV.p, dist, (size_t)V * V * 8, cudaMemcpyHostToDevice, st));
   } else {
-    D2G_CUDA(dSym.alloc(col));
-    D2G_CUDA(dV.alloc((size_t)V * dim));
-    D2G_CUDA(cudaMemcpyAsync(dSym.p, sym, col * 4, cudaMemcpyHostToDevice, st));
-    D2G_CUDA(cudaMemcpyAsync(dV.p, vocab, (size_t)V * dim * 8, cudaMemcpyHostToDevice, st));
+    D2G_CUDA(dCS.alloc(K * str * dim));
+    D2G_CUDA(cudaMemcpyAsync(dCS.p, c_supp, K * str * dim * 8, cudaMemcpyHostToDevice, st));
+    if (metric == D2_EUCLIDEAN_L2) {
+      D2G_CUDA(dS.alloc((size_t)col * dim));
+      D2G_CUDA(cudaMemcpyAsync(dS.p, supp, (size_t)col * dim * 8, cudaMemcpyHostToDevice, st));
+    } else {
+      D2G_CUDA(dSym.alloc(col));
+      D2G_CUDA(dV.alloc((size_t)V * dim));
+      D2G_CUDA(cudaMemcpyAsync(dSym.p, sym, col * 4, cudaMemcpyHostToDevice, st));
+      D2G_CUDA(cudaMemcpyAsync(dV.p, vocab, (size_t)V * dim * 8, cudaMemcpyHostToDevice, st));
+    }
   }
   D2G_CUDA(dCI.alloc(col));
   D2G_CUDA(dL.alloc(size));
@@ -1198,7 +1412,9 @@ int distmat_fp64(int dim, int str, size_t size, const int *p_str, int metric, co
   PlainArgs a{};
   a.C = dC.p;
   a.supp = dS.p;
-  a.vocab = dV.p;
+  a.vocab = ng ? nullptr : dV.p;
+  a.dist = ng ? dV.p : nullptr;
+  a.csym = dCsym.p;
   a.sym = dSym.p;
   a.col_inst = dCI.p;
   a.label = dL.p;
@@ -1260,10 +1476,13 @@ int d2g_phase_create(const d2g_phase_desc *d, int precision, d2g_phase **out) {
       !d->label)
     return fail(D2G_E_INVAL, "incomplete phase description");
   const int mt = d->metric_type;
-  if (mt == D2_N_GRAM || mt == D2_CITYBLOCK_L1)
+  if (mt == D2_CITYBLOCK_L1)
     return fail(D2G_E_UNSUPPORTED, "metric type " + std::to_string(mt) + " is not supported");
-  if (mt != D2_EUCLIDEAN_L2 && mt != D2_WORD_EMBED && mt != D2_HISTOGRAM && mt != D2_SPARSE_HISTOGRAM)
+  if (mt != D2_EUCLIDEAN_L2 && mt != D2_WORD_EMBED && mt != D2_HISTOGRAM && mt != D2_SPARSE_HISTOGRAM &&
+      mt != D2_N_GRAM)
     return fail(D2G_E_INVAL, "unknown metric type");
+  if (mt == D2_N_GRAM && (d->dim < 1 || !d->p_supp_sym || !d->dist_mat || d->vocab_size < 1))
+    return fail(D2G_E_INVAL, "n-gram phase needs symbols and a symbol cost matrix");
   if (mt == D2_EUCLIDEAN_L2 && (d->dim < 1 || !d->p_supp)) return fail(D2G_E_INVAL, "supports missing");
   if (mt == D2_WORD_EMBED && (d->dim < 1 || !d->p_supp_sym || !d->vocab_vec || d->vocab_size < 1))
     return fail(D2G_E_INVAL, "embedding phase needs ids and vocabulary");
@@ -1277,7 +1496,7 @@ int d2g_phase_create(const d2g_phase_desc *d, int precision, d2g_phase **out) {
 
   d2g_phase *ph = new d2g_phase();
   ph->metric = mt;
-  ph->dim = (mt == D2_EUCLIDEAN_L2 || mt == D2_WORD_EMBED) ? d->dim : 0;
+  ph->dim = (mt == D2_EUCLIDEAN_L2 || mt == D2_WORD_EMBED || mt == D2_N_GRAM) ? d->dim : 0;
   ph->str = d->str;
   ph->K = d->num_of_labels;
   ph->vocab_size = d->vocab_size;
@@ -1295,12 +1514,14 @@ int d2g_phase_create(const d2g_phase_desc *d, int precision, d2g_phase **out) {
     c += d->p_str[i];
   }
   ph->col = (size_t)c;
-  if (mt == D2_SPARSE_HISTOGRAM || mt == D2_WORD_EMBED)
-    for (size_t j = 0; j < ph->col; ++j)
+  if (mt == D2_SPARSE_HISTOGRAM || mt == D2_WORD_EMBED || mt == D2_N_GRAM) {
+    const size_t nsym = mt == D2_N_GRAM ? ph->col * (size_t)d->dim : ph->col;
+    for (size_t j = 0; j < nsym; ++j)
       if (d->p_supp_sym[j] < 0 || d->p_supp_sym[j] >= d->vocab_size) {
         delete ph;
         return fail(D2G_E_INVAL, "vocabulary id out of range");
       }
+  }
   std::string why;
   ph->path = (precision == 1 || !batched_supported(d, &why)) ? 1 : 0;
   int rc = D2G_OK;
@@ -1410,7 +1631,15 @@ int d2g_phase_get_scratch(d2g_phase *ph, double *X, double *Y, double *C) {
 int d2g_badmm_run(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, double *c_supp,
                   const char *label_switch) {
   if (!ph) return D2G_E_INVAL;
-  return run_impl(ph, opt, c_w, c_supp, label_switch);
+  if (ph->metric == D2_N_GRAM) return fail(D2G_E_INVAL, "n-gram phases run through d2g_badmm_run_sym");
+  return run_impl(ph, opt, c_w, c_supp, nullptr, label_switch);
+}
+
+int d2g_badmm_run_sym(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, int *c_sym,
+                      const char *label_switch) {
+  if (!ph) return D2G_E_INVAL;
+  if (ph->metric != D2_N_GRAM) return fail(D2G_E_INVAL, "d2g_badmm_run_sym is for n-gram phases");
+  return run_impl(ph, opt, c_w, nullptr, c_sym, label_switch);
 }
 
 int d2g_phase_get_tuning(d2g_phase *ph, d2g_tuning *t) {
@@ -1432,7 +1661,10 @@ int d2g_phase_autotune(d2g_phase *ph, const d2g_badmm_opts *opt, const double *c
                        int *n_out) {
   if (!ph || !opt || !c_w || max_out < 0) return fail(D2G_E_INVAL, "bad autotune arguments");
   const bool euc = ph->metric == D2_EUCLIDEAN_L2, emb = ph->metric == D2_WORD_EMBED;
+  const bool ng = ph->metric == D2_N_GRAM;
   if ((euc || emb) && !c_supp) return fail(D2G_E_INVAL, "c_supp required for this metric");
+  if (ng && ph->h_csym.empty())
+    return fail(D2G_E_INVAL, "an n-gram phase is tuned from the centroid symbols of its last run");
   if (n_out) *n_out = 0;
   if (ph->path != 0) return D2G_OK;  // the FP64 form has no launch-shape choices
   // candidates: every combination of the choices that apply to this phase
@@ -1457,6 +1689,8 @@ int d2g_phase_autotune(d2g_phase *ph, const d2g_badmm_opts *opt, const double *c
   }
   const size_t ncw = (size_t)ph->K * ph->str, ncs = (euc || emb) ? ncw * ph->dim : 0;
   std::vector<double> cw(ncw), cs(ncs);
+  const std::vector<int> sym0 = ph->h_csym;
+  std::vector<int> sym;
   d2g_badmm_opts o = *opt;
   o.time_budget = 0;
   std::vector<double> t(cand.size(), 1e300);
@@ -1466,7 +1700,8 @@ int d2g_phase_autotune(d2g_phase *ph, const d2g_badmm_opts *opt, const double *c
     for (int rep = 0; rep < 3 && !rc; ++rep) {  // the first run captures the graph
       std::copy(c_w, c_w + ncw, cw.begin());
       if (ncs) std::copy(c_supp, c_supp + ncs, cs.begin());
-      rc = run_impl(ph, &o, cw.data(), ncs ? cs.data() : nullptr, nullptr);
+      sym = sym0;
+      rc = run_impl(ph, &o, cw.data(), ncs ? cs.data() : nullptr, ng ? sym.data() : nullptr, nullptr);
       if (!rc && rep > 0) t[i] = std::min(t[i], ph->stats.total_ms);
     }
   }
@@ -1479,6 +1714,7 @@ int d2g_phase_autotune(d2g_phase *ph, const d2g_badmm_opts *opt, const double *c
     cudaStreamSynchronize(ph->st);
   }
   ph->plans_valid = had_plans;
+  ph->h_csym = sym0;
   if (rc) return rc;
   tune_cache_put(tune_key(ph), ph->tune);
   for (int i = 0; i < (int)cand.size() && i < max_out; ++i) {

@@ -161,6 +161,7 @@ struct PlainArgs {
   double *C, *X, *Y, *Z, *Z0;
   const double *w, *supp, *vocab, *dist;
   const int *sym, *col_inst, *p_str, *label;
+  const int *csym;          // n-gram centroid symbols [K*str*dim]
   const long long *cum;     // p_str_cum
   const char *reinit;
   double *zr;               // [size * str] row sums
@@ -231,10 +232,30 @@ cudaError_t launch_to_f32(const double *a, size_t n, float *b, cudaStream_t st);
 cudaError_t launch_embed_support(const EmbedArgs &e, cudaStream_t st);
 cudaError_t launch_embed_table(const EmbedArgs &e, cudaStream_t st);
 
+// ngram_kernels.cu (n-gram phases, both forms)
+struct NgramArgs {
+  const int *key, *ptr, *occ;  // occurrence lists: key (l*dim + t)*V + v, columns in order
+  int nlists;
+  const float *Z32;            // batched: packed plans (column stride MP), or
+  const double *Z64;           // plain: reference-layout plans (column stride str)
+  long long zstride;
+  double *cnt;                 // [K][m][dim][V] weighted symbol counts
+  const double *dist;          // [V*V] symbol cost
+  int *csym;                   // [K*m*dim] centroid symbols
+  const int *tup;              // [U*dim] distinct instance tuples (batched table)
+  float *T;                    // [K][U][MP] cost table (batched)
+  Ctl *ctl;
+  int iter, K, m, dim, V, U, MP;
+};
+// step 5: counts, then the new centroid symbols (skipped past the time budget)
+cudaError_t launch_ngram_support(const NgramArgs &g, cudaStream_t st);
+// the batched form's cost table of the current centroid symbols
+cudaError_t launch_ngram_table(const NgramArgs &g, cudaStream_t st);
+
 // d2g_host.cu
 int distmat_fp64(int dim, int str, size_t size, const int *p_str, int metric, const double *supp,
                  const int *sym, const double *vocab, int V, const int *label, const double *c_supp,
-                 size_t K, double *C_host);
+                 size_t K, double *C_host, const double *dist = nullptr, const int *c_sym = nullptr);
 
 // error helpers (d2g_host.cu)
 void set_error(const std::string &msg);

@@ -54,6 +54,13 @@ __device__ __forceinline__ double plain_cost_at(const PlainArgs &a, long long c,
     }
     return s;
   }
+  if (a.metric == D2_N_GRAM) {  // blas_like64.c:232-242
+    const int *A = a.csym + ((size_t)l * a.str + k) * a.dim;
+    const int *B = a.sym + (size_t)c * a.dim;
+    double s = 0.0;
+    for (int t = 0; t < a.dim; ++t) s += a.dist[(size_t)A[t] * a.vocab_size + B[t]];
+    return s;
+  }
   if (a.metric == D2_HISTOGRAM) {
     const long long j = c - a.cum[i];
     return a.dist[(size_t)j * a.str + k];
@@ -211,7 +218,7 @@ __global__ void plain_check_partial(const PlainArgs a) {  // :300-305
 }
 
 cudaError_t plain_cost(const PlainArgs &a, cudaStream_t st) {
-  if (a.metric == D2_EUCLIDEAN_L2 || a.metric == D2_WORD_EMBED || a.iter < 0) {
+  if (a.metric == D2_EUCLIDEAN_L2 || a.metric == D2_WORD_EMBED || a.metric == D2_N_GRAM || a.iter < 0) {
     plain_cost_kernel<<<grid_for(a.nent), kPT, 0, st>>>(a, a.iter >= 0 ? 1 : 0);
   }
   return cudaGetLastError();

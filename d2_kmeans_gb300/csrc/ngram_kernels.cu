@@ -1,0 +1,135 @@
+// N-gram phases (D2_N_GRAM): supports are tuples of `dim` symbols over an
+// alphabet of V symbols with a V x V symbol cost.
+//
+// Ground cost (src/d2/centroid_util.c:31-33 -> _dpdist_symbolic,
+// src/utils/blas_like64.c:232-242): centroid support k of cluster l against an
+// instance support with symbols x_0..x_{dim-1},
+//   C = sum_t dist[c_{l,k,t} * V + x_t].
+// The batched form numbers the distinct instance tuples u = 0..U-1 and keeps
+// one table per cluster, T[l][u][k] (FP32 of the FP64 sum), which the plan
+// kernel reads row by row exactly as it reads a word-embedding phase's table.
+//
+// Support update (src/d2/centroid_Bregman.c:269-294, every updatePerLoops
+// iterations after the first): with the plans Z of that iteration,
+//   cnt[l][k][t][v] = sum over the columns of cluster l whose symbol at
+//                     position t is v of Z[k, col]   (entries above 1e-10;
+//                     accumulate_symbolic, include/d2/centroid_util.h:15-23)
+//   c_{l,k,t}       = the first v minimising sum_u dist[v + u*V] * cnt[l][k][t][u]
+//                     (minimize_symbolic, centroid_util.h:25-37: a column-major
+//                     GEMM dist * cnt, then an argmin per column)
+// The counts run per occurrence list (cluster, position, symbol) in a fixed
+// column order, in FP64; the cost sums run over u in order with separately
+// rounded products and sums, as the reference's BLAS computes them.
+#include "d2g_internal.cuh"
+
+namespace d2g {
+
+// cnt[(l*m + k)*dim + t][v] from the list of key (l*dim + t)*V + v: one warp
+// per list, lanes over the centroid supports k.
+template <typename TZ>
+__global__ void ngram_count_kernel(const int *__restrict__ key, const int *__restrict__ ptr,
+                                   const int *__restrict__ occ, int nlists, const TZ *__restrict__ Z,
+                                   long long zstride, int m, int dim, int V, double *__restrict__ cnt,
+                                   const Ctl *ctl, int iter) {
+  if (iter >= ctl->stop_iter) return;
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= nlists) return;
+  const int kk = key[w];
+  const int v = kk % V, lt = kk / V, t = lt % dim, l = lt / dim;
+  const int b = ptr[w], e = ptr[w + 1];
+  for (int k = lane; k < m; k += 32) {
+    double s = 0.0;
+    for (int o = b; o < e; ++o) {
+      const TZ z = Z[(size_t)occ[o] * zstride + k];
+      if (z > (TZ)1E-10) s += (double)z;
+    }
+    cnt[(((size_t)l * m + k) * dim + t) * V + v] = s;
+  }
+}
+
+// one warp per (cluster, support, position) column q = (l*m + k)*dim + t;
+// lanes over candidate symbols r; the first minimum wins, as in the reference
+__global__ void ngram_min_kernel(const double *__restrict__ cnt, int ncols, int V,
+                                 const double *__restrict__ dist, int *__restrict__ csym,
+                                 const Ctl *ctl, int iter) {
+  if (iter >= ctl->stop_iter) return;
+  const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (q >= ncols) return;
+  const double *z = cnt + (size_t)q * V;
+  double best = 0.0;
+  int arg = -1;
+  for (int r = lane; r < V; r += 32) {
+    double s = 0.0;
+    for (int u = 0; u < V; ++u) s = __dadd_rn(s, __dmul_rn(z[u], dist[(size_t)r + (size_t)u * V]));
+    if (arg < 0 || s < best) {
+      best = s;
+      arg = r;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const int oa = __shfl_xor_sync(0xffffffffu, arg, o);
+    if (oa >= 0 && (arg < 0 || ob < best || (ob == best && oa < arg))) {
+      best = ob;
+      arg = oa;
+    }
+  }
+  if (lane == 0) csym[q] = arg;
+}
+
+// T[l][u][k] = sum_t dist[csym[(l*m + k)*dim + t] * V + tup[u*dim + t]] for
+// k < m, 0 in the padded rows k < MP
+__global__ void ngram_table_kernel(const int *__restrict__ csym, const int *__restrict__ tup, int U,
+                                   int K, int m, int MP, int dim, int V,
+                                   const double *__restrict__ dist, float *__restrict__ T,
+                                   const Ctl *ctl, int iter) {
+  if (iter >= ctl->stop_iter) return;
+  const long long n = (long long)K * U * MP;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(i % MP);
+    const long long lu = i / MP;
+    const int u = (int)(lu % U), l = (int)(lu / U);
+    float c = 0.f;
+    if (k < m) {
+      const int *cs = csym + ((size_t)l * m + k) * dim;
+      const int *x = tup + (size_t)u * dim;
+      double s = 0.0;
+      for (int t = 0; t < dim; ++t) s += dist[(size_t)cs[t] * V + x[t]];
+      c = (float)s;
+    }
+    T[i] = c;
+  }
+}
+
+cudaError_t launch_ngram_support(const NgramArgs &g, cudaStream_t st) {
+  const size_t ncnt = (size_t)g.K * g.m * g.dim * g.V;
+  cudaError_t e = cudaMemsetAsync(g.cnt, 0, ncnt * sizeof(double), st);
+  if (e != cudaSuccess) return e;
+  if (g.nlists > 0) {
+    const unsigned nb = (unsigned)(((long long)g.nlists * 32 + 255) / 256);
+    if (g.Z32)
+      ngram_count_kernel<float><<<nb, 256, 0, st>>>(g.key, g.ptr, g.occ, g.nlists, g.Z32, g.zstride,
+                                                    g.m, g.dim, g.V, g.cnt, g.ctl, g.iter);
+    else
+      ngram_count_kernel<double><<<nb, 256, 0, st>>>(g.key, g.ptr, g.occ, g.nlists, g.Z64, g.zstride,
+                                                     g.m, g.dim, g.V, g.cnt, g.ctl, g.iter);
+  }
+  const int ncols = g.K * g.m * g.dim;
+  ngram_min_kernel<<<(unsigned)(((long long)ncols * 32 + 255) / 256), 256, 0, st>>>(
+      g.cnt, ncols, g.V, g.dist, g.csym, g.ctl, g.iter);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ngram_table(const NgramArgs &g, cudaStream_t st) {
+  const long long n = (long long)g.K * g.U * g.MP;
+  long long nb = (n + 255) / 256;
+  if (nb > 152LL * 32) nb = 152LL * 32;
+  ngram_table_kernel<<<(unsigned)(nb < 1 ? 1 : nb), 256, 0, st>>>(g.csym, g.tup, g.U, g.K, g.m, g.MP,
+                                                                   g.dim, g.V, g.dist, g.T, g.ctl,
+                                                                   g.iter);
+  return cudaGetLastError();
+}
+
+}  // namespace d2g

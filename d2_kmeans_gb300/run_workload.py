@@ -3,7 +3,7 @@
     python -m d2_kmeans_gb300.run_workload --workload batched --scale 0.1 --iters 3
 
 Workloads (d2_kmeans_gb300.synth.workload): plain, batched, hist,
-twophase_euclid, embed.  --scale shrinks the number of instances only;
+twophase_euclid, embed, ngram.  --scale shrinks the number of instances only;
 --iters sets maxIters (the loop runs maxIters+1 iterations); --precision 1
 selects the FP64 form; --cost-gemm 1 computes the word-embedding cost table
 on FP32 CUDA cores instead of the tensor cores.  Prints the run statistics

@@ -123,11 +123,11 @@ int d2_free_work_sphBregman(var_sphBregman *var_phwork);
 /* Replaces d2_centroid_sphBregman, src/d2/centroid_Bregman.c:51-325
  * (clustering.h:226-230).  Same inputs (phase idx_ph of p_data, labels,
  * label_switch, c0 as the warm start), same outputs: c->p_w and c->p_supp
- * updated in place, the plans Z left in var_work->l_var_sphBregman[idx_ph].Z
- * for the next call's warm start.  Honours p_badmm_options (maxIters+1
- * iterations, rhoCoeff, updatePerLoops) and the global time_budget.
- * Metric types: D2_EUCLIDEAN_L2, D2_WORD_EMBED, D2_HISTOGRAM,
- * D2_SPARSE_HISTOGRAM; D2_N_GRAM returns D2G_E_UNSUPPORTED.  c0 == NULL
+ * updated in place (c->p_supp_sym for n-gram phases), the plans Z left in
+ * var_work->l_var_sphBregman[idx_ph].Z for the next call's warm start.
+ * Honours p_badmm_options (maxIters+1 iterations, rhoCoeff, updatePerLoops)
+ * and the global time_budget.  Metric types: D2_EUCLIDEAN_L2, D2_WORD_EMBED,
+ * D2_HISTOGRAM, D2_SPARSE_HISTOGRAM, D2_N_GRAM.  c0 == NULL
  * (:95-98) initialises c with d2_centroid_rands when the program links it
  * (src/d2/centroid_rand.c:161-295, found by dlsym), else returns
  * D2G_E_UNSUPPORTED.  The host X, Y
@@ -138,7 +138,8 @@ int d2_centroid_sphBregman(mph *p_data, var_mph *var_work, int idx_ph, sph *c0, 
 /* Replaces calculate_distmat, src/d2/centroid_util.c:8-36 (declared
  * include/d2/centroid_util.h:40): the per-instance str x p_str[i] ground-cost
  * blocks between each instance and its labelled centroid, written into the
- * host array C at offset str*p_str_cum[i].  Computed on the GPU in FP64. */
+ * host array C at offset str*p_str_cum[i].  Computed on the GPU in FP64
+ * (Euclidean, word-embedding and n-gram phases; histogram costs are fixed). */
 void calculate_distmat(sph *data_ph, int *label, size_t size, sph *c, double *C);
 
 /* No counterpart in the reference.  The ground costs of calculate_distmat for
@@ -195,17 +196,20 @@ const char *d2g_last_error(void);
 typedef struct d2g_phase d2g_phase;
 
 typedef struct {
-  int metric_type;          /* D2_EUCLIDEAN_L2, D2_WORD_EMBED, D2_HISTOGRAM, D2_SPARSE_HISTOGRAM */
-  int dim;                  /* support dimension (0 for histograms) */
+  int metric_type;          /* D2_EUCLIDEAN_L2, D2_WORD_EMBED, D2_HISTOGRAM, D2_SPARSE_HISTOGRAM,
+                               D2_N_GRAM */
+  int dim;                  /* support dimension (0 for histograms; n-gram length) */
   int str;                  /* centroid support size m */
   size_t size;              /* instances n */
   const int *p_str;         /* [size] */
   const double *p_w;        /* [col] */
   const double *p_supp;     /* [col*dim] Euclidean supports */
-  const int *p_supp_sym;    /* [col] 0-based ids (embedding, sparse histogram) */
+  const int *p_supp_sym;    /* [col] 0-based ids (embedding, sparse histogram);
+                               [col*dim] symbols, dim per support point (n-gram) */
   const double *vocab_vec;  /* [vocab_size*dim] embedding vectors */
-  const double *dist_mat;   /* [vocab_size*vocab_size] histogram bin cost */
-  int vocab_size;           /* vocabulary size / number of bins */
+  const double *dist_mat;   /* [vocab_size*vocab_size] histogram bin cost, or the
+                               symbol cost of an n-gram phase (row: centroid symbol) */
+  int vocab_size;           /* vocabulary size / number of bins / n-gram alphabet size */
   const int *label;         /* [size] */
   int num_of_labels;        /* k */
   size_t global_size;       /* N normalising obj/primres/dualres (0 = size) */
@@ -246,9 +250,17 @@ int d2g_phase_set_plans(d2g_phase *ph, const double *Z);
 int d2g_phase_get_plans(d2g_phase *ph, double *Z);
 /* One centroid update.  c_w [k*str] and c_supp [k*str*dim] (NULL for
  * histograms) are host arrays, read as the start point and overwritten with
- * the result.  label_switch [size] (NULL = all 1) selects plans to re-initialise. */
+ * the result.  label_switch [size] (NULL = all 1) selects plans to re-initialise.
+ * N-gram phases use d2g_badmm_run_sym. */
 int d2g_badmm_run(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, double *c_supp,
                   const char *label_switch);
+/* One centroid update of an n-gram phase (src/d2/centroid_Bregman.c:269-294):
+ * c_sym [k*str*dim] holds the centroids' symbols (the reference's
+ * c->p_supp_sym), read as the start point and overwritten with the result;
+ * every updatePerLoops iterations after the first, each centroid symbol
+ * moves to the symbol of least expected cost under the plans. */
+int d2g_badmm_run_sym(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, int *c_sym,
+                      const char *label_switch);
 /* obj/primres/dualres of the last run: 4 doubles (iter+1, obj, primres, dualres) per check */
 int d2g_phase_trace(d2g_phase *ph, double *trace, int cap, int *n);
 int d2g_phase_stats(d2g_phase *ph, d2g_run_stats *st);
@@ -374,7 +386,9 @@ int d2g_phase_set_tuning(d2g_phase *ph, const d2g_tuning *t);
  * and restored afterwards), keep the fastest on the phase and record it under
  * the phase's shape key: in this process, and in the text file named by the
  * environment variable D2G_TUNE_CACHE when set.  Phases created later with
- * the same shape start from the recorded tuning.  Up to max_out candidates
+ * the same shape start from the recorded tuning.  An n-gram phase (c_supp
+ * NULL) starts every trial from the centroid symbols of its last
+ * d2g_badmm_run_sym call.  Up to max_out candidates
  * and their loop times (ms, best of two graph replays) are written to cands /
  * ms (either may be NULL); *n_out receives the number of candidates. */
 int d2g_phase_autotune(d2g_phase *ph, const d2g_badmm_opts *opt, const double *c_w,

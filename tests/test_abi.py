@@ -74,6 +74,9 @@ def test_invalid_phase_is_rejected_without_a_gpu(lib):
     one = (C.c_int * 1)(1)
     w = (C.c_double * 1)(1.0)
     d.p_str, d.p_w, d.label = C.addressof(one), C.addressof(w), C.addressof((C.c_int * 1)(0))
+    # an n-gram phase needs its symbols and symbol cost
+    assert lib.d2g_phase_create(C.byref(d), 0, C.byref(h)) == L.D2G_E_INVAL
+    d.metric_type = 1  # D2_CITYBLOCK_L1: no B-ADMM support update in the reference either
     assert lib.d2g_phase_create(C.byref(d), 0, C.byref(h)) == L.D2G_E_UNSUPPORTED
 
 

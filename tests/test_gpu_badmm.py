@@ -10,6 +10,7 @@ Tolerances (FP32 plans + FP64 cross-plan reductions against FP64):
                                       support point (Euclidean norm over the d
                                       coordinates, floored at 1e-3 of the largest
                                       |c_k,ref| of the phase)
+  n-gram centroid symbols             identical
 The FP64 path (precision=1) is held to 1e-9.
 """
 import numpy as np
@@ -37,6 +38,9 @@ def assert_close(res, ref, k, m, fp64=False, trace_atol=0.0):
         nrm = np.linalg.norm(sr, axis=1)
         rel = (np.linalg.norm(s - sr, axis=1) / np.maximum(nrm, 1e-3 * nrm.max())).max()
         assert rel <= (1e-9 if fp64 else SUPP_TOL), f"support rel err {rel}"
+    if ref.get("c_sym") is not None:
+        np.testing.assert_array_equal(np.asarray(res["c_sym"]).reshape(-1),
+                                      np.asarray(ref["c_sym"]).reshape(-1), err_msg="c_sym")
     tr, trr = np.asarray(res["trace"]), np.asarray(ref["trace"])
     assert tr.shape == trr.shape, (tr.shape, trr.shape)
     if trr.size == 0:
@@ -48,7 +52,8 @@ def assert_close(res, ref, k, m, fp64=False, trace_atol=0.0):
 
 
 def golden_ref(exp):
-    return {"c_w": exp["out_c_w"], "c_supp": exp.get("out_c_supp"), "trace": exp["out_trace"]}
+    return {"c_w": exp["out_c_w"], "c_supp": exp.get("out_c_supp"), "c_sym": exp.get("out_c_sym"),
+            "trace": exp["out_trace"]}
 
 
 def run_phase(d2g, ph, c0, opts, precision, exp=None):
@@ -96,7 +101,7 @@ def test_dropin_matches_golden(d2g, name):
     else:
         d = d2g.DropIn(ph, c0)
         assert d.call(opts) == 0
-    res = {"c_w": d.c_w, "c_supp": d.c_supp}
+    res = {"c_w": d.c_w, "c_supp": d.c_supp, "c_sym": d.c_sym}
     Z = d.Z()
     d.close()
     ref = golden_ref(exp)
