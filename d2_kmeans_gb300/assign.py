@@ -90,7 +90,8 @@ class Mph:
                 arrs["p_supp"] = np.array(ph["p_supp"], np.float64)
                 s.p_supp = self._ptr(arrs["p_supp"], C.c_double)
             if ph.get("p_supp_sym") is not None:
-                s.p_supp_sym = self._ptr(np.ascontiguousarray(ph["p_supp_sym"], np.int32), C.c_int)
+                arrs["p_supp_sym"] = np.array(ph["p_supp_sym"], np.int32)
+                s.p_supp_sym = self._ptr(arrs["p_supp_sym"], C.c_int)
             if ph.get("dist_mat") is not None:
                 s.dist_mat = self._ptr(np.ascontiguousarray(ph["dist_mat"], np.float64), C.c_double)
             if ph.get("vocab_vec") is not None:

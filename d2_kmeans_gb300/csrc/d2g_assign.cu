@@ -213,6 +213,8 @@ namespace {
 // supports or bin ids)
 struct DevPhase {
   DevMem w, cum, str, supp, sym;
+  DevMem tup;     // n-gram phases: the distinct tuples [ntup * dim]; sym holds each support's tuple
+  int ntup = 0;
   // what the copy was made from
   const void *kw = nullptr, *ks = nullptr, *ky = nullptr;
   size_t size = 0, col = 0;
@@ -246,6 +248,19 @@ int upload_phase(const sph *s, size_t size, DevPhase &d, cudaStream_t st) {
   if (!rc) rc = upload(d.str, d.h_str.data(), size, st);
   if (!rc && s->metric_type == D2_EUCLIDEAN_L2) rc = upload(d.supp, s->p_supp, c * (size_t)s->dim, st);
   const bool symbolic = s->metric_type == D2_SPARSE_HISTOGRAM || s->metric_type == D2_WORD_EMBED;
+  if (!rc && s->metric_type == D2_N_GRAM) {
+    // number the distinct symbol tuples; every support keyed by its tuple
+    const int dim = s->dim, V = s->vocab_size;
+    if (!s->p_supp_sym || V <= 0 || dim < 1) return D2G_E_INVAL;
+    std::vector<int> key, tup;
+    d.ntup = number_tuples(s->p_supp_sym, c, dim, V, key, tup);
+    if (d.ntup < 0) {
+      set_error("labeling: an n-gram symbol outside the alphabet");
+      return D2G_E_INVAL;
+    }
+    rc = upload(d.sym, key.data(), c, st);
+    if (!rc) rc = upload(d.tup, tup.data(), tup.size(), st);
+  }
   if (!rc && symbolic) {
     if (!s->p_supp_sym || s->vocab_size <= 0) return D2G_E_INVAL;
     for (size_t e = 0; e < c; ++e)
@@ -377,9 +392,11 @@ struct AssignCache {
 AssignCache g_assign;
 
 // launch the pairs sel[] (indices into pa / pb) with the arguments a and add
-// their costs to d[]
+// their costs to d[]; an n-gram phase (ngram_dim > 0) adds 2 * cost / dim,
+// its cost per symbol counted twice (src/d2/clustering.c:112-115)
 int run_pairs(EmdArgs a, const std::vector<int> &pa, const std::vector<int> &pb,
-              const std::vector<size_t> &sel, std::vector<double> &d, cudaStream_t st) {
+              const std::vector<size_t> &sel, std::vector<double> &d, cudaStream_t st,
+              int ngram_dim = 0) {
   const size_t np = sel.size();
   if (np == 0) return D2G_OK;
   std::vector<int> qa(np), qb(np);
@@ -409,7 +426,7 @@ int run_pairs(EmdArgs a, const std::vector<int> &pa, const std::vector<int> &pb,
       set_error("labeling: a transport problem did not reach an optimal basis");
       return D2G_E_NUMERIC;
     }
-    d[sel[p]] += h[p];
+    d[sel[p]] += ngram_dim ? 2 * (h[p] / ngram_dim) : h[p];
   }
   return D2G_OK;
 }
@@ -547,8 +564,41 @@ int phase_pairs(const sph *sa, const DevPhase &A, const sph *sb, const DevPhase 
       }
       return D2G_OK;
     }
+  } else if (metric == D2_N_GRAM) {
+    // costs between the distinct centroid tuples (rows) and the distinct
+    // instance tuples (columns), _dpdist_symbolic (blas_like64.c:232-242) with
+    // the instance phase's alphabet and symbol cost
+    const int dim = sa->dim, V = sa->vocab_size;
+    if (dim < 1 || sb->dim != dim || !sa->dist_mat || V <= 0 || !sb->p_supp_sym) return D2G_E_INVAL;
+    const size_t cells = (size_t)B.ntup * A.ntup;
+    if (cells * 12 > ((size_t)4 << 30)) {
+      set_error("labeling: n-gram tuple cost table above 4 GiB");
+      return D2G_E_UNSUPPORTED;
+    }
+    DevMem dist, T64, T32;
+    int rc = upload(dist, sa->dist_mat, (size_t)V * V, st);
+    if (rc) return rc;
+    D2G_CUDA(cudaMalloc(&T64.p, cells * sizeof(double)));
+    D2G_CUDA(cudaMalloc(&T32.p, cells * sizeof(float)));
+    D2G_CUDA(launch_ngram_pair_table(B.tup.get<int>(), B.ntup, A.tup.get<int>(), A.ntup, dim, V,
+                                     dist.get<double>(), T64.get<double>(), T32.get<float>(), st));
+    double mx = 0.0;
+    for (size_t e = 0; e < (size_t)V * V; ++e) mx = std::max(mx, fabs(sa->dist_mat[e]));
+    a.mode = EMD_TABLE;
+    a.T32 = T32.get<float>();
+    a.T64 = T64.get<double>();
+    a.V = A.ntup;
+    a.tscale = (float)(dim * mx);  // bounds every tuple cost
+    a.rsym = B.sym.get<int>();
+    a.csym = A.sym.get<int>();
+    if (a.nmax > 8192 || emd_slice(a.nmax, a.mode, a.dim) > 220 * 1024) {
+      set_error("labeling: a pair too large for one warp's shared memory");
+      return D2G_E_UNSUPPORTED;
+    }
+    a.max_piv = 64 * a.nmax + 1024;
+    return run_pairs(a, pa, pb, all, d, st, dim);
   } else {
-    set_error("labeling: metric type without an exact-transport path (n-grams)");
+    set_error("labeling: metric type without an exact-transport path");
     return D2G_E_UNSUPPORTED;
   }
   if (a.nmax > 8192 || emd_slice(a.nmax, a.mode, a.dim) > 220 * 1024) {

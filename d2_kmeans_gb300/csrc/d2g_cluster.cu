@@ -104,6 +104,7 @@ struct CentroidCopy {
   std::vector<std::vector<int>> p_str;
   std::vector<std::vector<size_t>> cum;
   std::vector<std::vector<double>> w, supp;
+  std::vector<std::vector<int>> sym;
 };
 
 void copy_centroids(const mph *a, CentroidCopy &b) {
@@ -112,6 +113,7 @@ void copy_centroids(const mph *a, CentroidCopy &b) {
   b.cum.resize(a->s_ph);
   b.w.resize(a->s_ph);
   b.supp.resize(a->s_ph);
+  b.sym.resize(a->s_ph);
   for (int n = 0; n < a->s_ph; ++n) {
     const sph &s = a->ph[n];
     sph &d = b.ph[n];
@@ -126,6 +128,10 @@ void copy_centroids(const mph *a, CentroidCopy &b) {
     if (s.metric_type == D2_EUCLIDEAN_L2 && s.p_supp) {
       b.supp[n].assign(s.p_supp, s.p_supp + s.col * (size_t)s.dim);
       d.p_supp = b.supp[n].data();
+    }
+    if (s.metric_type == D2_N_GRAM && s.p_supp_sym) {  // the symbols; dist_mat is shared
+      b.sym[n].assign(s.p_supp_sym, s.p_supp_sym + s.col * (size_t)s.dim);
+      d.p_supp_sym = b.sym[n].data();
     }
   }
   b.m = *a;
@@ -196,7 +202,9 @@ int init_centroids(mph *p, mph *c, int sel) {
     d.p_str_cum = (size_t *)calloc(k, sizeof(size_t));
     d.p_w = (double *)malloc(m * sizeof(double));
     if (d.metric_type == D2_EUCLIDEAN_L2) d.p_supp = (double *)malloc(m * (size_t)s.dim * sizeof(double));
-    if (!d.p_str || !d.p_str_cum || !d.p_w || (d.metric_type == D2_EUCLIDEAN_L2 && !d.p_supp))
+    if (d.metric_type == D2_N_GRAM) d.p_supp_sym = (int *)malloc(m * (size_t)s.dim * sizeof(int));
+    if (!d.p_str || !d.p_str_cum || !d.p_w || (d.metric_type == D2_EUCLIDEAN_L2 && !d.p_supp) ||
+        (d.metric_type == D2_N_GRAM && !d.p_supp_sym))
       return D2G_E_NOMEM;
     rands(p, n, &d);
   }

@@ -14,10 +14,8 @@
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
-#include <map>
 #include <mutex>
 #include <string>
-#include <unordered_map>
 #include <vector>
 
 #include "d2g_internal.cuh"
@@ -639,36 +637,6 @@ static int set_labels_impl(d2g_phase *ph, const int *label) {
 }
 
 // ------------------------------------------------------------------ create
-// n-gram phases: number the distinct instance tuples in order of first
-// appearance (h_tup), map every reference column to its tuple (h_sym)
-static void number_tuples(d2g_phase *ph) {
-  const int dim = ph->dim, V = ph->vocab_size;
-  const size_t col = ph->col;
-  ph->h_sym.resize(col);
-  ph->h_tup.clear();
-  const int *x = ph->h_nsym.data();
-  if (dim * std::log2((double)V) < 62.0) {  // tuples as base-V integers
-    std::unordered_map<unsigned long long, int> id;
-    id.reserve(1024);
-    for (size_t c = 0; c < col; ++c) {
-      unsigned long long code = 0;
-      for (int t = 0; t < dim; ++t) code = code * (unsigned long long)V + (unsigned long long)x[c * dim + t];
-      auto it = id.emplace(code, (int)id.size());
-      if (it.second) ph->h_tup.insert(ph->h_tup.end(), x + c * dim, x + c * dim + dim);
-      ph->h_sym[c] = it.first->second;
-    }
-  } else {
-    std::map<std::vector<int>, int> id;
-    for (size_t c = 0; c < col; ++c) {
-      std::vector<int> key(x + c * dim, x + c * dim + dim);
-      auto it = id.emplace(key, (int)id.size());
-      if (it.second) ph->h_tup.insert(ph->h_tup.end(), key.begin(), key.end());
-      ph->h_sym[c] = it.first->second;
-    }
-  }
-  ph->ntab = (int)(ph->h_tup.size() / dim);
-}
-
 // per-column data: reference layout -> staging -> packed FP32 (+ histogram cost table)
 static int upload_columns_batched(d2g_phase *ph, const d2g_phase_desc *d) {
   const bool euc = ph->metric == D2_EUCLIDEAN_L2;
@@ -685,7 +653,8 @@ static int upload_columns_batched(d2g_phase *ph, const d2g_phase_desc *d) {
   }
   if (ph->metric == D2_N_GRAM) {  // packed columns carry their tuple's table row
     ph->h_nsym.assign(d->p_supp_sym, d->p_supp_sym + ph->col * ph->dim);
-    number_tuples(ph);
+    ph->ntab = number_tuples(ph->h_nsym.data(), ph->col, ph->dim, ph->vocab_size, ph->h_sym, ph->h_tup);
+    if (ph->ntab < 0) return fail(D2G_E_INVAL, "n-gram symbol out of range");
     D2G_CUDA(tsym.alloc(ph->col));
     D2G_CUDA(cudaMemcpyAsync(tsym.p, ph->h_sym.data(), ph->col * 4, cudaMemcpyHostToDevice, ph->st));
     D2G_CUDA(ph->ntup.alloc(ph->h_tup.size()));

@@ -35,6 +35,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/d2g.h"
 
@@ -251,6 +252,14 @@ struct NgramArgs {
 cudaError_t launch_ngram_support(const NgramArgs &g, cudaStream_t st);
 // the batched form's cost table of the current centroid symbols
 cudaError_t launch_ngram_table(const NgramArgs &g, cudaStream_t st);
+// the distinct tuples of count supports of dim symbols each, numbered in order
+// of first appearance: key[e] = tuple of support e, tup [ntuples * dim];
+// returns the number of tuples, or -1 for a symbol outside [0, V)
+int number_tuples(const int *sym, size_t count, int dim, int V, std::vector<int> &key,
+                  std::vector<int> &tup);
+// assignment step: T[r * Uc + c] for row tuples rt [Ur*dim], column tuples ct [Uc*dim]
+cudaError_t launch_ngram_pair_table(const int *rt, int Ur, const int *ct, int Uc, int dim, int V,
+                                    const double *dist, double *T64, float *T32, cudaStream_t st);
 
 // d2g_host.cu
 int distmat_fp64(int dim, int str, size_t size, const int *p_str, int metric, const double *supp,

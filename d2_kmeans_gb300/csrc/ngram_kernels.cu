@@ -20,9 +20,41 @@
 // The counts run per occurrence list (cluster, position, symbol) in a fixed
 // column order, in FP64; the cost sums run over u in order with separately
 // rounded products and sums, as the reference's BLAS computes them.
+#include <cmath>
+#include <map>
+#include <unordered_map>
+
 #include "d2g_internal.cuh"
 
 namespace d2g {
+
+int number_tuples(const int *sym, size_t count, int dim, int V, std::vector<int> &key,
+                  std::vector<int> &tup) {
+  key.resize(count);
+  tup.clear();
+  for (size_t e = 0; e < count * dim; ++e)
+    if (sym[e] < 0 || sym[e] >= V) return -1;
+  if (dim * std::log2((double)V) < 62.0) {  // a tuple as a base-V integer
+    std::unordered_map<unsigned long long, int> id;
+    id.reserve(1024);
+    for (size_t e = 0; e < count; ++e) {
+      unsigned long long code = 0;
+      for (int t = 0; t < dim; ++t) code = code * (unsigned long long)V + (unsigned long long)sym[e * dim + t];
+      auto it = id.emplace(code, (int)id.size());
+      if (it.second) tup.insert(tup.end(), sym + e * dim, sym + (e + 1) * dim);
+      key[e] = it.first->second;
+    }
+    return (int)id.size();
+  }
+  std::map<std::vector<int>, int> id;
+  for (size_t e = 0; e < count; ++e) {
+    std::vector<int> t(sym + e * dim, sym + (e + 1) * dim);
+    auto it = id.emplace(t, (int)id.size());
+    if (it.second) tup.insert(tup.end(), t.begin(), t.end());
+    key[e] = it.first->second;
+  }
+  return (int)id.size();
+}
 
 // cnt[(l*m + k)*dim + t][v] from the list of key (l*dim + t)*V + v: one warp
 // per list, lanes over the centroid supports k.
@@ -101,6 +133,34 @@ __global__ void ngram_table_kernel(const int *__restrict__ csym, const int *__re
     }
     T[i] = c;
   }
+}
+
+// Exact-transport costs of n-gram supports for the assignment step
+// (src/d2/clustering.c:102-115): rows are the distinct centroid tuples, columns
+// the distinct instance tuples, cost = sum_t dist[row symbol * V + column symbol]
+// in FP64 and its FP32 rounding.
+__global__ void ngram_pair_table_kernel(const int *__restrict__ rt, int Ur, const int *__restrict__ ct,
+                                        int Uc, int dim, int V, const double *__restrict__ dist,
+                                        double *__restrict__ T64, float *__restrict__ T32) {
+  const long long n = (long long)Ur * Uc;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i / Uc), c = (int)(i - (long long)r * Uc);
+    double s = 0.0;
+    for (int t = 0; t < dim; ++t) s += dist[(size_t)rt[(size_t)r * dim + t] * V + ct[(size_t)c * dim + t]];
+    T64[i] = s;
+    T32[i] = (float)s;
+  }
+}
+
+cudaError_t launch_ngram_pair_table(const int *rt, int Ur, const int *ct, int Uc, int dim, int V,
+                                    const double *dist, double *T64, float *T32, cudaStream_t st) {
+  const long long n = (long long)Ur * Uc;
+  long long nb = (n + 255) / 256;
+  if (nb > 152LL * 32) nb = 152LL * 32;
+  ngram_pair_table_kernel<<<(unsigned)(nb < 1 ? 1 : nb), 256, 0, st>>>(rt, Ur, ct, Uc, dim, V, dist,
+                                                                       T64, T32);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_ngram_support(const NgramArgs &g, cudaStream_t st) {

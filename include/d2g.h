@@ -317,10 +317,10 @@ int d2g_emd_pairs(int metric_type, int dim, const d2g_dists *rows, const d2g_dis
 
 /* The assignment step on the reference's structures (src/d2/clustering.c:
  * 33-376); every distance is the square root of the phases' summed exact
- * transport costs, as d2_compute_distance returns it.  Metric types:
- * D2_EUCLIDEAN_L2, D2_HISTOGRAM, D2_SPARSE_HISTOGRAM, D2_WORD_EMBED; n-grams
- * return D2G_E_UNSUPPORTED.  The instances' device copy is kept across calls
- * while their arrays stay the same. */
+ * transport costs, as d2_compute_distance returns it (an n-gram phase adds
+ * 2 * cost / dim, clustering.c:102-115).  Metric types: D2_EUCLIDEAN_L2,
+ * D2_HISTOGRAM, D2_SPARSE_HISTOGRAM, D2_WORD_EMBED, D2_N_GRAM.  The instances'
+ * device copy is kept across calls while their arrays stay the same. */
 
 /* out[p] = d2_compute_distance(a, ia[p], b, jb[p], selected_phase, ...) */
 int d2g_compute_distances(mph *a, mph *b, int selected_phase, size_t npairs, const int *ia,

@@ -7,7 +7,8 @@
  * with every transport cost from d2o_emd (emd_oracle.c) where the reference
  * calls MOSEK through d2_match_by_distmat.  Same loops, same order, same
  * comparisons; the printing and the time_budget side effect are left out.
- * Metric types: Euclidean, histogram, sparse histogram, word embeddings.
+ * Metric types: Euclidean, histogram, sparse histogram, word embeddings,
+ * n-grams.
  */
 #include <float.h>
 #include <math.h>
@@ -63,11 +64,25 @@ static double distance(const mph *a, size_t i, const mph *b, size_t j, int selec
             C[(size_t)c * nr + r] =
                 as->dist_mat[(size_t)as->p_supp_sym[ca + c] * as->vocab_size + r];
         break;
+      case D2_N_GRAM: /* _dpdist_symbolic (blas_like64.c:232-242), rows b's symbols */
+        for (int c = 0; c < nc; ++c)
+          for (int r = 0; r < nr; ++r) {
+            double s = 0.0;
+            for (int t = 0; t < dim; ++t)
+              s += as->dist_mat[(size_t)bs->p_supp_sym[(rb + r) * dim + t] * as->vocab_size +
+                                as->p_supp_sym[(ca + c) * dim + t]];
+            C[(size_t)c * nr + r] = s;
+          }
+        break;
       default:
         free(C);
         return NAN;
     }
-    d += d2o_emd(nr, nc, C, bs->p_w + rb, as->p_w + ca, NULL);
+    const double val = d2o_emd(nr, nc, C, bs->p_w + rb, as->p_w + ca, NULL);
+    if (as->metric_type == D2_N_GRAM)
+      d += 2 * (val / dim); /* :112-115: the cost per symbol, counted twice */
+    else
+      d += val;
     free(C);
   }
   if (d <= 0) return 0.;

@@ -4,7 +4,7 @@ import numpy as np
 
 from d2_kmeans_gb300.assign import EUCLIDEAN, HISTOGRAM, SPARSE_HISTOGRAM, Mph, Work
 
-WORD_EMBED = 7
+N_GRAM, WORD_EMBED = 6, 7
 
 
 def euclid_phase(rng, n, dim, lo, hi, k, m, spread=3.0):
@@ -116,12 +116,16 @@ def oracle_clustering(oracle_mod, data_phases, cent_phases, n, k, label, max_ite
         if changed < 0.001 * n:
             break
         old = Mph([dict(ph, p_w=cents.arrays[i]["p_w"].copy(),
-                        p_supp=None if "p_supp" not in cents.arrays[i] else cents.arrays[i]["p_supp"].copy())
+                        p_supp=None if "p_supp" not in cents.arrays[i] else cents.arrays[i]["p_supp"].copy(),
+                        p_supp_sym=(None if "p_supp_sym" not in cents.arrays[i]
+                                    else cents.arrays[i]["p_supp_sym"].copy()))
                    for i, ph in enumerate(cent_phases)], k, num_of_labels=k)
         for i, ph in enumerate(data_phases):
             phase = dict(ph, label=data.label.copy(), num_of_labels=k,
                          label_switch=work.label_switch.copy())
             cw = {"c_w": cents.arrays[i]["p_w"], "c_supp": cents.arrays[i].get("p_supp")}
+            if ph["metric"] == N_GRAM:
+                cw["c_sym"] = cents.arrays[i]["p_supp_sym"]
             if Z[i] is not None:
                 cw["Z"] = Z[i]
             r = oracle_mod.badmm(phase, cw, opts, "port", want=())
@@ -129,6 +133,8 @@ def oracle_clustering(oracle_mod, data_phases, cent_phases, n, k, label, max_ite
             cents.arrays[i]["p_w"][:] = r["c_w"]
             if "p_supp" in cents.arrays[i]:
                 cents.arrays[i]["p_supp"][:] = r["c_supp"][:cents.arrays[i]["p_supp"].size]
+            if ph["metric"] == N_GRAM:
+                cents.arrays[i]["p_supp_sym"][:] = r["c_sym"]
             Z[i] = r["Z"]
         if use_triangle:
             lab.labeling_post(data, old, cents, work)
@@ -157,4 +163,29 @@ def embed_phase(rng, n, k, V, dim, m, lo=3, hi=30):
                              for j in range(k)])
     c_w = np.concatenate([rng.dirichlet(np.ones(m)) for _ in range(k)])
     cent = dict(metric=EUCLIDEAN, dim=dim, str=m, p_w=c_w, p_supp=c_supp.reshape(-1))
+    return data, cent
+
+
+def ngram_phase(rng, n, k, m, dim, V, lo=10, hi=80):
+    """sequences over V symbols from k families as distributions of their
+    distinct dim-grams; centroids: m n-grams of each family with Dirichlet weights"""
+    from d2_kmeans_gb300 import synth
+    dist = synth.symbol_cost(V, int(rng.integers(1 << 30)))
+    fam = rng.dirichlet(np.full(V, 0.4), size=k)
+    lab = rng.integers(0, k, size=n)
+    radix = V ** np.arange(dim - 1, -1, -1)
+    p_str, sym, w = [], [], []
+    for i in range(n):
+        seq = rng.choice(V, size=int(rng.integers(lo, hi + 1)), p=fam[lab[i]])
+        code, cnt = np.unique(np.lib.stride_tricks.sliding_window_view(seq, dim) @ radix,
+                              return_counts=True)
+        p_str.append(code.size)
+        sym.append(((code[:, None] // radix[None, :]) % V).reshape(-1))
+        w.append(cnt / cnt.sum())
+    data = dict(metric=N_GRAM, dim=dim, str=m, p_str=np.array(p_str, np.int32), p_w=np.concatenate(w),
+                p_supp_sym=np.concatenate(sym).astype(np.int32), dist_mat=dist.reshape(-1), vocab_size=V)
+    c_sym = np.concatenate([rng.choice(V, size=m * dim, p=fam[j]) for j in range(k)]).astype(np.int32)
+    c_w = np.concatenate([rng.dirichlet(np.ones(m)) for _ in range(k)])
+    cent = dict(metric=N_GRAM, dim=dim, str=m, p_w=c_w, p_supp_sym=c_sym, dist_mat=dist.reshape(-1),
+                vocab_size=V)
     return data, cent

@@ -158,11 +158,22 @@ def test_reference_entry_points(port):
     assert abs(d - port.distance(dp, 3, cnp, 1)) <= RTOL * d
 
 
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_ngrams(port, dim):
+    """n-gram phases: exact transport between the distinct centroid and
+    instance tuples, 2 * cost / dim per phase (clustering.c:102-115)"""
+    rng = np.random.default_rng(20 + dim)
+    dph, cph = AD.ngram_phase(rng, 150, 5, 8, dim, 20, lo=10, hi=120)
+    label = rng.integers(-1, 5, size=150)
+    rounds(port, [dph], [cph], 150, 5, label, 3, rng, prep=True)
+    rounds(port, [dph], [cph], 150, 5, label, 1, rng, prep=False)
+
+
 def test_unsupported_metric_is_refused(port):
     from d2_kmeans_gb300._lib import D2GError
     rng = np.random.default_rng(8)
     d0, c0 = AD.euclid_phase(rng, 10, 3, 2, 5, 2, 3)
-    d0 = dict(d0, metric=6)  # n-grams: no exact-transport path here
+    d0 = dict(d0, metric=1)  # D2_CITYBLOCK_L1: no exact-transport path
     dg, cg = AD.build([d0], [c0], 10, 2, np.zeros(10, int))
     with pytest.raises(D2GError):
         assign.labeling(dg, cg, Work(10, 2, 1))

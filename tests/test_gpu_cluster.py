@@ -105,3 +105,22 @@ def test_random_initialisation(lib, rands_stub):
     assert np.array_equal(data.label, data2.label)
     assert np.array_equal(got_w, cents2.arrays[0]["p_w"])
     assert np.array_equal(got_s, cents2.arrays[0]["p_supp"])
+
+
+@pytest.mark.parametrize("tri", [0, 1])
+def test_ngram_clustering_matches_oracle_loop(lib, oracle_mod, tri):
+    """n-gram phases through the whole loop: exact-transport labels (2 * cost /
+    dim) and B-ADMM rounds with symbol updates; labels and symbols identical,
+    weights within the B-ADMM tolerance"""
+    rng = np.random.default_rng(40 + tri)
+    n, k, m = 120, 3, 6
+    dph, cph = AD.ngram_phase(rng, n, k, m, 2, 10, lo=10, hi=60)
+    label = np.full(n, -1)
+    lab_o, cents_o, rounds_o = AD.oracle_clustering(oracle_mod, [dph], [cph], n, k, label, 5, tri)
+    data = Mph([dph], n, label=label.copy(), num_of_labels=k)
+    cents = Mph([cph], k, num_of_labels=k)
+    rounds = assign.clustering(data, cents, k, 5, use_triangle=bool(tri))
+    assert rounds == rounds_o and rounds >= 2
+    assert np.array_equal(data.label, lab_o)
+    assert np.array_equal(cents.arrays[0]["p_supp_sym"], cents_o.arrays[0]["p_supp_sym"])
+    close_centroids(cents, cents_o, k, m)

@@ -100,3 +100,12 @@ def test_histograms(both, sparse):
     dph, cph = AD.hist_phase(rng, 60, 4, 4, sparse=sparse, asym=True)
     label = rng.integers(-1, 4, size=60)
     run_both(both, [dph], [cph], 60, 4, label, rounds=2, rng=rng, prep=True)
+
+
+@pytest.mark.parametrize("dim", [1, 3])
+def test_ngrams(both, dim):
+    """n-gram phases: 2 * transport cost / dim per phase (clustering.c:102-115)"""
+    rng = np.random.default_rng(9 + dim)
+    dph, cph = AD.ngram_phase(rng, 60, 4, 6, dim, 12)
+    label = rng.integers(-1, 4, size=60)
+    run_both(both, [dph], [cph], 60, 4, label, rounds=2, rng=rng, prep=True)
