@@ -13,7 +13,11 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libd2g.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]
+# host code: no contraction of a*b+c into FMA (the FP64 restatements of the
+# reference's host arithmetic, e.g. centroid initialisation, then round alike
+# on x86 and Arm hosts)
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
+         "--expt-relaxed-constexpr"]
 
 
 def _nvcc() -> str:

@@ -176,14 +176,9 @@ void write_log(const char *log_file, const mph *c, const mph *p) {
 }
 
 // centroids->ph == NULL: arrays as d2_allocate_sph lays them out, filled by
-// the program's d2_centroid_rands (clustering.c:383-404)
+// d2_centroid_rands (clustering.c:383-404): the program's own, else this
+// library's d2g_centroid_rands
 int init_centroids(mph *p, mph *c, int sel) {
-  typedef int (*rands_fn)(mph *, int, sph *);
-  const rands_fn rands = (rands_fn)dlsym(RTLD_DEFAULT, "d2_centroid_rands");
-  if (!rands) {
-    d2g::set_error("d2_clustering: no centroids given and no d2_centroid_rands linked");
-    return D2G_E_UNSUPPORTED;
-  }
   const int k = p->num_of_labels;
   c->s_ph = p->s_ph;
   c->size = k;
@@ -206,7 +201,8 @@ int init_centroids(mph *p, mph *c, int sel) {
     if (!d.p_str || !d.p_str_cum || !d.p_w || (d.metric_type == D2_EUCLIDEAN_L2 && !d.p_supp) ||
         (d.metric_type == D2_N_GRAM && !d.p_supp_sym))
       return D2G_E_NOMEM;
-    rands(p, n, &d);
+    const int rc = d2g::centroid_rands(p, n, &d);
+    if (rc) return rc;
   }
   return D2G_OK;
 }

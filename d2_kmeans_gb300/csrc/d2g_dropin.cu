@@ -125,16 +125,14 @@ int centroid_update(mph *p_data, var_mph *var_work, int idx_ph, sph *c0, sph *c)
   if (!p_data || !var_work || !c || idx_ph < 0 || idx_ph >= p_data->s_ph || !var_work->l_var_sphBregman)
     return err(D2G_E_INVAL, "bad arguments");
   if (!c0) {
-    // :95-98 initialises c at random with the reference's own d2_centroid_rands
-    // (src/d2/centroid_rand.c:161-295), which stays in a program that links
-    // this library in place of centroid_Bregman.c.  One process: there is no
-    // broadcast_centroids step.
-    typedef int (*rands_fn)(mph *, int, sph *);
-    const rands_fn rands = (rands_fn)dlsym(RTLD_DEFAULT, "d2_centroid_rands");
-    if (!rands)
-      return err(D2G_E_UNSUPPORTED, "c0 == NULL needs d2_centroid_rands (src/d2/centroid_rand.c) linked");
+    // :95-98 initialises c at random with d2_centroid_rands
+    // (src/d2/centroid_rand.c:161-295): the program's own where it links one
+    // (a program that links this library in place of centroid_Bregman.c keeps
+    // centroid_rand.c), else this library's d2g_centroid_rands, which gives
+    // the same result.  One process: there is no broadcast_centroids step.
     if (c->str != p_data->ph[idx_ph].str) return err(D2G_E_INVAL, "c->str differs from the phase's str");
-    rands(p_data, idx_ph, c);
+    const int rc0 = d2g::centroid_rands(p_data, idx_ph, c);
+    if (rc0) return rc0;
   } else {
     *c = *c0;  // :100 warm start
   }

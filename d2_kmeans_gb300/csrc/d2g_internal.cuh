@@ -266,6 +266,10 @@ int distmat_fp64(int dim, int str, size_t size, const int *p_str, int metric, co
                  const int *sym, const double *vocab, int V, const int *label, const double *c_supp,
                  size_t K, double *C_host, const double *dist = nullptr, const int *c_sym = nullptr);
 
+// d2g_init.cu: random centroids, the program's d2_centroid_rands where it
+// links one, else d2g_centroid_rands
+int centroid_rands(mph *p_data, int idx_ph, sph *c);
+
 // error helpers (d2g_host.cu)
 void set_error(const std::string &msg);
 int cuda_fail(cudaError_t e, const char *what);

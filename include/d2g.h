@@ -129,8 +129,8 @@ int d2_free_work_sphBregman(var_sphBregman *var_phwork);
  * and the global time_budget.  Metric types: D2_EUCLIDEAN_L2, D2_WORD_EMBED,
  * D2_HISTOGRAM, D2_SPARSE_HISTOGRAM, D2_N_GRAM.  c0 == NULL
  * (:95-98) initialises c with d2_centroid_rands when the program links it
- * (src/d2/centroid_rand.c:161-295, found by dlsym), else returns
- * D2G_E_UNSUPPORTED.  The host X, Y
+ * (src/d2/centroid_rand.c:161-295, found by dlsym), else with
+ * d2g_centroid_rands.  The host X, Y
  * and C buffers are scratch for the reference's callers and are only written
  * back when d2g_config.sync_scratch is set. */
 int d2_centroid_sphBregman(mph *p_data, var_mph *var_work, int idx_ph, sph *c0, sph *c);
@@ -160,6 +160,19 @@ int d2g_distmat_noalloc(int metric_type, int dim, int str, size_t size, size_t c
                         const int *p_str, const double *p_supp, const int *p_supp_sym,
                         const double *vocab_vec, int vocab_size, const int *label,
                         int num_of_labels, const double *c_supp, double *C, void *stream);
+
+/* The result of d2_centroid_rands, src/d2/centroid_rand.c:161-295 (declared
+ * include/d2/clustering.h:216-218), for a program that does not link the
+ * reference's own: random instances (glibc rand() order after srand(0), as
+ * the reference's shuffle in a single process, src/d2/math.c:40-58) with at
+ * least str supports become the centroids of phase idx_ph, larger ones
+ * merged down to str (merge / merge_symbolic, centroid_rand.c:53-159).  c's
+ * arrays are the caller's (d2_allocate_sph's layout); the process-wide rand()
+ * state is not touched.  D2G_E_INVAL where the reference exit(1)s for too few
+ * instances.  d2_centroid_sphBregman with c0 == NULL and d2g_clustering with
+ * no centroids use the program's d2_centroid_rands when it links one, else
+ * this. */
+int d2g_centroid_rands(mph *p_data, int idx_ph, sph *c);
 
 /* Option structs of src/d2/centroid_Bregman.c:17-22 (the caller swaps
  * p_badmm_options, e.g. src/app/main.cc:234-236). */
@@ -352,7 +365,7 @@ extern int d2_alg_type; /* clustering.c:24; label_switch is written when 0 (B-AD
  * labeling (Elkan's pruning when use_triangle) and B-ADMM centroid updates
  * (p_badmm_options) until fewer than 0.1 % of the instances change label or
  * max_iter rounds; centroids->ph == NULL initialises them with the program's
- * d2_centroid_rands.  Log files <log_file>_c.d2 / <log_file>.label every
+ * d2_centroid_rands, or d2g_centroid_rands where it links none.  Log files <log_file>_c.d2 / <log_file>.label every
  * tenth round when log_file is given.  *rounds (optional): rounds run. */
 int d2g_clustering(int num_of_clusters, int max_iter, mph *p_data, mph *centroids,
                    int selected_phase, int use_triangle, const char *log_file, int *rounds);

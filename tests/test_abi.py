@@ -139,15 +139,32 @@ def _small_dropin():
     return ph, badmm.DropIn(ph, c)
 
 
-def test_random_init_without_rands_is_unsupported(lib):
-    """c0 == NULL with no d2_centroid_rands in the program: D2G_E_UNSUPPORTED,
-    before any device work."""
+def test_random_init_without_rands_uses_the_librarys(lib):
+    """c0 == NULL with no d2_centroid_rands in the program: c is filled by
+    d2g_centroid_rands (the same result as calling it directly).  Without a
+    GPU the update itself then fails with a device error, leaving the
+    initialisation in c."""
+    import torch
     if hasattr(C.CDLL(None), "d2_centroid_rands"):
         pytest.skip("a d2_centroid_rands is already loaded into this process")
-    _, d = _small_dropin()
-    c_w = d.c_w.copy()
-    assert d.call({}, random_init=True) == L.D2G_E_UNSUPPORTED
-    assert np.array_equal(d.c_w, c_w)
+    if torch.cuda.is_available():
+        pytest.skip("covered with the update by the GPU tests")
+    ph, d = _small_dropin()
+    d.c_w[:] = -1.0
+    d.c_supp[:] = -1.0
+    rc = d.call({}, random_init=True)
+    assert rc not in (0, L.D2G_E_UNSUPPORTED, L.D2G_E_INVAL)
+    w = np.full(d.c_w.size, np.nan)
+    s = np.full(d.c_supp.size, np.nan)
+    c = L.sph()
+    c.dim, c.str, c.max_str, c.metric_type = d.dim, d.m, d.m, 0
+    p_str, cum = np.zeros(d.k, np.int32), np.zeros(d.k, np.uint64)
+    c.p_str = p_str.ctypes.data_as(C.POINTER(C.c_int))
+    c.p_str_cum = cum.ctypes.data_as(C.POINTER(C.c_size_t))
+    c.p_w = w.ctypes.data_as(C.POINTER(C.c_double))
+    c.p_supp = s.ctypes.data_as(C.POINTER(C.c_double))
+    assert lib.d2g_centroid_rands(C.byref(d.mph), 0, C.byref(c)) == 0
+    assert np.array_equal(d.c_w, w) and np.array_equal(d.c_supp, s)
     d.close()
 
 
