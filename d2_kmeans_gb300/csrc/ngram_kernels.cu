@@ -18,8 +18,10 @@
 //                     (minimize_symbolic, centroid_util.h:25-37: a column-major
 //                     GEMM dist * cnt, then an argmin per column)
 // The counts run per occurrence list (cluster, position, symbol) in a fixed
-// column order, in FP64; the cost sums run over u in order with separately
-// rounded products and sums, as the reference's BLAS computes them.
+// column order: FP64 one column after the other in the FP64 form; FP32 over
+// chunks of 32 columns and FP64 across chunks in the batched form.  The cost
+// sums run over u in order with separately rounded products and sums, as the
+// reference's BLAS computes them.
 #include <cmath>
 #include <map>
 #include <unordered_map>
@@ -56,13 +58,13 @@ int number_tuples(const int *sym, size_t count, int dim, int V, std::vector<int>
   return (int)id.size();
 }
 
-// cnt[(l*m + k)*dim + t][v] from the list of key (l*dim + t)*V + v: one warp
-// per list, lanes over the centroid supports k.
-template <typename TZ>
-__global__ void ngram_count_kernel(const int *__restrict__ key, const int *__restrict__ ptr,
-                                   const int *__restrict__ occ, int nlists, const TZ *__restrict__ Z,
-                                   long long zstride, int m, int dim, int V, double *__restrict__ cnt,
-                                   const Ctl *ctl, int iter) {
+// FP64 form: cnt[(l*m + k)*dim + t][v] from the list of key (l*dim + t)*V + v,
+// one warp per list, lanes over the centroid supports k, the columns added
+// one by one in list (reference) order.
+__global__ void ngram_count64_kernel(const int *__restrict__ key, const int *__restrict__ ptr,
+                                     const int *__restrict__ occ, int nlists, const double *__restrict__ Z,
+                                     long long zstride, int m, int dim, int V, double *__restrict__ cnt,
+                                     const Ctl *ctl, int iter) {
   if (iter >= ctl->stop_iter) return;
   const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (w >= nlists) return;
@@ -72,10 +74,56 @@ __global__ void ngram_count_kernel(const int *__restrict__ key, const int *__res
   for (int k = lane; k < m; k += 32) {
     double s = 0.0;
     for (int o = b; o < e; ++o) {
-      const TZ z = Z[(size_t)occ[o] * zstride + k];
-      if (z > (TZ)1E-10) s += (double)z;
+      const double z = Z[(size_t)occ[o] * zstride + k];
+      if (z > 1E-10) s += z;
     }
     cnt[(((size_t)l * m + k) * dim + t) * V + v] = s;
+  }
+}
+
+// Batched form: one CTA per list.  Warp w takes the chunks w, w + 8, ... of
+// kChunk columns; a chunk is summed in FP32 (its loads independent, so they
+// overlap), the chunk sums in FP64; the 8 warps' sums are added in warp
+// order.  The order is fixed, so the counts repeat bit for bit.
+constexpr int kCountWarps = 8, kChunk = 32;
+__global__ void __launch_bounds__(kCountWarps * 32) ngram_count32_kernel(
+    const int *__restrict__ key, const int *__restrict__ ptr, const int *__restrict__ occ,
+    const float *__restrict__ Z, long long zstride, int m, int dim, int V, double *__restrict__ cnt,
+    const Ctl *ctl, int iter) {
+  if (iter >= ctl->stop_iter) return;
+  __shared__ double part[kCountWarps][32];
+  __shared__ int cols[kCountWarps][kChunk];
+  const int lst = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int kk = key[lst];
+  const int v = kk % V, lt = kk / V, t = lt % dim, l = lt / dim;
+  const int b = ptr[lst], e = ptr[lst + 1];
+  for (int k0 = 0; k0 < m; k0 += 32) {
+    const int k = k0 + lane;
+    double acc = 0.0;
+    for (int c0 = b + warp * kChunk; c0 < e; c0 += kCountWarps * kChunk) {
+      const int nc = min(kChunk, e - c0);
+      __syncwarp();
+      if (lane < nc) cols[warp][lane] = occ[c0 + lane];
+      __syncwarp();
+      float s = 0.f;
+      if (k < m) {
+#pragma unroll 8
+        for (int j = 0; j < nc; ++j) {
+          const float z = __ldg(Z + (size_t)cols[warp][j] * zstride + k);
+          s += z > 1E-10f ? z : 0.f;
+        }
+      }
+      acc += (double)s;
+    }
+    part[warp][lane] = acc;
+    __syncthreads();
+    if (warp == 0 && k < m) {
+      double tot = 0.0;
+#pragma unroll
+      for (int w = 0; w < kCountWarps; ++w) tot += part[w][lane];
+      cnt[(((size_t)l * m + k) * dim + t) * V + v] = tot;
+    }
+    __syncthreads();
   }
 }
 
@@ -168,13 +216,12 @@ cudaError_t launch_ngram_support(const NgramArgs &g, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(g.cnt, 0, ncnt * sizeof(double), st);
   if (e != cudaSuccess) return e;
   if (g.nlists > 0) {
-    const unsigned nb = (unsigned)(((long long)g.nlists * 32 + 255) / 256);
     if (g.Z32)
-      ngram_count_kernel<float><<<nb, 256, 0, st>>>(g.key, g.ptr, g.occ, g.nlists, g.Z32, g.zstride,
-                                                    g.m, g.dim, g.V, g.cnt, g.ctl, g.iter);
+      ngram_count32_kernel<<<g.nlists, kCountWarps * 32, 0, st>>>(g.key, g.ptr, g.occ, g.Z32, g.zstride, g.m,
+                                                                  g.dim, g.V, g.cnt, g.ctl, g.iter);
     else
-      ngram_count_kernel<double><<<nb, 256, 0, st>>>(g.key, g.ptr, g.occ, g.nlists, g.Z64, g.zstride,
-                                                     g.m, g.dim, g.V, g.cnt, g.ctl, g.iter);
+      ngram_count64_kernel<<<(unsigned)(((long long)g.nlists * 32 + 255) / 256), 256, 0, st>>>(
+          g.key, g.ptr, g.occ, g.nlists, g.Z64, g.zstride, g.m, g.dim, g.V, g.cnt, g.ctl, g.iter);
   }
   const int ncols = g.K * g.m * g.dim;
   ngram_min_kernel<<<(unsigned)(((long long)ncols * 32 + 255) / 256), 256, 0, st>>>(
