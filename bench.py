@@ -283,6 +283,28 @@ def fp64_errors(name, seed=0):
     return res
 
 
+# bounded CPU samples of the secondary workloads (oracle port, 1 core):
+# instances kept, iterations run
+CPU_SAMPLE = {"embed": (100, 20), "hist": (100, 20), "twophase_euclid": (5000, 20), "ngram": (1000, 20)}
+
+
+def workload_cpu(name):
+    """The oracle port (the reference's algorithm in FP64, bit-identical to
+    it) on the first instances of the workload, timed on one host core."""
+    import oracle
+    from d2_kmeans_gb300 import synth
+    ensure_oracle()
+    keep, iters = CPU_SAMPLE[name]
+    full = {"embed": 20000, "hist": 100000, "twophase_euclid": 100000, "ngram": 20000}[name]
+    ph, c, opts = synth.workload(name, seed=0, scale=keep / full)
+    t = time.perf_counter()
+    r = oracle.badmm(ph, c, dict(opts, maxIters=iters - 1), "port", want=())
+    el = time.perf_counter() - t
+    n = len(ph["p_str"])
+    return {"value": n * r["iters"] / el, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{n} instances of the workload, {r['iters']} iterations, {el:.1f} s"}
+
+
 def workload_leg(name, steps, hbm, tf32_peak):
     """One secondary workload: autotuned, timed over whole centroid updates,
     then the plan-update (and cost-table) launches timed alone (profile mode),
@@ -319,6 +341,8 @@ def workload_leg(name, steps, hbm, tf32_peak):
                                           "the BF16 rate)"}
     if "fp64" not in SKIP:
         out["error_vs_fp64"] = fp64_errors(name)
+    if "cpu" not in SKIP:
+        out["cpu_baseline"] = workload_cpu(name)
     return out
 
 
@@ -499,8 +523,23 @@ def serve_leg(rates=(2000.0, 5000.0, 10000.0, 20000.0), per_rate=1500):
         r.pop("results")
         out.append(r)
     S.close()
-    return {"workload": SERVE_WORKLOAD, "per_rate": out,
-            "capacity_req_per_s": max(r["throughput"] for r in out)}
+    res = {"workload": SERVE_WORKLOAD, "per_rate": out,
+           "capacity_req_per_s": max(r["throughput"] for r in out)}
+    if "cpu" not in SKIP:
+        # the oracle's fixed-centroid solve (FP64, 1 core) of two queries for
+        # 20 iterations, scaled to the 200 iterations of a request (its time
+        # is linear in the iterations)
+        import oracle
+        ensure_oracle()
+        qs = synth.serving_queries(2, means, sizes=(4, 512), seed=7)
+        t = time.perf_counter()
+        for w, sp in qs:
+            oracle.serve_query(c_w, c_supp, w, sp, iters=20)
+        per_req = (time.perf_counter() - t) / len(qs) * 10
+        res["cpu_baseline"] = {"value": 1.0 / per_req, "unit": "requests/s", "cores": 1, "kind": "port",
+                               "sample": f"2 queries (m_q {qs[0][0].size}, {qs[1][0].size}) x 20 "
+                                         f"iterations, scaled to 200: {per_req:.2f} s per request"}
+    return res
 
 
 def main():
