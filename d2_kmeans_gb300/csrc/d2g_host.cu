@@ -95,6 +95,8 @@ struct d2g_phase {
   int max_checks = 0;
   DBuf<double> cw64, cs64;
   DBuf<double> stage;  // reference-layout FP64 staging
+  DBuf<double> colstage;  // reference-layout weights and supports on their way to the packed layout
+  DBuf<int> symstage;
   DBuf<double> part;   // cluster partials
   int chunk = 256, nchunk = 1;
   DBuf<int> cl_ptr, cl_plans;
@@ -641,8 +643,11 @@ static int set_labels_impl(d2g_phase *ph, const int *label) {
 static int upload_columns_batched(d2g_phase *ph, const d2g_phase_desc *d) {
   const bool euc = ph->metric == D2_EUCLIDEAN_L2;
   const size_t ns = ph->col * (size_t)(1 + (euc ? ph->dim : 0));
-  DBuf<double> tmp;
-  DBuf<int> tsym;
+  // reference-layout staging, kept on the phase: a drop-in call re-sends the
+  // columns every time, and a fresh allocation per call would cost more than
+  // the copy
+  DBuf<double> &tmp = ph->colstage;
+  DBuf<int> &tsym = ph->symstage;
   D2G_CUDA(tmp.alloc(ns));
   D2G_CUDA(cudaMemcpyAsync(tmp.p, d->p_w, ph->col * 8, cudaMemcpyHostToDevice, ph->st));
   if (euc)
@@ -1522,6 +1527,14 @@ int d2g_phase_refresh(d2g_phase *ph, const d2g_phase_desc *d) {
   int rc = ph->path == 0 ? upload_columns_batched(ph, d) : upload_columns_plain(ph, d);
   if (rc) return rc;
   ph->global_size = d->global_size ? d->global_size : d->size;
+  // what set_labels_impl derives (cluster lists, plan slots, group records)
+  // depends on the labels alone for Euclidean and histogram phases: kept while
+  // they are unchanged (word-embedding and n-gram lists also follow the ids)
+  const bool label_only = ph->metric == D2_EUCLIDEAN_L2 || ph->metric == D2_HISTOGRAM ||
+                          ph->metric == D2_SPARSE_HISTOGRAM;
+  if (label_only && ph->label.size() == ph->size &&
+      memcmp(ph->label.data(), d->label, ph->size * sizeof(int)) == 0)
+    return D2G_OK;
   return set_labels_impl(ph, d->label);
 }
 
