@@ -63,7 +63,7 @@ class BADMM_options(C.Structure):
 class d2g_config(C.Structure):
     _fields_ = [("precision", C.c_int), ("verbose", C.c_int), ("use_graph", C.c_int),
                 ("sync_scratch", C.c_int), ("profile", C.c_int), ("cost_gemm", C.c_int),
-                ("keep_time_budget", C.c_int)]
+                ("keep_time_budget", C.c_int), ("pair_iterations", C.c_int)]
 
 
 class d2g_phase_desc(C.Structure):

@@ -35,7 +35,7 @@ static int fail(int code, const std::string &msg) {
 }
 
 std::mutex g_cfg_mu;
-d2g_config g_cfg = {0, 1, 1, 0, 0, 0, 0};
+d2g_config g_cfg = {0, 1, 1, 0, 0, 0, 0, 1};
 d2g_config cfg_snapshot() {
   std::lock_guard<std::mutex> lk(g_cfg_mu);
   return g_cfg;
@@ -132,6 +132,11 @@ struct d2g_phase {
   bool defer = false;
   DBuf<float> rowpart, rowsc;
   DBuf<int4> wide;                       // {slot, slices with columns, label, 0} per wide plan
+  // two iterations per pass (phases without wide plans): second-iteration row
+  // sums (normalised / raw) and the label of every slot
+  bool pairs = false;
+  DBuf<float> rowsum2, rawsum;
+  DBuf<int> slot_label;
   DBuf<unsigned char> def_iter;          // per iteration: 1 if it ran deferred
   std::vector<unsigned char> h_def_iter;
 
@@ -446,6 +451,8 @@ static PlanArgs base_args(d2g_phase *ph) {
   a.col_crow = tables ? ph->col_crow.p : ph->col_sym.p;
   a.stage_costs = ph->stage_costs;
   a.wide = ph->nwide > 0;
+  a.rowsum2_out = ph->rowsum2.p;
+  a.rawsum_out = ph->rawsum.p;
   return a;
 }
 
@@ -534,6 +541,12 @@ static int set_labels_impl(d2g_phase *ph, const int *label) {
     for (size_t q = 0; q < n; ++q) slot[lists[q]] = (int)q;
     D2G_CUDA(ph->plan_slot.alloc(n));
     D2G_CUDA(cudaMemcpyAsync(ph->plan_slot.p, slot.data(), n * 4, cudaMemcpyHostToDevice, ph->st));
+    if (ph->slot_label.n > 0) {  // pair passes: the label of each slot
+      std::vector<int> sl(n);
+      for (size_t p = 0; p < n; ++p) sl[slot[p]] = pl[p];
+      D2G_CUDA(cudaMemcpyAsync(ph->slot_label.p, sl.data(), n * 4, cudaMemcpyHostToDevice, ph->st));
+      D2G_CUDA(cudaStreamSynchronize(ph->st));
+    }
     // group records: {slot, plan's first group, label, groups << 4 | valid}
     const std::vector<int> &gplan = ph->h_grp_plan;
     for (size_t gi = 0; gi < ph->h_grp_rec.size(); ++gi) {
@@ -770,6 +783,11 @@ static int create_batched(d2g_phase *ph, const d2g_phase_desc *d) {
   if (ph->nwide > 0) {
     D2G_CUDA(ph->rowpart.alloc((size_t)ph->nplans * kMaxCluster * ph->MP));
     D2G_CUDA(ph->rowsc.alloc((size_t)ph->nplans * ph->MP));
+  } else if (ph->MP <= 128 && ph->metric != D2_N_GRAM) {  // pair passes possible
+    D2G_CUDA(ph->rowsc.alloc((size_t)ph->nplans * ph->MP));
+    D2G_CUDA(ph->rowsum2.alloc((size_t)ph->nplans * ph->MP));
+    D2G_CUDA(ph->rawsum.alloc((size_t)ph->nplans * ph->MP));
+    D2G_CUDA(ph->slot_label.alloc(ph->nplans));
   }
   PlanArgs base = base_args(ph);
   ph->smem_plan = plan_smem_bytes(ph->MP, 0, 1);
@@ -931,7 +949,8 @@ static std::vector<unsigned long long> loop_signature(d2g_phase *ph) {
           (unsigned long long)ph->stage_costs, (unsigned long long)ph->tune.ctas_per_sm,
           (unsigned long long)ph->defer, u(ph->ncnt.p), u(ph->csym.p), u(ph->nkey.p), u(ph->nptr.p),
           u(ph->nocc.p), (unsigned long long)ph->nlists, u(ph->ntup.p), u(ph->ndist.p),
-          (unsigned long long)ph->ntab};
+          (unsigned long long)ph->ntab, (unsigned long long)ph->pairs, u(ph->rowsum2.p), u(ph->rawsum.p),
+          u(ph->slot_label.p)};
 }
 
 static bool has_collision(int maxIters, int upl) {
@@ -1006,9 +1025,91 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
   std::vector<cudaEvent_t> evs, tevs;  // plan launches, cost-table launches (profile mode)
   if (ph->path == 0) {
     PlanArgs base = base_args(ph);
+    // Two iterations in one pass (plan_pair.cuh) where that is exact: `it` is
+    // no support update and it + 1 no residual check.  Which pairs to take: the
+    // fewest passes over the plans, counting the pass that applies a pair's
+    // deferred scale before a single pass or at the end (a short dynamic
+    // programme over the iterations).
+    std::vector<char> pair_at((size_t)maxIters + 2, 0);
+    if (ph->pairs) {
+      const int N = maxIters + 1;
+      auto upd_at = [&](int i) { return (i % upl == 0) && (euc || emb); };
+      auto can_pair = [&](int i) { return i + 1 < N && !upd_at(i) && !is_check_iter(i + 1); };
+      std::vector<int> f0((size_t)N + 2, 0), f1((size_t)N + 2, 1);  // passes left; f1: a pair is pending
+      f0[N] = 0;
+      f1[N] = 1;
+      for (int i = N - 1; i >= 0; --i) {
+        for (int pend = 0; pend < 2; ++pend) {
+          int best = pend + 1 + f0[i + 1];                          // single pass (finalize first)
+          if (can_pair(i)) best = std::min(best, 1 + f1[i + 2 <= N ? i + 2 : N]);
+          (pend ? f1 : f0)[i] = best;
+        }
+      }
+      int pend = 0;
+      for (int i = 0; i < N;) {
+        const int single = pend + 1 + f0[i + 1];
+        if (can_pair(i) && 1 + f1[i + 2 <= N ? i + 2 : N] <= single) {
+          pair_at[i] = 1;
+          pend = 1;
+          i += 2;
+        } else {
+          pend = 0;
+          i += 1;
+        }
+      }
+    }
+    bool pend = false;  // Z / Y hold a pair pass's deferred output (its scale in rowsc)
     for (int it = 0; it <= maxIters; ++it) {
       // n-gram supports move from the second update iteration on (:270)
       const bool upd = (it % upl == 0) && (euc || emb || (ng && it > 0));
+      if (pair_at[it]) {
+        const int t1 = it + 1;
+        const bool upd1 = (t1 % upl == 0) && (euc || emb);
+        const bool chk0 = is_check_iter(it);
+        if (profile) {
+          cudaEvent_t a0, b0;
+          cudaEventCreate(&a0);
+          cudaEventCreate(&b0);
+          evs.push_back(a0);
+          evs.push_back(b0);
+          cudaEventRecord(a0, ph->st);
+        }
+        const d2g_phase::Bucket &b = ph->buckets[0];
+        PlanArgs a = bucket_args(ph, base, b);
+        a.iter = it;
+        a.flags = (pend ? PF_IN_DEF : 0) | (upd1 && euc ? PF_UPDATE : 0) | (upd1 && emb ? PF_WRITE_X : 0);
+        D2G_CUDA(launch_plan_pair(ph->MP, ph->mode, chk0, a, b.nitems, ph->st));
+        if (profile) cudaEventRecord(evs.back(), ph->st);
+        // step 4 of `it` (c_w), the second iteration's row scale from that c_w,
+        // then step 4 (and step 5) of it + 1
+        D2G_CUDA(launch_cluster_reduce(cluster_args(ph, it, false), ph->st));
+        D2G_CUDA(launch_pair_scale(ph->rawsum.p, ph->slot_label.p, ph->cw32.p, ph->nplans, ph->MP, ph->str,
+                                   ph->rowsc.p, ph->ctl.p, t1, ph->st));
+        ClusterArgs c1 = cluster_args(ph, t1, upd1 && euc);
+        c1.rowsum32 = ph->rowsum2.p;
+        D2G_CUDA(launch_cluster_reduce(c1, ph->st));
+        nl += 6;
+        if (upd1 && emb) {
+          D2G_CUDA(launch_embed_support(embed_args(ph, t1), ph->st));
+          D2G_CUDA(launch_embed_table(embed_args(ph, t1), ph->st));
+          nl += 6;
+        }
+        if (chk0) {
+          D2G_CUDA(launch_resid_final(ph->resid_part.p, ph->total_blocks, ph->ctl.p,
+                                      ph->trace.p + 4 * chk_idx, it, false, ph->st));
+          ++nl;
+          ++chk_idx;
+        }
+        pend = true;
+        ++it;  // the loop's increment moves past it + 1
+        continue;
+      }
+      if (pend) {  // a single pass follows a pair: apply the pending scale first
+        D2G_CUDA(launch_pair_finalize(ph->Z.p, ph->Y.p, ph->grp_rec.p, ph->ngroups, ph->geo.S, ph->MP,
+                                      ph->rowsc.p, ph->st));
+        ++nl;
+        pend = false;
+      }
       const bool chk = is_check_iter(it);
       const bool collide = upd && chk;
       int flags = (upd && euc ? PF_UPDATE : 0) | (chk ? PF_CHECK : 0) |
@@ -1083,6 +1184,11 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
         ++nl;
         ++chk_idx;
       }
+    }
+    if (pend) {  // the loop ended on a pair: its second iteration's scale
+      D2G_CUDA(launch_pair_finalize(ph->Z.p, ph->Y.p, ph->grp_rec.p, ph->ngroups, ph->geo.S, ph->MP,
+                                    ph->rowsc.p, ph->st));
+      ++nl;
     }
     if (ph->defer) {  // the scale of the last iteration that ran, if it ran deferred
       for (auto &b : ph->buckets)
@@ -1236,6 +1342,12 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
     launches += 5;
   }
 
+  // two iterations per pass: phases whose plans fit in one CTA, no time budget
+  // (the reference may stop after any iteration), not n-grams (their support
+  // update needs the final Z of its iteration)
+  ph->pairs = cfg.pair_iterations && ph->path == 0 && ph->nwide == 0 && ph->buckets.size() == 1 &&
+              ph->buckets[0].cs == 1 && ph->MP <= 128 && !ng && ph->slot_label.n > 0 &&
+              h.budget_ns == ~0ULL;
   // deferred-exchange schedule of the wide plans
   ph->h_def_iter.assign((size_t)opt->maxIters + 1, 0);
   if (ph->path == 0 && ph->defer) {
@@ -1421,7 +1533,8 @@ int d2g_get_config(d2g_config *cfg) {
 
 int d2g_set_config(const d2g_config *cfg) {
   if (!cfg || cfg->precision < 0 || cfg->precision > 1 || cfg->cost_gemm < 0 || cfg->cost_gemm > 1 ||
-      cfg->keep_time_budget < 0 || cfg->keep_time_budget > 1)
+      cfg->keep_time_budget < 0 || cfg->keep_time_budget > 1 || cfg->pair_iterations < 0 ||
+      cfg->pair_iterations > 1)
     return D2G_E_INVAL;
   std::lock_guard<std::mutex> lk(g_cfg_mu);
   g_cfg = *cfg;

@@ -98,6 +98,8 @@ struct PlanArgs {
   const int *col_crow;      // per packed column: cost-table row (label * V + token, or the bin)
   int stage_costs;          // table costs (16 <= MP <= 128): next unit's rows by cp.async into smem
   int wide;                 // the phase has plans wider than one CTA
+  float *rowsum2_out;       // pair pass: step-4 row sums of the second iteration, by slot
+  float *rawsum_out;        // pair pass: raw row sums of the second iteration's Z', by slot
 };
 
 // per-MP launch geometry
@@ -121,6 +123,8 @@ cudaError_t launch_pack_columns(int MP, const PlanArgs &a, int nitems, const lon
                                 float *col_w, float *col_supp, int *col_sym, int dim, int DS,
                                 int dense_hist, cudaStream_t st);
 cudaError_t launch_obj(int MP, int mode, const PlanArgs &a, int nitems, cudaStream_t st);
+// plan_pair.cuh: two iterations per pass (phases without plans wider than a CTA, MP <= 128)
+cudaError_t launch_plan_pair(int MP, int mode, bool check, const PlanArgs &a, int nitems, cudaStream_t st);
 
 // defer_kernels.cu: deferred row normalisation of plans wider than one CTA
 cudaError_t launch_rowsum_combine(const int4 *wide, int nwide, const float *rowpart,
@@ -130,6 +134,13 @@ cudaError_t launch_plan_finalize(float *Z, float *Y, const int *item_g0, const i
                                  int nitems, int cs, int G, int S, int MP, const int4 *grp_rec,
                                  const float *rowsc, const unsigned char *def_iter, const Ctl *ctl,
                                  cudaStream_t st);
+// pair passes: the row scale c_w / rowsum(Z') of every plan (by slot), after the
+// cluster reduction of the pair's first iteration; and Z = Z' * scale,
+// Y = U - Z over every packed column, where a single pass or the end follows
+cudaError_t launch_pair_scale(const float *rawsum, const int *slot_label, const float *cw32, int nplans,
+                              int MP, int m, float *rowsc, const Ctl *ctl, int iter, cudaStream_t st);
+cudaError_t launch_pair_finalize(float *Z, float *Y, const int4 *grp_rec, int ngroups, int S, int MP,
+                                 const float *rowsc, cudaStream_t st);
 
 // kernels_reduce.cu
 struct ClusterArgs {

@@ -12,6 +12,10 @@
 // entry is that of the synchronous form: Z is the same product Z' * scale, Y
 // gets X and -Z in two roundings instead of one.  plan_finalize_kernel
 // applies the scale of the last iteration when the loop ends deferred.
+//
+// The pair passes of plan_pair.cuh leave every plan deferred the same way:
+// pair_scale_kernel forms the scale of every plan from its raw row sums, and
+// pair_finalize_kernel applies it where a single pass or the end follows.
 #include "d2g_internal.cuh"
 
 namespace d2g {
@@ -71,6 +75,50 @@ __global__ void __launch_bounds__(256) plan_finalize_kernel(float *__restrict__ 
     Z[base + e] = z;
     Y[base + e] = fmaf(-kLog2eF, z, Y[base + e]);
   }
+}
+
+// pair passes: one thread per (slot, row)
+__global__ void pair_scale_kernel(const float *__restrict__ rawsum, const int *__restrict__ slot_label,
+                                  const float *__restrict__ cw32, int nplans, int MP, int m,
+                                  float *__restrict__ rowsc, const Ctl *ctl, int iter) {
+  if (iter >= ctl->stop_iter) return;
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= (long long)nplans * MP) return;
+  const int slot = (int)(i / MP), k = (int)(i - (long long)slot * MP);
+  rowsc[i] = k < m ? __ldg(cw32 + (size_t)__ldg(slot_label + slot) * MP + k) / rawsum[i] : 0.f;
+}
+
+// Z = Z' * scale, Y = U - Z over every packed column (grid-stride over groups)
+__global__ void __launch_bounds__(256) pair_finalize_kernel(float *__restrict__ Z, float *__restrict__ Y,
+                                                            const int4 *__restrict__ grp_rec, int ngroups,
+                                                            int S, int MP, const float *__restrict__ rowsc) {
+  const int per = S * MP;
+  for (long long gi = blockIdx.x; gi < ngroups; gi += gridDim.x) {
+    const float *sc = rowsc + (size_t)__ldg(&grp_rec[gi].x) * MP;
+    const size_t base = (size_t)gi * per;
+    for (int e = threadIdx.x; e < per; e += blockDim.x) {
+      const float z = Z[base + e] * sc[e & (MP - 1)];
+      Z[base + e] = z;
+      Y[base + e] = fmaf(-kLog2eF, z, Y[base + e]);
+    }
+  }
+}
+
+cudaError_t launch_pair_scale(const float *rawsum, const int *slot_label, const float *cw32, int nplans,
+                              int MP, int m, float *rowsc, const Ctl *ctl, int iter, cudaStream_t st) {
+  const long long n = (long long)nplans * MP;
+  if (n <= 0) return cudaSuccess;
+  pair_scale_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rawsum, slot_label, cw32, nplans, MP, m,
+                                                                 rowsc, ctl, iter);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pair_finalize(float *Z, float *Y, const int4 *grp_rec, int ngroups, int S, int MP,
+                                 const float *rowsc, cudaStream_t st) {
+  if (ngroups <= 0) return cudaSuccess;
+  const int blocks = ngroups < 152 * 16 ? ngroups : 152 * 16;
+  pair_finalize_kernel<<<blocks, 256, 0, st>>>(Z, Y, grp_rec, ngroups, S, MP, rowsc);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_rowsum_combine(const int4 *wide, int nwide, const float *rowpart,

@@ -17,6 +17,8 @@ cudaError_t launch_pack_columns_mp(const PlanArgs &, int, const long long *, con
                                    int, int, cudaStream_t);
 template <int MP>
 cudaError_t launch_obj_mp(int, const PlanArgs &, int, cudaStream_t);
+template <int MP>
+cudaError_t launch_pair_mp(int, bool, const PlanArgs &, int, cudaStream_t);
 
 #define D2G_MP_SWITCH(MPV, CALL) \
   switch (MPV) {                 \
@@ -79,6 +81,12 @@ cudaError_t launch_pack_columns(int MP, const PlanArgs &a, int nitems, const lon
 #define C_(X)                                                                                   \
   launch_pack_columns_mp<X>(a, nitems, plan_cum, w_ref, supp_ref, sym_ref, col_w, col_supp,    \
                             col_sym, dim, DS, dense_hist, st)
+  D2G_MP_SWITCH(MP, C_)
+#undef C_
+}
+
+cudaError_t launch_plan_pair(int MP, int mode, bool check, const PlanArgs &a, int nitems, cudaStream_t st) {
+#define C_(X) launch_pair_mp<X>(mode, check, a, nitems, st)
   D2G_MP_SWITCH(MP, C_)
 #undef C_
 }

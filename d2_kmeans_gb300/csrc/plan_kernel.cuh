@@ -1149,6 +1149,12 @@ cudaError_t launch_obj_mp(int mode, const PlanArgs &a, int nitems, cudaStream_t 
   return cudaGetLastError();
 }
 
+}  // namespace d2g
+
+#include "plan_pair.cuh"
+
+namespace d2g {
+
 #define D2G_INSTANTIATE_MP(MPV)                                                                \
   template cudaError_t launch_plan_mp<MPV>(int, bool, const PlanArgs &, int, size_t,           \
                                            cudaStream_t);                                      \
@@ -1160,6 +1166,7 @@ cudaError_t launch_obj_mp(int mode, const PlanArgs &a, int nitems, cudaStream_t 
                                                    const double *, const double *, const int *, \
                                                    float *, float *, int *, int, int, int,      \
                                                    cudaStream_t);                               \
-  template cudaError_t launch_obj_mp<MPV>(int, const PlanArgs &, int, cudaStream_t);
+  template cudaError_t launch_obj_mp<MPV>(int, const PlanArgs &, int, cudaStream_t);          \
+  template cudaError_t launch_pair_mp<MPV>(int, bool, const PlanArgs &, int, cudaStream_t);
 
 }  // namespace d2g

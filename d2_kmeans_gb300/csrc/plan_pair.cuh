@@ -1,0 +1,513 @@
+// Two B-ADMM iterations per HBM pass, for phases whose plans each fit in one
+// CTA (included by plan_kernel.cuh).
+//
+// Iteration t runs in full: its row scale c_w[label] / rowsum(Z') needs only
+// the CTA's own columns and c_w as it stands after iteration t-1, which the
+// cluster reduction has produced before the pass.  Iteration t+1 then runs
+// step 1 and the first half of step 2 on the Z and Y of iteration t, still in
+// registers, and leaves deferred: Z' and U = Y + X are stored with the raw row
+// sums of Z' (its step-4 row sums too).  Once the cluster reduction of
+// iteration t has produced c_w, pair_scale_kernel forms the row scale
+// c_w / rowsum(Z') of every plan, and the next pass (or pair_finalize_kernel)
+// applies it on load: Z = Z' * scale, Y = U - Z.  Z and Y cross HBM once per two
+// iterations; the arithmetic per entry is that of two single passes, except
+// that the deferred Y is rounded twice (U, then U - Z).
+//
+// The host pairs iterations (t, t+1) only where this is exact: t is no
+// support-update iteration (its update would change the costs of t+1), t+1 is
+// no residual-check iteration (its check needs the final Z of t+1), and no
+// time budget is set (the reference may stop after any single iteration).
+//
+// flags: PF_IN_DEF   the input is deferred: every plan's row scale in a.rowsc [slot][MP]
+//        PF_UPDATE   iteration t+1 is a Euclidean support update: its X moments
+//        PF_WRITE_X  iteration t+1's X is stored (word-embedding support update)
+// CHECK: iteration t is a residual-check iteration.
+#pragma once
+
+namespace d2g {
+
+// seg_sum over the TPC lanes of this thread's aligned segment, with only those
+// lanes taking part (callable where other segments of the warp diverge)
+template <int TPC>
+__device__ __forceinline__ float seg_sum_lanes(float v) {
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned mask = TPC == 32 ? 0xffffffffu : (((1u << TPC) - 1u) << (lane & ~(unsigned)(TPC - 1)));
+#pragma unroll
+  for (int o = TPC / 2; o >= 1; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+  return v;
+}
+
+template <int MP, int MODE, bool CHECK, bool FULL>
+__global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanArgs a, int nitems) {
+  using T = Tile<MP, MODE>;
+  constexpr int RPT = T::RPT, TPC = T::TPC, G = T::G, S = T::S;
+  constexpr int TILE = tma_tile_floats<MP>();
+  constexpr int JC = G * S;
+  constexpr int CW = T::EUC ? T::DS : 1;
+  constexpr bool SCC = plan_stages_costs(MP, MODE);
+  constexpr int CPR = MP / 4;
+  constexpr int NT = GeoT<MP>::NT;
+  constexpr int PPT = SCC ? TILE / 4 / NT : 1;
+  const bool SC = SCC && a.stage_costs;
+  extern __shared__ __align__(128) float smem[];
+  float *stZ = smem;                             // [2][TILE]
+  float *stY = smem + 2 * TILE;                  // [2][TILE]
+  int4 *stR = (int4 *)(smem + 4 * TILE);         // [2][G] group records
+  float *stW = (float *)(stR + 2 * G);           // [2][JC] weights
+  float *stC = stW + 2 * JC;                     // [2][JC*CW] supports / table rows
+  float *stK = stC + 2 * JC * CW;                // [2][TILE] staged table costs (SC)
+  float *sm_rs = stK + (SCC ? 2 * TILE : 0);     // [G][MP] row partials of iteration t
+  float *sm_rs2 = sm_rs + G * MP;                // [G][MP] row partials of iteration t+1
+  float *sm_mom = sm_rs2 + G * MP;               // [dim+1][G][MP] X moments of iteration t+1
+  __shared__ __align__(8) unsigned long long mbar[2];
+  __shared__ int sh_fail;
+  __shared__ int sh_g0[2], sh_ng[2];
+
+  if (a.iter >= a.ctl->stop_iter) return;
+  const int tid = threadIdx.x;
+  const int u0 = blockIdx.x, ustep = gridDim.x, nunits = nitems;
+  if (a.iter == 0 && blockIdx.x == 0 && tid == 0) a.ctl->t_start_ns = global_ns();
+  auto issue = [&](int g0, int ng, int stg) {
+    const size_t off = (size_t)g0 * S * MP;
+    const unsigned bytes = (unsigned)ng * S * MP * 4u;
+    const unsigned rb = (unsigned)ng * 16u, wb = (unsigned)ng * S * 4u, cb = wb * CW;
+    mbar_expect_tx(&mbar[stg], 2u * bytes + rb + wb + cb);
+    if (ng <= 0) return;
+    bulk_load(stZ + stg * TILE, a.Z + off, bytes, &mbar[stg]);
+    bulk_load(stY + stg * TILE, a.Y + off, bytes, &mbar[stg]);
+    bulk_load(stR + stg * G, a.grp_rec + g0, rb, &mbar[stg]);
+    bulk_load(stW + stg * JC, a.col_w + (size_t)g0 * S, wb, &mbar[stg]);
+    if constexpr (T::EUC)
+      bulk_load(stC + stg * JC * CW, a.col_supp + (size_t)g0 * S * CW, cb, &mbar[stg]);
+    else
+      bulk_load(stC + stg * JC * CW, a.col_sym + (size_t)g0 * S, cb, &mbar[stg]);
+  };
+  int crow_p[PPT];
+  auto load_rows_idx = [&](int g0, int ng) {
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+      const int c = (tid + NT * j) / CPR;
+      crow_p[j] = c < ng * S ? __ldg(a.col_crow + (size_t)g0 * S + c) : -1;
+    }
+  };
+  auto issue_rows = [&](int stg) {
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+      const int i = tid + NT * j, c = i / CPR, part = i - c * CPR;
+      if (crow_p[j] >= 0)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                         smem_u32(stK + stg * TILE + c * MP + part * 4)),
+                     "l"(a.ctab + (size_t)crow_p[j] * MP + part * 4)
+                     : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  int nx_g0 = 0, nx_ng = 0;
+  if (tid == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    sh_fail = 0;
+    mbar_fence_init();
+    if (u0 < nunits) {
+      const int g0 = a.item_g0[u0], ng = a.item_ng[u0];
+      sh_g0[0] = g0;
+      sh_ng[0] = ng;
+      issue(g0, ng, 0);
+      if (u0 + ustep < nunits) {
+        nx_g0 = a.item_g0[u0 + ustep];
+        nx_ng = a.item_ng[u0 + ustep];
+      }
+    }
+  }
+  if (SC && u0 < nunits) {
+    __syncthreads();
+    load_rows_idx(sh_g0[0], sh_ng[0]);
+    issue_rows(0);
+  }
+  __syncthreads();
+
+  const int m = a.m;
+  const float inv_rho = a.ctl->inv_rho;
+  const float ir2 = a.ctl->inv_rho_l2;
+  const bool indef = a.flags & PF_IN_DEF;
+  const bool update = T::EUC && (a.flags & PF_UPDATE);
+  const bool write_x = a.flags & PF_WRITE_X;
+  double s_obj = 0.0, s_pr = 0.0, s_dr = 0.0;
+  int it = 0;
+  for (int u = u0; u < nunits; u += ustep, ++it) {
+    const int stg = it & 1;
+    if (!mbar_wait(&mbar[stg], (it >> 1) & 1)) sh_fail = 1;
+    if (SC) asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();
+    if (sh_fail) break;
+    const int cur_g0 = sh_g0[stg], cur_ng = sh_ng[stg];
+    if (tid == 0 && u + ustep < nunits) {
+      issue(nx_g0, nx_ng, stg ^ 1);
+      sh_g0[stg ^ 1] = nx_g0;
+      sh_ng[stg ^ 1] = nx_ng;
+      if (u + 2 * ustep < nunits) {
+        nx_g0 = a.item_g0[u + 2 * ustep];
+        nx_ng = a.item_ng[u + 2 * ustep];
+      }
+    }
+    const bool has_next = u + ustep < nunits;
+
+    T t;
+    t.init_rec(stR[stg * G + (threadIdx.x / TPC)], cur_g0, cur_ng);
+    t.load_costs_staged(a, stC + stg * JC * CW, (const int *)(stC + stg * JC * CW));
+    const float *zs = stZ + stg * TILE, *ys = stY + stg * TILE;
+    const int lcol0 = t.g * S;
+    float w[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) w[s] = s < t.nvalid ? stW[stg * JC + lcol0 + s] : 0.f;
+    // deferred input: this plan's row scale (slot t.p)
+    float scin[RPT];
+#pragma unroll
+    for (int q = 0; q < RPT; ++q)
+      scin[q] = (indef && t.active) ? __ldg(a.rowsc + (size_t)t.p * MP + t.k0 + q) : 1.f;
+    auto ld_zy = [&](int s, float (&z)[RPT], float (&y)[RPT]) {
+#pragma unroll
+      for (int q4 = 0; q4 < RPT / 4; ++q4) {
+        const float4 zz = *((const float4 *)(zs + (lcol0 + s) * MP + t.k0) + q4);
+        const float4 yy = *((const float4 *)(ys + (lcol0 + s) * MP + t.k0) + q4);
+        z[4 * q4] = zz.x; z[4 * q4 + 1] = zz.y; z[4 * q4 + 2] = zz.z; z[4 * q4 + 3] = zz.w;
+        y[4 * q4] = yy.x; y[4 * q4 + 1] = yy.y; y[4 * q4 + 2] = yy.z; y[4 * q4 + 3] = yy.w;
+      }
+      if (indef) {
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+          z[q] *= scin[q];
+          y[q] = fmaf(-kLog2e, z[q], y[q]);
+        }
+      }
+    };
+    auto costs = [&](int s, float (&c)[RPT]) {
+      if (SC) {
+#pragma unroll
+        for (int q4 = 0; q4 < RPT / 4; ++q4) {
+          const float4 v = *((const float4 *)(stK + stg * TILE + (lcol0 + s) * MP + t.k0) + q4);
+          c[4 * q4] = v.x; c[4 * q4 + 1] = v.y; c[4 * q4 + 2] = v.z; c[4 * q4 + 3] = v.w;
+        }
+      } else {
+        t.costs(s, c);
+      }
+    };
+    // steps 1 and 2 up to Z' of one column: x (X), zp (Z'); returns nothing, fills arrays
+    auto half = [&](int s, const float (&c)[RPT], const float (&z)[RPT], const float (&y)[RPT],
+                    float (&x)[RPT], float (&zp)[RPT]) {
+      const bool colok = s < t.nvalid;
+      float csum = 0.f;
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        float v;
+        if constexpr (FULL) {
+          v = fmaf(z[q], ex2f(-fmaf(c[q], ir2, y[q])), kRoundoff);
+        } else {
+          const bool ok = colok && t.k0 + q < m;
+          v = ok ? fmaf(z[q], ex2f(-fmaf(c[q], ir2, y[q])), kRoundoff) : 0.f;
+        }
+        x[q] = v;
+        csum += v;
+      }
+      csum = seg_sum<TPC>(csum);
+      const float f = (FULL || colok) ? __fdividef(w[s], csum) : 0.f;
+      const float eps2 = colok ? kRoundoff : 0.f;
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        x[q] *= f;
+        if constexpr (FULL) {
+          zp[q] = fmaf(x[q], ex2f(y[q]), eps2);
+        } else {
+          const bool ok = colok && t.k0 + q < m;
+          zp[q] = ok ? fmaf(x[q], ex2f(y[q]), kRoundoff) : 0.f;
+        }
+      }
+    };
+    // the plan totals of the row partials in buf: the first group of each plan
+    // sums them once and publishes the total in place of its own partial
+    const int lo = t.active ? max(t.pl_g0 - t.cta_g0, 0) : 0;
+    const int hi = t.active ? min(t.pl_g0 + t.pl_ng - t.cta_g0, t.cta_ng) : 0;
+    const bool writer = t.active && t.g == lo;
+
+    // ---------------- iteration t: steps 1-3 in full
+    float x[S][RPT], zp[S][RPT];
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      float c[RPT], z[RPT], y[RPT];
+      costs(s, c);
+      ld_zy(s, z, y);
+      half(s, c, z, y, x[s], zp[s]);
+    }
+    {
+      float rp[RPT];
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        rp[q] = 0.f;
+#pragma unroll
+        for (int s = 0; s < S; ++s) rp[q] += zp[s][q];
+      }
+      st_rows_sm(sm_rs + t.g * MP + t.k0, rp);
+    }
+    __syncthreads();
+    if (SC && has_next) load_rows_idx(sh_g0[stg ^ 1], sh_ng[stg ^ 1]);
+    float tot[RPT];
+    if (writer) {
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) tot[q] = 0.f;
+      for (int j = lo; j < hi; ++j) {
+#pragma unroll
+        for (int q4 = 0; q4 < RPT / 4; ++q4) {
+          const float4 u4 = *((const float4 *)(sm_rs + j * MP + t.k0) + q4);
+          tot[4 * q4] += u4.x;
+          tot[4 * q4 + 1] += u4.y;
+          tot[4 * q4 + 2] += u4.z;
+          tot[4 * q4 + 3] += u4.w;
+        }
+      }
+      st_rows_sm(sm_rs + lo * MP + t.k0, tot);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q4 = 0; q4 < RPT / 4; ++q4) {
+      const float4 u4 = *((const float4 *)(sm_rs + lo * MP + t.k0) + q4);
+      tot[4 * q4] = u4.x;
+      tot[4 * q4 + 1] = u4.y;
+      tot[4 * q4 + 2] = u4.z;
+      tot[4 * q4 + 3] = u4.w;
+    }
+    {
+      float rsum = 0.f;  // step 4's per-instance normalisation of Zr (:180)
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) rsum += (FULL || t.k0 + q < m) ? tot[q] : 0.f;
+      rsum = seg_sum<TPC>(rsum);
+      if (writer) {
+        float zr[RPT];
+        const float inv = 1.f / rsum;
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) zr[q] = tot[q] * inv;
+        st_rows(a.rowsum_out + (size_t)t.p * MP + t.k0, zr);
+      }
+    }
+    float sc[RPT];
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+      const bool ok = t.active && (FULL || t.k0 + q < m);
+      sc[q] = ok ? __fdividef(__ldg(a.cw32 + (size_t)t.lab * MP + t.k0 + q), tot[q]) : 0.f;
+    }
+    // second half of step 2 and step 3: Z and Y of iteration t stay in registers
+    float zt[S][RPT], yt[S][RPT];
+    float i_obj = 0.f, i_pr = 0.f, i_dr = 0.f;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      float z0[RPT], y[RPT];
+      ld_zy(s, z0, y);
+      const bool colok = s < t.nvalid;
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        const float zn = colok ? zp[s][q] * sc[q] : 0.f;
+        zt[s][q] = zn;
+        yt[s][q] = colok ? fmaf(kLog2e, x[s][q] - zn, y[q]) : 0.f;
+      }
+      if constexpr (CHECK) {
+        if (colok) {
+          float c[RPT];
+          costs(s, c);
+#pragma unroll
+          for (int q = 0; q < RPT; ++q) {
+            i_obj = fmaf(c[q] * inv_rho, x[s][q], i_obj);
+            i_pr += fabsf(x[s][q] - zt[s][q]);
+            i_dr += fabsf(zt[s][q] - z0[q]);
+          }
+        }
+      }
+    }
+    if constexpr (CHECK) {
+      s_obj += i_obj;
+      s_pr += i_pr;
+      s_dr += i_dr;
+    }
+
+    // ---------------- iteration t+1: steps 1 and 2 up to Z', deferred output
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      float c[RPT];
+      costs(s, c);
+      half(s, c, zt[s], yt[s], x[s], zp[s]);
+      if (s < t.nvalid) {
+        float un[RPT];
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) un[q] = fmaf(kLog2e, x[s][q], yt[s][q]);  // U = Y + X
+        const size_t off = (t.colbase + s) * MP + t.k0;
+        st_rows(a.Z + off, zp[s]);
+        st_rows(a.Y + off, un);
+        if (write_x) st_rows(a.X_out + off, x[s]);
+      }
+    }
+    {
+      float rp[RPT];
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        rp[q] = 0.f;
+#pragma unroll
+        for (int s = 0; s < S; ++s) rp[q] += zp[s][q];
+      }
+      st_rows_sm(sm_rs2 + t.g * MP + t.k0, rp);
+    }
+    if constexpr (T::EUC) {
+      if (update) {  // X moments of iteration t+1 (step 5)
+        for (int d = 0; d <= a.dim; ++d) {
+          float mv[RPT];
+#pragma unroll
+          for (int q = 0; q < RPT; ++q) {
+            float acc = 0.f;
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+              float sv = 1.f;
+              if (d < a.dim) {
+#pragma unroll
+                for (int tt = 0; tt < T::DS; ++tt)
+                  if (tt == d) sv = t.sp[s][tt];
+              }
+              acc = fmaf(x[s][q], sv, acc);
+            }
+            mv[q] = acc;
+          }
+          st_rows_sm(sm_mom + (d * G + t.g) * MP + t.k0, mv);
+        }
+      }
+    }
+    __syncthreads();
+    if (writer) {
+      float tot2[RPT];
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) tot2[q] = 0.f;
+      for (int j = lo; j < hi; ++j) {
+#pragma unroll
+        for (int q4 = 0; q4 < RPT / 4; ++q4) {
+          const float4 u4 = *((const float4 *)(sm_rs2 + j * MP + t.k0) + q4);
+          tot2[4 * q4] += u4.x;
+          tot2[4 * q4 + 1] += u4.y;
+          tot2[4 * q4 + 2] += u4.z;
+          tot2[4 * q4 + 3] += u4.w;
+        }
+      }
+      st_rows(a.rawsum_out + (size_t)t.p * MP + t.k0, tot2);
+      float rsum = 0.f;
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) rsum += (FULL || t.k0 + q < m) ? tot2[q] : 0.f;
+      // the writer threads of one plan are the TPC threads of its first group,
+      // one aligned segment of the warp: the sum runs among those lanes only
+      rsum = seg_sum_lanes<TPC>(rsum);
+      float zr[RPT];
+      const float inv = 1.f / rsum;
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) zr[q] = tot2[q] * inv;
+      st_rows(a.rowsum2_out + (size_t)t.p * MP + t.k0, zr);
+      if (T::EUC && update) {
+        float *xo = a.xmom_out + (size_t)t.p * (a.dim + 1) * MP;
+        for (int d = 0; d <= a.dim; ++d) {
+          float mv[RPT];
+#pragma unroll
+          for (int q = 0; q < RPT; ++q) mv[q] = 0.f;
+          for (int j = lo; j < hi; ++j)
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) mv[q] += sm_mom[(d * G + j) * MP + t.k0 + q];
+          st_rows(xo + d * MP + t.k0, mv);
+        }
+      }
+    }
+    if (SC && has_next) issue_rows(stg ^ 1);
+    // No barrier here: the next unit's opening barrier orders every reuse of
+    // the stage, the row partials and the staged rows.
+  }
+  if (SC) asm volatile("cp.async.wait_all;" ::: "memory");
+  if (sh_fail) {
+    if (tid == 0) {
+      a.ctl->err = 7;
+      mbar_wait(&mbar[0], 0);
+      mbar_wait(&mbar[1], 0);
+    }
+    return;
+  }
+  if constexpr (CHECK) {
+    __shared__ double res[3];
+    block_sum3<NT>(s_obj, s_pr, s_dr, res);
+    if (tid == 0 && u0 < nitems) {
+      double *pp = a.resid_part + (size_t)(a.resid_off + u0) * 4;
+      pp[0] = res[0];
+      pp[1] = res[1];
+      pp[2] = res[2];
+      for (int item = u0 + ustep; item < nitems; item += ustep) {
+        double *qq = a.resid_part + (size_t)(a.resid_off + item) * 4;
+        qq[0] = qq[1] = qq[2] = 0.0;
+      }
+    }
+  }
+}
+
+// shared memory of plan_pair_kernel beyond its static part
+template <int MP>
+size_t pair_smem_bytes(int mode, int dim) {
+  using Gm = GeoT<MP>;
+  const int cw = mode == COST_TABLE ? 1 : (mode == COST_EUCLID8 ? 8 : 4);
+  return (size_t)4 * tma_tile_floats<MP>() * 4 + 2 * (size_t)Gm::G * 16 + 2 * (size_t)Gm::JC * 4 * (1 + cw) +
+         (plan_stages_costs(MP, mode) ? (size_t)2 * tma_tile_floats<MP>() * 4 : 0) +
+         (size_t)2 * Gm::G * MP * 4 + (size_t)(dim + 1) * Gm::G * MP * 4;
+}
+
+template <int MP, int MODE, bool CHECK, bool FULL>
+cudaError_t launch_pair_t(const PlanArgs &a, int nitems, cudaStream_t st) {
+  static int grid = 0, nsm = 0;
+  static size_t configured = 0;
+  const size_t sm = pair_smem_bytes<MP>(MODE, a.dim);
+  auto kern = plan_pair_kernel<MP, MODE, CHECK, FULL>;
+  if (configured < sm) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    configured = sm;
+    grid = 0;
+  }
+  if (grid == 0) {
+    int dev = 0, per = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, GeoT<MP>::NT, sm);
+    if (e != cudaSuccess) return e;
+    grid = (per > 0 ? per : 1) * nsm;
+  }
+  if (nitems <= 0) return cudaSuccess;
+  int cap = grid;
+  if (a.ctas_per_sm > 0) cap = std::min(cap, a.ctas_per_sm * nsm);
+  const int g = nitems < cap ? nitems : cap;
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = plan_cfg(g, GeoT<MP>::NT, sm, st, attr, 1);
+  return cudaLaunchKernelEx(&cfg, kern, a, nitems);
+}
+
+template <int MP, int MODE, bool CHECK>
+cudaError_t launch_pair_c(const PlanArgs &a, int nitems, cudaStream_t st) {
+  if (a.m == MP) return launch_pair_t<MP, MODE, CHECK, true>(a, nitems, st);
+  return launch_pair_t<MP, MODE, CHECK, false>(a, nitems, st);
+}
+
+// the pair kernel exists for MP <= 128: 256-row plans are always wider than a CTA
+template <int MP>
+cudaError_t launch_pair_mp(int mode, bool check, const PlanArgs &a, int nitems, cudaStream_t st) {
+  if constexpr (MP >= 256) {
+    return cudaErrorInvalidValue;
+  } else {
+    if (mode == COST_EUCLID3)
+      return check ? launch_pair_c<MP, COST_EUCLID3, true>(a, nitems, st)
+                   : launch_pair_c<MP, COST_EUCLID3, false>(a, nitems, st);
+    if (mode == COST_EUCLID4)
+      return check ? launch_pair_c<MP, COST_EUCLID4, true>(a, nitems, st)
+                   : launch_pair_c<MP, COST_EUCLID4, false>(a, nitems, st);
+    if (mode == COST_EUCLID8)
+      return check ? launch_pair_c<MP, COST_EUCLID8, true>(a, nitems, st)
+                   : launch_pair_c<MP, COST_EUCLID8, false>(a, nitems, st);
+    return check ? launch_pair_c<MP, COST_TABLE, true>(a, nitems, st)
+                 : launch_pair_c<MP, COST_TABLE, false>(a, nitems, st);
+  }
+}
+
+}  // namespace d2g

@@ -197,6 +197,8 @@ typedef struct {
                        0 tensor cores, 3xTF32 (default); 1 FP32 CUDA cores */
   int keep_time_budget; /* 0: the labelings set time_budget from their wall time as
                            the reference's do (default); 1: they leave it as it is */
+  int pair_iterations;  /* 1: the batched form runs two iterations per pass over the
+                           plans where that is exact (default); 0: one per pass */
 } d2g_config;
 
 int d2g_get_config(d2g_config *cfg);

@@ -405,3 +405,71 @@ def test_dropin_random_init_uses_the_programs_rands(d2g, rands_stub):
     assert np.array_equal(a.Z(), b.Z())
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("case", ["euclid_upl10", "euclid_upl7_odd", "euclid_d8", "hist16", "embed_small", "m6_d2"])
+def test_pair_passes_match_the_oracle_and_single_passes(d2g, oracle_mod, case):
+    """Two iterations per HBM pass (plan_pair.cuh) against the oracle and
+    against one iteration per pass: the same bounds; odd updatePerLoops and
+    odd iteration counts put single passes after pairs (their deferred scale
+    applied first)."""
+    if case == "euclid_upl10":
+        ph, c = synth.euclidean_phase(300, 5, 32, 3, (8, 128), True, 12, 0.5, seed=71)
+        opts = dict(maxIters=60, rhoCoeff=2.0, updatePerLoops=10)
+    elif case == "euclid_upl7_odd":
+        ph, c = synth.euclidean_phase(250, 4, 16, 3, (4, 60), False, 8, 1.0, seed=72)
+        opts = dict(maxIters=45, rhoCoeff=2.0, updatePerLoops=7)
+    elif case == "euclid_d8":
+        ph, c = synth.euclidean_phase(200, 4, 12, 7, (3, 40), False, 6, 1.0, seed=73)
+        opts = dict(maxIters=40, rhoCoeff=1.5, updatePerLoops=5)
+    elif case == "hist16":
+        ph, c = synth.histogram_phase(150, 4, side=4, alpha=0.2, seed=74)
+        opts = dict(maxIters=50, rhoCoeff=2.0, updatePerLoops=10)
+    elif case == "embed_small":
+        ph, c = synth.embed_phase(120, 3, 8, V=400, dim=16, sizes=(3, 30), seed=75)
+        opts = dict(maxIters=40, rhoCoeff=2.0, updatePerLoops=10)
+    else:
+        ph, c = synth.euclidean_phase(180, 3, 6, 2, (2, 20), False, 5, 1.0, seed=76)
+        opts = dict(maxIters=33, rhoCoeff=2.0, updatePerLoops=4)
+    k, m = ph["num_of_labels"], ph["str"]
+    ref = _port(oracle_mod, ph, c, opts)
+    passes = {}
+    for pairs in (1, 0):
+        d2g.set_config(pair_iterations=pairs)
+        try:
+            P = d2g.Phase(ph, 0)
+            r = P.run(c, opts)
+            r["Z"] = P.get_plans()
+            d2g.set_config(profile=1)  # one timed launch per pass over the plans
+            P.run(c, opts)
+            passes[pairs] = P.stats()["plan_launches"]
+            P.close()
+        finally:
+            d2g.set_config(pair_iterations=1, profile=0)
+        assert r["stats"]["iterations"] == opts["maxIters"] + 1
+        assert_close(r, ref, k, m)
+        assert _plan_l1(r["Z"], ref["Z"]) <= 1e-4
+    # about half the passes over the plans with pairs
+    assert passes[0] == opts["maxIters"] + 1
+    assert passes[1] <= 0.75 * passes[0], passes
+
+
+def test_pair_passes_warm_start_and_budget(d2g, oracle_mod):
+    """A warm-started second call on plans left by a pair pass; with a time
+    budget the loop runs single passes and stops after iteration 0."""
+    ph, c = synth.euclidean_phase(200, 4, 16, 3, (4, 40), False, 8, 1.0, seed=77)
+    o1 = dict(maxIters=30, rhoCoeff=2.0, updatePerLoops=10)
+    r1 = _port(oracle_mod, ph, c, o1)
+    ph2 = dict(ph, label_switch=np.zeros(len(ph["p_str"]), np.int8))
+    r2 = _port(oracle_mod, ph2, dict(c_w=r1["c_w"], c_supp=r1["c_supp"], Z=r1["Z"]), o1)
+    P = d2g.Phase(ph, 0)
+    g1 = P.run(c, o1)
+    assert_close(g1, r1, 4, 16)
+    assert _plan_l1(P.get_plans(), r1["Z"]) <= 1e-4
+    g2 = P.run(dict(c_w=g1["c_w"], c_supp=g1["c_supp"]), o1, label_switch=ph2["label_switch"])
+    assert_close(g2, r2, 4, 16)
+    r0 = _port(oracle_mod, ph, c, dict(maxIters=0, rhoCoeff=2.0, updatePerLoops=10))
+    g0 = P.run(c, dict(maxIters=30, rhoCoeff=2.0, updatePerLoops=10, time_budget=1e-9))
+    assert g0["stats"]["iterations"] == 1
+    assert np.abs(g0["c_w"] - r0["c_w"]).reshape(4, 16).sum(1).max() < 1e-5
+    P.close()
