@@ -14,7 +14,8 @@ Prints one JSON line:
              d2_centroid_sphBregman with host buffers (inputs from pinned host
              memory, results back to the caller's arrays) inside the timing
   plain_gpu  the plain FP64 one-kernel-per-step GPU form on the same inputs
-  roofline   the plan-update kernel against the measured HBM copy bandwidth
+  roofline   the plan-update pass against the measured HBM copy bandwidth (a pass
+             runs two B-ADMM iterations where that is exact, plan_pair.cuh)
   cpu_baseline  the C restatement of the reference (oracle port) on the host
   workloads  the word-embedding, 256-bin histogram and two-phase Euclidean
              workloads: plan-updates/s and the plan kernel against the HBM peak
@@ -604,9 +605,13 @@ def main():
         if os.path.exists(tp):
             with open(tp) as f:
                 traffic = json.load(f).get("traffic_bytes_per_launch")
+        passes = ps["plan_launches"]  # passes over the plans (profile mode times each one)
+        paired = passes < stats["iterations"]
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
-                "kernel": "plan_kernel_tma<32, EUCLID3>",
+                "kernel": ("plan_pair_kernel<32, EUCLID3> (two B-ADMM iterations per pass over the plans)"
+                           if paired else "plan_kernel_tma<32, EUCLID3>"),
+                "passes_per_step": passes, "iterations_per_pass": stats["iterations"] / passes,
                 "algo_bytes_per_launch": ps["plan_bytes"], "ms_per_launch": ps["plan_ms_avg"]}
     trace_b = r["trace"]
     cw_b = r["c_w"].copy()

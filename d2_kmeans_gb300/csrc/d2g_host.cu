@@ -453,6 +453,8 @@ static PlanArgs base_args(d2g_phase *ph) {
   a.wide = ph->nwide > 0;
   a.rowsum2_out = ph->rowsum2.p;
   a.rawsum_out = ph->rawsum.p;
+  a.nplans_chk = ph->nplans;
+  a.nlab_chk = ph->K;
   return a;
 }
 
@@ -802,6 +804,11 @@ static int create_batched(d2g_phase *ph, const d2g_phase_desc *d) {
     for (int chk = 0; chk < 2; ++chk)
       D2G_CUDA(launch_plan(ph->MP, ph->mode, chk, a, 0, ph->smem_plan_upd, ph->st));
   }
+  if (ph->rowsum2.n > 0) {  // the pair kernel too (its smem limit and grid), MP <= 128
+    PlanArgs a = base;
+    a.cs = 1;
+    for (int chk = 0; chk < 2; ++chk) D2G_CUDA(launch_plan_pair(ph->MP, ph->mode, chk, a, 0, ph->st));
+  }
   return D2G_OK;
 }
 
@@ -1084,7 +1091,7 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
         // then step 4 (and step 5) of it + 1
         D2G_CUDA(launch_cluster_reduce(cluster_args(ph, it, false), ph->st));
         D2G_CUDA(launch_pair_scale(ph->rawsum.p, ph->slot_label.p, ph->cw32.p, ph->nplans, ph->MP, ph->str,
-                                   ph->rowsc.p, ph->ctl.p, t1, ph->st));
+                                   ph->rowsc.p, ph->ctl.p, t1, ph->K, ph->st));
         ClusterArgs c1 = cluster_args(ph, t1, upd1 && euc);
         c1.rowsum32 = ph->rowsum2.p;
         D2G_CUDA(launch_cluster_reduce(c1, ph->st));
@@ -1106,7 +1113,7 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
       }
       if (pend) {  // a single pass follows a pair: apply the pending scale first
         D2G_CUDA(launch_pair_finalize(ph->Z.p, ph->Y.p, ph->grp_rec.p, ph->ngroups, ph->geo.S, ph->MP,
-                                      ph->rowsc.p, ph->st));
+                                      ph->rowsc.p, ph->nplans, &ph->ctl.p->err, ph->st));
         ++nl;
         pend = false;
       }
@@ -1187,7 +1194,7 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
     }
     if (pend) {  // the loop ended on a pair: its second iteration's scale
       D2G_CUDA(launch_pair_finalize(ph->Z.p, ph->Y.p, ph->grp_rec.p, ph->ngroups, ph->geo.S, ph->MP,
-                                    ph->rowsc.p, ph->st));
+                                    ph->rowsc.p, ph->nplans, &ph->ctl.p->err, ph->st));
       ++nl;
     }
     if (ph->defer) {  // the scale of the last iteration that ran, if it ran deferred

@@ -100,6 +100,7 @@ struct PlanArgs {
   int wide;                 // the phase has plans wider than one CTA
   float *rowsum2_out;       // pair pass: step-4 row sums of the second iteration, by slot
   float *rawsum_out;        // pair pass: raw row sums of the second iteration's Z', by slot
+  int nplans_chk, nlab_chk; // plans and clusters of the phase (self-check of staged records)
 };
 
 // per-MP launch geometry
@@ -138,9 +139,10 @@ cudaError_t launch_plan_finalize(float *Z, float *Y, const int *item_g0, const i
 // cluster reduction of the pair's first iteration; and Z = Z' * scale,
 // Y = U - Z over every packed column, where a single pass or the end follows
 cudaError_t launch_pair_scale(const float *rawsum, const int *slot_label, const float *cw32, int nplans,
-                              int MP, int m, float *rowsc, const Ctl *ctl, int iter, cudaStream_t st);
+                              int MP, int m, float *rowsc, const Ctl *ctl, int iter, int nlab,
+                              cudaStream_t st);
 cudaError_t launch_pair_finalize(float *Z, float *Y, const int4 *grp_rec, int ngroups, int S, int MP,
-                                 const float *rowsc, cudaStream_t st);
+                                 const float *rowsc, int nslot, int *err, cudaStream_t st);
 
 // kernels_reduce.cu
 struct ClusterArgs {

@@ -77,47 +77,74 @@ __global__ void __launch_bounds__(256) plan_finalize_kernel(float *__restrict__ 
   }
 }
 
-// pair passes: one thread per (slot, row)
-__global__ void pair_scale_kernel(const float *__restrict__ rawsum, const int *__restrict__ slot_label,
-                                  const float *__restrict__ cw32, int nplans, int MP, int m,
-                                  float *__restrict__ rowsc, const Ctl *ctl, int iter) {
+// pair passes: one thread per (slot, 4 rows)
+__global__ void pair_scale_kernel(const float4 *__restrict__ rawsum, const int *__restrict__ slot_label,
+                                  const float *__restrict__ cw32, long long n4, int MP, int m,
+                                  float4 *__restrict__ rowsc, const Ctl *ctl, int iter, int nlab) {
   if (iter >= ctl->stop_iter) return;
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i >= (long long)nplans * MP) return;
-  const int slot = (int)(i / MP), k = (int)(i - (long long)slot * MP);
-  rowsc[i] = k < m ? __ldg(cw32 + (size_t)__ldg(slot_label + slot) * MP + k) / rawsum[i] : 0.f;
+  if (i >= n4) return;
+  const long long e = i * 4;
+  const int slot = (int)(e / MP), k = (int)(e - (long long)slot * MP);
+  const int lab = __ldg(slot_label + slot);
+  if (lab < 0 || lab >= nlab || (k & 3)) {  // self-check: a label outside the clusters
+    ((Ctl *)ctl)->err = 9;
+    return;
+  }
+  const float4 cw = __ldg((const float4 *)(cw32 + (size_t)lab * MP + k));
+  const float4 r = rawsum[i];
+  rowsc[i] = make_float4(k + 0 < m ? cw.x / r.x : 0.f, k + 1 < m ? cw.y / r.y : 0.f,
+                         k + 2 < m ? cw.z / r.z : 0.f, k + 3 < m ? cw.w / r.w : 0.f);
 }
 
-// Z = Z' * scale, Y = U - Z over every packed column (grid-stride over groups)
-__global__ void __launch_bounds__(256) pair_finalize_kernel(float *__restrict__ Z, float *__restrict__ Y,
-                                                            const int4 *__restrict__ grp_rec, int ngroups,
-                                                            int S, int MP, const float *__restrict__ rowsc) {
-  const int per = S * MP;
-  for (long long gi = blockIdx.x; gi < ngroups; gi += gridDim.x) {
-    const float *sc = rowsc + (size_t)__ldg(&grp_rec[gi].x) * MP;
-    const size_t base = (size_t)gi * per;
-    for (int e = threadIdx.x; e < per; e += blockDim.x) {
-      const float z = Z[base + e] * sc[e & (MP - 1)];
-      Z[base + e] = z;
-      Y[base + e] = fmaf(-kLog2eF, z, Y[base + e]);
+// Z = Z' * scale, Y = U - Z over every packed column: one float4 (4 rows of a
+// column) per thread
+__global__ void __launch_bounds__(256) pair_finalize_kernel(float4 *__restrict__ Z, float4 *__restrict__ Y,
+                                                            const int4 *__restrict__ grp_rec, long long n4,
+                                                            int S, int MP, const float *__restrict__ rowsc,
+                                                            int nslot, int *err) {
+  const long long per4 = (long long)S * MP / 4;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int slot = __ldg(&grp_rec[i / per4].x);
+    const int k0 = (int)((i * 4) % MP);
+    if (slot < 0 || slot >= nslot) {  // self-check: a slot outside the plans
+      *err = 9;
+      continue;
     }
+    const float4 sc = __ldg((const float4 *)(rowsc + (size_t)slot * MP + k0));
+    float4 z = Z[i], y = Y[i];
+    z.x *= sc.x;
+    z.y *= sc.y;
+    z.z *= sc.z;
+    z.w *= sc.w;
+    y.x = fmaf(-kLog2eF, z.x, y.x);
+    y.y = fmaf(-kLog2eF, z.y, y.y);
+    y.z = fmaf(-kLog2eF, z.z, y.z);
+    y.w = fmaf(-kLog2eF, z.w, y.w);
+    Z[i] = z;
+    Y[i] = y;
   }
 }
 
 cudaError_t launch_pair_scale(const float *rawsum, const int *slot_label, const float *cw32, int nplans,
-                              int MP, int m, float *rowsc, const Ctl *ctl, int iter, cudaStream_t st) {
-  const long long n = (long long)nplans * MP;
-  if (n <= 0) return cudaSuccess;
-  pair_scale_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rawsum, slot_label, cw32, nplans, MP, m,
-                                                                 rowsc, ctl, iter);
+                              int MP, int m, float *rowsc, const Ctl *ctl, int iter, int nlab,
+                              cudaStream_t st) {
+  const long long n4 = (long long)nplans * MP / 4;
+  if (n4 <= 0) return cudaSuccess;
+  pair_scale_kernel<<<(unsigned)((n4 + 255) / 256), 256, 0, st>>>((const float4 *)rawsum, slot_label, cw32, n4,
+                                                                  MP, m, (float4 *)rowsc, ctl, iter, nlab);
   return cudaGetLastError();
 }
 
 cudaError_t launch_pair_finalize(float *Z, float *Y, const int4 *grp_rec, int ngroups, int S, int MP,
-                                 const float *rowsc, cudaStream_t st) {
-  if (ngroups <= 0) return cudaSuccess;
-  const int blocks = ngroups < 152 * 16 ? ngroups : 152 * 16;
-  pair_finalize_kernel<<<blocks, 256, 0, st>>>(Z, Y, grp_rec, ngroups, S, MP, rowsc);
+                                 const float *rowsc, int nslot, int *err, cudaStream_t st) {
+  const long long n4 = (long long)ngroups * S * MP / 4;
+  if (n4 <= 0) return cudaSuccess;
+  long long blocks = (n4 + 255) / 256;
+  if (blocks > 152LL * 32) blocks = 152LL * 32;
+  pair_finalize_kernel<<<(unsigned)blocks, 256, 0, st>>>((float4 *)Z, (float4 *)Y, grp_rec, n4, S, MP, rowsc,
+                                                         nslot, err);
   return cudaGetLastError();
 }
 

@@ -154,6 +154,18 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
 
     T t;
     t.init_rec(stR[stg * G + (threadIdx.x / TPC)], cur_g0, cur_ng);
+    // self-check of the staged group record: a plan inside this unit, a slot
+    // and label inside the phase (a bad record is reported and its group idles)
+    if (t.active && (t.p < 0 || t.p >= a.nplans_chk || t.lab < 0 || t.lab >= a.nlab_chk ||
+                     t.pl_g0 < cur_g0 || t.pl_g0 + t.pl_ng > cur_g0 + cur_ng || t.pl_ng < 1)) {
+      a.ctl->err = 9;
+      t.active = false;
+      t.nvalid = 0;
+      t.p = 0;
+      t.lab = 0;
+      t.pl_g0 = cur_g0;
+      t.pl_ng = 0;
+    }
     t.load_costs_staged(a, stC + stg * JC * CW, (const int *)(stC + stg * JC * CW));
     const float *zs = stZ + stg * TILE, *ys = stY + stg * TILE;
     const int lcol0 = t.g * S;
@@ -163,8 +175,14 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
     // deferred input: this plan's row scale (slot t.p)
     float scin[RPT];
 #pragma unroll
-    for (int q = 0; q < RPT; ++q)
-      scin[q] = (indef && t.active) ? __ldg(a.rowsc + (size_t)t.p * MP + t.k0 + q) : 1.f;
+    for (int q4 = 0; q4 < RPT / 4; ++q4) {
+      float4 v = make_float4(1.f, 1.f, 1.f, 1.f);
+      if (indef && t.active) v = __ldg((const float4 *)(a.rowsc + (size_t)t.p * MP + t.k0) + q4);
+      scin[4 * q4] = v.x;
+      scin[4 * q4 + 1] = v.y;
+      scin[4 * q4 + 2] = v.z;
+      scin[4 * q4 + 3] = v.w;
+    }
     auto ld_zy = [&](int s, float (&z)[RPT], float (&y)[RPT]) {
 #pragma unroll
       for (int q4 = 0; q4 < RPT / 4; ++q4) {
