@@ -1439,6 +1439,8 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
     ph->stats.plan_bytes = ph->path == 0 ? ((emb || ng) ? 20.0 : 16.0) * ent + colb + 4.0 * m * (double)n
                                          : 136.0 * ent;
   }
+  if (h.err == 9)  // a pair-pass self-check: a staged plan record or slot out of range
+    return fail(D2G_E_CUDA, "device self-check failed: a plan record out of range in a pair pass");
   if (h.err == kErrTcTimeout)
     return fail(D2G_E_CUDA, "tensor-core cost table: wait for the MMA completion timed out");
   if (h.err) return fail(D2G_E_NUMERIC, "non-positive or non-finite normaliser (device code " +
