@@ -612,6 +612,9 @@ def main():
                 "kernel": ("plan_pair_kernel<32, EUCLID3> (two B-ADMM iterations per pass over the plans)"
                            if paired else "plan_kernel_tma<32, EUCLID3>"),
                 "passes_per_step": passes, "iterations_per_pass": stats["iterations"] / passes,
+                "note": ("a pair pass reads and writes Z and Y once for two iterations (8 B per plan "
+                         "entry per iteration); its bound moves from HBM toward issue and latency"
+                         if paired else "one iteration per pass: 16 B per plan entry per iteration"),
                 "algo_bytes_per_launch": ps["plan_bytes"], "ms_per_launch": ps["plan_ms_avg"]}
     trace_b = r["trace"]
     cw_b = r["c_w"].copy()
