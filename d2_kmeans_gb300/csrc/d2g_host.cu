@@ -115,6 +115,7 @@ struct d2g_phase {
   std::vector<int> plan_inst, inst_plan;
   DBuf<float> Z, Y, Xp, col_w, col_supp, rowsum, xmom, cw32, cs32, ctab;
   DBuf<int> col_sym, grp_meta, plan_g0, plan_ng, plan_label, item_g0, item_ng;
+  DBuf<int2> item_pp;  // per item {first plan, plans} (packed order)
   DBuf<int> col_crow;  // word embeddings: cost-table row of each packed column
   DBuf<long long> plan_cum;
   DBuf<int4> grp_rec;
@@ -133,10 +134,9 @@ struct d2g_phase {
   DBuf<float> rowpart, rowsc;
   DBuf<int4> wide;                       // {slot, slices with columns, label, 0} per wide plan
   // two iterations per pass (phases without wide plans): second-iteration row
-  // sums (normalised / raw) and the label of every slot
+  // sums (normalised / raw, by slot)
   bool pairs = false;
   DBuf<float> rowsum2, rawsum;
-  DBuf<int> slot_label;
   DBuf<unsigned char> def_iter;          // per iteration: 1 if it ran deferred
   std::vector<unsigned char> h_def_iter;
 
@@ -342,7 +342,7 @@ static int build_packing(d2g_phase *ph, bool with_units) {
     for (int q = 0; q < ng[i]; ++q) {
       const int nv = std::min(S, ph->p_str[i] - q * S);
       h_meta.push_back((p << 4) | nv);
-      ph->h_grp_rec.push_back(make_int4(p, g, 0, (ng[i] << 4) | nv));
+      ph->h_grp_rec.push_back(make_int4(p, g, 0, (ng[i] << 12) | nv));
       ph->h_grp_plan.push_back(p);
     }
     g += ng[i];
@@ -402,6 +402,21 @@ static int build_packing(d2g_phase *ph, bool with_units) {
   ph->nplans = (int)n;
   ph->ncols_packed = (long long)g * S;
   if (ph->ncols_packed * ph->MP > (1LL << 40)) return fail(D2G_E_UNSUPPORTED, "phase too large");
+  // the plans of every item (contiguous in packed order); in the items of one
+  // CTA, each group record carries its plan's index among the item's plans
+  // (bits 4-11), which places the plan's row scale in the staged copy
+  std::vector<int2> h_item_pp(h_item_g0.size());
+  for (size_t it = 0; it < h_item_g0.size(); ++it) {
+    const int g0 = h_item_g0[it], gl = g0 + h_item_ng[it] - 1;
+    const int p0 = ph->h_grp_plan[g0];
+    h_item_pp[it] = make_int2(p0, ph->h_grp_plan[gl] - p0 + 1);
+    if (it >= it1_g0.size()) continue;
+    for (int gi = g0; gi <= gl; ++gi) {
+      const int lp = ph->h_grp_plan[gi] - p0;
+      if (lp > 255) return fail(D2G_E_UNSUPPORTED, "more than 256 plans in one item");
+      ph->h_grp_rec[gi].w |= lp << 4;
+    }
+  }
 
   D2G_CUDA(ph->grp_meta.alloc(h_meta.size()));
   D2G_CUDA(ph->plan_g0.alloc(n));
@@ -410,12 +425,15 @@ static int build_packing(d2g_phase *ph, bool with_units) {
   D2G_CUDA(ph->plan_cum.alloc(n));
   D2G_CUDA(ph->item_g0.alloc(h_item_g0.size()));
   D2G_CUDA(ph->item_ng.alloc(h_item_ng.size()));
+  D2G_CUDA(ph->item_pp.alloc(h_item_pp.size()));
   D2G_CUDA(cudaMemcpyAsync(ph->grp_meta.p, h_meta.data(), h_meta.size() * 4, cudaMemcpyHostToDevice, ph->st));
   D2G_CUDA(cudaMemcpyAsync(ph->plan_g0.p, h_plan_g0.data(), n * 4, cudaMemcpyHostToDevice, ph->st));
   D2G_CUDA(cudaMemcpyAsync(ph->plan_ng.p, h_plan_ng.data(), n * 4, cudaMemcpyHostToDevice, ph->st));
   D2G_CUDA(cudaMemcpyAsync(ph->plan_cum.p, h_plan_cum.data(), n * 8, cudaMemcpyHostToDevice, ph->st));
   D2G_CUDA(cudaMemcpyAsync(ph->item_g0.p, h_item_g0.data(), h_item_g0.size() * 4, cudaMemcpyHostToDevice, ph->st));
   D2G_CUDA(cudaMemcpyAsync(ph->item_ng.p, h_item_ng.data(), h_item_ng.size() * 4, cudaMemcpyHostToDevice, ph->st));
+  D2G_CUDA(cudaMemcpyAsync(ph->item_pp.p, h_item_pp.data(), h_item_pp.size() * sizeof(int2),
+                           cudaMemcpyHostToDevice, ph->st));
   D2G_CUDA(cudaStreamSynchronize(ph->st));
   return D2G_OK;
 }
@@ -462,6 +480,7 @@ static PlanArgs bucket_args(d2g_phase *ph, const PlanArgs &base, const d2g_phase
   PlanArgs a = base;
   a.item_g0 = ph->item_g0.p + b.item_off;
   a.item_ng = ph->item_ng.p + b.item_off;
+  a.item_pp = ph->item_pp.p + b.item_off;
   a.cs = b.cs;
   a.resid_off = b.block_off;
   return a;
@@ -543,13 +562,7 @@ static int set_labels_impl(d2g_phase *ph, const int *label) {
     for (size_t q = 0; q < n; ++q) slot[lists[q]] = (int)q;
     D2G_CUDA(ph->plan_slot.alloc(n));
     D2G_CUDA(cudaMemcpyAsync(ph->plan_slot.p, slot.data(), n * 4, cudaMemcpyHostToDevice, ph->st));
-    if (ph->slot_label.n > 0) {  // pair passes: the label of each slot
-      std::vector<int> sl(n);
-      for (size_t p = 0; p < n; ++p) sl[slot[p]] = pl[p];
-      D2G_CUDA(cudaMemcpyAsync(ph->slot_label.p, sl.data(), n * 4, cudaMemcpyHostToDevice, ph->st));
-      D2G_CUDA(cudaStreamSynchronize(ph->st));
-    }
-    // group records: {slot, plan's first group, label, groups << 4 | valid}
+    // group records: {slot, plan's first group, label, groups << 12 | plan in item << 4 | valid}
     const std::vector<int> &gplan = ph->h_grp_plan;
     for (size_t gi = 0; gi < ph->h_grp_rec.size(); ++gi) {
       const int p = gplan[gi];
@@ -789,7 +802,6 @@ static int create_batched(d2g_phase *ph, const d2g_phase_desc *d) {
     D2G_CUDA(ph->rowsc.alloc((size_t)ph->nplans * ph->MP));
     D2G_CUDA(ph->rowsum2.alloc((size_t)ph->nplans * ph->MP));
     D2G_CUDA(ph->rawsum.alloc((size_t)ph->nplans * ph->MP));
-    D2G_CUDA(ph->slot_label.alloc(ph->nplans));
   }
   PlanArgs base = base_args(ph);
   ph->smem_plan = plan_smem_bytes(ph->MP, 0, 1);
@@ -957,7 +969,7 @@ static std::vector<unsigned long long> loop_signature(d2g_phase *ph) {
           (unsigned long long)ph->defer, u(ph->ncnt.p), u(ph->csym.p), u(ph->nkey.p), u(ph->nptr.p),
           u(ph->nocc.p), (unsigned long long)ph->nlists, u(ph->ntup.p), u(ph->ndist.p),
           (unsigned long long)ph->ntab, (unsigned long long)ph->pairs, u(ph->rowsum2.p), u(ph->rawsum.p),
-          u(ph->slot_label.p)};
+          u(ph->plan_label.p), u(ph->item_pp.p)};
 }
 
 static bool has_collision(int maxIters, int upl) {
@@ -1090,8 +1102,8 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
         // step 4 of `it` (c_w), the second iteration's row scale from that c_w,
         // then step 4 (and step 5) of it + 1
         D2G_CUDA(launch_cluster_reduce(cluster_args(ph, it, false), ph->st));
-        D2G_CUDA(launch_pair_scale(ph->rawsum.p, ph->slot_label.p, ph->cw32.p, ph->nplans, ph->MP, ph->str,
-                                   ph->rowsc.p, ph->ctl.p, t1, ph->K, ph->st));
+        D2G_CUDA(launch_pair_scale(ph->rawsum.p, ph->plan_slot.p, ph->plan_label.p, ph->cw32.p, ph->nplans,
+                                   ph->MP, ph->str, ph->rowsc.p, ph->ctl.p, t1, ph->K, ph->st));
         ClusterArgs c1 = cluster_args(ph, t1, upd1 && euc);
         c1.rowsum32 = ph->rowsum2.p;
         D2G_CUDA(launch_cluster_reduce(c1, ph->st));
@@ -1112,7 +1124,7 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
         continue;
       }
       if (pend) {  // a single pass follows a pair: apply the pending scale first
-        D2G_CUDA(launch_pair_finalize(ph->Z.p, ph->Y.p, ph->grp_rec.p, ph->ngroups, ph->geo.S, ph->MP,
+        D2G_CUDA(launch_pair_finalize(ph->Z.p, ph->Y.p, ph->grp_meta.p, ph->ngroups, ph->geo.S, ph->MP,
                                       ph->rowsc.p, ph->nplans, &ph->ctl.p->err, ph->st));
         ++nl;
         pend = false;
@@ -1193,7 +1205,7 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
       }
     }
     if (pend) {  // the loop ended on a pair: its second iteration's scale
-      D2G_CUDA(launch_pair_finalize(ph->Z.p, ph->Y.p, ph->grp_rec.p, ph->ngroups, ph->geo.S, ph->MP,
+      D2G_CUDA(launch_pair_finalize(ph->Z.p, ph->Y.p, ph->grp_meta.p, ph->ngroups, ph->geo.S, ph->MP,
                                     ph->rowsc.p, ph->nplans, &ph->ctl.p->err, ph->st));
       ++nl;
     }
@@ -1353,7 +1365,7 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
   // (the reference may stop after any iteration), not n-grams (their support
   // update needs the final Z of its iteration)
   ph->pairs = cfg.pair_iterations && ph->path == 0 && ph->nwide == 0 && ph->buckets.size() == 1 &&
-              ph->buckets[0].cs == 1 && ph->MP <= 128 && !ng && ph->slot_label.n > 0 &&
+              ph->buckets[0].cs == 1 && ph->MP <= 128 && !ng && ph->rawsum.n > 0 &&
               h.budget_ns == ~0ULL;
   // deferred-exchange schedule of the wide plans
   ph->h_def_iter.assign((size_t)opt->maxIters + 1, 0);

@@ -60,6 +60,7 @@ enum PlanFlags {
   PF_CHECK = 4,    // residual-check iteration
   PF_IN_DEF = 8,   // wide plans arrive deferred: Z' and U = Y + X, scaled by rowsc on load
   PF_OUT_DEF = 16, // wide plans leave deferred: Z', U and per-slice row partials
+  PF_STAGE_SC = 32,// pair pass with deferred input: each unit's row scales come with its tiles
 };
 
 // Device control block, one per phase.  Everything an iteration reads that
@@ -90,10 +91,13 @@ struct PlanArgs {
   double *resid_part;       // 4 doubles per CTA (obj, primres, dualres, -)
   Ctl *ctl;
   int m, dim, flags, cs, iter, resid_off;
-  const int4 *grp_rec;      // per group {plan slot, plan first group, label, plan groups << 4 | valid}
+  // per group {plan slot, plan first group, label, plan groups << 12 | plan within its item << 4 | valid}
+  const int4 *grp_rec;
   const int *plan_slot;     // plan -> slot: position in cluster-sorted order (row-sum outputs)
   float *rowpart;           // [slot][8][MP] per-slice row sums of Z' (deferred wide plans)
-  const float *rowsc;       // [slot][MP] row scale c_w / rowsum(Z') of the previous iteration
+  // row scale c_w / rowsum(Z') of the previous iteration: [slot][MP] for wide
+  // plans, [plan][MP] in packed order for pair passes
+  const float *rowsc;
   int ctas_per_sm;          // persistent grid of plain launches: CTAs per SM (0: occupancy limit)
   const int *col_crow;      // per packed column: cost-table row (label * V + token, or the bin)
   int stage_costs;          // table costs (16 <= MP <= 128): next unit's rows by cp.async into smem
@@ -101,6 +105,7 @@ struct PlanArgs {
   float *rowsum2_out;       // pair pass: step-4 row sums of the second iteration, by slot
   float *rawsum_out;        // pair pass: raw row sums of the second iteration's Z', by slot
   int nplans_chk, nlab_chk; // plans and clusters of the phase (self-check of staged records)
+  const int2 *item_pp;      // per item {first plan in packed order, plans}
 };
 
 // per-MP launch geometry
@@ -135,14 +140,15 @@ cudaError_t launch_plan_finalize(float *Z, float *Y, const int *item_g0, const i
                                  int nitems, int cs, int G, int S, int MP, const int4 *grp_rec,
                                  const float *rowsc, const unsigned char *def_iter, const Ctl *ctl,
                                  cudaStream_t st);
-// pair passes: the row scale c_w / rowsum(Z') of every plan (by slot), after the
-// cluster reduction of the pair's first iteration; and Z = Z' * scale,
-// Y = U - Z over every packed column, where a single pass or the end follows
-cudaError_t launch_pair_scale(const float *rawsum, const int *slot_label, const float *cw32, int nplans,
-                              int MP, int m, float *rowsc, const Ctl *ctl, int iter, int nlab,
-                              cudaStream_t st);
-cudaError_t launch_pair_finalize(float *Z, float *Y, const int4 *grp_rec, int ngroups, int S, int MP,
-                                 const float *rowsc, int nslot, int *err, cudaStream_t st);
+// pair passes: the row scale c_w / rowsum(Z') of every plan (packed order, from
+// the raw sums by slot), after the cluster reduction of the pair's first
+// iteration; and Z = Z' * scale, Y = U - Z over every packed column, where a
+// single pass or the end follows
+cudaError_t launch_pair_scale(const float *rawsum, const int *plan_slot, const int *plan_label,
+                              const float *cw32, int nplans, int MP, int m, float *rowsc, const Ctl *ctl,
+                              int iter, int nlab, cudaStream_t st);
+cudaError_t launch_pair_finalize(float *Z, float *Y, const int *grp_meta, int ngroups, int S, int MP,
+                                 const float *rowsc, int nplans, int *err, cudaStream_t st);
 
 // kernels_reduce.cu
 struct ClusterArgs {

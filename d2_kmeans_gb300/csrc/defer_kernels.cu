@@ -77,42 +77,44 @@ __global__ void __launch_bounds__(256) plan_finalize_kernel(float *__restrict__ 
   }
 }
 
-// pair passes: one thread per (slot, 4 rows)
-__global__ void pair_scale_kernel(const float4 *__restrict__ rawsum, const int *__restrict__ slot_label,
-                                  const float *__restrict__ cw32, long long n4, int MP, int m,
-                                  float4 *__restrict__ rowsc, const Ctl *ctl, int iter, int nlab) {
+// pair passes: one thread per (plan in packed order, 4 rows)
+__global__ void pair_scale_kernel(const float *__restrict__ rawsum, const int *__restrict__ plan_slot,
+                                  const int *__restrict__ plan_label, const float *__restrict__ cw32,
+                                  long long n4, int MP, int m, float4 *__restrict__ rowsc, const Ctl *ctl,
+                                  int iter, int nplans, int nlab) {
   if (iter >= ctl->stop_iter) return;
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= n4) return;
   const long long e = i * 4;
-  const int slot = (int)(e / MP), k = (int)(e - (long long)slot * MP);
-  const int lab = __ldg(slot_label + slot);
-  if (lab < 0 || lab >= nlab || (k & 3)) {  // self-check: a label outside the clusters
+  const int p = (int)(e / MP), k = (int)(e - (long long)p * MP);
+  const int slot = __ldg(plan_slot + p), lab = __ldg(plan_label + p);
+  // self-check: a slot outside the plans or a label outside the clusters
+  if (slot < 0 || slot >= nplans || lab < 0 || lab >= nlab || (k & 3)) {
     ((Ctl *)ctl)->err = 9;
     return;
   }
   const float4 cw = __ldg((const float4 *)(cw32 + (size_t)lab * MP + k));
-  const float4 r = rawsum[i];
+  const float4 r = *(const float4 *)(rawsum + (size_t)slot * MP + k);
   rowsc[i] = make_float4(k + 0 < m ? cw.x / r.x : 0.f, k + 1 < m ? cw.y / r.y : 0.f,
                          k + 2 < m ? cw.z / r.z : 0.f, k + 3 < m ? cw.w / r.w : 0.f);
 }
 
 // Z = Z' * scale, Y = U - Z over every packed column: one float4 (4 rows of a
-// column) per thread
+// column) per thread; the plan of a group is grp_meta >> 4
 __global__ void __launch_bounds__(256) pair_finalize_kernel(float4 *__restrict__ Z, float4 *__restrict__ Y,
-                                                            const int4 *__restrict__ grp_rec, long long n4,
+                                                            const int *__restrict__ grp_meta, long long n4,
                                                             int S, int MP, const float *__restrict__ rowsc,
-                                                            int nslot, int *err) {
+                                                            int nplans, int *err) {
   const long long per4 = (long long)S * MP / 4;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4;
        i += (long long)gridDim.x * blockDim.x) {
-    const int slot = __ldg(&grp_rec[i / per4].x);
+    const int p = __ldg(&grp_meta[i / per4]) >> 4;
     const int k0 = (int)((i * 4) % MP);
-    if (slot < 0 || slot >= nslot) {  // self-check: a slot outside the plans
+    if (p < 0 || p >= nplans) {  // self-check: a plan outside the phase
       *err = 9;
       continue;
     }
-    const float4 sc = __ldg((const float4 *)(rowsc + (size_t)slot * MP + k0));
+    const float4 sc = __ldg((const float4 *)(rowsc + (size_t)p * MP + k0));
     float4 z = Z[i], y = Y[i];
     z.x *= sc.x;
     z.y *= sc.y;
@@ -127,24 +129,24 @@ __global__ void __launch_bounds__(256) pair_finalize_kernel(float4 *__restrict__
   }
 }
 
-cudaError_t launch_pair_scale(const float *rawsum, const int *slot_label, const float *cw32, int nplans,
-                              int MP, int m, float *rowsc, const Ctl *ctl, int iter, int nlab,
-                              cudaStream_t st) {
+cudaError_t launch_pair_scale(const float *rawsum, const int *plan_slot, const int *plan_label,
+                              const float *cw32, int nplans, int MP, int m, float *rowsc, const Ctl *ctl,
+                              int iter, int nlab, cudaStream_t st) {
   const long long n4 = (long long)nplans * MP / 4;
   if (n4 <= 0) return cudaSuccess;
-  pair_scale_kernel<<<(unsigned)((n4 + 255) / 256), 256, 0, st>>>((const float4 *)rawsum, slot_label, cw32, n4,
-                                                                  MP, m, (float4 *)rowsc, ctl, iter, nlab);
+  pair_scale_kernel<<<(unsigned)((n4 + 255) / 256), 256, 0, st>>>(rawsum, plan_slot, plan_label, cw32, n4, MP,
+                                                                  m, (float4 *)rowsc, ctl, iter, nplans, nlab);
   return cudaGetLastError();
 }
 
-cudaError_t launch_pair_finalize(float *Z, float *Y, const int4 *grp_rec, int ngroups, int S, int MP,
-                                 const float *rowsc, int nslot, int *err, cudaStream_t st) {
+cudaError_t launch_pair_finalize(float *Z, float *Y, const int *grp_meta, int ngroups, int S, int MP,
+                                 const float *rowsc, int nplans, int *err, cudaStream_t st) {
   const long long n4 = (long long)ngroups * S * MP / 4;
   if (n4 <= 0) return cudaSuccess;
   long long blocks = (n4 + 255) / 256;
   if (blocks > 152LL * 32) blocks = 152LL * 32;
-  pair_finalize_kernel<<<(unsigned)blocks, 256, 0, st>>>((float4 *)Z, (float4 *)Y, grp_rec, n4, S, MP, rowsc,
-                                                         nslot, err);
+  pair_finalize_kernel<<<(unsigned)blocks, 256, 0, st>>>((float4 *)Z, (float4 *)Y, grp_meta, n4, S, MP, rowsc,
+                                                         nplans, err);
   return cudaGetLastError();
 }
 

@@ -113,6 +113,7 @@ struct Tile {
   static constexpr int NDIM = MODE == COST_EUCLID3 ? 3 : DS;     // coordinates summed
 
   int g, r, k0, rank, cta_g0, cta_ng, p, nvalid, pl_g0, pl_ng, lab;
+  int lp;  // staged records: the plan's index among the plans of its item
   bool active;
   size_t colbase;
   float sp[EUC ? S : 1][DS];      // column supports
@@ -167,11 +168,13 @@ struct Tile {
     pl_g0 = 0;
     pl_ng = 0;
     lab = 0;
+    lp = 0;
     if (active) {
       p = rec.x;
       pl_g0 = rec.y;
       lab = rec.z;
-      pl_ng = rec.w >> 4;
+      pl_ng = rec.w >> 12;
+      lp = (rec.w >> 4) & 255;
       nvalid = rec.w & 15;
     }
     colbase = (size_t)(item_g0 + g) * S;
@@ -583,7 +586,7 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
     slot = -1;
     if (indef && ng > 0) {
       const int4 r = a.grp_rec[g0];
-      if ((r.w >> 4) > G) slot = r.x;
+      if ((r.w >> 12) > G) slot = r.x;
     }
   };
   // staged table costs: the table row of each piece of the next unit (-1: none)
@@ -786,7 +789,7 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
       bool one_slice = false;
       if (outdef) {
         const int4 r0 = stR[stg * G];
-        one_slice = (r0.w >> 4) > G && r0.y + (r0.w >> 4) >= cur_g0 + cur_ng;
+        one_slice = (r0.w >> 12) > G && r0.y + (r0.w >> 12) >= cur_g0 + cur_ng;
       }
       writer = t.active && t.g == lo;
       if (writer) {

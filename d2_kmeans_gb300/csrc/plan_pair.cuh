@@ -18,7 +18,10 @@
 // no residual-check iteration (its check needs the final Z of t+1), and no
 // time budget is set (the reference may stop after any single iteration).
 //
-// flags: PF_IN_DEF   the input is deferred: every plan's row scale in a.rowsc [slot][MP]
+// flags: PF_IN_DEF   the input is deferred: every plan's row scale in a.rowsc [plan][MP]
+//                     (packed order: the plans of a unit are contiguous)
+//        PF_STAGE_SC each unit's row scales arrive with its tiles (bulk copy into
+//                     shared memory, the same transaction); else read per thread
 //        PF_UPDATE   iteration t+1 is a Euclidean support update: its X moments
 //        PF_WRITE_X  iteration t+1's X is stored (word-embedding support update)
 // CHECK: iteration t is a residual-check iteration.
@@ -59,20 +62,35 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
   float *sm_rs = stK + (SCC ? 2 * TILE : 0);     // [G][MP] row partials of iteration t
   float *sm_rs2 = sm_rs + G * MP;                // [G][MP] row partials of iteration t+1
   float *sm_mom = sm_rs2 + G * MP;               // [dim+1][G][MP] X moments of iteration t+1
+  float *stS = sm_mom + (a.dim + 1) * G * MP;    // [2][G][MP] row scales of the unit's plans
   __shared__ __align__(8) unsigned long long mbar[2];
   __shared__ int sh_fail;
   __shared__ int sh_g0[2], sh_ng[2];
+  __shared__ int2 sh_pp[2];
 
   if (a.iter >= a.ctl->stop_iter) return;
   const int tid = threadIdx.x;
   const int u0 = blockIdx.x, ustep = gridDim.x, nunits = nitems;
   if (a.iter == 0 && blockIdx.x == 0 && tid == 0) a.ctl->t_start_ns = global_ns();
-  auto issue = [&](int g0, int ng, int stg) {
+  const bool indef = a.flags & PF_IN_DEF;
+  const bool stage_sc = indef && (a.flags & PF_STAGE_SC);
+  // the plans {first, count} of unit u, checked against the phase (thread 0)
+  auto unit_plans = [&](int u) {
+    int2 pp = indef ? a.item_pp[u] : make_int2(0, 0);
+    if (pp.x < 0 || pp.y < 0 || pp.y > G || pp.x > a.nplans_chk - pp.y) {
+      a.ctl->err = 9;
+      pp = make_int2(0, 0);
+    }
+    return pp;
+  };
+  auto issue = [&](int g0, int ng, int2 pp, int stg) {
     const size_t off = (size_t)g0 * S * MP;
     const unsigned bytes = (unsigned)ng * S * MP * 4u;
     const unsigned rb = (unsigned)ng * 16u, wb = (unsigned)ng * S * 4u, cb = wb * CW;
-    mbar_expect_tx(&mbar[stg], 2u * bytes + rb + wb + cb);
+    const unsigned sb = stage_sc && ng > 0 ? (unsigned)pp.y * MP * 4u : 0u;
+    mbar_expect_tx(&mbar[stg], 2u * bytes + rb + wb + cb + sb);
     if (ng <= 0) return;
+    if (sb) bulk_load(stS + stg * G * MP, a.rowsc + (size_t)pp.x * MP, sb, &mbar[stg]);
     bulk_load(stZ + stg * TILE, a.Z + off, bytes, &mbar[stg]);
     bulk_load(stY + stg * TILE, a.Y + off, bytes, &mbar[stg]);
     bulk_load(stR + stg * G, a.grp_rec + g0, rb, &mbar[stg]);
@@ -103,6 +121,7 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
     asm volatile("cp.async.commit_group;" ::: "memory");
   };
   int nx_g0 = 0, nx_ng = 0;
+  int2 nx_pp = make_int2(0, 0);
   if (tid == 0) {
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
@@ -110,12 +129,15 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
     mbar_fence_init();
     if (u0 < nunits) {
       const int g0 = a.item_g0[u0], ng = a.item_ng[u0];
+      const int2 pp = unit_plans(u0);
       sh_g0[0] = g0;
       sh_ng[0] = ng;
-      issue(g0, ng, 0);
+      sh_pp[0] = pp;
+      issue(g0, ng, pp, 0);
       if (u0 + ustep < nunits) {
         nx_g0 = a.item_g0[u0 + ustep];
         nx_ng = a.item_ng[u0 + ustep];
+        nx_pp = unit_plans(u0 + ustep);
       }
     }
   }
@@ -129,7 +151,6 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
   const int m = a.m;
   const float inv_rho = a.ctl->inv_rho;
   const float ir2 = a.ctl->inv_rho_l2;
-  const bool indef = a.flags & PF_IN_DEF;
   const bool update = T::EUC && (a.flags & PF_UPDATE);
   const bool write_x = a.flags & PF_WRITE_X;
   double s_obj = 0.0, s_pr = 0.0, s_dr = 0.0;
@@ -141,13 +162,16 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
     __syncthreads();
     if (sh_fail) break;
     const int cur_g0 = sh_g0[stg], cur_ng = sh_ng[stg];
+    const int2 cur_pp = sh_pp[stg];
     if (tid == 0 && u + ustep < nunits) {
-      issue(nx_g0, nx_ng, stg ^ 1);
+      issue(nx_g0, nx_ng, nx_pp, stg ^ 1);
       sh_g0[stg ^ 1] = nx_g0;
       sh_ng[stg ^ 1] = nx_ng;
+      sh_pp[stg ^ 1] = nx_pp;
       if (u + 2 * ustep < nunits) {
         nx_g0 = a.item_g0[u + 2 * ustep];
         nx_ng = a.item_ng[u + 2 * ustep];
+        nx_pp = unit_plans(u + 2 * ustep);
       }
     }
     const bool has_next = u + ustep < nunits;
@@ -155,9 +179,11 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
     T t;
     t.init_rec(stR[stg * G + (threadIdx.x / TPC)], cur_g0, cur_ng);
     // self-check of the staged group record: a plan inside this unit, a slot
-    // and label inside the phase (a bad record is reported and its group idles)
+    // and label inside the phase, the plan among the unit's row scales (a bad
+    // record is reported and its group idles)
     if (t.active && (t.p < 0 || t.p >= a.nplans_chk || t.lab < 0 || t.lab >= a.nlab_chk ||
-                     t.pl_g0 < cur_g0 || t.pl_g0 + t.pl_ng > cur_g0 + cur_ng || t.pl_ng < 1)) {
+                     t.pl_g0 < cur_g0 || t.pl_g0 + t.pl_ng > cur_g0 + cur_ng || t.pl_ng < 1 ||
+                     (indef && t.lp >= cur_pp.y))) {
       a.ctl->err = 9;
       t.active = false;
       t.nvalid = 0;
@@ -172,12 +198,15 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
     float w[S];
 #pragma unroll
     for (int s = 0; s < S; ++s) w[s] = s < t.nvalid ? stW[stg * JC + lcol0 + s] : 0.f;
-    // deferred input: this plan's row scale (slot t.p)
+    // deferred input: this plan's row scale (plan cur_pp.x + t.lp in packed order)
     float scin[RPT];
 #pragma unroll
     for (int q4 = 0; q4 < RPT / 4; ++q4) {
       float4 v = make_float4(1.f, 1.f, 1.f, 1.f);
-      if (indef && t.active) v = __ldg((const float4 *)(a.rowsc + (size_t)t.p * MP + t.k0) + q4);
+      if (stage_sc && t.active)
+        v = *((const float4 *)(stS + (stg * G + t.lp) * MP + t.k0) + q4);
+      else if (indef && t.active)
+        v = __ldg((const float4 *)(a.rowsc + (size_t)(cur_pp.x + t.lp) * MP + t.k0) + q4);
       scin[4 * q4] = v.x;
       scin[4 * q4 + 1] = v.y;
       scin[4 * q4 + 2] = v.z;
@@ -463,7 +492,8 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
   }
 }
 
-// shared memory of plan_pair_kernel beyond its static part
+// shared memory of plan_pair_kernel beyond its static part (without the
+// staged row scales of pair_scale_bytes)
 template <int MP>
 size_t pair_smem_bytes(int mode, int dim) {
   using Gm = GeoT<MP>;
@@ -473,33 +503,57 @@ size_t pair_smem_bytes(int mode, int dim) {
          (size_t)2 * Gm::G * MP * 4 + (size_t)(dim + 1) * Gm::G * MP * 4;
 }
 
+// two stages of row scales, one row per plan of a unit (at most G plans)
+template <int MP>
+constexpr size_t pair_scale_bytes() {
+  return (size_t)2 * GeoT<MP>::G * MP * 4;
+}
+
+// The row scales of deferred input are staged in shared memory when that
+// keeps the CTAs per SM of the unstaged kernel; otherwise each thread reads
+// its plan's scale from global memory.
 template <int MP, int MODE, bool CHECK, bool FULL>
 cudaError_t launch_pair_t(const PlanArgs &a, int nitems, cudaStream_t st) {
   static int grid = 0, nsm = 0;
+  static bool stage = false;
   static size_t configured = 0;
-  const size_t sm = pair_smem_bytes<MP>(MODE, a.dim);
+  const size_t sm0 = pair_smem_bytes<MP>(MODE, a.dim), sm1 = sm0 + pair_scale_bytes<MP>();
   auto kern = plan_pair_kernel<MP, MODE, CHECK, FULL>;
-  if (configured < sm) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-    configured = sm;
+  if (configured < sm1) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+    if (e != cudaSuccess) {  // beyond the opt-in limit: the kernel without staged scales
+      (void)cudaGetLastError();
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm0);
+      if (e != cudaSuccess) return e;
+      configured = sm0;
+      stage = false;
+    } else {
+      configured = sm1;
+    }
     grid = 0;
   }
   if (grid == 0) {
-    int dev = 0, per = 0;
+    int dev = 0, per0 = 0, per1 = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, GeoT<MP>::NT, sm);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per0, kern, GeoT<MP>::NT, sm0);
+    if (e == cudaSuccess && configured >= sm1)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, kern, GeoT<MP>::NT, sm1);
     if (e != cudaSuccess) return e;
+    stage = configured >= sm1 && per1 >= per0;
+    const int per = stage ? per1 : per0;
     grid = (per > 0 ? per : 1) * nsm;
   }
   if (nitems <= 0) return cudaSuccess;
   int cap = grid;
   if (a.ctas_per_sm > 0) cap = std::min(cap, a.ctas_per_sm * nsm);
   const int g = nitems < cap ? nitems : cap;
+  PlanArgs b = a;
+  if (stage && (a.flags & PF_IN_DEF)) b.flags |= PF_STAGE_SC;
+  const size_t sm = (b.flags & PF_STAGE_SC) ? sm1 : sm0;
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = plan_cfg(g, GeoT<MP>::NT, sm, st, attr, 1);
-  return cudaLaunchKernelEx(&cfg, kern, a, nitems);
+  return cudaLaunchKernelEx(&cfg, kern, b, nitems);
 }
 
 template <int MP, int MODE, bool CHECK>
