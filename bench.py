@@ -616,6 +616,13 @@ def main():
                          "entry per iteration); its bound moves from HBM toward issue and latency"
                          if paired else "one iteration per pass: 16 B per plan entry per iteration"),
                 "algo_bytes_per_launch": ps["plan_bytes"], "ms_per_launch": ps["plan_ms_avg"]}
+        # the same launch against 16 B per plan entry per iteration (Z and Y read
+        # and written once per iteration, the one-iteration-per-pass formulation)
+        ipp = stats["iterations"] / passes
+        ubytes = 16.0 * stats["plan_entries"] * ipp
+        roof["plan_update_bytes_per_launch"] = ubytes
+        roof["plan_update_equiv_gbs"] = ubytes / (ps["plan_ms_avg"] / 1e3) / 1e9
+        roof["plan_update_equiv_frac"] = roof["plan_update_equiv_gbs"] / hbm
     trace_b = r["trace"]
     cw_b = r["c_w"].copy()
     P.close()
