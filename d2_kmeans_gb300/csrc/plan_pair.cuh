@@ -297,6 +297,18 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
     }
     __syncthreads();
     if (SC && has_next) load_rows_idx(sh_g0[stg ^ 1], sh_ng[stg ^ 1]);
+    // c_w of the plan's cluster for iteration t's row scale, read before the
+    // totals barrier so that its latency overlaps the wait
+    float cwv[RPT];
+#pragma unroll
+    for (int q4 = 0; q4 < RPT / 4; ++q4) {
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (t.active) v = __ldg((const float4 *)(a.cw32 + (size_t)t.lab * MP + t.k0) + q4);
+      cwv[4 * q4] = v.x;
+      cwv[4 * q4 + 1] = v.y;
+      cwv[4 * q4 + 2] = v.z;
+      cwv[4 * q4 + 3] = v.w;
+    }
     float tot[RPT];
     if (writer) {
 #pragma unroll
@@ -339,7 +351,7 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
 #pragma unroll
     for (int q = 0; q < RPT; ++q) {
       const bool ok = t.active && (FULL || t.k0 + q < m);
-      sc[q] = ok ? __fdividef(__ldg(a.cw32 + (size_t)t.lab * MP + t.k0 + q), tot[q]) : 0.f;
+      sc[q] = ok ? __fdividef(cwv[q], tot[q]) : 0.f;
     }
     // second half of step 2 and step 3: Z and Y of iteration t stay in registers
     float zt[S][RPT], yt[S][RPT];
