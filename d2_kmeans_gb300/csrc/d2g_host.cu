@@ -798,7 +798,7 @@ static int create_batched(d2g_phase *ph, const d2g_phase_desc *d) {
   if (ph->nwide > 0) {
     D2G_CUDA(ph->rowpart.alloc((size_t)ph->nplans * kMaxCluster * ph->MP));
     D2G_CUDA(ph->rowsc.alloc((size_t)ph->nplans * ph->MP));
-  } else if (ph->MP <= 128 && ph->metric != D2_N_GRAM) {  // pair passes possible
+  } else if (ph->MP <= 128) {  // pair passes possible
     D2G_CUDA(ph->rowsc.alloc((size_t)ph->nplans * ph->MP));
     D2G_CUDA(ph->rowsum2.alloc((size_t)ph->nplans * ph->MP));
     D2G_CUDA(ph->rawsum.alloc((size_t)ph->nplans * ph->MP));
@@ -1052,7 +1052,7 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
     std::vector<char> pair_at((size_t)maxIters + 2, 0);
     if (ph->pairs) {
       const int N = maxIters + 1;
-      auto upd_at = [&](int i) { return (i % upl == 0) && (euc || emb); };
+      auto upd_at = [&](int i) { return (i % upl == 0) && (euc || emb || (ng && i > 0)); };
       auto can_pair = [&](int i) { return i + 1 < N && !upd_at(i) && !is_check_iter(i + 1); };
       std::vector<int> f0((size_t)N + 2, 0), f1((size_t)N + 2, 1);  // passes left; f1: a pair is pending
       f0[N] = 0;
@@ -1083,7 +1083,7 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
       const bool upd = (it % upl == 0) && (euc || emb || (ng && it > 0));
       if (pair_at[it]) {
         const int t1 = it + 1;
-        const bool upd1 = (t1 % upl == 0) && (euc || emb);
+        const bool upd1 = (t1 % upl == 0) && (euc || emb || ng);  // t1 >= 1
         const bool chk0 = is_check_iter(it);
         if (profile) {
           cudaEvent_t a0, b0;
@@ -1112,6 +1112,16 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
           D2G_CUDA(launch_embed_support(embed_args(ph, t1), ph->st));
           D2G_CUDA(launch_embed_table(embed_args(ph, t1), ph->st));
           nl += 6;
+        }
+        if (upd1 && ng) {  // step 5 of it + 1 from its deferred Z (Z' * rowsc), then the new table
+          NgramArgs g = ngram_args(ph, t1);
+          g.rowsc = ph->rowsc.p;
+          g.grp_meta = ph->grp_meta.p;
+          g.S = ph->geo.S;
+          g.nplans = ph->nplans;
+          D2G_CUDA(launch_ngram_support(g, ph->st));
+          D2G_CUDA(launch_ngram_table(g, ph->st));
+          nl += 3;
         }
         if (chk0) {
           D2G_CUDA(launch_resid_final(ph->resid_part.p, ph->total_blocks, ph->ctl.p,
@@ -1362,11 +1372,9 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
   }
 
   // two iterations per pass: phases whose plans fit in one CTA, no time budget
-  // (the reference may stop after any iteration), not n-grams (their support
-  // update needs the final Z of its iteration)
+  // (the reference may stop after any iteration)
   ph->pairs = cfg.pair_iterations && ph->path == 0 && ph->nwide == 0 && ph->buckets.size() == 1 &&
-              ph->buckets[0].cs == 1 && ph->MP <= 128 && !ng && ph->rawsum.n > 0 &&
-              h.budget_ns == ~0ULL;
+              ph->buckets[0].cs == 1 && ph->MP <= 128 && ph->rawsum.n > 0 && h.budget_ns == ~0ULL;
   // deferred-exchange schedule of the wide plans
   ph->h_def_iter.assign((size_t)opt->maxIters + 1, 0);
   if (ph->path == 0 && ph->defer) {

@@ -266,6 +266,11 @@ struct NgramArgs {
   float *T;                    // [K][U][MP] cost table (batched)
   Ctl *ctl;
   int iter, K, m, dim, V, U, MP;
+  // batched plans left deferred by a pair pass: Z = Z' * rowsc[plan][row], the
+  // plan of packed column c being grp_meta[c / S] >> 4 (null: Z is final)
+  const float *rowsc;
+  const int *grp_meta;
+  int S, nplans;
 };
 // step 5: counts, then the new centroid symbols (skipped past the time budget)
 cudaError_t launch_ngram_support(const NgramArgs &g, cudaStream_t st);

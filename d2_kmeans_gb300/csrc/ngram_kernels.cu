@@ -21,7 +21,10 @@
 // column order: FP64 one column after the other in the FP64 form; FP32 over
 // chunks of 32 columns and FP64 across chunks in the batched form.  The cost
 // sums run over u in order with separately rounded products and sums, as the
-// reference's BLAS computes them.
+// reference's BLAS computes them.  When the update iteration is the second of
+// a pair pass, the batched plans are still deferred (Z' with one row scale
+// per plan): the counts form Z = Z' * scale as they read, the product the
+// pass that follows would store.
 #include <cmath>
 #include <map>
 #include <unordered_map>
@@ -89,27 +92,42 @@ constexpr int kCountWarps = 8, kChunk = 32;
 __global__ void __launch_bounds__(kCountWarps * 32) ngram_count32_kernel(
     const int *__restrict__ key, const int *__restrict__ ptr, const int *__restrict__ occ,
     const float *__restrict__ Z, long long zstride, int m, int dim, int V, double *__restrict__ cnt,
-    const Ctl *ctl, int iter) {
+    const Ctl *ctl, int iter, const float *__restrict__ rowsc, const int *__restrict__ grp_meta, int S,
+    int nplans) {
   if (iter >= ctl->stop_iter) return;
   __shared__ double part[kCountWarps][32];
   __shared__ int cols[kCountWarps][kChunk];
+  __shared__ int plans[kCountWarps][kChunk];
   const int lst = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int kk = key[lst];
   const int v = kk % V, lt = kk / V, t = lt % dim, l = lt / dim;
   const int b = ptr[lst], e = ptr[lst + 1];
+  const bool deferred = rowsc != nullptr;
   for (int k0 = 0; k0 < m; k0 += 32) {
     const int k = k0 + lane;
     double acc = 0.0;
     for (int c0 = b + warp * kChunk; c0 < e; c0 += kCountWarps * kChunk) {
       const int nc = min(kChunk, e - c0);
       __syncwarp();
-      if (lane < nc) cols[warp][lane] = occ[c0 + lane];
+      if (lane < nc) {
+        const int c = occ[c0 + lane];
+        cols[warp][lane] = c;
+        if (deferred) {
+          int p = __ldg(grp_meta + c / S) >> 4;
+          if (p < 0 || p >= nplans) {  // self-check: a plan outside the phase
+            ((Ctl *)ctl)->err = 9;
+            p = 0;
+          }
+          plans[warp][lane] = p;
+        }
+      }
       __syncwarp();
       float s = 0.f;
       if (k < m) {
 #pragma unroll 8
         for (int j = 0; j < nc; ++j) {
-          const float z = __ldg(Z + (size_t)cols[warp][j] * zstride + k);
+          float z = __ldg(Z + (size_t)cols[warp][j] * zstride + k);
+          if (deferred) z *= __ldg(rowsc + (size_t)plans[warp][j] * zstride + k);
           s += z > 1E-10f ? z : 0.f;
         }
       }
@@ -218,7 +236,8 @@ cudaError_t launch_ngram_support(const NgramArgs &g, cudaStream_t st) {
   if (g.nlists > 0) {
     if (g.Z32)
       ngram_count32_kernel<<<g.nlists, kCountWarps * 32, 0, st>>>(g.key, g.ptr, g.occ, g.Z32, g.zstride, g.m,
-                                                                  g.dim, g.V, g.cnt, g.ctl, g.iter);
+                                                                  g.dim, g.V, g.cnt, g.ctl, g.iter, g.rowsc,
+                                                                  g.grp_meta, g.S, g.nplans);
     else
       ngram_count64_kernel<<<(unsigned)(((long long)g.nlists * 32 + 255) / 256), 256, 0, st>>>(
           g.key, g.ptr, g.occ, g.nlists, g.Z64, g.zstride, g.m, g.dim, g.V, g.cnt, g.ctl, g.iter);

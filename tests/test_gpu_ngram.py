@@ -130,3 +130,36 @@ def test_ngram_calculate_distmat(d2g):
     B = sym.reshape(col, 1, dim)                        # [col, 1, dim] instance symbols
     ref = dist.reshape(V, V)[A, B].sum(-1)              # [col, m]
     np.testing.assert_allclose(out, ref.reshape(-1), rtol=1e-15, atol=0)
+
+
+@pytest.mark.parametrize("n,k,m,dim,V,lengths,upl,iters,seed", [
+    (200, 5, 16, 1, 23, (10, 60), 10, 60, 67),   # 1-grams (the protein application's form)
+    (150, 4, 8, 2, 8, (10, 80), 7, 45, 68),      # 2-grams over 8 symbols, odd updatePerLoops
+])
+def test_ngram_pair_passes_match_the_oracle_and_single_passes(d2g, oracle_mod, n, k, m, dim, V, lengths,
+                                                               upl, iters, seed):
+    """Plans that fit one CTA run two iterations per pass; a symbol update on
+    a pair's second iteration counts its deferred Z (Z' times the plan's row
+    scale).  Same symbols and bounds as the oracle, with about half the passes."""
+    ph, c = synth.ngram_phase(n, k, m, dim, V, lengths, 4, seed=seed)
+    opts = dict(maxIters=iters, rhoCoeff=2.0, updatePerLoops=upl)
+    ref = _port(oracle_mod, ph, c, opts)
+    assert np.any(ref["c_sym"] != c["c_sym"])  # the symbols moved
+    passes = {}
+    for pairs in (1, 0):
+        d2g.set_config(pair_iterations=pairs)
+        try:
+            P = d2g.Phase(ph, 0)
+            r = P.run(c, opts)
+            r["Z"] = P.get_plans()
+            d2g.set_config(profile=1)  # one timed launch per pass over the plans
+            P.run(c, opts)
+            passes[pairs] = P.stats()["plan_launches"]
+            P.close()
+        finally:
+            d2g.set_config(pair_iterations=1, profile=0)
+        assert r["stats"]["iterations"] == iters + 1
+        assert_close(r, ref, k, m)
+        assert _plan_l1(r["Z"], ref["Z"]) <= 1e-4
+    assert passes[0] == iters + 1
+    assert passes[1] <= 0.75 * passes[0], passes
