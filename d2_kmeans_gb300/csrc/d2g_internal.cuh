@@ -15,8 +15,9 @@
 //   col_supp    float [ncols_packed * DS]   Euclidean supports (DS = 4 or 8)
 //   col_sym     int   [ncols_packed]        table row (bin / vocabulary id)
 //   grp_meta    int   [ngroups]             plan << 4 | valid columns (1..S)
-//   grp_rec     int4  [ngroups]             {plan, plan's first group, label,
-//                                            plan's groups << 4 | valid columns}
+//   grp_rec     int4  [ngroups]             {plan's slot, plan's first group, label,
+//                                            plan's groups << 12 | plan's index
+//                                            among its item's plans << 4 | valid}
 //   plan_*      int   [nplans]              first group, group count, label,
 //                                           instance id, m_i
 //   rowsum      float [nplans * MP]         per-plan row sums of step 2, normalised
