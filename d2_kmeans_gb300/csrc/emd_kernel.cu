@@ -44,6 +44,8 @@
 // correct tree cannot do); the host turns either into an error.
 #include <math.h>
 
+#include <mutex>
+
 #include "d2g_internal.cuh"
 
 namespace d2g {
@@ -818,10 +820,14 @@ cudaError_t launch_emd_t(const EmdArgs &a, cudaStream_t st) {
   if (wpb < 1) return cudaErrorInvalidValue;
   const size_t smem = (size_t)wpb * slice;
   static size_t configured = 0;
-  if (smem > configured) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = smem;
+  {  // the attribute only grows; calls from other host threads see it set first
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
+    if (smem > configured) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      configured = smem;
+    }
   }
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, wpb * 32, smem);

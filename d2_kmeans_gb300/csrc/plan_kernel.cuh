@@ -27,6 +27,7 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "d2g_internal.cuh"
 
@@ -1027,6 +1028,9 @@ static inline cudaLaunchConfig_t plan_cfg(int nblocks, int threads, size_t smem,
 template <int MP, int MODE, bool CHECK, bool FULL, bool WIDE>
 cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaStream_t st) {
   // persistent grid: as many clusters of a.cs CTAs as are resident at once
+  // (cached per instantiation; phases on other host threads share the cache)
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lk(mu);
   static int grid[kMaxCluster + 1] = {0};
   constexpr int JC = GeoT<MP>::JC;
   constexpr int CW = MODE == COST_TABLE ? 1 : (MODE == COST_EUCLID8 ? 8 : 4);
@@ -1035,7 +1039,6 @@ cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaSt
                     (plan_stages_costs(MP, MODE) ? (size_t)2 * tma_tile_floats<MP>() * 4 : 0) +
                     (size_t)2 * 8 * MP * 4 + (size_t)2 * (a.dim + 1) * MP * 4;
   static size_t configured_smem = 0;
-  static bool nonportable = false;
   auto kern = plan_kernel_tma<MP, MODE, CHECK, FULL, WIDE>;
   if (configured_smem < sm) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -1043,7 +1046,6 @@ cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaSt
     for (int c = 0; c <= kMaxCluster; ++c) grid[c] = 0;
     configured_smem = sm;
   }
-  (void)nonportable;
   const int cs = a.cs;
   if (grid[cs] == 0) {
     cudaLaunchConfig_t cfg = {};

@@ -526,6 +526,8 @@ constexpr size_t pair_scale_bytes() {
 // its plan's scale from global memory.
 template <int MP, int MODE, bool CHECK, bool FULL>
 cudaError_t launch_pair_t(const PlanArgs &a, int nitems, cudaStream_t st) {
+  static std::mutex mu;  // the cached launch shape is shared by phases on other host threads
+  std::lock_guard<std::mutex> lk(mu);
   static int grid = 0, nsm = 0;
   static bool stage = false;
   static size_t configured = 0;
