@@ -24,6 +24,7 @@
 // warp its 32 lanes = 32 rows) and writes T, one coalesced 128-byte row
 // segment per vocabulary column and warp.  Every wait is bounded.
 #include <cstdint>
+#include <mutex>
 
 #include "d2g_internal.cuh"
 
@@ -300,11 +301,15 @@ cudaError_t launch_cost_table_tc(const float *cs, int nrows, const float *vsplit
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev >= 64) return cudaErrorInvalidDevice;
-  if (!configured[dev]) {
-    e = cudaFuncSetAttribute(cost_table_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)tc::kSmemBytes);
-    if (e != cudaSuccess) return e;
-    configured[dev] = true;
+  {
+    static std::mutex mu;  // phases on other host threads
+    std::lock_guard<std::mutex> lk(mu);
+    if (!configured[dev]) {
+      e = cudaFuncSetAttribute(cost_table_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)tc::kSmemBytes);
+      if (e != cudaSuccess) return e;
+      configured[dev] = true;
+    }
   }
   e = launch_tf32_split(cs, nrows, d, tc::TM, csplit, st);
   if (e != cudaSuccess) return e;
