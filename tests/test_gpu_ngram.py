@@ -2,7 +2,7 @@
 (the C restatement, bit-identical to the reference's src/d2/centroid_Bregman.c
 :269-294 and blas_like64.c:232-242) on the same seeded inputs.
 
-Tolerances: the batched FP32 form to the benchmark spec's bounds (objective 1e-5
+Tolerances: the batched FP32 form to the metric's bounds (objective 1e-5
 relative, c_w L1 1e-4 per cluster), the FP64 form to 1e-9; the centroid
 symbols must be identical in both forms.  The reference's own protein
 1-gram fixtures run through test_gpu_badmm's golden tests."""
