@@ -133,6 +133,7 @@ SIGNATURES = {
     "d2g_phase_stats": (C.c_int, [C.c_void_p, C.POINTER(d2g_run_stats)]),
     "d2g_phase_get_scratch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "d2g_phase_stream": (C.c_void_p, [C.c_void_p]),
+    "d2g_phase_test_wait": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double]),
     "d2g_read": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(mph)]),
     "d2g_mph_alloc": (C.c_int, [C.c_int, C.c_size_t, ip, ip, ip, C.POINTER(C.POINTER(mph))]),
     "d2g_mph_free": (C.c_int, [C.POINTER(mph)]),

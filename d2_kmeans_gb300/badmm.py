@@ -161,6 +161,13 @@ class Phase:
                 for i in range(min(n.value, cap))]
         return {"best": self.tuning(), "candidates": rows}
 
+    def test_wait(self, iter: int = -1, unit: int = -1, wait_s: float = 0.0):
+        """Test hook of the bounded device waits (d2g_phase_test_wait): the plan
+        pass of iteration ``iter`` withholds the tile copy of ``unit`` and every
+        wait gives up after ``wait_s`` seconds (0: one second)."""
+        L.check(self.lib.d2g_phase_test_wait(self.h, int(iter), int(unit), float(wait_s)),
+                "d2g_phase_test_wait")
+
     def stats(self) -> dict:
         st = L.d2g_run_stats()
         L.check(self.lib.d2g_phase_stats(self.h, C.byref(st)), "d2g_phase_stats")

@@ -89,6 +89,10 @@ struct d2g_phase {
   cudaStream_t st = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
+  // ---- test hook of the bounded device waits (d2g_phase_test_wait)
+  unsigned long long wait_ns = 0;
+  int fault_iter = -1, fault_unit = -1;
+
   // ---- common device state
   DBuf<Ctl> ctl;
   DBuf<double> trace;
@@ -473,6 +477,8 @@ static PlanArgs base_args(d2g_phase *ph) {
   a.rawsum_out = ph->rawsum.p;
   a.nplans_chk = ph->nplans;
   a.nlab_chk = ph->K;
+  a.ctab_rows = tables ? ph->K * ph->ntab
+                       : ((ph->metric == D2_HISTOGRAM || ph->metric == D2_SPARSE_HISTOGRAM) ? ph->vocab_size : 0);
   return a;
 }
 
@@ -1330,6 +1336,9 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
   h.budget_ns = (tb > 0 && tb < 1.8e10) ? (unsigned long long)(tb * 1e9) : ~0ULL;
   h.rho_coeff = opt->rhoCoeff;
   h.global_size = (double)ph->global_size;
+  h.wait_ns = ph->wait_ns;
+  h.fault_iter = ph->fault_iter;
+  h.fault_unit = ph->fault_unit;
   D2G_CUDA(cudaMemcpyAsync(ph->ctl.p, &h, sizeof h, cudaMemcpyHostToDevice, ph->st));
 
   long long launches = 0;
@@ -1459,8 +1468,10 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
     ph->stats.plan_bytes = ph->path == 0 ? ((emb || ng) ? 20.0 : 16.0) * ent + colb + 4.0 * m * (double)n
                                          : 136.0 * ent;
   }
-  if (h.err == 9)  // a pair-pass self-check: a staged plan record or slot out of range
-    return fail(D2G_E_CUDA, "device self-check failed: a plan record out of range in a pair pass");
+  if (h.err == 9)  // a plan-pass self-check: a staged plan record, slot or table row out of range
+    return fail(D2G_E_CUDA, "device self-check failed: a plan record or table row out of range in a plan pass");
+  if (h.err == 7)
+    return fail(D2G_E_CUDA, "a plan pass gave up waiting for a bulk copy of its tiles (bounded wait ran out)");
   if (h.err == kErrTcTimeout)
     return fail(D2G_E_CUDA, "tensor-core cost table: wait for the MMA completion timed out");
   if (h.err) return fail(D2G_E_NUMERIC, "non-positive or non-finite normaliser (device code " +
@@ -1481,8 +1492,22 @@ int distmat_fp64(int dim, int str, size_t size, const int *p_str, int metric, co
   long long col = 0;
   for (size_t i = 0; i < size; ++i) {
     if (label[i] < 0 || (size_t)label[i] >= K) return fail(D2G_E_INVAL, "label out of range");
+    if (p_str[i] < 0) return fail(D2G_E_INVAL, "negative support size");
     cum[i] = col;
     col += p_str[i];
+  }
+  // every id the cost kernel indexes with must lie inside its table (a
+  // negative word-embedding id is the reference's ||centroid||^2 case)
+  if (metric == D2_WORD_EMBED || ng) {
+    if (!sym || V < 1 || (!ng && !vocab)) return fail(D2G_E_INVAL, "distmat: ids or vocabulary missing");
+    const size_t nsym = ng ? (size_t)col * dim : (size_t)col;
+    for (size_t j = 0; j < nsym; ++j)
+      if (sym[j] >= V || (ng && sym[j] < 0)) return fail(D2G_E_INVAL, "distmat: id out of range");
+    if (ng)
+      for (size_t j = 0; j < K * str * (size_t)dim; ++j)
+        if (c_sym[j] < 0 || c_sym[j] >= V) return fail(D2G_E_INVAL, "distmat: centroid symbol out of range");
+  } else if (metric == D2_EUCLIDEAN_L2 && !supp && col > 0) {
+    return fail(D2G_E_INVAL, "distmat: supports missing");
   }
   std::vector<int> ci(col);
   for (size_t i = 0; i < size; ++i)
@@ -1858,6 +1883,15 @@ int d2g_phase_trace(d2g_phase *ph, double *trace, int cap, int *n) {
 }
 
 void *d2g_phase_stream(d2g_phase *ph) { return ph ? (void *)ph->st : nullptr; }
+
+int d2g_phase_test_wait(d2g_phase *ph, int iter, int unit, double wait_s) {
+  if (!ph) return fail(D2G_E_INVAL, "null phase");
+  if (!(wait_s >= 0 && wait_s <= 10)) return fail(D2G_E_INVAL, "wait limit outside 0..10 s");
+  ph->fault_iter = unit >= 0 ? iter : -1;
+  ph->fault_unit = unit >= 0 ? unit : -1;
+  ph->wait_ns = (unsigned long long)(wait_s * 1e9);
+  return D2G_OK;
+}
 
 int d2g_phase_stats(d2g_phase *ph, d2g_run_stats *st) {
   if (!ph || !st) return D2G_E_INVAL;

@@ -77,7 +77,16 @@ struct Ctl {
   int err;                   // nonzero: numeric failure seen on device
   double rho_coeff;
   double global_size;
+  // bounded waits of the plan kernels: limit in ns (0 = one second), and a
+  // test hook that withholds the tile copy of unit fault_unit in the plan
+  // pass of iteration fault_iter (-1 = none), so that one wait runs out
+  unsigned long long wait_ns;
+  int fault_iter, fault_unit;
 };
+
+// record a device failure in the control block; the first one wins (later
+// kernels of the same run may fail as a consequence and must not hide it)
+__device__ __forceinline__ void ctl_fail(Ctl *c, int code) { atomicCAS(&c->err, 0, code); }
 
 struct PlanArgs {
   float *Z, *Y;
@@ -107,6 +116,7 @@ struct PlanArgs {
   float *rawsum_out;        // pair pass: raw row sums of the second iteration's Z', by slot
   int nplans_chk, nlab_chk; // plans and clusters of the phase (self-check of staged records)
   const int2 *item_pp;      // per item {first plan in packed order, plans}
+  int ctab_rows;            // rows of MP floats in ctab (bound of the staged row gather)
 };
 
 // per-MP launch geometry

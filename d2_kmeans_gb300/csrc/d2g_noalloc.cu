@@ -9,8 +9,9 @@
 // data.  This entry point keeps that working data - the p_str prefix sums and
 // the column-to-instance map that calculate_distmat builds in freshly
 // allocated buffers - in one fixed, file-scope device array instead, so the
-// call itself allocates nothing: no cudaMalloc, no cudaFree, no allocating
-// library routine, no host heap.
+// call itself allocates no device memory: no cudaMalloc, no cudaFree, no
+// allocating library routine.  (Its error paths do format their message on
+// the host heap.)
 //
 // Limits and sharing rules:
 //   * the scratch array is kNoallocScratchBytes (8 MiB) on every GPU that
@@ -24,7 +25,14 @@
 //     ordering between them) race on the array: serialise them;
 //   * the first call on each device looks up the array's device address with
 //     cudaGetSymbolAddress (with that device current); make that first call
-//     before any stream capture on the device.
+//     before any stream capture on the device;
+//   * with CUDA's lazy module loading (the default unless
+//     CUDA_MODULE_LOADING=EAGER), the array itself comes into existence when
+//     this library's device code is first loaded on a device, which can be
+//     that same first call: it may then grow the device footprint by 8 MiB or
+//     fail for lack of memory.  Callers that must not allocate during a job
+//     make the first call at set-up time.
+#include <climits>
 #include <mutex>
 
 #include "d2g_internal.cuh"
@@ -135,6 +143,12 @@ extern "C" int d2g_distmat_noalloc(int metric_type, int dim, int str, size_t siz
       !c_supp || !C || (metric_type == D2_EUCLIDEAN_L2 && !p_supp) ||
       (metric_type == D2_WORD_EMBED && (!p_supp_sym || !vocab_vec || vocab_size < 1))) {
     set_error("d2g_distmat_noalloc: missing or invalid argument");
+    return D2G_E_INVAL;
+  }
+  // refuse sizes whose scratch need would not even fit a size_t before
+  // computing it (8 * size or 4 * col could wrap around)
+  if (size > kNoallocScratchBytes / 8 || col > kNoallocScratchBytes / 4 || size > (size_t)INT_MAX) {
+    set_error("d2g_distmat_noalloc: size or col beyond the 8 MiB fixed array");
     return D2G_E_INVAL;
   }
   const size_t need = 256 + 8 * size + 4 * col;

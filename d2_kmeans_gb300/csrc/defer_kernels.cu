@@ -90,7 +90,7 @@ __global__ void pair_scale_kernel(const float *__restrict__ rawsum, const int *_
   const int slot = __ldg(plan_slot + p), lab = __ldg(plan_label + p);
   // self-check: a slot outside the plans or a label outside the clusters
   if (slot < 0 || slot >= nplans || lab < 0 || lab >= nlab || (k & 3)) {
-    ((Ctl *)ctl)->err = 9;
+    ctl_fail((Ctl *)ctl, 9);
     return;
   }
   const float4 cw = __ldg((const float4 *)(cw32 + (size_t)lab * MP + k));
@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(256) pair_finalize_kernel(float4 *__restrict__
     const int p = __ldg(&grp_meta[i / per4]) >> 4;
     const int k0 = (int)((i * 4) % MP);
     if (p < 0 || p >= nplans) {  // self-check: a plan outside the phase
-      *err = 9;
+      atomicCAS(err, 0, 9);
       continue;
     }
     const float4 sc = __ldg((const float4 *)(rowsc + (size_t)p * MP + k0));

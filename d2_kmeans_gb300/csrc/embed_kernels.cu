@@ -171,7 +171,7 @@ __global__ void support_final_kernel(const float *__restrict__ part, int nchunk,
       num += (double)p[t];
       den += (double)p[d];
     }
-    if (!(den > 0.0)) ctl->err = 2;
+    if (!(den > 0.0)) ctl_fail(ctl, 2);
     const double v = num / den;
     cs64[((size_t)l * m + k) * d + t] = v;
     cs32f[((size_t)l * m + k) * d + t] = (float)v;  // row-major (K*m) x d for the table GEMM

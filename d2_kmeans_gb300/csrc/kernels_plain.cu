@@ -118,7 +118,7 @@ __global__ void plain_step1b(const PlainArgs a) {  // cnorm + grms, :158-159
     double *x = a.X + (size_t)c * a.str;
     double s = 0.0;
     for (int k = 0; k < a.str; ++k) s += x[k];
-    if (!(s > 0.0)) a.ctl->err = 4;
+    if (!(s > 0.0)) ctl_fail(a.ctl, 4);
     const double w = a.w[c];
     for (int k = 0; k < a.str; ++k) {
       x[k] /= s;
@@ -143,7 +143,7 @@ __global__ void plain_step2b(const PlainArgs a) {  // rnorm + gcms per instance,
     const int mi = a.p_str[i];
     double s = 0.0;
     for (int j = 0; j < mi; ++j) s += z[(size_t)j * a.str];
-    if (!(s > 0.0)) a.ctl->err = 5;
+    if (!(s > 0.0)) ctl_fail(a.ctl, 5);
     const double cw = a.cw64[(size_t)a.label[i] * a.str + k];
     for (int j = 0; j < mi; ++j) {
       z[(size_t)j * a.str] /= s;

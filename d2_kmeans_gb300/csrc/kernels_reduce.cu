@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(kRedThreads) cluster_final_kernel(const Cluste
       double t = 0.0;
       for (int k = 0; k < m; ++k) t += sv[k];
       tot_sh = t;
-      if (!(t > 0.0) || !isfinite(t)) a.ctl->err = 1;
+      if (!(t > 0.0) || !isfinite(t)) ctl_fail(a.ctl, 1);
     }
     __syncthreads();
     const double t = tot_sh;
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(kRedThreads) cluster_final_kernel(const Cluste
   } else if (plane < a.dim) {  // support numerator plane t = plane (:219-221)
     for (int k = threadIdx.x; k < m; k += kRedThreads) {
       const double num = chunk_sum(plane, k), den = chunk_sum(a.dim, k);
-      if (!(den > 0.0)) a.ctl->err = 2;
+      if (!(den > 0.0)) ctl_fail(a.ctl, 2);
       const double v = num / den;
       a.cs64[((size_t)l * m + k) * a.dim + plane] = v;
       if (a.cs32) a.cs32[((size_t)l * a.MP + k) * a.DS + plane] = (float)v;
@@ -210,7 +210,7 @@ __global__ void rho_final_kernel(const double *part, int n, Ctl *ctl, double nen
     ctl->rho = rho;
     ctl->inv_rho = (float)(1.0 / rho);
     ctl->inv_rho_l2 = (float)(1.4426950408889634 / rho);  // log2(e)/rho
-    if (!(rho > 0.0) || !isfinite(rho)) ctl->err = 3;
+    if (!(rho > 0.0) || !isfinite(rho)) ctl_fail(ctl, 3);
   }
 }
 

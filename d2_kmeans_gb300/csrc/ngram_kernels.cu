@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(kCountWarps * 32) ngram_count32_kernel(
         if (deferred) {
           int p = __ldg(grp_meta + c / S) >> 4;
           if (p < 0 || p >= nplans) {  // self-check: a plan outside the phase
-            ((Ctl *)ctl)->err = 9;
+            ctl_fail((Ctl *)ctl, 9);
             p = 0;
           }
           plans[warp][lane] = p;

@@ -484,16 +484,27 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *b, unsigned pa
       : "memory");
   return ok != 0;
 }
-// Bounded wait (about one second of device time), so a lost copy reports an
-// error instead of hanging the GPU.
-__device__ __forceinline__ bool mbar_wait(unsigned long long *b, unsigned parity) {
+// Bounded wait (limit_ns of device time, one second unless the control block
+// sets another), so a lost copy reports an error instead of hanging the GPU.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *b, unsigned parity,
+                                          unsigned long long limit_ns) {
   if (mbar_try_wait(b, parity)) return true;
   const unsigned long long t0 = global_ns();
   for (;;) {
     for (int i = 0; i < 64; ++i)
       if (mbar_try_wait(b, parity)) return true;
-    if (global_ns() - t0 > 1000000000ull) return false;
+    if (global_ns() - t0 > limit_ns) return false;
   }
+}
+// the wait limit of a launch: Ctl::wait_ns, or one second
+__device__ __forceinline__ unsigned long long wait_limit(const Ctl *c) {
+  const unsigned long long w = c->wait_ns;
+  return w ? w : 1000000000ull;
+}
+// the unit whose tile copy this launch withholds (Ctl::fault_iter/fault_unit,
+// a test hook that makes one bounded wait run out), or -1
+__device__ __forceinline__ int withheld_unit(const Ctl *c, int iter) {
+  return c->fault_iter == iter ? c->fault_unit : -1;
 }
 
 template <int MP>
@@ -560,15 +571,20 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
   const int ustep = clustered ? (int)(gridDim.x / CS) : (int)gridDim.x;
   const int nunits = nitems;
   if (a.iter == 0 && a.resid_off == 0 && blockIdx.x == 0 && tid == 0) a.ctl->t_start_ns = global_ns();
+  const unsigned long long wlim = wait_limit(a.ctl);
+  // the test hook never applies to cluster launches: a CTA that gives up there
+  // still meets its peers at the unit's cluster barrier, which has no bound
+  const int fault_u = clustered ? -1 : withheld_unit(a.ctl, a.iter);
   // one stage = the slice's Z and Y tiles, group records, weights and supports
   // (+ the deferred row scale of its wide plan, slot >= 0)
-  auto issue = [&](int g0, int ng, int slot, int stg) {
+  auto issue = [&](int unit, int g0, int ng, int slot, int stg) {
     const size_t off = (size_t)g0 * S * MP;
     const unsigned bytes = (unsigned)ng * S * MP * 4u;
     const unsigned rb = (unsigned)ng * 16u, wb = (unsigned)ng * S * 4u, cb = wb * CW;
     const unsigned sb = slot >= 0 ? (unsigned)MP * 4u : 0u;
     mbar_expect_tx(&mbar[stg], 2u * bytes + rb + wb + cb + sb);
     if (ng <= 0) return;  // an empty slice: the phase completes on the arrival alone
+    if (unit == fault_u) return;  // test hook: the stage's transaction never completes
     bulk_load(stZ + stg * TILE, a.Z + off, bytes, &mbar[stg]);
     bulk_load(stY + stg * TILE, a.Y + off, bytes, &mbar[stg]);
     bulk_load(stR + stg * G, a.grp_rec + g0, rb, &mbar[stg]);
@@ -597,6 +613,10 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
     for (int j = 0; j < PPT; ++j) {
       const int c = (tid + NT * j) / CPR;
       crow_p[j] = c < ng * S ? __ldg(a.col_crow + (size_t)g0 * S + c) : -1;
+      if (crow_p[j] >= a.ctab_rows) {  // a table row outside the table: reported, not read
+        ctl_fail(a.ctl, 9);
+        crow_p[j] = -1;
+      }
     }
   };
   auto issue_rows = [&](int stg) {
@@ -623,7 +643,7 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
       slice(u0, g0, ng, sl);
       sh_g0[0] = g0;
       sh_ng[0] = ng;
-      issue(g0, ng, sl, 0);
+      issue(u0, g0, ng, sl, 0);
       if (u0 + ustep < nunits) slice(u0 + ustep, nx_g0, nx_ng, nx_slot);
     }
   }
@@ -641,16 +661,25 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
   const bool write_x = a.flags & PF_WRITE_X;
   double s_obj = 0.0, s_pr = 0.0, s_dr = 0.0;  // FP64 across items, FP32 within one item
   int it = 0;
+  bool failed = false;
   for (int u = u0; u < nunits; u += ustep, ++it) {
     const int stg = it & 1;
-    if (!mbar_wait(&mbar[stg], (it >> 1) & 1)) sh_fail = 1;
+    if (!mbar_wait(&mbar[stg], (it >> 1) & 1, wlim)) sh_fail = 1;
     if (SC) asm volatile("cp.async.wait_all;" ::: "memory");  // this unit's table rows
     __syncthreads();
-    if (sh_fail) break;
+    failed = sh_fail != 0;
+    if (clustered) {
+      // the ranks of a cluster leave together: one that gave up alone would
+      // leave its peers at the unit's cluster barrier for good
+      cg::cluster_group cl = cg::this_cluster();
+      cl.sync();
+      for (int rk = 0; rk < CS; ++rk) failed |= *cl.map_shared_rank(&sh_fail, rk) != 0;
+    }
+    if (failed) break;
     const int cur_g0 = sh_g0[stg], cur_ng = sh_ng[stg];
     const int rank = crank;
     if (tid == 0 && u + ustep < nunits) {
-      issue(nx_g0, nx_ng, nx_slot, stg ^ 1);
+      issue(u + ustep, nx_g0, nx_ng, nx_slot, stg ^ 1);
       sh_g0[stg ^ 1] = nx_g0;
       sh_ng[stg ^ 1] = nx_ng;
       if (u + 2 * ustep < nunits) slice(u + 2 * ustep, nx_g0, nx_ng, nx_slot);
@@ -979,13 +1008,17 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
   }
   // rank 0 may still be reading a peer's shared memory (the moments of the
   // last item): no CTA of a cluster leaves before all of them are done
-  if (clustered && !sh_fail) cg::this_cluster().sync();
+  if (clustered && !failed) cg::this_cluster().sync();
   if (SC) asm volatile("cp.async.wait_all;" ::: "memory");  // no table-row copy outlives the CTA
-  if (sh_fail) {
+  if (failed) {
     if (tid == 0) {
-      a.ctl->err = 7;  // a bulk copy did not complete: let the copies in flight land first
-      mbar_wait(&mbar[0], 0);
-      mbar_wait(&mbar[1], 0);
+      ctl_fail(a.ctl, 7);
+      // A bulk copy did not complete.  The only copy that can be in flight is
+      // the one of the unit that failed (it), on stage it & 1 at phase parity
+      // (it >> 1) & 1; the next stage is issued only after a successful wait.
+      // Wait for it once more, again bounded, so that no copy lands in the
+      // shared memory of a CTA that has left.
+      mbar_wait(&mbar[it & 1], (it >> 1) & 1, wlim);
     }
     return;
   }

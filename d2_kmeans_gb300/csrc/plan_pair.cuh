@@ -72,24 +72,27 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
   const int tid = threadIdx.x;
   const int u0 = blockIdx.x, ustep = gridDim.x, nunits = nitems;
   if (a.iter == 0 && blockIdx.x == 0 && tid == 0) a.ctl->t_start_ns = global_ns();
+  const unsigned long long wlim = wait_limit(a.ctl);
+  const int fault_u = withheld_unit(a.ctl, a.iter);
   const bool indef = a.flags & PF_IN_DEF;
   const bool stage_sc = indef && (a.flags & PF_STAGE_SC);
   // the plans {first, count} of unit u, checked against the phase (thread 0)
   auto unit_plans = [&](int u) {
     int2 pp = indef ? a.item_pp[u] : make_int2(0, 0);
     if (pp.x < 0 || pp.y < 0 || pp.y > G || pp.x > a.nplans_chk - pp.y) {
-      a.ctl->err = 9;
+      ctl_fail(a.ctl, 9);
       pp = make_int2(0, 0);
     }
     return pp;
   };
-  auto issue = [&](int g0, int ng, int2 pp, int stg) {
+  auto issue = [&](int unit, int g0, int ng, int2 pp, int stg) {
     const size_t off = (size_t)g0 * S * MP;
     const unsigned bytes = (unsigned)ng * S * MP * 4u;
     const unsigned rb = (unsigned)ng * 16u, wb = (unsigned)ng * S * 4u, cb = wb * CW;
     const unsigned sb = stage_sc && ng > 0 ? (unsigned)pp.y * MP * 4u : 0u;
     mbar_expect_tx(&mbar[stg], 2u * bytes + rb + wb + cb + sb);
     if (ng <= 0) return;
+    if (unit == fault_u) return;  // test hook: the stage's transaction never completes
     if (sb) bulk_load(stS + stg * G * MP, a.rowsc + (size_t)pp.x * MP, sb, &mbar[stg]);
     bulk_load(stZ + stg * TILE, a.Z + off, bytes, &mbar[stg]);
     bulk_load(stY + stg * TILE, a.Y + off, bytes, &mbar[stg]);
@@ -106,6 +109,10 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
     for (int j = 0; j < PPT; ++j) {
       const int c = (tid + NT * j) / CPR;
       crow_p[j] = c < ng * S ? __ldg(a.col_crow + (size_t)g0 * S + c) : -1;
+      if (crow_p[j] >= a.ctab_rows) {  // a table row outside the table: reported, not read
+        ctl_fail(a.ctl, 9);
+        crow_p[j] = -1;
+      }
     }
   };
   auto issue_rows = [&](int stg) {
@@ -133,7 +140,7 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
       sh_g0[0] = g0;
       sh_ng[0] = ng;
       sh_pp[0] = pp;
-      issue(g0, ng, pp, 0);
+      issue(u0, g0, ng, pp, 0);
       if (u0 + ustep < nunits) {
         nx_g0 = a.item_g0[u0 + ustep];
         nx_ng = a.item_ng[u0 + ustep];
@@ -157,14 +164,14 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
   int it = 0;
   for (int u = u0; u < nunits; u += ustep, ++it) {
     const int stg = it & 1;
-    if (!mbar_wait(&mbar[stg], (it >> 1) & 1)) sh_fail = 1;
+    if (!mbar_wait(&mbar[stg], (it >> 1) & 1, wlim)) sh_fail = 1;
     if (SC) asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();
     if (sh_fail) break;
     const int cur_g0 = sh_g0[stg], cur_ng = sh_ng[stg];
     const int2 cur_pp = sh_pp[stg];
     if (tid == 0 && u + ustep < nunits) {
-      issue(nx_g0, nx_ng, nx_pp, stg ^ 1);
+      issue(u + ustep, nx_g0, nx_ng, nx_pp, stg ^ 1);
       sh_g0[stg ^ 1] = nx_g0;
       sh_ng[stg ^ 1] = nx_ng;
       sh_pp[stg ^ 1] = nx_pp;
@@ -184,7 +191,7 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
     if (t.active && (t.p < 0 || t.p >= a.nplans_chk || t.lab < 0 || t.lab >= a.nlab_chk ||
                      t.pl_g0 < cur_g0 || t.pl_g0 + t.pl_ng > cur_g0 + cur_ng || t.pl_ng < 1 ||
                      (indef && t.lp >= cur_pp.y))) {
-      a.ctl->err = 9;
+      ctl_fail(a.ctl, 9);
       t.active = false;
       t.nvalid = 0;
       t.p = 0;
@@ -482,9 +489,11 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
   if (SC) asm volatile("cp.async.wait_all;" ::: "memory");
   if (sh_fail) {
     if (tid == 0) {
-      a.ctl->err = 7;
-      mbar_wait(&mbar[0], 0);
-      mbar_wait(&mbar[1], 0);
+      ctl_fail(a.ctl, 7);
+      // the one copy that can be in flight is the failed unit's (it): stage
+      // it & 1, phase parity (it >> 1) & 1 (the next stage is issued only
+      // after a successful wait); wait for it once more, bounded
+      mbar_wait(&mbar[it & 1], (it >> 1) & 1, wlim);
     }
     return;
   }

@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(128, 1)
       }
     }
   } else if (tid == 0) {
-    atomicExch(err, kErrTcTimeout);
+    atomicCAS(err, 0, kErrTcTimeout);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();

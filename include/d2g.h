@@ -149,11 +149,14 @@ void calculate_distmat(sph *data_ph, int *label, size_t size, sph *c, double *C)
  * [col*dim] or p_supp_sym [col] + vocab_vec [vocab_size*dim], label [size],
  * c_supp [num_of_labels*str*dim] in, C [str*col] out - and the working data
  * (prefix sums, column map) lives in an 8 MiB array fixed inside libd2g.so
- * on each GPU, so the call allocates nothing.  Needs 8*size + 4*col + 256
- * bytes of that array and returns D2G_E_INVAL beyond it.  Calls share the
- * array: calls whose GPU work overlaps race, so serialise them.  The first
- * call on a device looks up the array's address; make it before any stream
- * capture.  Runs on `stream` (a cudaStream_t, NULL for the default stream)
+ * on each GPU, so the call allocates no device memory.  Needs 8*size +
+ * 4*col + 256 bytes of that array and returns D2G_E_INVAL beyond it.  Calls
+ * share the array: calls whose GPU work overlaps race, so serialise them.
+ * The first call on a device looks up the array's address; make it before
+ * any stream capture.  Under CUDA's lazy module loading (the default unless
+ * CUDA_MODULE_LOADING=EAGER) the array is created when the library's device
+ * code first loads on a device, which may be that first call: make it at
+ * set-up time.  Runs on `stream` (a cudaStream_t, NULL for the default stream)
  * and returns after the inputs are validated, with the cost kernel queued.
  * Euclidean and word-embedding phases only. */
 int d2g_distmat_noalloc(int metric_type, int dim, int str, size_t size, size_t col,
@@ -284,6 +287,15 @@ void *d2g_phase_stream(d2g_phase *ph);
 /* the last run's X (after step 1, or X-Z after a check iteration as the
  * reference leaves it), Y and C (divided by rho), reference layout, FP64 */
 int d2g_phase_get_scratch(d2g_phase *ph, double *X, double *Y, double *C);
+/* Test hook of the bounded device waits (no counterpart in the reference).
+ * Every wait of the batched plan kernels for their bulk copies gives up after
+ * wait_s seconds (0: one second), reports through the phase's control block
+ * and the run returns D2G_E_CUDA; the phase and the CUDA context stay usable.
+ * With unit >= 0 the plan pass of iteration iter withholds the tile copy of
+ * that unit (its CTA's wait then runs out); unit < 0 turns the hook off.
+ * Cluster launches (plans wider than one CTA, exchanged synchronously) ignore
+ * the hook. */
+int d2g_phase_test_wait(d2g_phase *ph, int iter, int unit, double wait_s);
 
 /* ------------------------------------------------------------ d2 input files
  * Replaces d2_read, src/d2/clustering_io.c:14-201 (declared

@@ -100,6 +100,14 @@ static void calc_distmat(const d2o_phase *ph, const size_t *cum, const double *c
   for (size_t i = 0; i < ph->size; ++i) cost_block(ph, i, cum[i], c_supp, C + ph->str * cum[i]);
 }
 
+void d2o_cost_blocks(const d2o_phase *ph, const double *c_supp, double *C) {
+  size_t cum = 0;
+  for (size_t i = 0; i < ph->size; ++i) {
+    cost_block(ph, i, cum, c_supp, C + ph->str * cum);
+    cum += (size_t)ph->p_str[i];
+  }
+}
+
 /* column-normalise an m x n column-major block; sums into sa (blas_like64.c:122-136) */
 static int cnorm(size_t m, size_t n, double *a, double *sa) {
   for (size_t i = 0; i < n; ++i) {

@@ -93,6 +93,16 @@ int d2o_serve_query(int dim, int str, int k, const double *c_w, const double *c_
                     int m_q, const double *w_q, const double *supp_q, int iters,
                     double rhoCoeff, double *cost_out);
 
+/* Ground costs of every instance against its cluster's centroid, C [str*col],
+ * instance i's block column-major str x m_i at str*cum[i] (the per-instance
+ * blocks of calculate_distmat, src/d2/centroid_util.c:8-36, through
+ * _dpdist2 / _dpdist2_sym / _dpdist_symbolic, src/utils/blas_like64.c:199-242;
+ * histograms get the copy of their cost matrix that the harness fills in,
+ * because the reference's calculate_distmat leaves their C untouched).
+ * c_supp: [k*str*dim] Euclidean / embedding centroids; n-gram centroids come
+ * from ph->c_sym. */
+void d2o_cost_blocks(const d2o_phase *ph, const double *c_supp, double *C);
+
 /*
  * d2 input files (the reference's d2_read, src/d2/clustering_io.c:14-201,
  * into the mph of its d2_allocate, src/d2/clustering_util.c:93-130).  The

@@ -23,7 +23,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libd2ref.so")
-REF_TREE = "/root/reference"
+# where the reference's source tree is read from (the build of oracle/_ref and
+# the tests that read its data files); absent trees are skipped
+REF_TREE = os.environ.get("D2_REFERENCE_TREE", "/root/reference")
 
 METRIC = {"euclidean": 0, "histogram": 5, "ngram": 6, "embed": 7, "sparse_histogram": 12}
 
@@ -160,6 +162,43 @@ def badmm(phase: dict, centroids: dict, opts: dict, kind: str = "port",
            "iters": iters.value}
     res.update({n: v for n, v in outs.items() if v is not None})
     return res
+
+
+def cost_blocks(phase: dict, centroids: dict) -> np.ndarray:
+    """Every instance's ground-cost block against its cluster's centroid
+    (d2o_cost_blocks): C [str*col], the blocks of calculate_distmat."""
+    lib = _lib("port")
+    lib.d2o_cost_blocks.restype = None
+    lib.d2o_cost_blocks.argtypes = [C.POINTER(_Phase), C.c_void_p, C.c_void_p]
+    keep = []
+
+    def arr(a, dtype):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=dtype)
+        keep.append(a)
+        return a
+    p_str = arr(phase["p_str"], np.int32)
+    m = int(phase["str"])
+    col = int(p_str.sum())
+    ph = _Phase()
+    ph.metric = METRIC[phase["metric"]] if isinstance(phase["metric"], str) else int(phase["metric"])
+    ph.dim, ph.str, ph.size, ph.col = int(phase.get("dim", 0)), m, p_str.size, col
+    ph.p_str = p_str.ctypes.data
+    ph.p_w = _ptr(arr(phase.get("p_w"), np.float64))
+    ph.p_supp = _ptr(arr(phase.get("p_supp"), np.float64))
+    ph.p_supp_sym = _ptr(arr(phase.get("p_supp_sym"), np.int32))
+    ph.vocab_vec = _ptr(arr(phase.get("vocab_vec"), np.float64))
+    ph.vocab_size = int(phase.get("vocab_size", 0))
+    ph.dist_mat = _ptr(arr(phase.get("dist_mat"), np.float64))
+    ph.label = _ptr(arr(phase["label"], np.int32))
+    ph.num_of_labels = int(phase["num_of_labels"])
+    ph.global_size = p_str.size
+    ph.c_sym = _ptr(arr(centroids.get("c_sym"), np.int32))
+    cs = arr(centroids.get("c_supp"), np.float64)
+    out = np.zeros(m * col)
+    lib.d2o_cost_blocks(C.byref(ph), _ptr(cs), out.ctypes.data)
+    return out
 
 
 def serve_query(c_w, c_supp, w_q, supp_q, iters=200, rho_coeff=2.0):

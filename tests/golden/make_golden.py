@@ -25,7 +25,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import oracle  # noqa: E402
 from d2_kmeans_gb300 import synth  # noqa: E402
 
-REF_DATA = "/root/reference/data"
+REF_DATA = os.path.join(oracle.REF_TREE, "data")
 
 
 def digest(z: np.ndarray) -> np.ndarray:
@@ -85,6 +85,40 @@ def read_protein_1gram(limit):
             D.reshape(len(keys), len(keys)))
 
 
+def read_mountain():
+    """Phase 0 of the reference's data/mountaindat.d2 (2000 objects, d = 3,
+    11 011 support points) read by the reference's own d2_read, labels i % 10,
+    and initial centroids (k = 10, m = 6) from the reference's own
+    d2_centroid_rands (src/d2/centroid_rand.c:161-295; srand(0) order), both
+    compiled into oracle/_ref: the centroid update of the reference's
+    mountaindat example, whose objective trace over 100 iterations runs
+    949.94 / 800.13 / 751.01 / 737.56 / 731.14 at iterations 20 ... 100."""
+    import ctypes as C
+    from d2_kmeans_gb300 import _lib as L
+    from d2_kmeans_gb300.assign import Mph
+    rc, arr = oracle.read("ref", os.path.join(REF_DATA, "mountaindat.d2"), 2000, [3, 3], [0, 0],
+                          avg_strides=[6, 11])
+    assert rc == 0 and arr["size"] == 2000
+    p0 = arr["phases"][0]
+    n, k, m, d = arr["size"], 10, 6, 3
+    label = (np.arange(n) % k).astype(np.int32)
+    ph = dict(metric=0, dim=d, str=m, p_str=p0["p_str"].astype(np.int32), p_w=p0["p_w"],
+              p_supp=p0["p_supp"], label=label, num_of_labels=k, label_switch=np.ones(n, np.int8))
+    data = Mph([ph], n, label=label, num_of_labels=k)
+    w, supp = np.full(k * m, np.nan), np.full(k * m * d, np.nan)
+    p_str, cum = np.zeros(k, np.int32), np.zeros(k, np.uint64)
+    c = L.sph()
+    c.dim, c.str, c.max_str, c.metric_type = d, m, m, 0
+    c.p_str = p_str.ctypes.data_as(C.POINTER(C.c_int))
+    c.p_str_cum = cum.ctypes.data_as(C.POINTER(C.c_size_t))
+    c.p_w = w.ctypes.data_as(C.POINTER(C.c_double))
+    c.p_supp = supp.ctypes.data_as(C.POINTER(C.c_double))
+    rands = oracle._lib("ref").d2_centroid_rands
+    rands.restype = C.c_int
+    assert rands(C.byref(data.mph), 0, C.byref(c)) == 0
+    return ph, dict(c_w=w, c_supp=supp)
+
+
 def cases():
     out = {}
     ph, c = synth.euclidean_phase(300, 6, 16, 3, (4, 16), False, 10, 1.0, seed=11)
@@ -124,6 +158,8 @@ def cases():
     out["protein_kat"] = (ph, c, dict(maxIters=60, rhoCoeff=1.0, updatePerLoops=60))
     ph2 = dict(ph)
     out["protein_upd10"] = (ph2, c, dict(maxIters=40, rhoCoeff=1.0, updatePerLoops=10))
+    ph, c = read_mountain()
+    out["mountain_kat"] = (ph, c, dict(maxIters=100, rhoCoeff=2.0, updatePerLoops=10))
     return out
 
 

@@ -14,7 +14,9 @@ from d2_kmeans_gb300 import _lib as L
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INCLUDE = os.path.join(ROOT, "include")
-REF_INCLUDE = "/root/reference/include"
+import oracle  # noqa: E402
+
+REF_INCLUDE = os.path.join(oracle.REF_TREE, "include")
 
 
 def declared_functions():

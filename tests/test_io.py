@@ -18,7 +18,9 @@ import pytest
 from d2_kmeans_gb300 import d2io
 from d2_kmeans_gb300._lib import D2G_E_INVAL, D2GError
 
-REF_DATA = "/root/reference/data/mountaindat.d2"
+import oracle  # noqa: E402
+
+REF_DATA = os.path.join(oracle.REF_TREE, "data", "mountaindat.d2")
 
 
 @pytest.fixture(scope="module")
