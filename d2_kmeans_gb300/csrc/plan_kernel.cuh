@@ -354,12 +354,16 @@ __global__ void __launch_bounds__(GeoT<MP>::NT) pack_convert_kernel(const PlanAr
   const long long base = plan_refcol[t.p] * str;  // plan_refcol holds p_str_cum (columns)
   const int jj0 = (t.cta_g0 + t.g - t.pl_g0) * S;
   if (dir == 2 && !reinit[t.p]) return;
-  for (int s = 0; s < t.nvalid; ++s) {
+  // a re-initialised plan is written whole, its pad columns too (zeros): the
+  // plan kernels rely on pad columns holding Z = 0, and a pass that failed
+  // part-way may have left anything there
+  const int ncols = dir == 2 ? S : t.nvalid;
+  for (int s = 0; s < ncols; ++s) {
     const size_t off = (t.colbase + s) * MP + t.k0;
     const long long rc = base + (long long)(jj0 + s) * str;
     float v[RPT];
     if (dir == 2) {  // re-initialised plan Z = w (x) c_w, in FP32 (GB300's FP64 pipe is narrow)
-      const float wj = a.col_w[t.colbase + s];
+      const float wj = s < t.nvalid ? a.col_w[t.colbase + s] : 0.f;
 #pragma unroll
       for (int q = 0; q < RPT; ++q) {
         const int k = t.k0 + q;
