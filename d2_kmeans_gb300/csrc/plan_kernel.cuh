@@ -576,9 +576,7 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
   const int nunits = nitems;
   if (a.iter == 0 && a.resid_off == 0 && blockIdx.x == 0 && tid == 0) a.ctl->t_start_ns = global_ns();
   const unsigned long long wlim = wait_limit(a.ctl);
-  // the test hook never applies to cluster launches: a CTA that gives up there
-  // still meets its peers at the unit's cluster barrier, which has no bound
-  const int fault_u = clustered ? -1 : withheld_unit(a.ctl, a.iter);
+  const int fault_u = withheld_unit(a.ctl, a.iter);
   // one stage = the slice's Z and Y tiles, group records, weights and supports
   // (+ the deferred row scale of its wide plan, slot >= 0)
   auto issue = [&](int unit, int g0, int ng, int slot, int stg) {
@@ -617,17 +615,16 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
     for (int j = 0; j < PPT; ++j) {
       const int c = (tid + NT * j) / CPR;
       crow_p[j] = c < ng * S ? __ldg(a.col_crow + (size_t)g0 * S + c) : -1;
-      if (crow_p[j] >= a.ctab_rows) {  // a table row outside the table: reported, not read
-        ctl_fail(a.ctl, 9);
-        crow_p[j] = -1;
-      }
     }
   };
   auto issue_rows = [&](int stg) {
 #pragma unroll
     for (int j = 0; j < PPT; ++j) {
       const int i = tid + NT * j, c = i / CPR, part = i - c * CPR;
-      if (crow_p[j] >= 0)
+      // (the row index is checked here, where the loaded value is consumed
+      // anyway: a row outside the table is reported, not read)
+      if (crow_p[j] >= a.ctab_rows) ctl_fail(a.ctl, 9);
+      else if (crow_p[j] >= 0)
         asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
                          smem_u32(stK + stg * TILE + c * MP + part * 4)),
                      "l"(a.ctab + (size_t)crow_p[j] * MP + part * 4)
@@ -665,24 +662,25 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
   const bool write_x = a.flags & PF_WRITE_X;
   double s_obj = 0.0, s_pr = 0.0, s_dr = 0.0;  // FP64 across items, FP32 within one item
   int it = 0;
-  bool failed = false;
+  // A CTA whose wait ran out leaves the loop at once, except in a cluster
+  // launch: there it stays "dry" for its remaining units (no waits, no copies,
+  // no stores, every group idle) so that it still meets its peers at each
+  // unit's cluster barrier, and leaves with them.
+  bool dry = false;
+  int fail_it = 0;
   for (int u = u0; u < nunits; u += ustep, ++it) {
     const int stg = it & 1;
-    if (!mbar_wait(&mbar[stg], (it >> 1) & 1, wlim)) sh_fail = 1;
+    if (!dry && !mbar_wait(&mbar[stg], (it >> 1) & 1, wlim)) sh_fail = 1;
     if (SC) asm volatile("cp.async.wait_all;" ::: "memory");  // this unit's table rows
     __syncthreads();
-    failed = sh_fail != 0;
-    if (clustered) {
-      // the ranks of a cluster leave together: one that gave up alone would
-      // leave its peers at the unit's cluster barrier for good
-      cg::cluster_group cl = cg::this_cluster();
-      cl.sync();
-      for (int rk = 0; rk < CS; ++rk) failed |= *cl.map_shared_rank(&sh_fail, rk) != 0;
+    if (sh_fail && !dry) {
+      fail_it = it;
+      if (!clustered) break;
+      dry = true;
     }
-    if (failed) break;
-    const int cur_g0 = sh_g0[stg], cur_ng = sh_ng[stg];
+    const int cur_g0 = sh_g0[stg], cur_ng = dry ? 0 : sh_ng[stg];
     const int rank = crank;
-    if (tid == 0 && u + ustep < nunits) {
+    if (tid == 0 && u + ustep < nunits && !dry) {
       issue(u + ustep, nx_g0, nx_ng, nx_slot, stg ^ 1);
       sh_g0[stg ^ 1] = nx_g0;
       sh_ng[stg ^ 1] = nx_ng;
@@ -808,7 +806,7 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
     }
     __syncthreads();
     // the next unit's bounds are visible now: fetch its table-row indices
-    if (SC && has_next) load_rows_idx(sh_g0[stg ^ 1], sh_ng[stg ^ 1]);
+    if (SC && has_next && !dry) load_rows_idx(sh_g0[stg ^ 1], sh_ng[stg ^ 1]);
 
     float tot[RPT];
     bool writer = false;
@@ -1005,24 +1003,24 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
       s_pr += i_pr;
       s_dr += i_dr;
     }
-    if (SC && has_next) issue_rows(stg ^ 1);  // lands during the next unit's wait
+    if (SC && has_next && !dry) issue_rows(stg ^ 1);  // lands during the next unit's wait
     // No barrier here: every reader of this unit's stage, row partials and
     // staged rows passes the next unit's opening barrier before thread 0
     // reissues the stage (two units later) or anyone writes partials again.
   }
   // rank 0 may still be reading a peer's shared memory (the moments of the
   // last item): no CTA of a cluster leaves before all of them are done
-  if (clustered && !failed) cg::this_cluster().sync();
+  if (clustered) cg::this_cluster().sync();
   if (SC) asm volatile("cp.async.wait_all;" ::: "memory");  // no table-row copy outlives the CTA
-  if (failed) {
+  if (sh_fail) {
     if (tid == 0) {
       ctl_fail(a.ctl, 7);
       // A bulk copy did not complete.  The only copy that can be in flight is
-      // the one of the unit that failed (it), on stage it & 1 at phase parity
-      // (it >> 1) & 1; the next stage is issued only after a successful wait.
-      // Wait for it once more, again bounded, so that no copy lands in the
-      // shared memory of a CTA that has left.
-      mbar_wait(&mbar[it & 1], (it >> 1) & 1, wlim);
+      // the one of the unit that failed (fail_it), on stage fail_it & 1 at
+      // phase parity (fail_it >> 1) & 1: the next stage is issued only after
+      // a successful wait.  Wait for it once more, again bounded, so that no
+      // copy lands in the shared memory of a CTA that has left.
+      mbar_wait(&mbar[fail_it & 1], (fail_it >> 1) & 1, wlim);
     }
     return;
   }

@@ -109,17 +109,16 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
     for (int j = 0; j < PPT; ++j) {
       const int c = (tid + NT * j) / CPR;
       crow_p[j] = c < ng * S ? __ldg(a.col_crow + (size_t)g0 * S + c) : -1;
-      if (crow_p[j] >= a.ctab_rows) {  // a table row outside the table: reported, not read
-        ctl_fail(a.ctl, 9);
-        crow_p[j] = -1;
-      }
     }
   };
   auto issue_rows = [&](int stg) {
 #pragma unroll
     for (int j = 0; j < PPT; ++j) {
       const int i = tid + NT * j, c = i / CPR, part = i - c * CPR;
-      if (crow_p[j] >= 0)
+      // (the row index is checked here, where the loaded value is consumed
+      // anyway: a row outside the table is reported, not read)
+      if (crow_p[j] >= a.ctab_rows) ctl_fail(a.ctl, 9);
+      else if (crow_p[j] >= 0)
         asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
                          smem_u32(stK + stg * TILE + c * MP + part * 4)),
                      "l"(a.ctab + (size_t)crow_p[j] * MP + part * 4)
