@@ -598,16 +598,20 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
     if (sb) bulk_load(stS + stg * MP, a.rowsc + (size_t)slot * MP, sb, &mbar[stg]);
   };
   // bounds of unit u; slot of its leading wide slice when that arrives deferred, else -1
-  auto slice = [&](int u, int &g0, int &ng, int &slot) {
-    g0 = a.item_g0[u] + crank * G;
-    ng = min(G, a.item_ng[u] - crank * G);
+  // Thread 0 fetches unit bounds ahead of use, in three steps one unit apart:
+  // the item's raw bounds, then this rank's slice and its leading group
+  // record, then the slot and the copy.  Any arithmetic on a loaded value
+  // right after the load would stall warp 0, and with it every warp at the
+  // unit's next barrier.
+  auto resolve = [&](int ig0, int ing, int &g0, int &ng) {
+    g0 = ig0 + crank * G;
+    ng = min(G, ing - crank * G);
     if (ng < 0) ng = 0;
-    slot = -1;
-    if (indef && ng > 0) {
-      const int4 r = a.grp_rec[g0];
-      if ((r.w >> 12) > G) slot = r.x;
-    }
   };
+  auto lead_rec = [&](int g0, int ng) {
+    return (indef && ng > 0) ? a.grp_rec[g0] : make_int4(0, 0, 0, 0);
+  };
+  auto slot_of = [&](int4 r, int ng) { return (indef && ng > 0 && (r.w >> 12) > G) ? r.x : -1; };
   // staged table costs: the table row of each piece of the next unit (-1: none)
   int crow_p[PPT];
   auto load_rows_idx = [&](int g0, int ng) {
@@ -632,20 +636,28 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
   };
-  // thread 0 keeps the bounds of the next unit in registers, loaded one unit early
-  int nx_g0 = 0, nx_ng = 0, nx_slot = -1;
+  // thread 0: the next unit's slice and lead record (n1_*), the unit after's raw bounds (n2_*)
+  int n1_g0 = 0, n1_ng = 0, n2_ig0 = 0, n2_ing = 0;
+  int4 n1_rec = make_int4(0, 0, 0, 0);
   if (tid == 0) {
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
     sh_fail = 0;
     mbar_fence_init();
     if (u0 < nunits) {
-      int g0, ng, sl;
-      slice(u0, g0, ng, sl);
+      int g0, ng;
+      resolve(a.item_g0[u0], a.item_ng[u0], g0, ng);
       sh_g0[0] = g0;
       sh_ng[0] = ng;
-      issue(u0, g0, ng, sl, 0);
-      if (u0 + ustep < nunits) slice(u0 + ustep, nx_g0, nx_ng, nx_slot);
+      issue(u0, g0, ng, slot_of(lead_rec(g0, ng), ng), 0);
+      if (u0 + ustep < nunits) {
+        resolve(a.item_g0[u0 + ustep], a.item_ng[u0 + ustep], n1_g0, n1_ng);
+        n1_rec = lead_rec(n1_g0, n1_ng);
+      }
+      if (u0 + 2 * ustep < nunits) {
+        n2_ig0 = a.item_g0[u0 + 2 * ustep];
+        n2_ing = a.item_ng[u0 + 2 * ustep];
+      }
     }
   }
   if (SC && u0 < nunits) {  // the first unit's rows
@@ -681,10 +693,17 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
     const int cur_g0 = sh_g0[stg], cur_ng = dry ? 0 : sh_ng[stg];
     const int rank = crank;
     if (tid == 0 && u + ustep < nunits && !dry) {
-      issue(u + ustep, nx_g0, nx_ng, nx_slot, stg ^ 1);
-      sh_g0[stg ^ 1] = nx_g0;
-      sh_ng[stg ^ 1] = nx_ng;
-      if (u + 2 * ustep < nunits) slice(u + 2 * ustep, nx_g0, nx_ng, nx_slot);
+      issue(u + ustep, n1_g0, n1_ng, slot_of(n1_rec, n1_ng), stg ^ 1);
+      sh_g0[stg ^ 1] = n1_g0;
+      sh_ng[stg ^ 1] = n1_ng;
+      if (u + 2 * ustep < nunits) {
+        resolve(n2_ig0, n2_ing, n1_g0, n1_ng);
+        n1_rec = lead_rec(n1_g0, n1_ng);
+        if (u + 3 * ustep < nunits) {
+          n2_ig0 = a.item_g0[u + 3 * ustep];
+          n2_ing = a.item_ng[u + 3 * ustep];
+        }
+      }
     }
     const bool has_next = u + ustep < nunits;
 

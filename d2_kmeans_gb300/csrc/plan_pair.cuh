@@ -76,9 +76,12 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
   const int fault_u = withheld_unit(a.ctl, a.iter);
   const bool indef = a.flags & PF_IN_DEF;
   const bool stage_sc = indef && (a.flags & PF_STAGE_SC);
-  // the plans {first, count} of unit u, checked against the phase (thread 0)
-  auto unit_plans = [&](int u) {
-    int2 pp = indef ? a.item_pp[u] : make_int2(0, 0);
+  // The plans {first, count} of unit u (thread 0).  Thread 0 loads the
+  // bounds of a unit one unit before it issues that unit's copy, and checks
+  // them only then: any use of a loaded value right after the load would stall
+  // warp 0, and with it every warp at the unit's next barrier.
+  auto unit_plans = [&](int u) { return indef ? a.item_pp[u] : make_int2(0, 0); };
+  auto checked = [&](int2 pp) {
     if (pp.x < 0 || pp.y < 0 || pp.y > G || pp.x > a.nplans_chk - pp.y) {
       ctl_fail(a.ctl, 9);
       pp = make_int2(0, 0);
@@ -135,7 +138,7 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
     mbar_fence_init();
     if (u0 < nunits) {
       const int g0 = a.item_g0[u0], ng = a.item_ng[u0];
-      const int2 pp = unit_plans(u0);
+      const int2 pp = checked(unit_plans(u0));
       sh_g0[0] = g0;
       sh_ng[0] = ng;
       sh_pp[0] = pp;
@@ -170,6 +173,7 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
     const int cur_g0 = sh_g0[stg], cur_ng = sh_ng[stg];
     const int2 cur_pp = sh_pp[stg];
     if (tid == 0 && u + ustep < nunits) {
+      nx_pp = checked(nx_pp);
       issue(u + ustep, nx_g0, nx_ng, nx_pp, stg ^ 1);
       sh_g0[stg ^ 1] = nx_g0;
       sh_ng[stg ^ 1] = nx_ng;
