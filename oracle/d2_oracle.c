@@ -122,9 +122,16 @@ static int cnorm(size_t m, size_t n, double *a, double *sa) {
   return 0;
 }
 
-int d2o_badmm(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_supp,
-              double *Z, double *Xout, double *Yout, double *Cout, double *trace, int *ntrace,
-              double *rho_out, int *iters_out) {
+/* The update, with the reference's MPI exchanges (`#ifdef __USE_MPI__` in
+ * src/d2/centroid_Bregman.c) made through `xr` when it is given: an in-place
+ * SUM of n doubles over all ranks (label counts :142, cluster weights :188,
+ * support numerators and X row sums :215-217 / :250-252, n-gram symbol counts
+ * :282, obj / primres / dualres :308-310).  Like the reference, each rank
+ * takes rho from its own instances (:109); global_rho != 0 sums |C| and the
+ * entry count over the ranks first instead (not in the reference). */
+static int badmm_impl(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_supp,
+                      double *Z, double *Xout, double *Yout, double *Cout, double *trace, int *ntrace,
+                      double *rho_out, int *iters_out, d2o_allreduce_fn xr, void *xctx, int global_rho) {
   const int str = ph->str, dim = ph->dim, K = ph->num_of_labels;
   const size_t size = ph->size, col = ph->col, nent = (size_t)str * col;
   const int euclid = ph->metric == D2O_EUCLIDEAN_L2, embed = ph->metric == D2O_WORD_EMBED;
@@ -160,6 +167,11 @@ int d2o_badmm(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_s
   double asum = 0;
   for (size_t e = 0; e < nent; ++e) asum += fabs(C[e]);
   double rho = opt->rhoCoeff * asum / (double)nent;
+  if (xr && global_rho) {
+    double g[2] = {asum, (double)nent};
+    if (xr(g, 2, xctx)) { rc = -2; goto done; }
+    rho = opt->rhoCoeff * g[0] / g[1];
+  }
   for (size_t e = 0; e < nent; ++e) C[e] /= rho;
 
   /* warm start: re-initialise only switched instances, :116-124 */
@@ -172,6 +184,11 @@ int d2o_badmm(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_s
   for (size_t e = 0; e < nent; ++e) Y[e] = 0; /* :128 */
 
   for (size_t i = 0; i < size; ++i) ++count[ph->label[i]]; /* :138-144 */
+  if (xr) { /* :142 */
+    for (int l = 0; l < K; ++l) Xc[l] = (double)count[l];
+    if (xr(Xc, (size_t)K, xctx)) { rc = -2; goto done; }
+    for (int l = 0; l < K; ++l) count[l] = (size_t)Xc[l];
+  }
   for (int l = 0; l < K; ++l)
     if (count[l] == 0) { rc = -5; goto done; }
 
@@ -213,6 +230,7 @@ int d2o_badmm(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_s
       double *cwl = c_w + (size_t)ph->label[i] * str;
       for (int k = 0; k < str; ++k) cwl[k] += Zr[str * i + k];
     }
+    if (xr && xr(c_w, (size_t)str * K, xctx)) { rc = -2; goto done; } /* :188 */
     if ((rc = cnorm(str, K, c_w, Xc))) goto done;
 
     /* step 5, :194-267 */
@@ -245,6 +263,10 @@ int d2o_badmm(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_s
           }
         }
       }
+      if (xr && (xr(c_supp, sxd * K, xctx) || xr(Zr, (size_t)str * K, xctx))) { /* :215-217 */
+        rc = -2;
+        goto done;
+      }
       for (int l = 0; l < K; ++l) { /* irms, :219-221 */
         double *cs = c_supp + l * sxd, *zr = Zr + (size_t)l * str;
         for (int k = 0; k < str; ++k)
@@ -274,6 +296,7 @@ int d2o_badmm(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_s
               for (int t = 0; t < dim; ++t) z[(size_t)V * (dim * k + t) + si[j * dim + t]] += val;
           }
       }
+      if (xr && xr(zsym, sxdv * K, xctx)) { rc = -2; goto done; } /* :282 */
       /* each centroid symbol moves to the symbol of least expected cost
        * (minimize_symbolic, centroid_util.h:25-37): zbuf = dist_mat * z as the
        * column-major dgemm computes it (a running sum over u), first minimum */
@@ -305,6 +328,13 @@ int d2o_badmm(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_s
       for (size_t e = 0; e < nent; ++e) Z0[e] += -1 * Z[e];
       for (size_t e = 0; e < nent; ++e) pr += fabs(X[e]);
       for (size_t e = 0; e < nent; ++e) dr += fabs(Z0[e]);
+      if (xr) { /* :308-310 */
+        double g[3] = {obj, pr, dr};
+        if (xr(g, 3, xctx)) { rc = -2; goto done; }
+        obj = g[0];
+        pr = g[1];
+        dr = g[2];
+      }
       obj *= rho / ph->global_size;
       pr /= ph->global_size;
       dr /= ph->global_size;
@@ -328,6 +358,20 @@ done:
   free(cum); free(C); free(X); free(Y); free(Z0); free(Xc); free(Zr); free(count);
   free(zsym); free(zbuf);
   return rc;
+}
+
+int d2o_badmm(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_supp,
+              double *Z, double *Xout, double *Yout, double *Cout, double *trace, int *ntrace,
+              double *rho_out, int *iters_out) {
+  return badmm_impl(ph, opt, c_w, c_supp, Z, Xout, Yout, Cout, trace, ntrace, rho_out, iters_out,
+                    NULL, NULL, 0);
+}
+
+int d2o_badmm_mpi(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_supp,
+                  double *Z, double *trace, int *ntrace, double *rho_out, int *iters_out,
+                  d2o_allreduce_fn xr, void *xctx, int global_rho) {
+  return badmm_impl(ph, opt, c_w, c_supp, Z, NULL, NULL, NULL, trace, ntrace, rho_out, iters_out,
+                    xr, xctx, global_rho);
 }
 
 int d2o_serve_query(int dim, int str, int k, const double *c_w, const double *c_supp,

@@ -75,6 +75,17 @@ int d2o_badmm(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_s
               double *Z, double *X, double *Y, double *C, double *trace, int *ntrace,
               double *rho_out, int *iters_out);
 
+/* The reference's MPI build of the same update (src/d2/centroid_Bregman.c
+ * with __USE_MPI__): this process holds one shard of the instances
+ * (global_size = all ranks' instances) and every MPI_Allreduce of the
+ * reference becomes a call of xr, which must SUM the n doubles of buf in
+ * place over all ranks and return 0.  Each rank's rho comes from its own
+ * instances, as in the reference; global_rho != 0 takes it over all ranks. */
+typedef int (*d2o_allreduce_fn)(double *buf, size_t n, void *ctx);
+int d2o_badmm_mpi(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_supp,
+                  double *Z, double *trace, int *ntrace, double *rho_out, int *iters_out,
+                  d2o_allreduce_fn xr, void *xctx, int global_rho);
+
 int d2r_badmm(const d2o_phase *ph, const d2o_opts *opt, double *c_w, double *c_supp,
               double *Z, double *X, double *Y, double *C, double *trace, int *ntrace,
               double *rho_out, int *iters_out);

@@ -164,6 +164,101 @@ def badmm(phase: dict, centroids: dict, opts: dict, kind: str = "port",
     return res
 
 
+ALLREDUCE_FN = C.CFUNCTYPE(C.c_int, C.POINTER(C.c_double), C.c_size_t, C.c_void_p)
+
+
+def badmm_mpi(phase: dict, centroids: dict, opts: dict, allreduce, global_rho: bool = False) -> dict:
+    """The reference's MPI build of the update on this process's shard
+    (d2o_badmm_mpi): ``allreduce(buf)`` must sum the float64 numpy array
+    ``buf`` in place over all ranks.  ``phase["global_size"]`` is the number
+    of instances of all ranks together."""
+    lib = _lib("port")
+    fn = lib.d2o_badmm_mpi
+    fn.restype = C.c_int
+    fn.argtypes = [C.POINTER(_Phase), C.POINTER(_Opts)] + [C.c_void_p] * 7 + [ALLREDUCE_FN, C.c_void_p,
+                                                                              C.c_int]
+    keep = []
+
+    def arr(a, dtype):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=dtype)
+        keep.append(a)
+        return a
+    p_str = arr(phase["p_str"], np.int32)
+    m, k = int(phase["str"]), int(phase["num_of_labels"])
+    dim = int(phase.get("dim", 0))
+    col = int(p_str.sum())
+    ph = _Phase()
+    ph.metric = METRIC[phase["metric"]] if isinstance(phase["metric"], str) else int(phase["metric"])
+    ph.dim, ph.str, ph.size, ph.col = dim, m, p_str.size, col
+    ph.p_str = p_str.ctypes.data
+    ph.p_w = _ptr(arr(phase["p_w"], np.float64))
+    ph.p_supp = _ptr(arr(phase.get("p_supp"), np.float64))
+    ph.p_supp_sym = _ptr(arr(phase.get("p_supp_sym"), np.int32))
+    ph.vocab_vec = _ptr(arr(phase.get("vocab_vec"), np.float64))
+    ph.vocab_size = int(phase.get("vocab_size", 0))
+    ph.dist_mat = _ptr(arr(phase.get("dist_mat"), np.float64))
+    ph.label = _ptr(arr(phase["label"], np.int32))
+    ph.num_of_labels = k
+    ls = arr(phase.get("label_switch", np.ones(p_str.size, np.int8)), np.int8)
+    ph.label_switch = ls.ctypes.data
+    ph.global_size = int(phase.get("global_size", p_str.size))
+    c_sym = None
+    if centroids.get("c_sym") is not None:
+        c_sym = np.array(centroids["c_sym"], dtype=np.int32, copy=True).reshape(-1)
+        ph.c_sym = c_sym.ctypes.data
+    op = _Opts()
+    op.maxIters = int(opts.get("maxIters", 100))
+    op.rhoCoeff = float(opts.get("rhoCoeff", 2.0))
+    op.updatePerLoops = int(opts.get("updatePerLoops", 10))
+    op.time_budget = 1e300
+    c_w = np.array(centroids["c_w"], dtype=np.float64, copy=True).reshape(-1)
+    cs = centroids.get("c_supp")
+    c_supp = np.zeros(max(k * m * dim, 1)) if cs is None else np.array(cs, np.float64, copy=True).reshape(-1)
+    Z = np.zeros(m * col)
+    trace = np.zeros(4 * (op.maxIters // 20 + 8))
+    ntrace, rho, iters = C.c_int(0), C.c_double(0), C.c_int(0)
+    errors = []
+
+    def cb(buf, n, _ctx):
+        try:
+            allreduce(np.ctypeslib.as_array(buf, shape=(n,)))
+            return 0
+        except Exception as e:  # reported after the call
+            errors.append(e)
+            return 1
+    cfn = ALLREDUCE_FN(cb)
+    rc = fn(C.byref(ph), C.byref(op), c_w.ctypes.data, c_supp.ctypes.data, Z.ctypes.data,
+            trace.ctypes.data, C.addressof(ntrace), C.addressof(rho), C.addressof(iters), cfn, None,
+            1 if global_rho else 0)
+    if errors:
+        raise errors[0]
+    return {"rc": rc, "c_w": c_w, "c_supp": c_supp, "c_sym": c_sym, "Z": Z,
+            "trace": trace[: 4 * ntrace.value].reshape(-1, 4), "rho": rho.value, "iters": iters.value}
+
+
+def shard_phase(phase: dict, lo: int, hi: int) -> dict:
+    """Instances [lo, hi) of a phase as one rank's shard, global_size kept at
+    the whole phase's instance count.  (The reference's d2_write_split writes
+    contiguous batches of 1 + (n-1)/splits instances of a shuffled order,
+    src/d2/clustering_io.c:329-362, and rank r reads file.r, :20-28.)"""
+    p_str = np.asarray(phase["p_str"])
+    cum = np.concatenate([[0], np.cumsum(p_str, dtype=np.int64)])
+    a, b = int(cum[lo]), int(cum[hi])
+    d = int(phase.get("dim", 0))
+    out = dict(phase, p_str=p_str[lo:hi], p_w=np.asarray(phase["p_w"])[a:b],
+               label=np.asarray(phase["label"])[lo:hi],
+               label_switch=np.asarray(phase.get("label_switch", np.ones(p_str.size, np.int8)))[lo:hi],
+               global_size=int(phase.get("global_size", p_str.size)))
+    if phase.get("p_supp") is not None:
+        out["p_supp"] = np.asarray(phase["p_supp"])[a * d:b * d]
+    if phase.get("p_supp_sym") is not None:
+        w = d if int(phase["metric"] if not isinstance(phase["metric"], str) else METRIC[phase["metric"]]) == 6 else 1
+        out["p_supp_sym"] = np.asarray(phase["p_supp_sym"])[a * w:b * w]
+    return out
+
+
 def cost_blocks(phase: dict, centroids: dict) -> np.ndarray:
     """Every instance's ground-cost block against its cluster's centroid
     (d2o_cost_blocks): C [str*col], the blocks of calculate_distmat."""
