@@ -19,6 +19,7 @@ D2_EUCLIDEAN_L2, D2_CITYBLOCK_L1, D2_HISTOGRAM, D2_N_GRAM, D2_WORD_EMBED, D2_SPA
 
 D2G_OK, D2G_E_INVAL, D2G_E_CUDA, D2G_E_NOMEM, D2G_E_UNSUPPORTED = 0, -1, -2, -3, -4
 D2G_E_EMPTY_CLUSTER, D2G_E_NUMERIC, D2G_E_ADMISSION, D2G_E_NOTFOUND = -5, -6, -7, -8
+D2G_SHARD_GLOBAL_RHO = 1
 
 dp = C.POINTER(C.c_double)
 ip = C.POINTER(C.c_int)
@@ -134,6 +135,9 @@ SIGNATURES = {
     "d2g_phase_get_scratch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "d2g_phase_stream": (C.c_void_p, [C.c_void_p]),
     "d2g_phase_test_wait": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double]),
+    "d2g_phase_set_allreduce": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "d2g_badmm_run_shards": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(d2g_badmm_opts), C.c_int,
+                                       C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
     "d2g_read": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(mph)]),
     "d2g_mph_alloc": (C.c_int, [C.c_int, C.c_size_t, ip, ip, ip, C.POINTER(C.POINTER(mph))]),
     "d2g_mph_free": (C.c_int, [C.POINTER(mph)]),

@@ -210,6 +210,31 @@ class Phase:
         return {"c_w": c_w, "c_supp": c_supp, "trace": self.trace(), "stats": self.stats()}
 
 
+def run_shards(phases, centroids: dict, opts: dict, global_rho: bool = False):
+    """The sharded centroid update of several phases on this device
+    (d2g_badmm_run_shards): each phase holds one shard of the instances, with
+    ``global_size`` the instance count of all shards.  Returns each shard's
+    centroids, trace and statistics (the centroids are the same on every
+    shard)."""
+    lib = L.load()
+    n = len(phases)
+    o = L.d2g_badmm_opts()
+    o.maxIters = int(opts.get("maxIters", 100))
+    o.rhoCoeff = float(opts.get("rhoCoeff", 2.0))
+    o.updatePerLoops = int(opts.get("updatePerLoops", 10))
+    o.time_budget = float(opts.get("time_budget", 0.0))
+    cws = [np.array(centroids["c_w"], np.float64).reshape(-1) for _ in range(n)]
+    cs = centroids.get("c_supp")
+    css = None if cs is None else [np.array(cs, np.float64).reshape(-1) for _ in range(n)]
+    hs = (C.c_void_p * n)(*[p.h.value for p in phases])
+    pw = (C.c_void_p * n)(*[a.ctypes.data for a in cws])
+    ps = None if css is None else (C.c_void_p * n)(*[a.ctypes.data for a in css])
+    L.check(lib.d2g_badmm_run_shards(hs, n, C.byref(o), L.D2G_SHARD_GLOBAL_RHO if global_rho else 0, pw, ps),
+            "d2g_badmm_run_shards")
+    return [{"c_w": cws[i], "c_supp": None if css is None else css[i], "trace": phases[i].trace(),
+             "stats": phases[i].stats()} for i in range(n)]
+
+
 class DropIn:
     """The reference's own calling convention for d2_centroid_sphBregman.
 

@@ -14,8 +14,10 @@
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
+#include <condition_variable>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "d2g_internal.cuh"
@@ -92,6 +94,15 @@ struct d2g_phase {
   // ---- test hook of the bounded device waits (d2g_phase_test_wait)
   unsigned long long wait_ns = 0;
   int fault_iter = -1, fault_unit = -1;
+
+  // ---- sharded update: the exchange of the cluster sums between shards
+  // (d2g_phase_set_allreduce, d2g_badmm_run_shards)
+  d2g_allreduce_fn xfn = nullptr;
+  void *xctx = nullptr;
+  int xflags = 0;
+  bool shard_pairs = false;  // every shard of the run can take pair passes
+  DBuf<double> xbuf;
+  std::vector<int> local_count;  // this shard's instances per cluster
 
   // ---- common device state
   DBuf<Ctl> ctl;
@@ -543,11 +554,16 @@ static int set_labels_impl(d2g_phase *ph, const int *label) {
   std::vector<int> cnt(ph->K + 1, 0);
   for (size_t i = 0; i < n; ++i) ++cnt[label[i] + 1];
   int maxc = 0;
+  ph->local_count.assign(cnt.begin() + 1, cnt.end());
+  // a shard of a larger set (global_size > size) may hold no instance of a
+  // cluster: the check then runs over all shards when the update starts
+  const bool shard = ph->global_size > ph->size;
   for (int l = 0; l < ph->K; ++l) {
-    if (cnt[l + 1] == 0)
+    if (cnt[l + 1] == 0 && !shard)
       return fail(D2G_E_EMPTY_CLUSTER, "cluster " + std::to_string(l) + " has no instance");
     maxc = std::max(maxc, cnt[l + 1]);
   }
+  maxc = std::max(maxc, 1);
   for (int l = 0; l < ph->K; ++l) cnt[l + 1] += cnt[l];
   std::vector<int> pos(cnt.begin(), cnt.end() - 1), lists(n);
   const bool batched = ph->path == 0;
@@ -1041,6 +1057,44 @@ static NgramArgs ngram_args(d2g_phase *ph, int iter) {
 }
 
 // ------------------------------------------------------------- the loop
+// Sharded update: SUM of n doubles of the phase's exchange buffer over all
+// shards, in place, enqueued on the phase's stream by the exchange function.
+static int xchg(d2g_phase *ph, double *buf, size_t n) {
+  const int rc = ph->xfn(buf, n, (void *)ph->st, ph->xctx);
+  if (rc) return fail(D2G_E_CUDA, "sharded update: the exchange between shards failed (" +
+                                      std::to_string(rc) + ")");
+  return D2G_OK;
+}
+
+// Step 4 (and 5) over the clusters; a shard adds its chunks first and the
+// exchange sums those over all shards before the final.
+static int cluster_reduce(d2g_phase *ph, ClusterArgs c) {
+  if (!ph->xfn) {
+    D2G_CUDA(launch_cluster_reduce(c, ph->st));
+    return D2G_OK;
+  }
+  D2G_CUDA(launch_cluster_partial(c, ph->st));
+  D2G_CUDA(launch_cluster_local(c, ph->xbuf.p, ph->st));
+  int rc = xchg(ph, ph->xbuf.p, cluster_xsum_count(c));
+  if (rc) return rc;
+  c.xsum = ph->xbuf.p;
+  D2G_CUDA(launch_cluster_final(c, ph->st));
+  return D2G_OK;
+}
+
+// Step 6: obj, primres, dualres; a shard's three sums are exchanged first.
+static int resid_final(d2g_phase *ph, const double *part, int n, double *slot, int iter, bool from3) {
+  if (!ph->xfn) {
+    D2G_CUDA(launch_resid_final(part, n, ph->ctl.p, slot, iter, from3, ph->st));
+    return D2G_OK;
+  }
+  D2G_CUDA(launch_resid_final(part, n, ph->ctl.p, slot, iter, from3, ph->st, 1, ph->xbuf.p));
+  int rc = xchg(ph, ph->xbuf.p, 3);
+  if (rc) return rc;
+  D2G_CUDA(launch_resid_final(part, n, ph->ctl.p, slot, iter, from3, ph->st, 2, ph->xbuf.p));
+  return D2G_OK;
+}
+
 static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long long *launches,
                         double *plan_ms, int *plan_timed) {
   const bool euc = ph->metric == D2_EUCLIDEAN_L2, emb = ph->metric == D2_WORD_EMBED;
@@ -1107,12 +1161,18 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
         if (profile) cudaEventRecord(evs.back(), ph->st);
         // step 4 of `it` (c_w), the second iteration's row scale from that c_w,
         // then step 4 (and step 5) of it + 1
-        D2G_CUDA(launch_cluster_reduce(cluster_args(ph, it, false), ph->st));
+        {
+          int rc = cluster_reduce(ph, cluster_args(ph, it, false));
+          if (rc) return rc;
+        }
         D2G_CUDA(launch_pair_scale(ph->rawsum.p, ph->plan_slot.p, ph->plan_label.p, ph->cw32.p, ph->nplans,
                                    ph->MP, ph->str, ph->rowsc.p, ph->ctl.p, t1, ph->K, ph->st));
         ClusterArgs c1 = cluster_args(ph, t1, upd1 && euc);
         c1.rowsum32 = ph->rowsum2.p;
-        D2G_CUDA(launch_cluster_reduce(c1, ph->st));
+        {
+          int rc = cluster_reduce(ph, c1);
+          if (rc) return rc;
+        }
         nl += 6;
         if (upd1 && emb) {
           D2G_CUDA(launch_embed_support(embed_args(ph, t1), ph->st));
@@ -1130,8 +1190,8 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
           nl += 3;
         }
         if (chk0) {
-          D2G_CUDA(launch_resid_final(ph->resid_part.p, ph->total_blocks, ph->ctl.p,
-                                      ph->trace.p + 4 * chk_idx, it, false, ph->st));
+          int rc = resid_final(ph, ph->resid_part.p, ph->total_blocks, ph->trace.p + 4 * chk_idx, it, false);
+          if (rc) return rc;
           ++nl;
           ++chk_idx;
         }
@@ -1182,7 +1242,10 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
         ++nl;
       }
       if (profile) cudaEventRecord(evs.back(), ph->st);
-      D2G_CUDA(launch_cluster_reduce(cluster_args(ph, it, upd && euc), ph->st));
+      {
+        int rc = cluster_reduce(ph, cluster_args(ph, it, upd && euc));
+        if (rc) return rc;
+      }
       nl += 2;
       if (upd && emb) {  // step 5 for word embeddings, then the new cost table
         D2G_CUDA(launch_embed_support(embed_args(ph, it), ph->st));
@@ -1214,8 +1277,8 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
         }
       }
       if (chk) {
-        D2G_CUDA(launch_resid_final(ph->resid_part.p, ph->total_blocks, ph->ctl.p,
-                                    ph->trace.p + 4 * chk_idx, it, collide, ph->st));
+        int rc = resid_final(ph, ph->resid_part.p, ph->total_blocks, ph->trace.p + 4 * chk_idx, it, collide);
+        if (rc) return rc;
         ++nl;
         ++chk_idx;
       }
@@ -1288,6 +1351,12 @@ static int enqueue_loop(d2g_phase *ph, int maxIters, int upl, bool profile, long
   return D2G_OK;
 }
 
+// two iterations per pass are possible: plans that each fit one CTA
+static bool pair_capable(const d2g_phase *ph, const d2g_config &cfg) {
+  return cfg.pair_iterations && ph->path == 0 && ph->nwide == 0 && ph->buckets.size() == 1 &&
+         ph->buckets[0].cs == 1 && ph->MP <= 128 && ph->rawsum.n > 0;
+}
+
 static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, double *c_supp,
                     int *c_sym, const char *label_switch) {
   const d2g_config cfg = cfg_snapshot();
@@ -1299,6 +1368,17 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
   if ((euc || emb) && !c_supp) return fail(D2G_E_INVAL, "c_supp required for this metric");
   const int K = ph->K, m = ph->str, dim = ph->dim;
   const size_t n = ph->size;
+  if (ph->xfn) {  // sharded update: what it covers
+    if (ph->path != 0) return fail(D2G_E_UNSUPPORTED, "sharded update: the batched form only");
+    if (!euc && ph->metric != D2_HISTOGRAM && ph->metric != D2_SPARSE_HISTOGRAM)
+      return fail(D2G_E_UNSUPPORTED, "sharded update: Euclidean and histogram phases only");
+    if (opt->time_budget > 0 && opt->time_budget < 1.8e10)
+      return fail(D2G_E_INVAL, "sharded update: no time budget (every shard must run every iteration)");
+  } else {
+    for (int l = 0; l < K; ++l)  // a shard run alone must hold every cluster
+      if (l < (int)ph->local_count.size() && ph->local_count[l] == 0)
+        return fail(D2G_E_EMPTY_CLUSTER, "cluster " + std::to_string(l) + " has no instance");
+  }
   if (ng) {
     if (!c_sym) return fail(D2G_E_INVAL, "centroid symbols required for an n-gram phase");
     for (size_t q = 0; q < (size_t)K * m * dim; ++q)
@@ -1341,6 +1421,21 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
   h.fault_unit = ph->fault_unit;
   D2G_CUDA(cudaMemcpyAsync(ph->ctl.p, &h, sizeof h, cudaMemcpyHostToDevice, ph->st));
 
+  if (ph->xfn) {
+    // exchange buffer: the largest exchange is the cluster sums with moments
+    D2G_CUDA(ph->xbuf.alloc(std::max<size_t>((size_t)K * (dim + 2) * m, (size_t)K) + 8));
+    // every cluster must hold an instance on some shard (:142-144)
+    std::vector<double> cnt(K);
+    for (int l = 0; l < K; ++l) cnt[l] = (double)ph->local_count[l];
+    D2G_CUDA(cudaMemcpyAsync(ph->xbuf.p, cnt.data(), K * 8, cudaMemcpyHostToDevice, ph->st));
+    int rc = xchg(ph, ph->xbuf.p, (size_t)K);
+    if (rc) return rc;
+    D2G_CUDA(cudaMemcpyAsync(cnt.data(), ph->xbuf.p, K * 8, cudaMemcpyDeviceToHost, ph->st));
+    D2G_CUDA(cudaStreamSynchronize(ph->st));
+    for (int l = 0; l < K; ++l)
+      if (!(cnt[l] > 0)) return fail(D2G_E_EMPTY_CLUSTER, "cluster " + std::to_string(l) + " has no instance on any shard");
+  }
+
   long long launches = 0;
   if (ph->path == 0 && (euc || emb || ng) && has_collision(opt->maxIters, opt->updatePerLoops))
     D2G_CUDA(ph->Xp.alloc((size_t)ph->ncols_packed * ph->MP));  // X kept for obj after step 5
@@ -1363,7 +1458,14 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
       PlanArgs a = bucket_args(ph, base, b);
       D2G_CUDA(launch_rho_partial(ph->MP, ph->mode, a, b.nitems, ph->rho_part.p + b.block_off, ph->st));
     }
-    D2G_CUDA(launch_rho_final(ph->rho_part.p, ph->total_blocks, ph->ctl.p, (double)ph->col * m, ph->st));
+    if (ph->xfn && (ph->xflags & D2G_SHARD_GLOBAL_RHO)) {  // rho over all shards' costs
+      D2G_CUDA(launch_rho_local(ph->rho_part.p, ph->total_blocks, (double)ph->col * m, ph->xbuf.p, ph->st));
+      int rc = xchg(ph, ph->xbuf.p, 2);
+      if (rc) return rc;
+      D2G_CUDA(launch_rho_set(ph->xbuf.p, ph->ctl.p, ph->st));
+    } else {  // this shard's own, as the reference's MPI build does (:109)
+      D2G_CUDA(launch_rho_final(ph->rho_part.p, ph->total_blocks, ph->ctl.p, (double)ph->col * m, ph->st));
+    }
     D2G_CUDA(cudaMemsetAsync(ph->Y.p, 0, (size_t)ph->ncols_packed * ph->MP * 4, ph->st));
     for (auto &b : ph->buckets) {
       PlanArgs a = bucket_args(ph, base, b);
@@ -1382,8 +1484,7 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
 
   // two iterations per pass: phases whose plans fit in one CTA, no time budget
   // (the reference may stop after any iteration)
-  ph->pairs = cfg.pair_iterations && ph->path == 0 && ph->nwide == 0 && ph->buckets.size() == 1 &&
-              ph->buckets[0].cs == 1 && ph->MP <= 128 && ph->rawsum.n > 0 && h.budget_ns == ~0ULL;
+  ph->pairs = pair_capable(ph, cfg) && h.budget_ns == ~0ULL && (!ph->xfn || ph->shard_pairs);
   // deferred-exchange schedule of the wide plans
   ph->h_def_iter.assign((size_t)opt->maxIters + 1, 0);
   if (ph->path == 0 && ph->defer) {
@@ -1403,7 +1504,7 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
   int plan_timed = 0;
   long long nl = 0;
   D2G_CUDA(cudaEventRecord(ph->ev0, ph->st));
-  if (profile || !cfg.use_graph) {
+  if (profile || !cfg.use_graph || ph->xfn) {  // (a sharded update enqueues directly)
     int rc = enqueue_loop(ph, opt->maxIters, opt->updatePerLoops, profile, &nl, &plan_ms, &plan_timed);
     if (rc) return rc;
   } else {
@@ -1789,6 +1890,186 @@ int d2g_badmm_run_sym(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, int
   if (!ph) return D2G_E_INVAL;
   if (ph->metric != D2_N_GRAM) return fail(D2G_E_INVAL, "d2g_badmm_run_sym is for n-gram phases");
   return run_impl(ph, opt, c_w, nullptr, c_sym, label_switch);
+}
+
+int d2g_phase_set_allreduce(d2g_phase *ph, d2g_allreduce_fn fn, void *ctx, int flags) {
+  if (!ph) return fail(D2G_E_INVAL, "null phase");
+  if (flags & ~D2G_SHARD_GLOBAL_RHO) return fail(D2G_E_INVAL, "unknown sharding flags");
+  ph->xfn = fn;
+  ph->xctx = ctx;
+  ph->xflags = fn ? flags : 0;
+  ph->shard_pairs = false;  // shards in other processes may differ in shape
+  return D2G_OK;
+}
+
+namespace {
+// The exchange between the shards of d2g_badmm_run_shards, all on one device.
+// Every shard's host thread reaches the same exchanges in the same order; at
+// each, the shards' buffers are summed in shard order on every shard's stream
+// (stream-ordered through events, no kernel waits on another).
+struct ShardGroup {
+  int n = 0;
+  std::mutex mu;
+  std::condition_variable cv;
+  int arrived = 0;
+  long long gen = 0;
+  bool abort = false;
+  std::vector<double *> buf, tmp;
+  std::vector<size_t> cnt;
+  std::vector<cudaEvent_t> ready, done;
+  size_t tmp_cap = 0;
+  bool meet() {  // host barrier of all shards; false once a shard has failed
+    std::unique_lock<std::mutex> lk(mu);
+    const long long g = gen;
+    if (++arrived == n) {
+      arrived = 0;
+      ++gen;
+      cv.notify_all();
+    } else {
+      cv.wait(lk, [&] { return gen != g || abort; });
+    }
+    return !abort;
+  }
+  void fail_all() {
+    std::lock_guard<std::mutex> lk(mu);
+    abort = true;
+    cv.notify_all();
+  }
+};
+struct ShardCtx {
+  ShardGroup *g;
+  int s;
+};
+
+int group_allreduce(double *buf, size_t count, void *stream, void *ctx) {
+  ShardCtx *c = (ShardCtx *)ctx;
+  ShardGroup *g = c->g;
+  const int s = c->s;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (count > g->tmp_cap) {
+    g->fail_all();
+    return 1;
+  }
+  g->buf[s] = buf;
+  g->cnt[s] = count;
+  if (cudaEventRecord(g->ready[s], st) != cudaSuccess) {
+    g->fail_all();
+    return 2;
+  }
+  if (!g->meet()) return 3;  // every shard's buffer is ready (in stream order)
+  ShardBufs b{};
+  b.n = g->n;
+  for (int r = 0; r < g->n; ++r) {
+    if (g->cnt[r] != count) {
+      g->fail_all();
+      return 4;
+    }
+    b.p[r] = g->buf[r];
+    if (r != s && cudaStreamWaitEvent(st, g->ready[r], 0) != cudaSuccess) {
+      g->fail_all();
+      return 2;
+    }
+  }
+  if (launch_shard_sum(b, count, g->tmp[s], st) != cudaSuccess ||
+      cudaEventRecord(g->done[s], st) != cudaSuccess) {
+    g->fail_all();
+    return 2;
+  }
+  if (!g->meet()) return 3;  // every shard has read every buffer before any is overwritten
+  for (int r = 0; r < g->n; ++r)
+    if (r != s && cudaStreamWaitEvent(st, g->done[r], 0) != cudaSuccess) {
+      g->fail_all();
+      return 2;
+    }
+  if (cudaMemcpyAsync(buf, g->tmp[s], count * 8, cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
+    g->fail_all();
+    return 2;
+  }
+  return 0;
+}
+}  // namespace
+
+int d2g_badmm_run_shards(d2g_phase *const *ph, int nshard, const d2g_badmm_opts *opt, int flags,
+                         double *const *c_w, double *const *c_supp) {
+  if (!ph || !opt || !c_w || nshard < 1 || nshard > kMaxShards)
+    return fail(D2G_E_INVAL, "d2g_badmm_run_shards: 1 to 8 shards, options and outputs required");
+  if (flags & ~D2G_SHARD_GLOBAL_RHO) return fail(D2G_E_INVAL, "unknown sharding flags");
+  const d2g_config cfg = cfg_snapshot();
+  size_t need = 8;
+  bool pairs = true;
+  for (int s = 0; s < nshard; ++s) {
+    if (!ph[s] || !c_w[s]) return fail(D2G_E_INVAL, "d2g_badmm_run_shards: null shard");
+    for (int r = 0; r < s; ++r)
+      if (ph[r] == ph[s]) return fail(D2G_E_INVAL, "d2g_badmm_run_shards: a phase given twice");
+    if (ph[s]->K != ph[0]->K || ph[s]->str != ph[0]->str || ph[s]->dim != ph[0]->dim ||
+        ph[s]->metric != ph[0]->metric || ph[s]->path != ph[0]->path)
+      return fail(D2G_E_INVAL, "d2g_badmm_run_shards: the shards differ in metric, k, str or dim");
+    need = std::max(need, (size_t)ph[s]->K * (ph[s]->dim + 2) * ph[s]->str + 8);
+    pairs = pairs && pair_capable(ph[s], cfg);
+  }
+  int dev = 0;
+  D2G_CUDA(cudaGetDevice(&dev));
+  ShardGroup g;
+  g.n = nshard;
+  g.buf.assign(nshard, nullptr);
+  g.tmp.assign(nshard, nullptr);
+  g.cnt.assign(nshard, 0);
+  g.ready.assign(nshard, nullptr);
+  g.done.assign(nshard, nullptr);
+  g.tmp_cap = need;
+  std::vector<ShardCtx> ctx(nshard);
+  int rc = D2G_OK;
+  for (int s = 0; s < nshard && !rc; ++s) {
+    ctx[s] = {&g, s};
+    if (cudaMalloc(&g.tmp[s], need * 8) != cudaSuccess ||
+        cudaEventCreateWithFlags(&g.ready[s], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&g.done[s], cudaEventDisableTiming) != cudaSuccess)
+      rc = fail(D2G_E_NOMEM, "d2g_badmm_run_shards: exchange buffers");
+  }
+  std::vector<int> rcs(nshard, D2G_OK);
+  std::vector<std::string> msgs(nshard);
+  if (!rc) {
+    for (int s = 0; s < nshard; ++s) {
+      ph[s]->xfn = group_allreduce;
+      ph[s]->xctx = &ctx[s];
+      ph[s]->xflags = flags;
+      ph[s]->shard_pairs = pairs;
+    }
+    std::vector<std::thread> th;
+    for (int s = 0; s < nshard; ++s)
+      th.emplace_back([&, s] {
+        cudaSetDevice(dev);
+        rcs[s] = run_impl(ph[s], opt, c_w[s], c_supp ? c_supp[s] : nullptr, nullptr, nullptr);
+        if (rcs[s]) {
+          msgs[s] = g_last_error;
+          g.fail_all();
+        }
+      });
+    for (auto &t : th) t.join();
+    for (int s = 0; s < nshard; ++s) {
+      ph[s]->xfn = nullptr;
+      ph[s]->xctx = nullptr;
+      ph[s]->xflags = 0;
+      ph[s]->shard_pairs = false;
+    }
+    // report the shard that failed first, not the ones stopped by it
+    int first = -1;
+    for (int s = 0; s < nshard; ++s)
+      if (rcs[s] && (first < 0 || (msgs[first].find("failed (3)") != std::string::npos &&
+                                   msgs[s].find("failed (3)") == std::string::npos)))
+        first = s;
+    if (first >= 0) {
+      rc = rcs[first];
+      set_error("shard " + std::to_string(first) + ": " + msgs[first]);
+    }
+  }
+  for (int s = 0; s < nshard; ++s) {
+    if (g.ready[s]) cudaStreamSynchronize(ph[s]->st);
+    if (g.tmp[s]) cudaFree(g.tmp[s]);
+    if (g.ready[s]) cudaEventDestroy(g.ready[s]);
+    if (g.done[s]) cudaEventDestroy(g.done[s]);
+  }
+  return rc;
 }
 
 int d2g_phase_get_tuning(d2g_phase *ph, d2g_tuning *t) {

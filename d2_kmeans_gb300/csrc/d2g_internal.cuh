@@ -177,12 +177,29 @@ struct ClusterArgs {
   Ctl *ctl;
   int iter;
   int do_weights, do_moments;
+  const double *xsum;        // sharded update: the cluster sums over all shards (else null)
 };
 cudaError_t launch_cluster_reduce(const ClusterArgs &a, cudaStream_t st);
+// the same in three steps for a sharded update: partials, this shard's sums
+// (cluster_xsum_count doubles into xsum), then, after the exchange, the final
+cudaError_t launch_cluster_partial(const ClusterArgs &a, cudaStream_t st);
+cudaError_t launch_cluster_local(const ClusterArgs &a, double *xsum, cudaStream_t st);
+cudaError_t launch_cluster_final(const ClusterArgs &a, cudaStream_t st);
+size_t cluster_xsum_count(const ClusterArgs &a);
 cudaError_t launch_rho_final(const double *part, int n, Ctl *ctl, double nent,
                              cudaStream_t st);
+cudaError_t launch_rho_local(const double *part, int n, double nent, double *xbuf, cudaStream_t st);
+cudaError_t launch_rho_set(const double *xbuf, Ctl *ctl, cudaStream_t st);
 cudaError_t launch_resid_final(const double *part, int n, Ctl *ctl, double *trace_slot,
-                               int iter, bool obj_from_slot3, cudaStream_t st);
+                               int iter, bool obj_from_slot3, cudaStream_t st, int xmode = 0,
+                               double *xbuf = nullptr);
+// sharded update on one device: the shards' exchange buffers summed in shard order
+constexpr int kMaxShards = 8;
+struct ShardBufs {
+  const double *p[kMaxShards];
+  int n;
+};
+cudaError_t launch_shard_sum(const ShardBufs &b, size_t n, double *out, cudaStream_t st);
 cudaError_t launch_centroid_to_f32(const double *cw64, const double *cs64, float *cw32,
                                    float *cs32, int K, int m, int dim, int MP, int DS,
                                    cudaStream_t st);

@@ -6,6 +6,8 @@
 // bit-reproducible run to run; there are no floating-point atomics.  These
 // sums replace the reference's MPI_Allreduce sites (:188, :215-217, :308-310)
 // on one GPU.
+#include <algorithm>
+
 #include "d2g_internal.cuh"
 
 namespace d2g {
@@ -130,7 +132,11 @@ __global__ void __launch_bounds__(kRedThreads) cluster_final_kernel(const Cluste
     plane = a.dim + 1;
   else
     plane = blockIdx.y;
+  // the cluster's sum over its chunks; a sharded update reads instead the
+  // sums over all shards that the exchange left in xsum
+  const int p0 = a.do_moments ? 0 : a.dim + 1, npu = a.do_moments ? a.dim + 2 : 1;
   auto chunk_sum = [&](int pl, int k) {
+    if (a.xsum) return a.xsum[((size_t)l * npu + (pl - p0)) * m + k];
     double s = 0.0;
     const double *pp = a.part + (((size_t)l * nplanes + pl) * a.nchunk) * m + k;
     for (int c = 0; c < a.nchunk; ++c) s += pp[(size_t)c * m];
@@ -172,6 +178,53 @@ __global__ void __launch_bounds__(kRedThreads) cluster_final_kernel(const Cluste
       if (a.cs32) a.cs32[((size_t)l * a.MP + k) * a.DS + plane] = (float)v;
     }
   }
+}
+
+// grid (K, planes used): a shard's sums over its chunks, in chunk order, into
+// xsum [K][planes used][m] for the exchange between shards (the planes used:
+// the weights alone, or the moments 0..dim and the weights)
+__global__ void __launch_bounds__(kRedThreads) cluster_local_kernel(const ClusterArgs a, double *xsum) {
+  if (a.iter >= a.ctl->stop_iter) return;
+  const int l = blockIdx.x, m = a.m, nplanes = a.dim + 2;
+  const int p0 = a.do_moments ? 0 : a.dim + 1, npu = a.do_moments ? a.dim + 2 : 1;
+  const int pl = p0 + (int)blockIdx.y;
+  for (int k = threadIdx.x; k < m; k += kRedThreads) {
+    double s = 0.0;
+    const double *pp = a.part + (((size_t)l * nplanes + pl) * a.nchunk) * m + k;
+    for (int c = 0; c < a.nchunk; ++c) s += pp[(size_t)c * m];
+    xsum[((size_t)l * npu + (pl - p0)) * m + k] = s;
+  }
+}
+
+size_t cluster_xsum_count(const ClusterArgs &a) {
+  return (size_t)a.K * (a.do_moments ? a.dim + 2 : 1) * a.m;
+}
+
+cudaError_t launch_cluster_partial(const ClusterArgs &a, cudaStream_t st) {
+  const int np_in = (a.do_moments ? a.dim + 1 : 0) + (a.do_weights ? 1 : 0);
+  dim3 g1(a.nchunk, a.K, np_in);
+  if (a.do_moments && !a.do_weights) g1.z = a.dim + 1;
+  const int nk = (a.m + 31) / 32;
+  if (nk <= 1)
+    cluster_partial_kernel<1><<<g1, kRedThreads, 0, st>>>(a);
+  else if (nk <= 2)
+    cluster_partial_kernel<2><<<g1, kRedThreads, 0, st>>>(a);
+  else if (nk <= 4)
+    cluster_partial_kernel<4><<<g1, kRedThreads, 0, st>>>(a);
+  else
+    cluster_partial_kernel<8><<<g1, kRedThreads, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cluster_local(const ClusterArgs &a, double *xsum, cudaStream_t st) {
+  cluster_local_kernel<<<dim3(a.K, a.do_moments ? a.dim + 2 : 1), kRedThreads, 0, st>>>(a, xsum);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cluster_final(const ClusterArgs &a, cudaStream_t st) {
+  const int np_out = (a.do_weights ? 1 : 0) + (a.do_moments ? a.dim : 0);
+  cluster_final_kernel<<<dim3(a.K, np_out), kRedThreads, 0, st>>>(a);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_cluster_reduce(const ClusterArgs &a, cudaStream_t st) {
@@ -219,11 +272,58 @@ cudaError_t launch_rho_final(const double *part, int n, Ctl *ctl, double nent, c
   return cudaGetLastError();
 }
 
+// sharded update, rho over all shards: this shard's {sum |C|, entries} into
+// xbuf for the exchange, then rho from the exchanged totals
+__global__ void rho_local_kernel(const double *part, int n, double nent, double *xbuf) {
+  __shared__ double sm[1024 / 32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += part[i];
+  s = wsum(s);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sm[w];
+    xbuf[0] = t;
+    xbuf[1] = nent;
+  }
+}
+
+__global__ void rho_set_kernel(const double *xbuf, Ctl *ctl) {
+  const double rho = ctl->rho_coeff * xbuf[0] / xbuf[1];
+  ctl->rho = rho;
+  ctl->inv_rho = (float)(1.0 / rho);
+  ctl->inv_rho_l2 = (float)(1.4426950408889634 / rho);
+  if (!(rho > 0.0) || !isfinite(rho)) ctl_fail(ctl, 3);
+}
+
+cudaError_t launch_rho_local(const double *part, int n, double nent, double *xbuf, cudaStream_t st) {
+  rho_local_kernel<<<1, 1024, 0, st>>>(part, n, nent, xbuf);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rho_set(const double *xbuf, Ctl *ctl, cudaStream_t st) {
+  rho_set_kernel<<<1, 1, 0, st>>>(xbuf, ctl);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------- residuals
 // part: 4 doubles per CTA (obj, primres, dualres, obj-after-support-update)
+// xmode 0: finalise; 1: this shard's three sums into xbuf (for the exchange
+// between shards); 2: finalise from the exchanged totals in xbuf
 __global__ void resid_final_kernel(const double *part, int n, Ctl *ctl, double *slot, int iter,
-                                   int obj_from_slot3) {
+                                   int obj_from_slot3, int xmode, double *xbuf) {
   if (iter >= ctl->stop_iter) return;
+  if (xmode == 2) {
+    if (threadIdx.x == 0) {
+      const double N = ctl->global_size;
+      slot[0] = iter + 1;
+      slot[1] = xbuf[0] * (ctl->rho / N);  // :312-314, this shard's rho as in the reference
+      slot[2] = xbuf[1] / N;
+      slot[3] = xbuf[2] / N;
+    }
+    return;
+  }
   __shared__ double sm[3][1024 / 32];
   double o = 0.0, p = 0.0, d = 0.0;
   const int oi = obj_from_slot3 ? 3 : 0;
@@ -248,6 +348,12 @@ __global__ void resid_final_kernel(const double *part, int n, Ctl *ctl, double *
       tp += sm[1][w];
       td += sm[2][w];
     }
+    if (xmode == 1) {
+      xbuf[0] = to;
+      xbuf[1] = tp;
+      xbuf[2] = td;
+      return;
+    }
     const double N = ctl->global_size;
     slot[0] = iter + 1;
     slot[1] = to * (ctl->rho / N);  // :312-314
@@ -257,8 +363,24 @@ __global__ void resid_final_kernel(const double *part, int n, Ctl *ctl, double *
 }
 
 cudaError_t launch_resid_final(const double *part, int n, Ctl *ctl, double *trace_slot, int iter,
-                               bool obj_from_slot3, cudaStream_t st) {
-  resid_final_kernel<<<1, 1024, 0, st>>>(part, n, ctl, trace_slot, iter, obj_from_slot3 ? 1 : 0);
+                               bool obj_from_slot3, cudaStream_t st, int xmode, double *xbuf) {
+  resid_final_kernel<<<1, 1024, 0, st>>>(part, n, ctl, trace_slot, iter, obj_from_slot3 ? 1 : 0, xmode,
+                                         xbuf);
+  return cudaGetLastError();
+}
+
+// sharded update: out[i] = sum over the shards' buffers in shard order
+__global__ void shard_sum_kernel(ShardBufs b, size_t n, double *out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int r = 0; r < b.n; ++r) s += b.p[r][i];
+    out[i] = s;
+  }
+}
+
+cudaError_t launch_shard_sum(const ShardBufs &b, size_t n, double *out, cudaStream_t st) {
+  const unsigned nb = (unsigned)std::min<size_t>((n + 255) / 256, 1024);
+  shard_sum_kernel<<<nb ? nb : 1, 256, 0, st>>>(b, n, out);
   return cudaGetLastError();
 }
 

@@ -287,6 +287,33 @@ void *d2g_phase_stream(d2g_phase *ph);
 /* the last run's X (after step 1, or X-Z after a check iteration as the
  * reference leaves it), Y and C (divided by rho), reference layout, FP64 */
 int d2g_phase_get_scratch(d2g_phase *ph, double *X, double *Y, double *C);
+/* ------------------------------------------------- sharded centroid update
+ * The reference's MPI build (src/d2/centroid_Bregman.c with __USE_MPI__)
+ * splits the instances of a phase over ranks and all-reduces, by SUM, the
+ * label counts (:142), the cluster weights (:188), the support numerators and
+ * X row sums (:215-217) and obj / primres / dualres (:308-310).  A phase
+ * created on one shard of the instances, with d2g_phase_desc.global_size set
+ * to the instance count of all shards, runs the same update here once it has
+ * an all-reduce: fn(buf, count, stream, ctx) must enqueue on `stream` (a
+ * cudaStream_t) an in-place SUM of the count FP64 values of the device buffer
+ * buf over all shards - e.g. ncclAllReduce(buf, buf, count, ncclDouble,
+ * ncclSum, comm, stream) - and return 0.  It is called on the host while the
+ * update is enqueued, the same calls in the same order on every shard; the
+ * loop then runs without a CUDA graph.  Each shard takes rho from its own
+ * instances, as the reference does; D2G_SHARD_GLOBAL_RHO takes it over all
+ * shards (two more values exchanged).  Covers the batched form of Euclidean
+ * and histogram phases without a time budget; fn == NULL turns it off. */
+typedef int (*d2g_allreduce_fn)(double *buf, size_t count, void *stream, void *ctx);
+#define D2G_SHARD_GLOBAL_RHO 1
+int d2g_phase_set_allreduce(d2g_phase *ph, d2g_allreduce_fn fn, void *ctx, int flags);
+/* The sharded update of nshard (<= 8) phases on the current device, one host
+ * thread per shard, the all-reduce done between the shards' streams (a sum
+ * over the shards' buffers in shard order).  c_w[s] and c_supp[s] are each
+ * shard's centroids in and out (c_supp may be NULL for histograms); every
+ * shard ends with the same centroids. */
+int d2g_badmm_run_shards(d2g_phase *const *ph, int nshard, const d2g_badmm_opts *opt, int flags,
+                         double *const *c_w, double *const *c_supp);
+
 /* Test hook of the bounded device waits (no counterpart in the reference).
  * Every wait of the batched plan kernels for their bulk copies gives up after
  * wait_s seconds (0: one second), reports through the phase's control block

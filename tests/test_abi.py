@@ -23,6 +23,7 @@ def declared_functions():
     names = set()
     for h in glob.glob(os.path.join(INCLUDE, "*.h")):
         txt = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        txt = re.sub(r"\btypedef\b[^;{]*;", "", txt)  # function-pointer types are not functions
         for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(\w+)\s*\([^;{]*\)\s*;", txt, re.M):
             if m.group(1) not in ("if", "while", "for", "return", "sizeof"):
                 names.add(m.group(1))
