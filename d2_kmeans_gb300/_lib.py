@@ -90,7 +90,8 @@ class d2g_run_stats(C.Structure):
 
 class d2g_tuning(C.Structure):
     _fields_ = [("exchange", C.c_int), ("stage_costs", C.c_int), ("ctas_per_sm", C.c_int),
-                ("cost_gemm", C.c_int)]
+                ("cost_gemm", C.c_int), ("pairs", C.c_int), ("unit_order", C.c_int),
+                ("stage_scales", C.c_int)]
 
 
 class d2g_dists(C.Structure):

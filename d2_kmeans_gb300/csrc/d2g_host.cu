@@ -114,6 +114,9 @@ struct d2g_phase {
   DBuf<int> symstage;
   DBuf<double> part;   // cluster partials
   int chunk = 256, nchunk = 1;
+  std::vector<int> h_item_g0, h_item_ng;  // item arrays as packed (before any reordering)
+  std::vector<int2> h_item_pp;
+  int cur_order = 0;                      // the unit order the device item arrays hold
   DBuf<int> cl_ptr, cl_plans;
   DBuf<char> reinit;
 
@@ -225,8 +228,8 @@ static bool tune_cache_get(const std::string &key, d2g_tuning *t) {
   bool found = false;
   char k[256];
   d2g_tuning r;
-  while (fscanf(f, "%255s %d %d %d %d", k, &r.exchange, &r.stage_costs, &r.ctas_per_sm,
-                &r.cost_gemm) == 5)
+  while (fscanf(f, "%255s %d %d %d %d %d %d %d", k, &r.exchange, &r.stage_costs, &r.ctas_per_sm,
+                &r.cost_gemm, &r.pairs, &r.unit_order, &r.stage_scales) == 8)
     if (key == k) {
       *t = r;
       found = true;
@@ -242,16 +245,40 @@ static void tune_cache_put(const std::string &key, const d2g_tuning &t) {
   if (!path || !*path) return;
   FILE *f = fopen(path, "a");
   if (!f) return;
-  fprintf(f, "%s %d %d %d %d\n", key.c_str(), t.exchange, t.stage_costs, t.ctas_per_sm, t.cost_gemm);
+  fprintf(f, "%s %d %d %d %d %d %d %d\n", key.c_str(), t.exchange, t.stage_costs, t.ctas_per_sm,
+          t.cost_gemm, t.pairs, t.unit_order, t.stage_scales);
   fclose(f);
 }
 
 // the run-time switches that follow from the phase's tuning
-static void apply_tuning(d2g_phase *ph) {
+static int apply_tuning(d2g_phase *ph) {
   ph->defer = ph->path == 0 && ph->nwide > 0 && ph->units.nitems > 0 &&
               ph->tune.exchange == 0;
   ph->stage_costs = ph->tune.stage_costs;
   ph->cost_gemm = ph->tune.cost_gemm;
+  // the walk order of the items that each fit one CTA (bucket 0): the item
+  // arrays are permuted in place, the plans stay where they are
+  if (ph->path == 0 && ph->tune.unit_order != ph->cur_order && !ph->h_item_g0.empty() &&
+      !ph->buckets.empty() && ph->buckets[0].cs == 1) {
+    const int n1 = ph->buckets[0].nitems;
+    std::vector<int> idx(n1);
+    for (int i = 0; i < n1; ++i) idx[i] = i;
+    if (ph->tune.unit_order == 1)
+      std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return ph->h_item_ng[a] > ph->h_item_ng[b]; });
+    std::vector<int> g0(n1), ng(n1);
+    std::vector<int2> pp(n1);
+    for (int i = 0; i < n1; ++i) {
+      g0[i] = ph->h_item_g0[idx[i]];
+      ng[i] = ph->h_item_ng[idx[i]];
+      pp[i] = ph->h_item_pp[idx[i]];
+    }
+    D2G_CUDA(cudaMemcpyAsync(ph->item_g0.p, g0.data(), n1 * 4, cudaMemcpyHostToDevice, ph->st));
+    D2G_CUDA(cudaMemcpyAsync(ph->item_ng.p, ng.data(), n1 * 4, cudaMemcpyHostToDevice, ph->st));
+    D2G_CUDA(cudaMemcpyAsync(ph->item_pp.p, pp.data(), n1 * sizeof(int2), cudaMemcpyHostToDevice, ph->st));
+    D2G_CUDA(cudaStreamSynchronize(ph->st));
+    ph->cur_order = ph->tune.unit_order;
+  }
+  return D2G_OK;
 }
 
 static bool batched_supported(const d2g_phase_desc *d, std::string *why) {
@@ -450,6 +477,10 @@ static int build_packing(d2g_phase *ph, bool with_units) {
   D2G_CUDA(cudaMemcpyAsync(ph->item_pp.p, h_item_pp.data(), h_item_pp.size() * sizeof(int2),
                            cudaMemcpyHostToDevice, ph->st));
   D2G_CUDA(cudaStreamSynchronize(ph->st));
+  ph->h_item_g0 = h_item_g0;  // (the autotuner's unit order permutes copies of these)
+  ph->h_item_ng = h_item_ng;
+  ph->h_item_pp = h_item_pp;
+  ph->cur_order = 0;
   return D2G_OK;
 }
 
@@ -475,6 +506,7 @@ static PlanArgs base_args(d2g_phase *ph) {
   a.resid_part = ph->resid_part.p;
   a.ctl = ph->ctl.p;
   a.ctas_per_sm = ph->tune.ctas_per_sm;
+  a.stage_scales = ph->tune.stage_scales;
   a.m = ph->str;
   a.dim = ph->metric == D2_EUCLIDEAN_L2 ? ph->dim : 0;
   a.grp_rec = ph->grp_rec.p;
@@ -814,6 +846,9 @@ static int create_batched(d2g_phase *ph, const d2g_phase_desc *d) {
     ph->tune.stage_costs = (sc && std::string(sc) == "0") ? 0 : 1;
     ph->tune.ctas_per_sm = 0;
     ph->tune.cost_gemm = cfg_snapshot().cost_gemm;
+    ph->tune.pairs = 1;
+    ph->tune.unit_order = 0;
+    ph->tune.stage_scales = 1;
     d2g_tuning rec;
     if (tune_cache_get(tune_key(ph), &rec)) ph->tune = rec;
   }
@@ -988,6 +1023,7 @@ static std::vector<unsigned long long> loop_signature(d2g_phase *ph) {
           (unsigned long long)ph->global_size, (unsigned long long)ph->cost_gemm,
           u(ph->wide.p), u(ph->def_iter.p), u(ph->rowpart.p), u(ph->rowsc.p), u(ph->col_crow.p),
           (unsigned long long)ph->stage_costs, (unsigned long long)ph->tune.ctas_per_sm,
+          (unsigned long long)ph->tune.stage_scales,
           (unsigned long long)ph->defer, u(ph->ncnt.p), u(ph->csym.p), u(ph->nkey.p), u(ph->nptr.p),
           u(ph->nocc.p), (unsigned long long)ph->nlists, u(ph->ntup.p), u(ph->ndist.p),
           (unsigned long long)ph->ntab, (unsigned long long)ph->pairs, u(ph->rowsum2.p), u(ph->rawsum.p),
@@ -1360,7 +1396,10 @@ static bool pair_capable(const d2g_phase *ph, const d2g_config &cfg) {
 static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, double *c_supp,
                     int *c_sym, const char *label_switch) {
   const d2g_config cfg = cfg_snapshot();
-  apply_tuning(ph);
+  {
+    int rc = apply_tuning(ph);
+    if (rc) return rc;
+  }
   if (!opt || opt->maxIters < 0 || opt->updatePerLoops <= 0 || !(opt->rhoCoeff > 0) || !c_w)
     return fail(D2G_E_INVAL, "bad B-ADMM options");
   const bool euc = ph->metric == D2_EUCLIDEAN_L2, emb = ph->metric == D2_WORD_EMBED;
@@ -1484,7 +1523,7 @@ static int run_impl(d2g_phase *ph, const d2g_badmm_opts *opt, double *c_w, doubl
 
   // two iterations per pass: phases whose plans fit in one CTA, no time budget
   // (the reference may stop after any iteration)
-  ph->pairs = pair_capable(ph, cfg) && h.budget_ns == ~0ULL && (!ph->xfn || ph->shard_pairs);
+  ph->pairs = pair_capable(ph, cfg) && ph->tune.pairs && h.budget_ns == ~0ULL && (!ph->xfn || ph->shard_pairs);
   // deferred-exchange schedule of the wide plans
   ph->h_def_iter.assign((size_t)opt->maxIters + 1, 0);
   if (ph->path == 0 && ph->defer) {
@@ -2080,7 +2119,9 @@ int d2g_phase_get_tuning(d2g_phase *ph, d2g_tuning *t) {
 
 int d2g_phase_set_tuning(d2g_phase *ph, const d2g_tuning *t) {
   if (!ph || !t || t->exchange < 0 || t->exchange > 1 || t->stage_costs < 0 || t->stage_costs > 1 ||
-      t->ctas_per_sm < 0 || t->ctas_per_sm > 32 || t->cost_gemm < 0 || t->cost_gemm > 1)
+      t->ctas_per_sm < 0 || t->ctas_per_sm > 32 || t->cost_gemm < 0 || t->cost_gemm > 1 ||
+      t->pairs < 0 || t->pairs > 1 || t->unit_order < 0 || t->unit_order > 1 || t->stage_scales < 0 ||
+      t->stage_scales > 1)
     return fail(D2G_E_INVAL, "bad tuning");
   ph->tune = *t;
   return D2G_OK;
@@ -2099,16 +2140,22 @@ int d2g_phase_autotune(d2g_phase *ph, const d2g_badmm_opts *opt, const double *c
   if (ph->path != 0) return D2G_OK;  // the FP64 form has no launch-shape choices
   // candidates: every combination of the choices that apply to this phase
   const d2g_tuning base = ph->tune;
-  std::vector<int> ex = {base.exchange}, sc = {0}, cp = {0}, cg = {base.cost_gemm};
+  std::vector<int> ex = {base.exchange}, sc = {0}, cp = {0}, cg = {base.cost_gemm}, pr = {0}, uo = {0};
   if (ph->nwide > 0 && ph->units.nitems > 0) ex = {0, 1};
   if (ph->mode == COST_TABLE && ph->MP >= 16 && ph->MP <= 128) sc = {0, 1};
   if (ph->MP < 256) cp = {0, 1};
   if (emb) cg = {0, 1};
+  if (pair_capable(ph, cfg_snapshot())) pr = {1, 0};
+  if (!ph->buckets.empty() && ph->buckets[0].cs == 1 && ph->buckets[0].nitems > 1) uo = {0, 1};
   std::vector<d2g_tuning> cand;
   for (int e : ex)
     for (int s2 : sc)
       for (int c : cp)
-        for (int g : cg) cand.push_back(d2g_tuning{e, s2, c, g});
+        for (int g : cg)
+          for (int p2 : pr)
+            for (int o2 : uo)
+              for (int ss : (p2 ? std::vector<int>{1, 0} : std::vector<int>{1}))
+                cand.push_back(d2g_tuning{e, s2, c, g, p2, o2, ss});
   // the phase's plans are re-initialised by the trial runs: keep them
   const size_t nz = (size_t)ph->ncols_packed * ph->MP;
   const bool had_plans = ph->plans_valid;

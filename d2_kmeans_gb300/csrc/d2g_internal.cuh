@@ -117,6 +117,7 @@ struct PlanArgs {
   int nplans_chk, nlab_chk; // plans and clusters of the phase (self-check of staged records)
   const int2 *item_pp;      // per item {first plan in packed order, plans}
   int ctab_rows;            // rows of MP floats in ctab (bound of the staged row gather)
+  int stage_scales;         // pair passes: deferred row scales staged with the tiles where possible
 };
 
 // per-MP launch geometry

@@ -575,7 +575,7 @@ cudaError_t launch_pair_t(const PlanArgs &a, int nitems, cudaStream_t st) {
   if (a.ctas_per_sm > 0) cap = std::min(cap, a.ctas_per_sm * nsm);
   const int g = nitems < cap ? nitems : cap;
   PlanArgs b = a;
-  if (stage && (a.flags & PF_IN_DEF)) b.flags |= PF_STAGE_SC;
+  if (stage && a.stage_scales && (a.flags & PF_IN_DEF)) b.flags |= PF_STAGE_SC;
   const size_t sm = (b.flags & PF_STAGE_SC) ? sm1 : sm0;
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = plan_cfg(g, GeoT<MP>::NT, sm, st, attr, 1);

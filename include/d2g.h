@@ -431,6 +431,12 @@ typedef struct {
                        default) or read through the cache (0) */
   int ctas_per_sm;  /* persistent plan-update grid: CTAs per SM, 0 = occupancy limit */
   int cost_gemm;    /* word-embedding cost table: 0 tensor cores (3xTF32), 1 CUDA cores */
+  int pairs;        /* plans that all fit one CTA: 1 two iterations per pass over the plans
+                       where the reference's schedule allows it, 0 one iteration per pass */
+  int unit_order;   /* order in which the persistent grid walks the units of plans that fit
+                       one CTA: 0 packing order, 1 largest unit first */
+  int stage_scales; /* pair passes: 1 each unit's deferred row scales arrive in shared memory
+                       with its tiles (where that keeps the CTAs per SM), 0 read by each thread */
 } d2g_tuning;
 
 int d2g_phase_get_tuning(d2g_phase *ph, d2g_tuning *t);

@@ -323,8 +323,8 @@ def test_word_embedding_cost_table_paths_agree(d2g):
 
 def test_autotune_times_every_candidate_and_keeps_results(d2g, oracle_mod, tmp_path, monkeypatch):
     """The autotuner times every candidate tuning (wide-plan exchange x table-cost
-    staging x CTAs per SM x cost-table GEMM for an embedding phase with plans
-    wider than one CTA), keeps the fastest, leaves the phase's plans as they
+    staging x CTAs per SM x cost-table GEMM x unit order for an embedding phase
+    with plans wider than one CTA), keeps the fastest, leaves the phase's plans as they
     were, records the choice in the D2G_TUNE_CACHE file, and a new phase of the
     same shape starts from it.  The tuned phase still matches the oracle."""
     cache = tmp_path / "tune.txt"
@@ -337,7 +337,7 @@ def test_autotune_times_every_candidate_and_keeps_results(d2g, oracle_mod, tmp_p
     z0 = P.get_plans()
     out = P.autotune(c, dict(maxIters=12, rhoCoeff=2.0, updatePerLoops=10))
     cands = out["candidates"]
-    assert len(cands) == 16
+    assert len(cands) == 32
     assert all(0 < ms < 1e9 for _, ms in cands)
     fastest = min(cands, key=lambda r: r[1])[0]
     assert out["best"] == fastest
@@ -345,11 +345,30 @@ def test_autotune_times_every_candidate_and_keeps_results(d2g, oracle_mod, tmp_p
     assert_close(P.run(c, opts), ref, 4, 64)
     P.close()
     rec = cache.read_text().split()
-    assert len(rec) == 5 and [int(v) for v in rec[1:]] == [fastest[k] for k in
-                                                           ("exchange", "stage_costs", "ctas_per_sm", "cost_gemm")]
+    keys = ("exchange", "stage_costs", "ctas_per_sm", "cost_gemm", "pairs", "unit_order", "stage_scales")
+    assert len(rec) == 8 and [int(v) for v in rec[1:]] == [fastest[k] for k in keys]
     Q = d2g.Phase(ph, 0)
     assert Q.tuning() == fastest
     Q.close()
+
+
+def test_autotune_tile_schedule_of_the_batched_phase(d2g, oracle_mod):
+    """Plans that all fit one CTA: the autotuner also chooses two iterations per
+    pass or one, the walk order of the units and whether a pair pass stages its
+    row scales (12 candidates with the CTAs per SM); every choice matches the
+    oracle."""
+    ph, c, opts = synth.workload("batched", seed=41, scale=0.01)
+    opts = dict(opts, maxIters=40)
+    ref = _port(oracle_mod, ph, c, opts)
+    P = d2g.Phase(ph, 0)
+    out = P.autotune(c, dict(opts, maxIters=12))
+    cands = [t for t, _ in out["candidates"]]
+    assert len(cands) == 12
+    assert {t["pairs"] for t in cands} == {0, 1} and {t["unit_order"] for t in cands} == {0, 1}
+    for t in cands:
+        P.set_tuning(**t)
+        assert_close(P.run(c, opts), ref, 64, 32)
+    P.close()
 
 
 @pytest.mark.parametrize("exchange", EXCHANGES)
