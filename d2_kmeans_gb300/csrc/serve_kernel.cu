@@ -106,6 +106,7 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
   __shared__ double sm_cost[G];
   __shared__ __align__(8) unsigned long long sm_bar[2];  // cluster: partials of all ranks landed, by parity
   __shared__ int sm_fail;
+  __shared__ float4 sm_w4[256], sm_cw4[256];  // per thread: its columns' weights, its rows' c_w
 
   const int tid = threadIdx.x, g = tid / TPC, r = tid % TPC, k0 = r * RPT;
   const int lane = tid & 31, warp = tid >> 5;
@@ -171,6 +172,8 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
 #pragma unroll
     for (int s = 0; s < S; ++s)
       *((float4 *)(cme + s * MP)) = make_float4(c[s][0], c[s][1], c[s][2], c[s][3]);
+    sm_w4[tid] = make_float4(w[0], w[1], w[2], w[3]);
+    sm_cw4[tid] = make_float4(cw[0], cw[1], cw[2], cw[3]);
   }
   const int m = a.m;
   const unsigned xbytes = (unsigned)cs * MP * 4u;  // one partial from every rank per iteration
@@ -223,7 +226,8 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
         csum += v[q];
       }
       csum = sv_seg_sum<TPC>(csum);
-      const float f = (FULL || colok) ? __fdividef(w[s], csum) : 0.f;
+      const float ws = s == 0 ? sm_w4[tid].x : s == 1 ? sm_w4[tid].y : s == 2 ? sm_w4[tid].z : sm_w4[tid].w;
+      const float f = (FULL || colok) ? __fdividef(ws, csum) : 0.f;
       const float eps2 = colok ? kRoundoff : 0.f;
 #pragma unroll
       for (int q = 0; q < RPT; ++q) {
@@ -284,7 +288,10 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
     // second half of step 2 with the fixed centroid weights, and step 3
     float sc[RPT];
 #pragma unroll
-    for (int q = 0; q < RPT; ++q) sc[q] = tot[q] > 0.f ? __fdividef(cw[q], tot[q]) : 0.f;
+    const float4 cw4 = sm_cw4[tid];
+    const float cwq[RPT] = {cw4.x, cw4.y, cw4.z, cw4.w};
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) sc[q] = tot[q] > 0.f ? __fdividef(cwq[q], tot[q]) : 0.f;
     if (wact)
 #pragma unroll
     for (int s = 0; s < S; ++s)

@@ -29,9 +29,8 @@ def _update_twice(d2g, ph, c, o):
         P.close()
 
 
-def test_phases_on_three_threads_match_runs_alone(d2g):
+def _three_threads(d2g):
     cases = _cases()
-    alone = [_update_twice(d2g, *cs) for cs in cases]
     out, errs = [None] * len(cases), []
 
     def work(i):
@@ -46,9 +45,48 @@ def test_phases_on_three_threads_match_runs_alone(d2g):
     for t in threads:
         t.join()
     assert not errs, errs
+    return out
+
+
+FRESH = r"""
+import os, sys, numpy as np
+sys.path.insert(0, {root!r}); sys.path.insert(0, os.path.join({root!r}, "tests"))
+from d2_kmeans_gb300 import badmm
+badmm.set_config(verbose=0, precision=0, use_graph=1, profile=0, sync_scratch=0, cost_gemm=0)
+import test_gpu_threads as T
+out = T._three_threads(badmm)
+np.savez({path!r}, **{{f"{{i}}_{{k}}": v for i, r in enumerate(out) for k, v in r.items()
+                      if k in ("c_w", "c_supp", "c_sym", "trace") and v is not None}})
+"""
+
+
+def test_phases_on_three_threads_match_runs_alone(d2g, tmp_path):
+    """The threads run first, in a fresh process: the launch shapes,
+    shared-memory attributes and graphs are all configured for the first time
+    while three phases race for them; then the same updates run alone."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    path = str(tmp_path / "threads.npz")
+    subprocess.run([sys.executable, "-c", FRESH.format(root=root, path=path)], check=True, timeout=600)
+    z = np.load(path)
+    out = []
+    for i in range(len(_cases())):
+        out.append({k: z[f"{i}_{k}"] for k in ("c_w", "c_supp", "c_sym", "trace") if f"{i}_{k}" in z.files})
+    alone = [_update_twice(d2g, *cs) for cs in _cases()]
     for a, b in zip(out, alone):
         np.testing.assert_array_equal(a["c_w"], b["c_w"])
         np.testing.assert_array_equal(a["trace"], b["trace"])
         for key in ("c_supp", "c_sym"):
             if b.get(key) is not None:
                 np.testing.assert_array_equal(a[key], b[key])
+
+
+def test_three_threads_in_this_process(d2g):
+    """The same with the caches already configured (after the tests above)."""
+    out = _three_threads(d2g)
+    alone = [_update_twice(d2g, *cs) for cs in _cases()]
+    for a, b in zip(out, alone):
+        np.testing.assert_array_equal(a["c_w"], b["c_w"])
+        np.testing.assert_array_equal(a["trace"], b["trace"])
