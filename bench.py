@@ -295,6 +295,7 @@ def e2e_steps(ph, c, opts, steps, warmup):
         if i >= warmup:
             times.append(el)
     d.close()
+    e2e_steps.step_ms = [round(1e3 * t, 2) for t in times]
     return statistics.mean(times), h2d, d2h
 
 
@@ -661,6 +662,9 @@ def main():
         e2e_value, e2e_ms = replica_throughput(sec * 1e3, n * iters)
         e2e = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_ms / 1e3,
+               "step_ms": e2e_steps.step_ms,
+               "note": "mean of the steps; a host copy of a step occasionally stalls for tens of ms "
+                       "on this host (the device time of the update does not change)",
                "api": "d2_centroid_sphBregman (reference structs, host buffers)"}
 
     hbm, peak_kind = peaks()
