@@ -129,6 +129,7 @@ SIGNATURES = {
     "d2g_badmm_run": (C.c_int, [C.c_void_p, C.POINTER(d2g_badmm_opts), C.c_void_p, C.c_void_p,
                                 C.c_void_p]),
     "d2g_centroid_rands": (C.c_int, [C.POINTER(mph), C.c_int, C.POINTER(sph)]),
+    "d2g_write_split": (C.c_int, [C.c_char_p, C.POINTER(mph), C.c_int, C.c_char]),
     "d2g_badmm_run_sym": (C.c_int, [C.c_void_p, C.POINTER(d2g_badmm_opts), C.c_void_p, C.c_void_p,
                                     C.c_void_p]),
     "d2g_phase_trace": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int)]),

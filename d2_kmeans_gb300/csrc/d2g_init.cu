@@ -263,6 +263,136 @@ extern "C" int d2g_centroid_rands(mph *p_data, int idx_ph, sph *c) {
   return D2G_OK;
 }
 
+// d2_write_split (src/d2/clustering_io.c:329-480): the instances in shuffled
+// order (math.c's shuffle after srand(0), the writing process being rank 0),
+// that order in <filename>.ind, and `splits` files <filename>.0 ... each with
+// a contiguous batch of 1 + (n-1)/splits instances in the d2 text format the
+// reader takes, one file per rank of a sharded run.  pre_processed != 0 writes
+// them as the reference's pre-processing does: word-embedding supports as
+// their vectors, Euclidean and embedding instances with more supports than
+// the phase's str merged down to str (Ward), dense histograms as their
+// non-zero bins.  The number formats are the reference's ("%lf", ids + 1), so
+// the files are the reference's byte for byte.  Where the reference would
+// read through a null pointer (pre-processed sparse histograms and n-grams)
+// this returns D2G_E_UNSUPPORTED; where its merge finds too few positive
+// weights (and writes uninitialised values), D2G_E_NUMERIC.
+extern "C" int d2g_write_split(const char *filename, mph *p_data, int splits, char is_pre_processed) {
+  if (!filename || !p_data || splits < 1 || (p_data->size > 0 && !p_data->ph))
+    return fail(D2G_E_INVAL, "d2g_write_split: bad arguments");
+  const int s_ph = p_data->s_ph;
+  const size_t size = p_data->size;
+  for (int j = 0; j < s_ph; ++j) {
+    const sph &ph = p_data->ph[j];
+    if (ph.col == 0) continue;
+    const int mt = ph.metric_type;
+    if (is_pre_processed && mt != D2_EUCLIDEAN_L2 && mt != D2_WORD_EMBED && mt != D2_HISTOGRAM)
+      return fail(D2G_E_UNSUPPORTED, "d2g_write_split: pre-processing covers Euclidean, word-embedding "
+                                     "and dense histogram phases");
+  }
+  std::vector<size_t> order(size);
+  for (size_t i = 0; i < size; ++i) order[i] = i;
+  SeededRand g(0);
+  shuffle(order, g);
+  const std::string base(filename);
+  {
+    FILE *f = fopen((base + ".ind").c_str(), "w+");
+    if (!f) return fail(D2G_E_INVAL, "d2g_write_split: cannot write " + base + ".ind");
+    for (size_t n = 0; n < size; ++n) fprintf(f, "%zd\n", order[n]);
+    fclose(f);
+  }
+  const size_t batch = size ? 1 + (size - 1) / (size_t)splits : 1;
+  std::vector<double> msupp, mw, csupp, cw;
+  std::vector<int> ssym;
+  for (int k = 0; k < splits; ++k) {
+    const std::string name = base + "." + std::to_string(k);
+    FILE *f = fopen(name.c_str(), "w+");
+    if (!f) return fail(D2G_E_INVAL, "d2g_write_split: cannot write " + name);
+    int rc = D2G_OK;
+    for (size_t idx = batch * (size_t)k; idx < size && idx < batch * (size_t)(k + 1) && !rc; ++idx) {
+      const size_t i = order[idx];
+      for (int j = 0; j < s_ph && !rc; ++j) {
+        const sph &ph = p_data->ph[j];
+        if (ph.col == 0) continue;
+        const int dim = ph.dim, mt = ph.metric_type;
+        int str = ph.p_str[i];
+        const size_t pos = ph.p_str_cum[i];
+        if (!is_pre_processed) {
+          if (mt == D2_HISTOGRAM)
+            fprintf(f, "%d %d ", dim, str);
+          else
+            fprintf(f, "%d\n%d\n", dim, str);
+          for (int q = 0; q < str; ++q) fprintf(f, "%lf ", ph.p_w[pos + q]);
+          fprintf(f, "\n");
+          if (mt == D2_EUCLIDEAN_L2) {
+            for (int q = 0; q < str; ++q) {
+              for (int d = 0; d < dim; ++d) fprintf(f, "%lf ", ph.p_supp[(pos + q) * dim + d]);
+              fprintf(f, "\n");
+            }
+          } else if (mt == D2_WORD_EMBED || mt == D2_SPARSE_HISTOGRAM) {
+            for (int q = 0; q < str; ++q) fprintf(f, "%d ", ph.p_supp_sym[pos + q] + 1);
+            fprintf(f, "\n");
+          }
+          continue;
+        }
+        // pre-processed (:396-466)
+        const double *w = ph.p_w + pos, *supp = nullptr, *pw = nullptr;
+        const int *psym = nullptr;
+        if (mt == D2_EUCLIDEAN_L2) {
+          supp = ph.p_supp + pos * dim;
+          pw = w;
+        } else if (mt == D2_WORD_EMBED) {
+          const int *sym = ph.p_supp_sym + pos;
+          msupp.resize((size_t)str * dim);
+          for (int q = 0; q < str; ++q)
+            for (int d = 0; d < dim; ++d) msupp[(size_t)q * dim + d] = ph.vocab_vec[(size_t)sym[q] * dim + d];
+          mw.assign(w, w + str);
+          supp = msupp.data();
+          pw = mw.data();
+        }
+        if ((mt == D2_EUCLIDEAN_L2 || mt == D2_WORD_EMBED) && str > ph.str) {
+          csupp.resize((size_t)ph.str * dim);
+          cw.resize(ph.str);
+          if (!merge(dim, supp, pw, str, csupp.data(), cw.data(), ph.str)) {
+            rc = fail(D2G_E_NUMERIC, "d2g_write_split: merge found no pair of positive weights");
+            break;
+          }
+          str = ph.str;
+          supp = csupp.data();
+          pw = cw.data();
+        }
+        if (mt == D2_HISTOGRAM) {  // the non-zero bins
+          ssym.clear();
+          mw.clear();
+          for (int q = 0; q < str; ++q)
+            if (w[q] > 0) {
+              ssym.push_back(q);
+              mw.push_back(w[q]);
+            }
+          str = (int)ssym.size();
+          psym = ssym.data();
+          pw = mw.data();
+        }
+        fprintf(f, "%d\n", dim);
+        fprintf(f, "%d\n", str);
+        for (int q = 0; q < str; ++q) fprintf(f, "%lf ", pw[q]);
+        fprintf(f, "\n");
+        if (mt == D2_EUCLIDEAN_L2 || mt == D2_WORD_EMBED) {
+          for (int q = 0; q < str; ++q) {
+            for (int d = 0; d < dim; ++d) fprintf(f, "%lf ", supp[(size_t)q * dim + d]);
+            fprintf(f, "\n");
+          }
+        } else if (mt == D2_HISTOGRAM) {
+          for (int q = 0; q < str; ++q) fprintf(f, "%d ", psym[q] + 1);
+          fprintf(f, "\n");
+        }
+      }
+    }
+    fclose(f);
+    if (rc) return rc;
+  }
+  return D2G_OK;
+}
+
 namespace d2g {
 
 // the program's d2_centroid_rands where it links one, else d2g_centroid_rands

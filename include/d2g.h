@@ -177,6 +177,19 @@ int d2g_distmat_noalloc(int metric_type, int dim, int str, size_t size, size_t c
  * this. */
 int d2g_centroid_rands(mph *p_data, int idx_ph, sph *c);
 
+/* The result of d2_write_split, src/d2/clustering_io.c:329-480 (declared
+ * include/d2/clustering.h:149), with the same signature: the shard files of
+ * a sharded run.  The instances in the reference's shuffled order (its
+ * shuffle after srand(0), one writing process) go to <filename>.ind and, in
+ * contiguous batches of 1 + (size-1)/splits, to <filename>.0 ..
+ * <filename>.<splits-1> in the d2 text format, byte for byte the reference's
+ * files; is_pre_processed != 0 applies the reference's pre-processing
+ * (embedding supports as vectors, supports merged down to str, dense
+ * histograms as their non-zero bins) to Euclidean, word-embedding and dense
+ * histogram phases and returns D2G_E_UNSUPPORTED for the others (where the
+ * reference reads through a null pointer). */
+int d2g_write_split(const char *filename, mph *p_data, int splits, char is_pre_processed);
+
 /* Option structs of src/d2/centroid_Bregman.c:17-22 (the caller swaps
  * p_badmm_options, e.g. src/app/main.cc:234-236). */
 extern BADMM_options badmm_clu_options;
