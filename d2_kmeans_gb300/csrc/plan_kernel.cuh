@@ -61,6 +61,16 @@ __device__ __forceinline__ float ex2f(float x) {
   asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
+// Row pairs through the packed FP32x2 instructions (one issue slot for two
+// lanes' arithmetic, each lane rounded exactly as its scalar form).
+__device__ __forceinline__ float2 bc2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 ex2f2(float2 x) { return make_float2(ex2f(x.x), ex2f(x.y)); }
+__device__ __forceinline__ float2 nex2f2(float2 x) { return make_float2(ex2f(-x.x), ex2f(-x.y)); }
+__device__ __forceinline__ float2 pr2(const float *v, int h) { return make_float2(v[2 * h], v[2 * h + 1]); }
+__device__ __forceinline__ void st2(float *v, int h, float2 u) {
+  v[2 * h] = u.x;
+  v[2 * h + 1] = u.y;
+}
 constexpr float kLog2e = 1.4426950408889634f;  // log2(e)
 constexpr float kLn2 = 0.6931471805599453f;    // ln(2) = 1/log2(e)
 

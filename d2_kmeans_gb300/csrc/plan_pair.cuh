@@ -232,9 +232,10 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
       }
       if (indef) {
 #pragma unroll
-        for (int q = 0; q < RPT; ++q) {
-          z[q] *= scin[q];
-          y[q] = fmaf(-kLog2e, z[q], y[q]);
+        for (int h = 0; h < RPT / 2; ++h) {
+          const float2 zz = __fmul2_rn(pr2(z, h), pr2(scin, h));
+          st2(z, h, zz);
+          st2(y, h, __ffma2_rn(bc2(-kLog2e), zz, pr2(y, h)));
         }
       }
     };
@@ -253,31 +254,30 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
     auto half = [&](int s, const float (&c)[RPT], const float (&z)[RPT], const float (&y)[RPT],
                     float (&x)[RPT], float (&zp)[RPT]) {
       const bool colok = s < t.nvalid;
-      float csum = 0.f;
+      float2 vs = bc2(0.f);
 #pragma unroll
-      for (int q = 0; q < RPT; ++q) {
-        float v;
-        if constexpr (FULL) {
-          v = fmaf(z[q], ex2f(-fmaf(c[q], ir2, y[q])), kRoundoff);
-        } else {
-          const bool ok = colok && t.k0 + q < m;
-          v = ok ? fmaf(z[q], ex2f(-fmaf(c[q], ir2, y[q])), kRoundoff) : 0.f;
+      for (int h = 0; h < RPT / 2; ++h) {
+        float2 v = __ffma2_rn(pr2(z, h), nex2f2(__ffma2_rn(pr2(c, h), bc2(ir2), pr2(y, h))), bc2(kRoundoff));
+        if constexpr (!FULL) {
+          if (!(colok && t.k0 + 2 * h < m)) v.x = 0.f;
+          if (!(colok && t.k0 + 2 * h + 1 < m)) v.y = 0.f;
         }
-        x[q] = v;
-        csum += v;
+        st2(x, h, v);
+        vs = h == 0 ? v : __fadd2_rn(vs, v);
       }
-      csum = seg_sum<TPC>(csum);
+      const float csum = seg_sum<TPC>(vs.x + vs.y);
       const float f = (FULL || colok) ? __fdividef(w[s], csum) : 0.f;
       const float eps2 = colok ? kRoundoff : 0.f;
 #pragma unroll
-      for (int q = 0; q < RPT; ++q) {
-        x[q] *= f;
-        if constexpr (FULL) {
-          zp[q] = fmaf(x[q], ex2f(y[q]), eps2);
-        } else {
-          const bool ok = colok && t.k0 + q < m;
-          zp[q] = ok ? fmaf(x[q], ex2f(y[q]), kRoundoff) : 0.f;
+      for (int h = 0; h < RPT / 2; ++h) {
+        const float2 xv = __fmul2_rn(pr2(x, h), bc2(f));
+        float2 zz = __ffma2_rn(xv, ex2f2(pr2(y, h)), bc2(eps2));
+        if constexpr (!FULL) {
+          if (!(t.k0 + 2 * h < m)) zz.x = 0.f;
+          if (!(t.k0 + 2 * h + 1 < m)) zz.y = 0.f;
         }
+        st2(x, h, xv);
+        st2(zp, h, zz);
       }
     };
     // the plan totals of the row partials in buf: the first group of each plan
@@ -298,10 +298,11 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
     {
       float rp[RPT];
 #pragma unroll
-      for (int q = 0; q < RPT; ++q) {
-        rp[q] = 0.f;
+      for (int h = 0; h < RPT / 2; ++h) {
+        float2 u = pr2(zp[0], h);
 #pragma unroll
-        for (int s = 0; s < S; ++s) rp[q] += zp[s][q];
+        for (int s = 1; s < S; ++s) u = __fadd2_rn(u, pr2(zp[s], h));
+        st2(rp, h, u);
       }
       st_rows_sm(sm_rs + t.g * MP + t.k0, rp);
     }
@@ -372,10 +373,12 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
       ld_zy(s, z0, y);
       const bool colok = s < t.nvalid;
 #pragma unroll
-      for (int q = 0; q < RPT; ++q) {
-        const float zn = colok ? zp[s][q] * sc[q] : 0.f;
-        zt[s][q] = zn;
-        yt[s][q] = colok ? fmaf(kLog2e, x[s][q] - zn, y[q]) : 0.f;
+      for (int h = 0; h < RPT / 2; ++h) {
+        const float2 zn = __fmul2_rn(pr2(zp[s], h), pr2(sc, h));
+        // (x - zn as fma(zn, -1, x): the same single rounding)
+        const float2 yn = __ffma2_rn(bc2(kLog2e), __ffma2_rn(zn, bc2(-1.f), pr2(x[s], h)), pr2(y, h));
+        st2(zt[s], h, colok ? zn : bc2(0.f));
+        st2(yt[s], h, colok ? yn : bc2(0.f));
       }
       if constexpr (CHECK) {
         if (colok) {
@@ -405,7 +408,8 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
       if (s < t.nvalid) {
         float un[RPT];
 #pragma unroll
-        for (int q = 0; q < RPT; ++q) un[q] = fmaf(kLog2e, x[s][q], yt[s][q]);  // U = Y + X
+        for (int h = 0; h < RPT / 2; ++h)  // U = Y + X
+          st2(un, h, __ffma2_rn(bc2(kLog2e), pr2(x[s], h), pr2(yt[s], h)));
         const size_t off = (t.colbase + s) * MP + t.k0;
         st_rows(a.Z + off, zp[s]);
         st_rows(a.Y + off, un);
@@ -415,10 +419,11 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, 2) plan_pair_kernel(const PlanAr
     {
       float rp[RPT];
 #pragma unroll
-      for (int q = 0; q < RPT; ++q) {
-        rp[q] = 0.f;
+      for (int h = 0; h < RPT / 2; ++h) {
+        float2 u = pr2(zp[0], h);
 #pragma unroll
-        for (int s = 0; s < S; ++s) rp[q] += zp[s][q];
+        for (int s = 1; s < S; ++s) u = __fadd2_rn(u, pr2(zp[s], h));
+        st2(rp, h, u);
       }
       st_rows_sm(sm_rs2 + t.g * MP + t.k0, rp);
     }

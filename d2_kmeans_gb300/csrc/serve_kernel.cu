@@ -89,6 +89,14 @@ __device__ __forceinline__ void sv_push4(const float *local, const unsigned long
       : "memory");
 }
 
+// Pairs of rows go through the packed FP32x2 instructions (one issue slot
+// for two lanes' worth of arithmetic, each lane rounded as its scalar form).
+__device__ __forceinline__ float2 sv_bc(float v) { return make_float2(v, v); }
+
+__device__ __forceinline__ float2 sv_ex2x2(float2 x) { return make_float2(sv_ex2(x.x), sv_ex2(x.y)); }
+
+__device__ __forceinline__ float2 sv_nex2x2(float2 x) { return make_float2(sv_ex2(-x.x), sv_ex2(-x.y)); }
+
 template <int TPC>
 __device__ __forceinline__ float sv_seg_sum(float v) {
 #pragma unroll
@@ -138,7 +146,9 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
   float *cme = sm_c + (g * S) * MP + k0;  // this thread's costs: column s at cme[s*MP + q]
 
   // costs (to shared memory), weights, start point
-  float z[S][RPT], y[S][RPT], w[S], cw[RPT];
+  // Z and Y of row pairs (k0, k0 + 1) and (k0 + 2, k0 + 3): z[s][h] = rows 2h, 2h + 1
+  float2 z[S][2], y[S][2];
+  float w[S], cw[RPT];
 #pragma unroll
   for (int q = 0; q < RPT; ++q) cw[q] = __ldg(a.c_w32 + (size_t)l * MP + k0 + q);
   {
@@ -148,10 +158,11 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
       const bool ok = s < nvalid;
       w[s] = ok ? __ldg(a.q_w + qcol0 + c0 + s) : 0.f;
 #pragma unroll
-      for (int q = 0; q < RPT; ++q) {
-        c[s][q] = 0.f;
-        z[s][q] = ok ? w[s] * cw[q] : 0.f;
-        y[s][q] = 0.f;
+      for (int q = 0; q < RPT; ++q) c[s][q] = 0.f;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        z[s][h] = ok ? make_float2(w[s] * cw[2 * h], w[s] * cw[2 * h + 1]) : sv_bc(0.f);
+        y[s][h] = sv_bc(0.f);
       }
     }
     for (int t = 0; t < a.dim; ++t) {
@@ -203,49 +214,47 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
   // slice, or unused groups of a packed CTA) skips the arithmetic and only
   // takes part in the row-sum exchange with zeros.
   const bool wact = __any_sync(0xffffffffu, active);
-  float pc = 0.f;
+  float2 pc2 = sv_bc(0.f);
   for (int iter = 0; iter < a.iters; ++iter) {
     const int buf = iter & 1;
     const bool last = iter == a.iters - 1;
-    float rp[RPT] = {0.f, 0.f, 0.f, 0.f};
+    float2 rp2[2] = {sv_bc(0.f), sv_bc(0.f)};
     if (wact) {
 #pragma unroll
     for (int s = 0; s < S; ++s) {
       const bool colok = s < nvalid;
       const float4 cc = *((const float4 *)(cme + s * MP));
-      const float c[RPT] = {cc.x, cc.y, cc.z, cc.w};
-      float v[RPT], csum = 0.f;
+      const float2 c[2] = {make_float2(cc.x, cc.y), make_float2(cc.z, cc.w)};
+      float2 v[2];
 #pragma unroll
-      for (int q = 0; q < RPT; ++q) {
-        if constexpr (FULL) {
-          v[q] = fmaf(z[s][q], sv_ex2(-fmaf(c[q], ir2, y[s][q])), kRoundoff);
-        } else {
-          const bool ok = colok && k0 + q < m;
-          v[q] = ok ? fmaf(z[s][q], sv_ex2(-fmaf(c[q], ir2, y[s][q])), kRoundoff) : 0.f;
+      for (int h = 0; h < 2; ++h) {
+        v[h] = __ffma2_rn(z[s][h], sv_nex2x2(__ffma2_rn(c[h], sv_bc(ir2), y[s][h])), sv_bc(kRoundoff));
+        if constexpr (!FULL) {
+          if (!(colok && k0 + 2 * h < m)) v[h].x = 0.f;
+          if (!(colok && k0 + 2 * h + 1 < m)) v[h].y = 0.f;
         }
-        csum += v[q];
       }
-      csum = sv_seg_sum<TPC>(csum);
+      const float2 vs = __fadd2_rn(v[0], v[1]);
+      const float csum = sv_seg_sum<TPC>(vs.x + vs.y);
       const float ws = s == 0 ? sm_w4[tid].x : s == 1 ? sm_w4[tid].y : s == 2 ? sm_w4[tid].z : sm_w4[tid].w;
       const float f = (FULL || colok) ? __fdividef(ws, csum) : 0.f;
       const float eps2 = colok ? kRoundoff : 0.f;
 #pragma unroll
-      for (int q = 0; q < RPT; ++q) {
-        const float xv = v[q] * f;
-        float zp;
-        if constexpr (FULL) {
-          zp = fmaf(xv, sv_ex2(y[s][q]), eps2);
-        } else {
-          const bool ok = colok && k0 + q < m;
-          zp = ok ? fmaf(xv, sv_ex2(y[s][q]), kRoundoff) : 0.f;
+      for (int h = 0; h < 2; ++h) {
+        const float2 xv = __fmul2_rn(v[h], sv_bc(f));
+        float2 zp = __ffma2_rn(xv, sv_ex2x2(y[s][h]), sv_bc(eps2));
+        if constexpr (!FULL) {
+          if (!(k0 + 2 * h < m)) zp.x = 0.f;
+          if (!(k0 + 2 * h + 1 < m)) zp.y = 0.f;
         }
-        y[s][q] = fmaf(kL2e, xv, y[s][q]);  // step 3, first half
-        z[s][q] = zp;
-        rp[q] += zp;
-        if (last) pc = fmaf(c[q], xv, pc);
+        y[s][h] = __ffma2_rn(sv_bc(kL2e), xv, y[s][h]);  // step 3, first half
+        z[s][h] = zp;
+        rp2[h] = __fadd2_rn(rp2[h], zp);
+        if (last) pc2 = __ffma2_rn(c[h], xv, pc2);
       }
     }
     }
+    float rp[RPT] = {rp2[0].x, rp2[0].y, rp2[1].x, rp2[1].y};
     float tot[RPT] = {0.f, 0.f, 0.f, 0.f};
     if (cs == 1) {
       *((float4 *)(sm_rs[buf] + g * MP + k0)) = make_float4(rp[0], rp[1], rp[2], rp[3]);
@@ -287,30 +296,25 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
     }
     // second half of step 2 with the fixed centroid weights, and step 3
     float sc[RPT];
-#pragma unroll
     const float4 cw4 = sm_cw4[tid];
     const float cwq[RPT] = {cw4.x, cw4.y, cw4.z, cw4.w};
 #pragma unroll
     for (int q = 0; q < RPT; ++q) sc[q] = tot[q] > 0.f ? __fdividef(cwq[q], tot[q]) : 0.f;
+    // (padded rows have tot = 0, so sc = 0 zeroes their Z; padded columns
+    // stay at Z = Y = 0 by themselves)
+    const float2 sc2[2] = {make_float2(sc[0], sc[1]), make_float2(sc[2], sc[3])};
     if (wact)
 #pragma unroll
     for (int s = 0; s < S; ++s)
 #pragma unroll
-      for (int q = 0; q < RPT; ++q) {  // second half of step 3: Y -= Z
-        if constexpr (FULL) {  // padded columns stay at Z = Y = 0 by themselves
-          const float zn = z[s][q] * sc[q];
-          y[s][q] = fmaf(-kL2e, zn, y[s][q]);
-          z[s][q] = zn;
-        } else {
-          const bool ok = s < nvalid && k0 + q < m;
-          const float zn = ok ? z[s][q] * sc[q] : 0.f;
-          y[s][q] = ok ? fmaf(-kL2e, zn, y[s][q]) : 0.f;
-          z[s][q] = zn;
-        }
+      for (int h = 0; h < 2; ++h) {  // second half of step 3: Y -= Z
+        const float2 zn = __fmul2_rn(z[s][h], sc2[h]);
+        y[s][h] = __ffma2_rn(sv_bc(-kL2e), zn, y[s][h]);
+        z[s][h] = zn;
       }
   }
   // cost_l = <C, X> of the last iteration, per plan
-  pc = sv_seg_sum<TPC>(pc);
+  float pc = sv_seg_sum<TPC>(pc2.x + pc2.y);
   if (r == 0) sm_cost[g] = (double)pc;
   if (cs == 1) {
     __syncthreads();
