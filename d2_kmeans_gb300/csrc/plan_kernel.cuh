@@ -71,6 +71,24 @@ __device__ __forceinline__ void st2(float *v, int h, float2 u) {
   v[2 * h] = u.x;
   v[2 * h + 1] = u.y;
 }
+// The same pair arithmetic as two scalar instructions (P = false), for
+// kernels at one CTA per SM where the packed form's longer dependent
+// latency costs more than the issue slots it saves.  Results are identical.
+template <bool P>
+__device__ __forceinline__ float2 fma2x(float2 a, float2 b, float2 c) {
+  if constexpr (P) return __ffma2_rn(a, b, c);
+  else return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
+}
+template <bool P>
+__device__ __forceinline__ float2 mul2x(float2 a, float2 b) {
+  if constexpr (P) return __fmul2_rn(a, b);
+  else return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y));
+}
+template <bool P>
+__device__ __forceinline__ float2 add2x(float2 a, float2 b) {
+  if constexpr (P) return __fadd2_rn(a, b);
+  else return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y));
+}
 constexpr float kLog2e = 1.4426950408889634f;  // log2(e)
 constexpr float kLn2 = 0.6931471805599453f;    // ln(2) = 1/log2(e)
 
@@ -538,6 +556,7 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
     plan_kernel_tma(const PlanArgs a, int nitems) {
   using T = Tile<MP, MODE>;
   constexpr int RPT = T::RPT, TPC = T::TPC, G = T::G, S = T::S;
+  constexpr bool PK = MP < 256;  // packed FP32x2 pair arithmetic (scalar at one CTA per SM)
   constexpr int TILE = tma_tile_floats<MP>();
   constexpr int JC = G * S;
   constexpr int CW = T::EUC ? T::DS : 1;  // staged column data: supports or table row
@@ -742,9 +761,10 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
       }
       if (sc_in) {
 #pragma unroll
-        for (int q = 0; q < RPT; ++q) {
-          z[q] *= scin[q];
-          y[q] = fmaf(-kLog2e, z[q], y[q]);
+        for (int h = 0; h < RPT / 2; ++h) {
+          const float2 zz = mul2x<PK>(pr2(z, h), pr2(scin, h));
+          st2(z, h, zz);
+          st2(y, h, fma2x<PK>(bc2(-kLog2e), zz, pr2(y, h)));
         }
       }
     };
@@ -769,44 +789,44 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
       costs(s, c);
       ld_zy(s, z, y);
       const bool colok = s < t.nvalid;
-      float csum = 0.f;
+      // Full height (m == MP): a padded column holds Z = Y = 0 and weight 0,
+      // so its X comes out 0 through the column scale and no mask is needed
+      // (its column sum is ROUNDOFF-positive); step 2 adds ROUNDOFF to valid
+      // columns only.  Rows go in pairs through the FP32x2 instructions.
+      float2 vs = bc2(0.f);
 #pragma unroll
-      for (int q = 0; q < RPT; ++q) {
-        // Full height (m == MP): a padded column holds Z = Y = 0 and weight 0,
-        // so its X comes out 0 through the column scale and no mask is needed
-        // (its column sum is ROUNDOFF-positive); step 2 adds ROUNDOFF to
-        // valid columns only.
-        float v;
-        if constexpr (FULL) {
-          v = fmaf(z[q], ex2f(-fmaf(c[q], ir2, y[q])), kRoundoff);
-        } else {
-          const bool ok = colok && t.k0 + q < m;
-          v = ok ? fmaf(z[q], ex2f(-fmaf(c[q], ir2, y[q])), kRoundoff) : 0.f;
+      for (int h = 0; h < RPT / 2; ++h) {
+        float2 v = fma2x<PK>(pr2(z, h), nex2f2(fma2x<PK>(pr2(c, h), bc2(ir2), pr2(y, h))), bc2(kRoundoff));
+        if constexpr (!FULL) {
+          if (!(colok && t.k0 + 2 * h < m)) v.x = 0.f;
+          if (!(colok && t.k0 + 2 * h + 1 < m)) v.y = 0.f;
         }
-        x[s][q] = v;
-        csum += v;
+        st2(x[s], h, v);
+        vs = h == 0 ? v : add2x<PK>(vs, v);
       }
-      csum = seg_sum<TPC>(csum);
+      const float csum = seg_sum<TPC>(vs.x + vs.y);
       const float f = (FULL || colok) ? __fdividef(w[s], csum) : 0.f;  // (column sum > 0)
       const float eps2 = colok ? kRoundoff : 0.f;
 #pragma unroll
-      for (int q = 0; q < RPT; ++q) {
-        x[s][q] *= f;
-        if constexpr (FULL) {
-          zp[s][q] = fmaf(x[s][q], ex2f(y[q]), eps2);
-        } else {
-          const bool ok = colok && t.k0 + q < m;
-          zp[s][q] = ok ? fmaf(x[s][q], ex2f(y[q]), kRoundoff) : 0.f;
+      for (int h = 0; h < RPT / 2; ++h) {
+        const float2 xv = mul2x<PK>(pr2(x[s], h), bc2(f));
+        float2 zz = fma2x<PK>(xv, ex2f2(pr2(y, h)), bc2(eps2));
+        if constexpr (!FULL) {
+          if (!(t.k0 + 2 * h < m)) zz.x = 0.f;
+          if (!(t.k0 + 2 * h + 1 < m)) zz.y = 0.f;
         }
+        st2(x[s], h, xv);
+        st2(zp[s], h, zz);
       }
     }
     {
       float rp[RPT];
 #pragma unroll
-      for (int q = 0; q < RPT; ++q) {
-        rp[q] = 0.f;
+      for (int h = 0; h < RPT / 2; ++h) {
+        float2 u = pr2(zp[0], h);
 #pragma unroll
-        for (int s = 0; s < S; ++s) rp[q] += zp[s][q];
+        for (int s = 1; s < S; ++s) u = add2x<PK>(u, pr2(zp[s], h));
+        st2(rp, h, u);
       }
       st_rows_sm(sm_rs + t.g * MP + t.k0, rp);
     }
@@ -1000,15 +1020,17 @@ __global__ void __launch_bounds__(GeoT<MP>::NT, MP >= 256 ? 1 : 2)
         }
         if (def_out) {  // Z' and U = Y + X
 #pragma unroll
-          for (int q = 0; q < RPT; ++q) {
-            zn[q] = zp[s][q];
-            yn[q] = fmaf(kLog2e, x[s][q], y[q]);
+          for (int h = 0; h < RPT / 2; ++h) {
+            st2(zn, h, pr2(zp[s], h));
+            st2(yn, h, fma2x<PK>(bc2(kLog2e), pr2(x[s], h), pr2(y, h)));
           }
         } else {
 #pragma unroll
-          for (int q = 0; q < RPT; ++q) {
-            zn[q] = zp[s][q] * sc[q];
-            yn[q] = fmaf(kLog2e, x[s][q] - zn[q], y[q]);
+          for (int h = 0; h < RPT / 2; ++h) {
+            const float2 zz = mul2x<PK>(pr2(zp[s], h), pr2(sc, h));
+            // (x - zn as fma(zn, -1, x): the same single rounding)
+            st2(zn, h, zz);
+            st2(yn, h, fma2x<PK>(bc2(kLog2e), fma2x<PK>(zz, bc2(-1.f), pr2(x[s], h)), pr2(y, h)));
           }
         }
         if constexpr (CHECK) {
