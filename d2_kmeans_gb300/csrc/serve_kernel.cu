@@ -20,6 +20,8 @@
 // spreads one plan over a cluster of cs CTAs.
 #include <cooperative_groups.h>
 
+#include <type_traits>
+
 #include "d2g_internal.cuh"
 
 namespace cg = cooperative_groups;
@@ -215,9 +217,10 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
   // takes part in the row-sum exchange with zeros.
   const bool wact = __any_sync(0xffffffffu, active);
   float2 pc2 = sv_bc(0.f);
-  for (int iter = 0; iter < a.iters; ++iter) {
+  // one iteration (the last one also accumulates <C, X>)
+  auto iteration = [&](const int iter, auto last_tag) {
+    constexpr bool last = decltype(last_tag)::value;
     const int buf = iter & 1;
-    const bool last = iter == a.iters - 1;
     float2 rp2[2] = {sv_bc(0.f), sv_bc(0.f)};
     if (wact) {
 #pragma unroll
@@ -250,7 +253,7 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
         y[s][h] = __ffma2_rn(sv_bc(kL2e), xv, y[s][h]);  // step 3, first half
         z[s][h] = zp;
         rp2[h] = __fadd2_rn(rp2[h], zp);
-        if (last) pc2 = __ffma2_rn(c[h], xv, pc2);
+        if constexpr (last) pc2 = __ffma2_rn(c[h], xv, pc2);
       }
     }
     }
@@ -312,7 +315,9 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
         y[s][h] = __ffma2_rn(sv_bc(-kL2e), zn, y[s][h]);
         z[s][h] = zn;
       }
-  }
+  };
+  for (int iter = 0; iter + 1 < a.iters; ++iter) iteration(iter, std::false_type{});
+  if (a.iters > 0) iteration(a.iters - 1, std::true_type{});
   // cost_l = <C, X> of the last iteration, per plan
   float pc = sv_seg_sum<TPC>(pc2.x + pc2.y);
   if (r == 0) sm_cost[g] = (double)pc;
