@@ -146,7 +146,7 @@ struct Tile {
   bool active;
   size_t colbase;
   float sp[EUC ? S : 1][DS];      // column supports
-  float cc[EUC ? RPT : 1][DS];    // centroid supports of this thread's rows
+  float2 cc[EUC ? RPT / 2 : 1][DS];  // centroid supports of this thread's row pairs
   int sym[S];
   const float *tab;
 
@@ -209,6 +209,22 @@ struct Tile {
     colbase = (size_t)(item_g0 + g) * S;
   }
 
+  // supports of the centroid rows k0 .. k0 + RPT - 1, as row pairs
+  __device__ __forceinline__ void load_centroids(const PlanArgs &a) {
+#pragma unroll
+    for (int h = 0; h < RPT / 2; ++h) {
+#pragma unroll
+      for (int t4 = 0; t4 < DS / 4; ++t4) {
+        const float4 u = __ldg((const float4 *)(a.cs32 + ((size_t)lab * MP + k0 + 2 * h) * DS) + t4);
+        const float4 v = __ldg((const float4 *)(a.cs32 + ((size_t)lab * MP + k0 + 2 * h + 1) * DS) + t4);
+        cc[h][4 * t4 + 0] = make_float2(u.x, v.x);
+        cc[h][4 * t4 + 1] = make_float2(u.y, v.y);
+        cc[h][4 * t4 + 2] = make_float2(u.z, v.z);
+        cc[h][4 * t4 + 3] = make_float2(u.w, v.w);
+      }
+    }
+  }
+
   // costs from staged column data: supports sp_sm [JC][DS] or table rows sym_sm [JC]
   __device__ __forceinline__ void load_costs_staged(const PlanArgs &a, const float *sp_sm,
                                                     const int *sym_sm) {
@@ -226,18 +242,7 @@ struct Tile {
           sp[s][4 * t4 + 3] = v.w;
         }
       }
-#pragma unroll
-      for (int q = 0; q < RPT; ++q) {
-#pragma unroll
-        for (int t4 = 0; t4 < DS / 4; ++t4) {
-          const float4 v =
-              __ldg((const float4 *)(a.cs32 + ((size_t)lab * MP + k0 + q) * DS) + t4);
-          cc[q][4 * t4 + 0] = v.x;
-          cc[q][4 * t4 + 1] = v.y;
-          cc[q][4 * t4 + 2] = v.z;
-          cc[q][4 * t4 + 3] = v.w;
-        }
-      }
+      load_centroids(a);
     } else {
 #pragma unroll
       for (int s = 0; s < S; ++s) sym[s] = s < nvalid ? sym_sm[lc + s] : 0;
@@ -259,18 +264,7 @@ struct Tile {
           sp[s][4 * t4 + 3] = v.w;
         }
       }
-#pragma unroll
-      for (int q = 0; q < RPT; ++q) {
-#pragma unroll
-        for (int t4 = 0; t4 < DS / 4; ++t4) {
-          const float4 v =
-              __ldg((const float4 *)(a.cs32 + ((size_t)lab * MP + k0 + q) * DS) + t4);
-          cc[q][4 * t4 + 0] = v.x;
-          cc[q][4 * t4 + 1] = v.y;
-          cc[q][4 * t4 + 2] = v.z;
-          cc[q][4 * t4 + 3] = v.w;
-        }
-      }
+      load_centroids(a);
     } else {
 #pragma unroll
       for (int s = 0; s < S; ++s) sym[s] = s < nvalid ? __ldg(a.col_sym + colbase + s) : 0;
@@ -281,15 +275,18 @@ struct Tile {
   // ground cost of column s for this thread's RPT rows (not divided by rho)
   __device__ __forceinline__ void costs(int s, float (&c)[RPT]) const {
     if constexpr (EUC) {
+      // two rows at a time through the FP32x2 instructions; cc - sp is
+      // formed as fma(sp, -1, cc), the same single rounding
 #pragma unroll
-      for (int q = 0; q < RPT; ++q) {
-        float acc = 0.f;
+      for (int h = 0; h < RPT / 2; ++h) {
+        float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
         for (int t = 0; t < NDIM; ++t) {  // (padded coordinates are 0 on both sides)
-          const float d = cc[q][t] - sp[s][t];
-          acc = fmaf(d, d, acc);
+          const float2 d = __ffma2_rn(make_float2(sp[s][t], sp[s][t]), make_float2(-1.f, -1.f), cc[h][t]);
+          acc = __ffma2_rn(d, d, acc);
         }
-        c[q] = acc;
+        c[2 * h] = acc.x;
+        c[2 * h + 1] = acc.y;
       }
     } else {
       const float *row = tab + (size_t)sym[s] * MP + k0;

@@ -107,7 +107,7 @@ __device__ __forceinline__ float sv_seg_sum(float v) {
 }
 
 template <int MP, bool FULL>
-__global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
+__global__ void __launch_bounds__(256, 4) serve_kernel(const ServeArgs a) {
   constexpr int RPT = 4, TPC = MP / RPT, G = 256 / TPC, S = 4;
   constexpr float kL2e = 1.4426950408889634f;  // log2(e)
   __shared__ __align__(16) float sm_c[G * S * MP];       // ground costs of the CTA's entries
@@ -177,9 +177,11 @@ __global__ void __launch_bounds__(256, 3) serve_kernel(const ServeArgs a) {
 #pragma unroll
       for (int s = 0; s < S; ++s)
 #pragma unroll
-        for (int q = 0; q < RPT; ++q) {
-          const float d = cv[q] - qv[s];
-          c[s][q] = fmaf(d, d, c[s][q]);
+        for (int h = 0; h < 2; ++h) {  // row pairs: cv - qv as fma(qv, -1, cv), one rounding
+          const float2 d = __ffma2_rn(sv_bc(qv[s]), sv_bc(-1.f), make_float2(cv[2 * h], cv[2 * h + 1]));
+          const float2 acc = __ffma2_rn(d, d, make_float2(c[s][2 * h], c[s][2 * h + 1]));
+          c[s][2 * h] = acc.x;
+          c[s][2 * h + 1] = acc.y;
         }
     }
 #pragma unroll
