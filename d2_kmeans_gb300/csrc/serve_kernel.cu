@@ -161,11 +161,6 @@ __global__ void __launch_bounds__(256, 4) serve_kernel(const ServeArgs a) {
       w[s] = ok ? __ldg(a.q_w + qcol0 + c0 + s) : 0.f;
 #pragma unroll
       for (int q = 0; q < RPT; ++q) c[s][q] = 0.f;
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        z[s][h] = ok ? make_float2(w[s] * cw[2 * h], w[s] * cw[2 * h + 1]) : sv_bc(0.f);
-        y[s][h] = sv_bc(0.f);
-      }
     }
     for (int t = 0; t < a.dim; ++t) {
       float cv[RPT], qv[S];
@@ -189,6 +184,13 @@ __global__ void __launch_bounds__(256, 4) serve_kernel(const ServeArgs a) {
       *((float4 *)(cme + s * MP)) = make_float4(c[s][0], c[s][1], c[s][2], c[s][3]);
     sm_w4[tid] = make_float4(w[0], w[1], w[2], w[3]);
     sm_cw4[tid] = make_float4(cw[0], cw[1], cw[2], cw[3]);
+#pragma unroll
+    for (int s = 0; s < S; ++s)  // start point, after the costs (fewer live registers there)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        z[s][h] = s < nvalid ? make_float2(w[s] * cw[2 * h], w[s] * cw[2 * h + 1]) : sv_bc(0.f);
+        y[s][h] = sv_bc(0.f);
+      }
   }
   const int m = a.m;
   const unsigned xbytes = (unsigned)cs * MP * 4u;  // one partial from every rank per iteration
@@ -280,14 +282,14 @@ __global__ void __launch_bounds__(256, 4) serve_kernel(const ServeArgs a) {
         for (int q = 0; q < RPT; ++q) rp[q] += __shfl_xor_sync(0xffffffffu, rp[q], o);
       if (lane < TPC) *((float4 *)(sm_rs[buf] + warp * MP + k0)) = make_float4(rp[0], rp[1], rp[2], rp[3]);
       __syncthreads();
-      if (warp == 0 && lane < TPC) {
+      if (warp < cs && lane < TPC) {  // warp w pushes to rank w
         float4 pt = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int w8 = 0; w8 < 8; ++w8) {
           const float4 u = *((const float4 *)(sm_rs[buf] + w8 * MP + k0));
           pt.x += u.x; pt.y += u.y; pt.z += u.z; pt.w += u.w;
         }
-        for (int rk = 0; rk < cs; ++rk) sv_push4(&sm_x[buf][rank][k0], &sm_bar[buf], (unsigned)rk, pt);
+        sv_push4(&sm_x[buf][rank][k0], &sm_bar[buf], (unsigned)warp, pt);
       }
       if (!sv_mbar_wait(&sm_bar[buf], (unsigned)(iter >> 1) & 1u)) sm_fail = 1;
       for (int rk = 0; rk < cs; ++rk) {
