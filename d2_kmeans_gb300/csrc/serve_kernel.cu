@@ -274,8 +274,8 @@ __global__ void __launch_bounds__(256, 4) serve_kernel(const ServeArgs a) {
       }
     } else {
       // one plan over the cluster: the warp's groups are pre-added with
-      // shuffles, warp 0 adds the warps' partials and pushes the CTA's partial
-      // into every rank; each rank then adds the cs partials in rank order
+      // shuffles; warp w < cs adds the warps' partials and pushes the CTA's
+      // partial into rank w; each rank then adds the cs partials in rank order
 #pragma unroll
       for (int o = TPC; o < 32; o <<= 1)
 #pragma unroll
