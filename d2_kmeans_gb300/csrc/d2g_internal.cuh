@@ -195,6 +195,15 @@ cudaError_t launch_resid_final(const double *part, int n, Ctl *ctl, double *trac
                                int iter, bool obj_from_slot3, cudaStream_t st, int xmode = 0,
                                double *xbuf = nullptr);
 // sharded update on one device: the shards' exchange buffers summed in shard order
+// Launchers cache each kernel's shared-memory attribute and resident grid per
+// device (both apply to the current device); device ordinals below this bound.
+constexpr int kMaxDevices = 64;
+inline cudaError_t launch_device(int *dev) {
+  cudaError_t e = cudaGetDevice(dev);
+  if (e == cudaSuccess && (*dev < 0 || *dev >= kMaxDevices)) e = cudaErrorInvalidDevice;
+  return e;
+}
+
 constexpr int kMaxShards = 8;
 struct ShardBufs {
   const double *p[kMaxShards];

@@ -802,7 +802,7 @@ cudaError_t launch_emd_t(const EmdArgs &a, cudaStream_t st) {
   const size_t slice = emd_slice_bytes(a.nmax, DP);
   auto kern = emd_kernel<MODE, DP>;
   int dev = 0, sms = 0, smem_sm = 0;
-  cudaGetDevice(&dev);
+  if (cudaError_t e = launch_device(&dev); e != cudaSuccess) return e;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
   // warps per block: the most warps per SM that the shared memory holds
@@ -819,14 +819,14 @@ cudaError_t launch_emd_t(const EmdArgs &a, cudaStream_t st) {
   }
   if (wpb < 1) return cudaErrorInvalidValue;
   const size_t smem = (size_t)wpb * slice;
-  static size_t configured = 0;
+  static size_t configured[kMaxDevices] = {};
   {  // the attribute only grows; calls from other host threads see it set first
     static std::mutex mu;
     std::lock_guard<std::mutex> lk(mu);
-    if (smem > configured) {
+    if (smem > configured[dev]) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
-      configured = smem;
+      configured[dev] = smem;
     }
   }
   int per_sm = 0;

@@ -1114,20 +1114,28 @@ cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaSt
   // (cached per instantiation; phases on other host threads share the cache)
   static std::mutex mu;
   std::lock_guard<std::mutex> lk(mu);
-  static int grid[kMaxCluster + 1] = {0};
+  struct Shape {
+    int grid[kMaxCluster + 1] = {0};  // resident CTAs for cluster size c (0: plain launches)
+    int nsm = 0;
+    size_t configured_smem = 0;
+  };
+  static Shape shapes[kMaxDevices];
+  int dev = 0;
+  if (cudaError_t e = launch_device(&dev); e != cudaSuccess) return e;
+  Shape &sh = shapes[dev];
+  int *grid = sh.grid;
   constexpr int JC = GeoT<MP>::JC;
   constexpr int CW = MODE == COST_TABLE ? 1 : (MODE == COST_EUCLID8 ? 8 : 4);
   const size_t sm = smem + (size_t)4 * tma_tile_floats<MP>() * sizeof(float) +
                     2 * (size_t)GeoT<MP>::G * 16 + 2 * (size_t)JC * 4 * (1 + CW) + (size_t)2 * MP * 4 +
                     (plan_stages_costs(MP, MODE) ? (size_t)2 * tma_tile_floats<MP>() * 4 : 0) +
                     (size_t)2 * 8 * MP * 4 + (size_t)2 * (a.dim + 1) * MP * 4;
-  static size_t configured_smem = 0;
   auto kern = plan_kernel_tma<MP, MODE, CHECK, FULL, WIDE>;
-  if (configured_smem < sm) {
+  if (sh.configured_smem < sm) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
     for (int c = 0; c <= kMaxCluster; ++c) grid[c] = 0;
-    configured_smem = sm;
+    sh.configured_smem = sm;
   }
   const int cs = a.cs;
   if (grid[cs] == 0) {
@@ -1147,21 +1155,19 @@ cudaError_t launch_plan_tma_t(const PlanArgs &a, int nitems, size_t smem, cudaSt
     if (e != cudaSuccess) return e;
     grid[cs] = (ncl > 0 ? ncl : 1) * cs;
   }
-  static int nsm = 0;
   if (grid[0] == 0) {  // plain launches: resident CTAs per SM x SMs
-    int dev = 0, per = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    int per = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&sh.nsm, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess)
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, GeoT<MP>::NT, sm);
     if (e != cudaSuccess) return e;
-    grid[0] = (per > 0 ? per : 1) * nsm;
+    grid[0] = (per > 0 ? per : 1) * sh.nsm;
   }
   if (nitems <= 0) return cudaSuccess;
   const bool plain = cs == 1;
   const long long units = (long long)nitems * cs;
   int cap = plain ? grid[0] : grid[cs];
-  if (plain && a.ctas_per_sm > 0) cap = std::min(cap, a.ctas_per_sm * nsm);
+  if (plain && a.ctas_per_sm > 0) cap = std::min(cap, a.ctas_per_sm * sh.nsm);
   const int g = units < cap ? (int)units : cap;
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = plan_cfg(g, GeoT<MP>::NT, sm, st, attr, plain ? 1 : cs);

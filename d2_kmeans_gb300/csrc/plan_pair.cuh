@@ -543,44 +543,49 @@ constexpr size_t pair_scale_bytes() {
 // its plan's scale from global memory.
 template <int MP, int MODE, bool CHECK, bool FULL>
 cudaError_t launch_pair_t(const PlanArgs &a, int nitems, cudaStream_t st) {
-  static std::mutex mu;  // the cached launch shape is shared by phases on other host threads
+  static std::mutex mu;  // the cached launch shapes are shared by phases on other host threads
   std::lock_guard<std::mutex> lk(mu);
-  static int grid = 0, nsm = 0;
-  static bool stage = false;
-  static size_t configured = 0;
+  struct Shape {
+    int grid = 0, nsm = 0;
+    bool stage = false;
+    size_t configured = 0;
+  };
+  static Shape shapes[kMaxDevices];
+  int dev = 0;
+  if (cudaError_t e = launch_device(&dev); e != cudaSuccess) return e;
+  Shape &sh = shapes[dev];
   const size_t sm0 = pair_smem_bytes<MP>(MODE, a.dim), sm1 = sm0 + pair_scale_bytes<MP>();
   auto kern = plan_pair_kernel<MP, MODE, CHECK, FULL>;
-  if (configured < sm1) {
+  if (sh.configured < sm1) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
     if (e != cudaSuccess) {  // beyond the opt-in limit: the kernel without staged scales
       (void)cudaGetLastError();
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm0);
       if (e != cudaSuccess) return e;
-      configured = sm0;
-      stage = false;
+      sh.configured = sm0;
+      sh.stage = false;
     } else {
-      configured = sm1;
+      sh.configured = sm1;
     }
-    grid = 0;
+    sh.grid = 0;
   }
-  if (grid == 0) {
-    int dev = 0, per0 = 0, per1 = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (sh.grid == 0) {
+    int per0 = 0, per1 = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&sh.nsm, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per0, kern, GeoT<MP>::NT, sm0);
-    if (e == cudaSuccess && configured >= sm1)
+    if (e == cudaSuccess && sh.configured >= sm1)
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, kern, GeoT<MP>::NT, sm1);
     if (e != cudaSuccess) return e;
-    stage = configured >= sm1 && per1 >= per0;
-    const int per = stage ? per1 : per0;
-    grid = (per > 0 ? per : 1) * nsm;
+    sh.stage = sh.configured >= sm1 && per1 >= per0;
+    const int per = sh.stage ? per1 : per0;
+    sh.grid = (per > 0 ? per : 1) * sh.nsm;
   }
   if (nitems <= 0) return cudaSuccess;
-  int cap = grid;
-  if (a.ctas_per_sm > 0) cap = std::min(cap, a.ctas_per_sm * nsm);
+  int cap = sh.grid;
+  if (a.ctas_per_sm > 0) cap = std::min(cap, a.ctas_per_sm * sh.nsm);
   const int g = nitems < cap ? nitems : cap;
   PlanArgs b = a;
-  if (stage && a.stage_scales && (a.flags & PF_IN_DEF)) b.flags |= PF_STAGE_SC;
+  if (sh.stage && a.stage_scales && (a.flags & PF_IN_DEF)) b.flags |= PF_STAGE_SC;
   const size_t sm = (b.flags & PF_STAGE_SC) ? sm1 : sm0;
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = plan_cfg(g, GeoT<MP>::NT, sm, st, attr, 1);

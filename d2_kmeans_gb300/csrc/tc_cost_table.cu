@@ -296,11 +296,10 @@ cudaError_t launch_cost_table_tc(const float *cs, int nrows, const float *vsplit
                                  float *csplit, int *err, cudaStream_t st) {
   if (nrows <= 0) return cudaSuccess;
   // per device; the first call for a device comes before any graph capture
-  static bool configured[64] = {};
+  static bool configured[kMaxDevices] = {};
   int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  cudaError_t e = launch_device(&dev);
   if (e != cudaSuccess) return e;
-  if (dev >= 64) return cudaErrorInvalidDevice;
   {
     static std::mutex mu;  // phases on other host threads
     std::lock_guard<std::mutex> lk(mu);
