@@ -8,10 +8,12 @@
 // cost_l = <C_l, X_l> for every centroid and its argmin.
 //
 // With the centroid weights fixed there is no coupling between plans, so a
-// plan's whole iteration loop runs on chip: C, Z and Y stay in registers,
-// column sums use shuffles, row sums go through shared memory (and DSMEM when a
-// plan spans a thread-block cluster).  Nothing touches HBM inside the loop;
-// the kernel is bound by MUFU ex2 and FP32 issue.
+// plan's whole iteration loop runs on chip: Z and Y stay in registers (row
+// pairs, for the packed FP32x2 instructions), C in shared memory, column sums
+// use shuffles, row sums go through shared memory (and DSMEM when a plan spans
+// a thread-block cluster).  Nothing touches HBM inside the loop; the kernel is
+// bound by issue and latency (MUFU ex2, FP32, the per-iteration row-sum
+// exchange).  64 registers: four CTAs of 256 threads per SM.
 //
 // Work items come from compact descriptors, not per-group tables:
 //   item = {request, first centroid l0, plans in the item, groups per plan}
