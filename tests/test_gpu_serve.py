@@ -43,6 +43,30 @@ def test_serve_matches_oracle(serve_mod, oracle_mod):
     S.close()
 
 
+@pytest.mark.parametrize("m", [12, 16, 32, 50])
+def test_serve_support_sizes(serve_mod, oracle_mod, m):
+    """Centroid supports of every padded size the server takes (16, 32, 64),
+    full (m = 16, 32) and with padded rows (m = 12, 50), each with queries
+    from one column group to 512 supports (several plans per CTA up to
+    clusters of 8 CTAs); the same tolerances as above."""
+    c_w, c_supp, means = synth.serving_centroids(k=8, m=m, dim=8, n_comp=6, seed=40 + m)
+    S = serve_mod.Server(c_w, c_supp, iters=200)
+    rng = np.random.default_rng(m)
+    try:
+        for mq in (3, 37, 130, 300, 512):
+            comp = rng.integers(0, means.shape[0], size=mq)
+            w = rng.dirichlet(np.ones(mq))
+            s = means[comp] + rng.normal(size=(mq, means.shape[1]))
+            lab, cost, _ = S.solve(w / w.sum(), s)
+            best, ref = oracle_mod.serve_query(c_w, c_supp, w / w.sum(), s, iters=200)
+            np.testing.assert_allclose(cost, ref, rtol=1e-4, err_msg=f"m={m} m_q={mq}")
+            order = np.sort(ref)
+            if (order[1] - order[0]) / order[0] > 1e-4:
+                assert lab == best
+    finally:
+        S.close()
+
+
 def test_same_result_alone_and_in_a_mix(serve_mod):
     c_w, c_supp, means = synth.serving_centroids(k=64, m=64, dim=32, n_comp=16, seed=5)
     S = serve_mod.Server(c_w, c_supp, iters=100)
