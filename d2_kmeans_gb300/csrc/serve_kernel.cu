@@ -378,8 +378,7 @@ cudaError_t launch_serve(int MP, const ServeArgs &a, int nitems, cudaStream_t st
     case 16: return full ? launch_serve_mp<16, true>(a, nitems, st) : launch_serve_mp<16, false>(a, nitems, st);
     case 32: return full ? launch_serve_mp<32, true>(a, nitems, st) : launch_serve_mp<32, false>(a, nitems, st);
     case 64: return full ? launch_serve_mp<64, true>(a, nitems, st) : launch_serve_mp<64, false>(a, nitems, st);
-    case 128: return full ? launch_serve_mp<128, true>(a, nitems, st) : launch_serve_mp<128, false>(a, nitems, st);
-    default: return cudaErrorInvalidValue;
+    default: return cudaErrorInvalidValue;  // (the server takes str <= 64: a 512-support query fits 8 CTAs)
   }
 }
 
