@@ -80,30 +80,49 @@ __global__ void __launch_bounds__(kRedThreads) cluster_partial_kernel(const Clus
       }
     }
   }
-  for (int ii = pb + warp; ii < pe && !(weights && slotted); ii += kRedWarps) {
-    const int p = slotted ? ii : a.cl_plans[ii];
-    if (weights) {
-      double v[NK], s = 0.0;
+  if (!weights) {
+    // moment planes: each warp adds its plans pb + warp, pb + warp + 8, ... in
+    // that order, U of them loaded before any is added (the loads overlap;
+    // the sums are those of the one-plan-at-a-time loop, bit for bit)
+    constexpr int U = NK <= 2 ? 8 : (NK == 4 ? 4 : 2);
+    for (int ii0 = pb + warp; ii0 < pe; ii0 += kRedWarps * U) {
+      double v[U][NK];
 #pragma unroll
-      for (int i = 0; i < NK; ++i) {
-        const int k = lane + 32 * i;
-        v[i] = 0.0;
-        if (k < m)
-          v[i] = a.rowsum32 ? (double)a.rowsum32[(size_t)p * a.rstride + k]
-                            : a.rowsum64[(size_t)p * a.rstride + k];
-        s += v[i];
+      for (int u = 0; u < U; ++u) {
+        const int ii = ii0 + u * kRedWarps;
+        const int p = ii < pe ? (slotted ? ii : a.cl_plans[ii]) : -1;
+        const size_t base = ((size_t)(p < 0 ? 0 : p) * (a.dim + 1) + plane) * a.rstride;
+#pragma unroll
+        for (int i = 0; i < NK; ++i) {
+          const int k = lane + 32 * i;
+          v[u][i] = 0.0;
+          if (p >= 0 && k < m) v[u][i] = a.xmom32 ? (double)a.xmom32[base + k] : a.xmom64[base + k];
+        }
       }
-      const double inv = 1.0 / wsum(s);  // step 4: the instance's Zr column normalised (:180)
 #pragma unroll
-      for (int i = 0; i < NK; ++i) acc[i] = fma(v[i], inv, acc[i]);
-    } else {
-      const size_t base = ((size_t)p * (a.dim + 1) + plane) * a.rstride;
+      for (int u = 0; u < U; ++u)
+        if (ii0 + u * kRedWarps < pe)
 #pragma unroll
-      for (int i = 0; i < NK; ++i) {
-        const int k = lane + 32 * i;
-        if (k < m) acc[i] += a.xmom32 ? (double)a.xmom32[base + k] : a.xmom64[base + k];
-      }
+          for (int i = 0; i < NK; ++i)
+            if (lane + 32 * i < m) acc[i] += v[u][i];
     }
+  }
+  // weights of the FP64 form: plans through the cluster's list, each one's
+  // row sums normalised here
+  for (int ii = pb + warp; ii < pe && weights && !slotted; ii += kRedWarps) {
+    const int p = a.cl_plans[ii];
+    double v[NK], s = 0.0;
+#pragma unroll
+    for (int i = 0; i < NK; ++i) {
+      const int k = lane + 32 * i;
+      v[i] = 0.0;
+      if (k < m)
+        v[i] = a.rowsum32 ? (double)a.rowsum32[(size_t)p * a.rstride + k] : a.rowsum64[(size_t)p * a.rstride + k];
+      s += v[i];
+    }
+    const double inv = 1.0 / wsum(s);  // step 4: the instance's Zr column normalised (:180)
+#pragma unroll
+    for (int i = 0; i < NK; ++i) acc[i] = fma(v[i], inv, acc[i]);
   }
   __shared__ double sm[kRedWarps][kMaxM];
 #pragma unroll
