@@ -425,10 +425,11 @@ __global__ void __launch_bounds__(GeoT<MP>::NT) pack_columns_kernel(
   using T = Tile<MP, COST_TABLE>;
   T t;
   t.init(a);
-  if (!t.active || t.r != 0) return;
+  // the first min(S, TPC) threads of a group take its columns in turn
+  if (!t.active || t.r >= T::S) return;
   const long long cum = plan_cum[t.p];
   const int jj0 = (t.cta_g0 + t.g - t.pl_g0) * T::S;
-  for (int s = 0; s < T::S; ++s) {
+  for (int s = t.r; s < T::S; s += T::TPC) {
     const size_t pc = t.colbase + s;
     const bool ok = s < t.nvalid;
     const long long rc = cum + jj0 + s;
