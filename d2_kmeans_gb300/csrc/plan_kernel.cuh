@@ -44,6 +44,9 @@ struct GeoT {
   static constexpr int G = NT / TPC;
   static constexpr int JC = G * S;
   static_assert(TPC >= 1 && TPC <= 32 && (32 % TPC) == 0, "TPC must divide a warp");
+  // a unit's column weights and symbols arrive by untiled bulk copy from
+  // col_w + g0 * S (ng * S * 4 bytes): 16-byte alignment needs S * 4 % 16 == 0
+  static_assert((S * 4) % 16 == 0, "columns per thread must keep the per-column bulk copies 16-byte aligned");
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
