@@ -8,7 +8,7 @@ sites, src/d2/centroid_Bregman.c:142,188,215-217,308-310).
   with the same centroids, bit for bit.
 * With each shard's own rho (the reference's MPI build), the shards match the
   oracle's restatement of that build run as two ranks.
-Tolerances are the benchmark spec's bounds of the other parity tests: objective
+Tolerances are those of the other parity tests: objective
 1e-5 relative, c_w L1 1e-4 per cluster, supports 1e-4 relative.
 """
 import threading
