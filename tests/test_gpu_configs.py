@@ -23,9 +23,8 @@ in seconds:
 
 Tolerances (the parity bounds of every batched test): objective 1e-5
 relative at every check, c_w L1 1e-4 per cluster, supports 1e-4 relative
-per support point; serving costs
-1e-4 relative, argmin identical wherever the oracle's two best costs differ
-by more than that.  The oracle runs for all cases start together on host
+per support point; serving costs 1e-4 relative, argmin identical wherever
+the oracle's two best costs differ by more than that.  The oracle runs for all cases start together on host
 threads when the module loads (the C oracle releases the GIL).
 """
 import concurrent.futures as cf
