@@ -270,6 +270,7 @@ __global__ void __launch_bounds__(256, 4) serve_kernel(const ServeArgs a) {
       __syncthreads();
       // every thread sums its own plan's partials (no second barrier: the
       // partials are double-buffered by iteration parity)
+#pragma unroll 4
       for (int j = lo; j < hi; ++j) {
         const float4 u = *((const float4 *)(sm_rs[buf] + j * MP + k0));
         tot[0] += u.x; tot[1] += u.y; tot[2] += u.z; tot[3] += u.w;
@@ -294,6 +295,7 @@ __global__ void __launch_bounds__(256, 4) serve_kernel(const ServeArgs a) {
         sv_push4(&sm_x[buf][rank][k0], &sm_bar[buf], (unsigned)warp, pt);
       }
       if (!sv_mbar_wait(&sm_bar[buf], (unsigned)(iter >> 1) & 1u)) sm_fail = 1;
+#pragma unroll 4
       for (int rk = 0; rk < cs; ++rk) {
         const float4 u = *((const float4 *)(&sm_x[buf][rk][0] + k0));
         tot[0] += u.x; tot[1] += u.y; tot[2] += u.z; tot[3] += u.w;
